@@ -1,0 +1,285 @@
+"""Seeded synthetic SPPM scenes as flat numpy arrays.
+
+A scene is a dict of arrays in exactly the per-facet form the reference builds
+in ``Scene::CreateScene`` (SPPM/SPPM/Scene.cpp:182-236): facet ``f`` has three
+corner positions, three corner normals and three corner UVs, plus a material
+(attribute) id.  Facet order is the OBJ face order, so the same arrays can be
+written as OBJ/MTL/PNG for the reference loader (``objio.write_scene``) and
+handed unchanged to the C-ABI (``fr_scene_desc``).
+
+Material records mirror the ``SURFACE_PARAM`` fields the reference's
+``SceneMaterialManager`` plug-in sets (SPPM/SPPM/material.h:35-90,
+SPPM/SPPM/main.cpp:14-114); ``type`` selects the ``Surface`` subclass:
+
+    0 DiffuseSurface   (material.h:163-177)
+    1 MetalSurface     (material.h:396-425)   perfect mirror
+    2 Roughconductor   (material.h:222-278)   GGX conductor
+    3 GGXGlass         (material.h:280-394)   GGX dielectric
+
+All randomness comes from ``numpy.random.Generator(PCG64(seed))``.
+"""
+from __future__ import annotations
+
+import math
+
+import numpy as np
+
+DIFFUSE, METAL, GGX_CONDUCTOR, GGX_DIELECTRIC = 0, 1, 2, 3
+PINHOLE, THINLENS = 0, 1
+
+CONFIG_SEED_BASE = 0x5EED0000
+
+
+def material(name, mtype, albedo=(0.75, 0.75, 0.75), emission=(0.0, 0.0, 0.0),
+             roughness=1.0, index=1.0, extinction=1.0, reflectance=1.0,
+             opaque=True, sppm=True, tex_albedo=-1, tex_roughness=-1, tex_bump=-1):
+    """One material record.  Defaults are the reference's SURFACE_PARAM()
+    defaults (material.h:76-89) except ``isSPPMSurface``, which the reference's
+    default manager leaves false (no hitpoints at all); scenes set it."""
+    return dict(name=name, type=int(mtype), albedo=tuple(float(x) for x in albedo),
+                emission=tuple(float(x) for x in emission), roughness=float(roughness),
+                index=float(index), extinction=float(extinction),
+                reflectance=float(reflectance), opaque=bool(opaque), sppm=bool(sppm),
+                tex_albedo=int(tex_albedo), tex_roughness=int(tex_roughness),
+                tex_bump=int(tex_bump))
+
+
+class _Builder:
+    def __init__(self):
+        self.pos, self.nrm, self.uv, self.mat = [], [], [], []
+
+    def tris(self, p, n, uv, mat_id):
+        p = np.asarray(p, np.float32).reshape(-1, 3, 3)
+        n = np.asarray(n, np.float32).reshape(-1, 3, 3)
+        uv = np.asarray(uv, np.float32).reshape(-1, 3, 2)
+        self.pos.append(p)
+        self.nrm.append(n)
+        self.uv.append(uv)
+        self.mat.append(np.full(len(p), mat_id, np.int32))
+
+    def quad(self, a, b, c, d, normal, mat_id, uvs=((0, 0), (1, 0), (1, 1), (0, 1))):
+        """Quad a-b-c-d as triangles (a,b,c) and (a,c,d), flat normal."""
+        a, b, c, d = (np.asarray(x, np.float32) for x in (a, b, c, d))
+        nrm = np.asarray(normal, np.float32)
+        u = [np.asarray(x, np.float32) for x in uvs]
+        self.tris([[a, b, c], [a, c, d]], [[nrm] * 3, [nrm] * 3],
+                  [[u[0], u[1], u[2]], [u[0], u[2], u[3]]], mat_id)
+
+    def build(self):
+        return dict(pos=np.concatenate(self.pos).astype(np.float32),
+                    nrm=np.concatenate(self.nrm).astype(np.float32),
+                    uv=np.concatenate(self.uv).astype(np.float32),
+                    mat=np.concatenate(self.mat).astype(np.int32))
+
+
+def _rot_y(deg):
+    t = math.radians(deg)
+    c, s = math.cos(t), math.sin(t)
+    return np.array([[c, 0, s], [0, 1, 0], [-s, 0, c]], np.float64)
+
+
+def _box(b, center, size, rot_deg, mat_id):
+    """Axis-aligned box rotated about y: 12 triangles, outward flat normals."""
+    R = _rot_y(rot_deg)
+    hx, hy, hz = (s * 0.5 for s in size)
+    corners = np.array([[x, y, z] for x in (-hx, hx) for y in (-hy, hy) for z in (-hz, hz)])
+    corners = corners @ R.T + np.asarray(center)
+    faces = [  # (corner ids ccw seen from outside, outward local normal)
+        ((0, 1, 3, 2), (-1, 0, 0)), ((4, 6, 7, 5), (1, 0, 0)),
+        ((0, 4, 5, 1), (0, -1, 0)), ((2, 3, 7, 6), (0, 1, 0)),
+        ((0, 2, 6, 4), (0, 0, -1)), ((1, 5, 7, 3), (0, 0, 1)),
+    ]
+    for (i0, i1, i2, i3), n in faces:
+        nw = R @ np.asarray(n, np.float64)
+        b.quad(corners[i0], corners[i1], corners[i2], corners[i3], nw, mat_id)
+
+
+def _camera(ctype, width, height, pos, target, fov, focal=1.0, dist=1.0,
+            lens=0.0):
+    return dict(type=int(ctype), width=int(width), height=int(height),
+                pos=tuple(float(x) for x in pos), target=tuple(float(x) for x in target),
+                fov=float(fov), focal=float(focal), dist=float(dist),
+                aspect=float(width) / float(height), lens=float(lens))
+
+
+def value_noise(rng, size, cells, channels=1):
+    """Seeded value noise: a coarse random grid, bilinearly upsampled (float64 in [0,1])."""
+    grid = rng.random((cells + 1, cells + 1, channels))
+    t = np.linspace(0.0, cells, size, endpoint=False)
+    i0 = np.floor(t).astype(int)
+    f = t - i0
+    g00 = grid[i0][:, i0]
+    g10 = grid[i0 + 1][:, i0]
+    g01 = grid[i0][:, i0 + 1]
+    g11 = grid[i0 + 1][:, i0 + 1]
+    fy = f[:, None, None]
+    fx = f[None, :, None]
+    return (g00 * (1 - fy) * (1 - fx) + g10 * fy * (1 - fx) + g01 * (1 - fy) * fx + g11 * fy * fx)
+
+
+def noise_texture(rng, size, kind):
+    """RGBA8 seeded texture.  ``kind``: 'albedo' | 'roughness' | 'normal' | 'emission'.
+    Alpha is 255 (opaque) so no surface takes the reference's translucency
+    pass-through (SPPM.cpp:138-142) unless a scene asks for it explicitly."""
+    n = value_noise(rng, size, max(4, size // 64), 3) * 0.6 + value_noise(rng, size, max(8, size // 16), 3) * 0.4
+    if kind == 'albedo':
+        rgb = 0.15 + 0.8 * n
+    elif kind == 'roughness':
+        rgb = np.repeat(n[..., :1], 3, axis=2) * 0.9 + 0.1
+    elif kind == 'normal':
+        rgb = np.empty_like(n)
+        rgb[..., 0] = 0.5 + 0.25 * (n[..., 0] - 0.5)
+        rgb[..., 1] = 0.5 + 0.25 * (n[..., 1] - 0.5)
+        rgb[..., 2] = 0.9 + 0.1 * n[..., 2]
+    elif kind == 'emission':
+        rgb = 0.3 + 0.7 * n
+    else:
+        raise ValueError(kind)
+    out = np.empty((size, size, 4), np.uint8)
+    out[..., :3] = np.clip(np.round(rgb * 255.0), 0, 255).astype(np.uint8)
+    out[..., 3] = 255
+    return out
+
+
+def cornell_box(seed=CONFIG_SEED_BASE + 0, width=256, height=256, light_rgb=(17.0, 12.0, 4.0)):
+    """Procedural Cornell box: unit cube with 5 diffuse walls, a diffuse box and
+    a GGX-conductor box (roughness 0.2) rotated by U(0,30) degrees, and a
+    0.25x0.25 ceiling quad light.  34 scene triangles + 2 light triangles.
+
+    The light sits 1e-3 below the ceiling so no camera or photon ray meets two
+    coplanar triangles at the same distance (the reference resolves such ties
+    by BVH visit order, bvh8.h:591)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    mats = [
+        material('white', DIFFUSE, (0.75, 0.75, 0.75)),
+        material('red', DIFFUSE, (0.75, 0.25, 0.25)),
+        material('green', DIFFUSE, (0.25, 0.75, 0.25)),
+        material('boxdiffuse', DIFFUSE, (0.75, 0.75, 0.75)),
+        material('boxconductor', GGX_CONDUCTOR, (0.9, 0.85, 0.8), roughness=0.2,
+                 index=1.1978, extinction=7.0488),
+        material('light', DIFFUSE, (1.0, 1.0, 1.0), emission=light_rgb),
+    ]
+    b = _Builder()
+    b.quad((0, 0, 0), (0, 0, 1), (1, 0, 1), (1, 0, 0), (0, 1, 0), 0)        # floor
+    b.quad((0, 1, 0), (1, 1, 0), (1, 1, 1), (0, 1, 1), (0, -1, 0), 0)       # ceiling
+    b.quad((0, 0, 1), (0, 1, 1), (1, 1, 1), (1, 0, 1), (0, 0, -1), 0)       # back
+    b.quad((0, 0, 0), (0, 1, 0), (0, 1, 1), (0, 0, 1), (1, 0, 0), 1)        # left (red)
+    b.quad((1, 0, 0), (1, 0, 1), (1, 1, 1), (1, 1, 0), (-1, 0, 0), 2)       # right (green)
+    r1, r2 = rng.uniform(0.0, 30.0, 2)
+    # Boxes float 1e-3 above the floor for the same reason (no coplanar faces).
+    _box(b, (0.33, 0.301, 0.62), (0.27, 0.6, 0.27), r1, 3)
+    _box(b, (0.68, 0.151, 0.35), (0.27, 0.3, 0.27), -r2, 4)
+    y = 1.0 - 1e-3
+    b.quad((0.375, y, 0.375), (0.625, y, 0.375), (0.625, y, 0.625), (0.375, y, 0.625),
+           (0, -1, 0), 5)
+    scene = b.build()
+    scene.update(materials=mats, textures=[],
+                 camera=_camera(PINHOLE, width, height, (0.5, 0.5, -1.35), (0.5, 0.5, 0.5), 38.0))
+    return scene
+
+
+def uv_sphere(b, center, radius, mat_id, n_lat=34, n_lon=36, uv_scale=1.0):
+    """UV sphere with smooth normals: 2*n_lon cap triangles + 2*n_lon*(n_lat-2) band triangles."""
+    c = np.asarray(center, np.float64)
+    th = np.linspace(0.0, math.pi, n_lat + 1)
+    ph = np.linspace(0.0, 2.0 * math.pi, n_lon + 1)
+    st, ct = np.sin(th), np.cos(th)
+    dirs = np.stack([st[:, None] * np.cos(ph)[None, :], np.repeat(ct[:, None], n_lon + 1, 1),
+                     st[:, None] * np.sin(ph)[None, :]], axis=-1)
+    pts = c + radius * dirs
+    uvs = np.stack(np.meshgrid(ph / (2 * math.pi), th / math.pi), -1) * uv_scale
+    P, N, U = [], [], []
+    for i in range(n_lat):
+        for j in range(n_lon):
+            a, bb = (i, j), (i, j + 1)
+            cc, d = (i + 1, j + 1), (i + 1, j)
+            if i != 0:
+                P.append([pts[a], pts[bb], pts[cc]]); N.append([dirs[a], dirs[bb], dirs[cc]])
+                U.append([uvs[a], uvs[bb], uvs[cc]])
+            if i != n_lat - 1:
+                P.append([pts[a], pts[cc], pts[d]]); N.append([dirs[a], dirs[cc], dirs[d]])
+                U.append([uvs[a], uvs[cc], uvs[d]])
+    b.tris(P, N, U, mat_id)
+
+
+def height_field(b, rng, n, x0, x1, z0, z1, amp, mat_id, uv_scale=4.0):
+    """n x n vertex grid of seeded value noise: 2*(n-1)^2 triangles, smooth normals."""
+    h = value_noise(rng, n, max(4, n // 32), 1)[..., 0] * amp
+    xs = np.linspace(x0, x1, n)
+    zs = np.linspace(z0, z1, n)
+    X, Z = np.meshgrid(xs, zs, indexing='xy')
+    P = np.stack([X, h, Z], -1)
+    gx = np.gradient(h, xs, axis=1)
+    gz = np.gradient(h, zs, axis=0)
+    Nn = np.stack([-gx, np.ones_like(h), -gz], -1)
+    Nn /= np.linalg.norm(Nn, axis=-1, keepdims=True)
+    U = np.stack(np.meshgrid(np.linspace(0, uv_scale, n), np.linspace(0, uv_scale, n), indexing='xy'), -1)
+    i, j = np.meshgrid(np.arange(n - 1), np.arange(n - 1), indexing='ij')
+    i, j = i.ravel(), j.ravel()
+    a, bb, cc, d = (i, j), (i, j + 1), (i + 1, j + 1), (i + 1, j)
+    def tri(p, q, r):
+        return (np.stack([P[p], P[q], P[r]], 1), np.stack([Nn[p], Nn[q], Nn[r]], 1),
+                np.stack([U[p], U[q], U[r]], 1))
+    t1 = tri(a, d, cc)
+    t2 = tri(a, cc, bb)
+    inter = lambda k: np.stack([t1[k], t2[k]], 1).reshape(-1, 3, t1[k].shape[-1])
+    b.tris(inter(0), inter(1), inter(2), mat_id)
+
+
+def mixed_materials(seed=CONFIG_SEED_BASE + 1, width=1280, height=720, n_spheres=200,
+                    field_n=512, tex_size=1024, light_tex=512, n_lat=34, n_lon=36,
+                    aperture=0.02):
+    """Mixed-materials scene: ``n_spheres`` UV spheres (radius U(0.05,0.3)) over a
+    ``field_n``^2 height field of seeded value noise.  Materials split equally
+    across diffuse, specular, GGX conductor and GGX dielectric (IOR 1.5),
+    roughness U(0.05,0.5).  The field carries albedo/roughness/normal textures
+    (``tex_size``^2 RGBA8), the area light a ``light_tex``^2 textured emission,
+    and the camera is a thin lens with aperture ``aperture``.
+    With the defaults: 997,444 triangles at 1280x720."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    textures = [noise_texture(rng, tex_size, 'albedo'), noise_texture(rng, tex_size, 'roughness'),
+                noise_texture(rng, tex_size, 'normal'), noise_texture(rng, light_tex, 'emission')]
+    mats = [material('field', DIFFUSE, (0.7, 0.7, 0.7), tex_albedo=0, tex_roughness=1, tex_bump=2),
+            material('light', DIFFUSE, (1, 1, 1), emission=(10.0, 9.0, 8.0), tex_albedo=3)]
+    b = _Builder()
+    ext = 4.0
+    height_field(b, rng, field_n, -ext, ext, -ext, ext, 0.25, 0)
+    for k in range(n_spheres):
+        mtype = k % 4
+        rough = float(rng.uniform(0.05, 0.5))
+        col = tuple(float(x) for x in rng.uniform(0.3, 0.95, 3))
+        name = 's%03d' % k
+        if mtype == DIFFUSE:
+            m = material(name, DIFFUSE, col)
+        elif mtype == METAL:
+            m = material(name, METAL, col, sppm=False)
+        elif mtype == GGX_CONDUCTOR:
+            m = material(name, GGX_CONDUCTOR, col, roughness=rough, index=1.1978, extinction=7.0488)
+        else:
+            m = material(name, GGX_DIELECTRIC, (0.98, 0.98, 0.98), roughness=rough, index=1.5,
+                         opaque=False, sppm=False)
+        mats.append(m)
+        r = float(rng.uniform(0.05, 0.3))
+        cx, cz = rng.uniform(-ext * 0.85, ext * 0.85, 2)
+        uv_sphere(b, (cx, 0.25 + r, cz), r, len(mats) - 1, n_lat, n_lon)
+    ly = 3.0
+    b.quad((-1, ly, -1), (1, ly, -1), (1, ly, 1), (-1, ly, 1), (0, -1, 0), 1)
+    scene = b.build()
+    scene.update(materials=mats, textures=textures,
+                 camera=_camera(THINLENS, width, height, (0.0, 2.6, -7.5), (0.0, 0.2, 0.0), 30.0,
+                                focal=0.9, dist=1.0, lens=aperture))
+    return scene
+
+
+def small_mixed(seed=CONFIG_SEED_BASE + 101, width=48, height=32, tex_size=64):
+    """A small scene with every feature of the mixed-materials config (four
+    material types, albedo/roughness/normal textures, textured light, thin
+    lens) at a size the reference and the oracle finish in seconds."""
+    return mixed_materials(seed=seed, width=width, height=height, n_spheres=12, field_n=24,
+                           tex_size=tex_size, light_tex=32, n_lat=10, n_lon=12, aperture=0.05)
+
+
+def scene_stats(scene):
+    return dict(triangles=int(len(scene['pos'])), materials=len(scene['materials']),
+                textures=len(scene['textures']), width=scene['camera']['width'],
+                height=scene['camera']['height'])
