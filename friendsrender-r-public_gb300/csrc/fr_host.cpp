@@ -1,0 +1,748 @@
+// Host side of the GPU SPPM renderer: scene upload, light tables, camera set-up,
+// the iteration driver and the C-ABI declared in include/friendsrender.h.
+//
+// Everything the reference computes once per scene on the host (camera basis,
+// light alias tables, textured-emission tables) is computed here with the same
+// float/double expressions, so the kernels see the reference's exact values.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/friendsrender.h"
+#include "fr_bvh.h"
+#include "fr_kernels.h"
+#include "fr_layout.h"
+
+using namespace fr;
+
+namespace {
+
+thread_local std::string g_error;
+
+int fail(int code, const char* fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  std::vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_error = buf;
+  return code;
+}
+
+#define FR_CUDA(call)                                                                     \
+  do {                                                                                    \
+    const cudaError_t e_ = (call);                                                        \
+    if (e_ != cudaSuccess) return fail(FR_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+// ------------------------------------------------------- host vector helpers
+// Float arithmetic in the reference's PTUtility::Vec3 order (Vec.h:179-243).
+struct H3 {
+  float x, y, z;
+};
+inline H3 operator+(H3 a, H3 b) { return {a.x + b.x, a.y + b.y, a.z + b.z}; }
+inline H3 operator-(H3 a, H3 b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline H3 operator*(H3 a, H3 b) { return {a.x * b.x, a.y * b.y, a.z * b.z}; }
+inline H3 operator*(float s, H3 a) { return {s * a.x, s * a.y, s * a.z}; }
+inline H3 operator*(H3 a, float s) { return {s * a.x, s * a.y, s * a.z}; }
+inline H3 operator/(H3 a, float s) { return {a.x / s, a.y / s, a.z / s}; }
+inline float dot(H3 a, H3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline H3 cross(H3 a, H3 b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline float norm2(H3 a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
+inline float norm(H3 a) { return std::sqrt(norm2(a)); }
+inline H3 normalized(H3 a) {
+  const float d = norm(a);
+  return {a.x / d, a.y / d, a.z / d};
+}
+inline H3 h3(const float* p) { return {p[0], p[1], p[2]}; }
+inline void put(float* d, H3 v) { d[0] = v.x; d[1] = v.y; d[2] = v.z; }
+
+// LinearSampler::Sample (TextureSampler.h:61-79) on the host, used to build
+// the textured-emission tables.
+struct HostTex {
+  int w, h;
+  const uint8_t* t;
+  void fetch(int idx, float o[4]) const {
+    for (int c = 0; c < 4; ++c) o[c] = t[4 * (size_t)idx + c] / 255.0f;
+  }
+  void bilinear(float u, float v, float out[4]) const {
+    const int iu = (int)((float)w * u), iv = (int)((float)h * v);
+    const int x1 = std::abs(iu) % w, y1 = std::abs(iv) % h;
+    const int x2 = std::min(w - 1, x1 + 1), y2 = std::min(h - 1, y1 + 1);
+    float t00[4], t10[4], t01[4], t11[4];
+    fetch(x1 + y1 * w, t00); fetch(x2 + y1 * w, t10); fetch(x1 + y2 * w, t01); fetch(x2 + y2 * w, t11);
+    const float fw = std::fabs(u * (float)w) - (float)std::abs(iu);
+    const float fh = std::fabs(v * (float)h) - (float)std::abs(iv);
+    for (int c = 0; c < 4; ++c) {
+      const float up = t00[c] * (1.0f - fw) + t10[c] * fw;
+      const float down = t01[c] * (1.0f - fw) + t11[c] * fw;
+      out[c] = up * (1.0f - fh) + down * fh;
+    }
+  }
+};
+
+// QRandSequence::HaltonCore<B>::Sample (QRandSequence.h:10-25), including its
+// digit count from double log2.
+float halton(int n, int B) {
+  float result = 0.0f;
+  if (n <= 0) return result;
+  const int keta = (int)(std::log2((double)n) / std::log2((double)B) + 1);
+  for (int i = 0; i < keta; ++i) {
+    result = (float)((double)result + (double)(n % B) * std::pow((double)B, (double)(-(i + 1))));
+    n /= B;
+  }
+  return result;
+}
+
+// TableSampler<T>::Init (TableSampler.h:44-120): the reference's alias
+// construction, step for step, so its bins (and so every light / emission
+// sample) are the reference's.
+struct AliasBin {
+  float prob = 1.0f;
+  int left = -1, right = -1;
+};
+std::vector<AliasBin> alias_table(const std::vector<float>& values, float* average) {
+  const int N = (int)values.size();
+  std::vector<AliasBin> table(N);
+  float avg = 0.0f;
+  for (int i = 0; i < N; ++i) avg += std::max(0.0f, values[i]);
+  avg /= N;
+  std::vector<std::pair<float, int>> bigger, smaller;
+  for (int i = 0; i < N; ++i) {
+    const float v = std::max(0.0f, values[i]);
+    if (v >= avg) bigger.push_back({v / avg, i});
+    else smaller.push_back({v / avg, i});
+  }
+  size_t ids = 0, idb = 0;
+  for (int i = 0; i < N; ++i) {
+    if (ids < smaller.size()) {
+      table[i].left = smaller[ids].second;
+      table[i].prob = smaller[ids].first;
+      ++ids;
+      if (idb < bigger.size()) {
+        table[i].right = bigger[idb].second;
+        bigger[idb].first -= (1.0f - table[i].prob);
+        if (bigger[idb].first < 1.0f) smaller.push_back(bigger[idb++]);
+      } else if (smaller.size() == ids) {
+        table[i].right = -1;
+        table[i].prob = 1.0f;
+      } else {
+        table[i].right = smaller[ids].second;
+      }
+    } else {
+      table[i].left = bigger[idb].second;
+      table[i].prob = 1.0f;
+      bigger[idb].first -= 1.0f;
+      if (bigger[idb].first < 1.0f) smaller.push_back(bigger[idb++]);
+    }
+  }
+  *average = avg;
+  return table;
+}
+
+float facet_area(H3 p0, H3 p1, H3 p2) { return 0.5f * norm(cross(p1 - p0, p2 - p0)); }  // Normal_Facet.h:45-47
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace
+
+struct fr_ctx {
+  cudaStream_t stream = nullptr;
+  std::vector<DevBuf> bufs;
+  size_t device_bytes = 0;
+  SceneGPU sc{};
+  CameraGPU cam{};
+  int W = 0, H = 0, P = 0;
+  float alpha = 0.9f, r0 = 0.015f, cell_scale = 2.0f;
+  uint32_t flags = 0;
+  float rr_eye[2] = {0.f, 0.f};
+  int bvh_depth = 0;
+  HitpointBuf hp{};
+  PixelState st{};
+  PhotonSlots ph{};
+  uint32_t* counts = nullptr;
+  PhotonGrid grid{};
+  GridInfo* gi = nullptr;
+  ScanTemp scan{};
+  int* err = nullptr;
+  int32_t* dbg_m = nullptr;
+  float4* dbg_phi = nullptr;
+  float4* image = nullptr;
+  int64_t iterations = 0, photons_total = 0;
+
+  template <typename T>
+  int alloc(T** out, size_t count) {
+    void* p = nullptr;
+    const size_t bytes = std::max<size_t>(count * sizeof(T), 16);
+    const cudaError_t e = cudaMalloc(&p, bytes);
+    if (e != cudaSuccess) return fail(FR_ERR_OOM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+    bufs.push_back({p, bytes});
+    device_bytes += bytes;
+    *out = static_cast<T*>(p);
+    return FR_OK;
+  }
+  template <typename T>
+  int upload(T** out, const T* src, size_t count) {
+    int rc = alloc(out, count);
+    if (rc) return rc;
+    if (count) FR_CUDA(cudaMemcpyAsync(*out, src, count * sizeof(T), cudaMemcpyHostToDevice, stream));
+    return FR_OK;
+  }
+  ~fr_ctx() {
+    if (stream) cudaStreamSynchronize(stream);
+    for (auto& b : bufs) cudaFree(b.p);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+namespace {
+
+int check_scene(const fr_scene_desc* s) {
+  if (!s || s->num_facets <= 0 || !s->positions || !s->normals || !s->uvs || !s->material_ids)
+    return fail(FR_ERR_INVALID, "scene: no facets or a NULL array");
+  if (s->num_materials <= 0 || !s->materials) return fail(FR_ERR_INVALID, "scene: no materials");
+  if (s->num_textures < 0 || (s->num_textures > 0 && !s->textures)) return fail(FR_ERR_INVALID, "scene: textures");
+  for (int t = 0; t < s->num_textures; ++t)
+    if (s->textures[t].width <= 0 || s->textures[t].height <= 0 || !s->textures[t].texels)
+      return fail(FR_ERR_INVALID, "scene: texture %d is empty", t);
+  for (int m = 0; m < s->num_materials; ++m) {
+    const fr_material_desc& d = s->materials[m];
+    if (d.type < 0 || d.type > 3) return fail(FR_ERR_INVALID, "material %d: type %d", m, d.type);
+    const int tex[3] = {d.tex_albedo, d.tex_roughness, d.tex_bump};
+    for (int k = 0; k < 3; ++k)
+      if (tex[k] < -1 || tex[k] >= s->num_textures) return fail(FR_ERR_INVALID, "material %d: texture index", m);
+  }
+  for (int f = 0; f < s->num_facets; ++f)
+    if (s->material_ids[f] < 0 || s->material_ids[f] >= s->num_materials)
+      return fail(FR_ERR_INVALID, "facet %d: material id %d out of range", f, s->material_ids[f]);
+  if (s->num_facets >= (1 << kLeafCountShift)) return fail(FR_ERR_INVALID, "scene: too many facets");
+  return FR_OK;
+}
+
+// iCamera constructor (Camera.h:132-151) and the thin-lens lens size.
+CameraGPU setup_camera(const fr_camera_desc& c) {
+  CameraGPU g{};
+  g.type = c.type;
+  g.width = c.width;
+  g.height = c.height;
+  const H3 pos = h3(c.position), tgt = h3(c.target);
+  const H3 dir = normalized(tgt - pos);
+  const float fov = (kPI * c.fov_degrees) / 360.0f;
+  const float pw = (float)(2.0 * (double)c.distance_to_lens * std::tan((double)fov) * (double)c.aspect);
+  const float ph = (float)(2.0 * (double)c.distance_to_lens * std::tan((double)fov));
+  H3 e1, e2;
+  if ((double)dir.y > 0.99) {
+    e1 = {1.f, 0.f, 0.f};
+    e2 = {0.f, 0.f, 1.f};
+  } else {
+    e1 = normalized(cross(H3{0.f, 1.f, 0.f}, dir));
+    e2 = normalized(cross(dir, e1));
+  }
+  put(g.pos, pos); put(g.dir, dir); put(g.e1, e1); put(g.e2, e2);
+  g.plane_w = pw;
+  g.plane_h = ph;
+  g.lens_w = c.lens_width > 0.0f ? c.lens_width : pw;
+  g.lens_h = c.lens_height > 0.0f ? c.lens_height : ph;
+  g.F = c.focal_length;
+  g.dist = c.distance_to_lens;
+  return g;
+}
+
+// Scene::CreateScene light collection (Scene.cpp:145-154), CreateAreaLight
+// (LightSampler.cpp:30-66) and CreateLightSampler (LightSampler.cpp:6-28).
+void build_lights(const fr_scene_desc& s, std::vector<LightGPU>& lights, std::vector<EmitEntry>& emit) {
+  std::vector<float> flux_norm;  // AreaLight::Evaluate = |_Flux| (LightSampler.cpp:113-115)
+  for (int f = 0; f < s.num_facets; ++f) {
+    const fr_material_desc& m = s.materials[s.material_ids[f]];
+    const H3 rad = h3(m.emission);
+    if (!(rad.x + rad.y + rad.z > 0.00001f)) continue;
+    const float* P = s.positions + 9 * (size_t)f;
+    const float* N = s.normals + 9 * (size_t)f;
+    const float* U = s.uvs + 6 * (size_t)f;
+    const H3 p0 = h3(P), p1 = h3(P + 3), p2 = h3(P + 6);
+    const float area = facet_area(p0, p1, p2);
+    LightGPU L{};
+    put(L.p0, p0); put(L.p1, p1); put(L.p2, p2);
+    put(L.normal, normalized(h3(N) + h3(N + 3) + h3(N + 6)));
+    L.pdf_point = 2.0f / std::fabs(norm(cross(p1 - p0, p2 - p0)));  // Sampling.cpp:347
+    H3 flux;
+    if (m.tex_albedo >= 0) {
+      const fr_texture_desc& td = s.textures[m.tex_albedo];
+      const HostTex tex{td.width, td.height, td.texels};
+      std::vector<H3> uvw(kEmitSamples), Ls(kEmitSamples);
+      H3 total{0.f, 0.f, 0.f};
+      for (int i = 0; i < kEmitSamples; ++i) {
+        H3 w{(float)i / (float)kEmitSamples, halton(i, 2), halton(i, 3)};  // Hammersley (QRandSequence.h:27-36)
+        if (w.y > w.x) { w.x *= 0.5f; w.y -= w.x; }
+        else { w.y *= 0.5f; w.x -= w.y; }
+        const float uvx = w.x * U[0] + w.y * U[2] + (1.0f - w.x - w.y) * U[4];
+        const float uvy = w.x * U[1] + w.y * U[3] + (1.0f - w.x - w.y) * U[5];
+        float c[4];
+        tex.bilinear(uvx, uvy, c);
+        H3 Lv = H3{c[0], c[1], c[2]} * rad;
+        if (norm2(Lv) < 0.01f) Lv = {0.f, 0.f, 0.f};
+        uvw[i] = w;
+        Ls[i] = Lv;
+        total = total + Lv;
+      }
+      if ((double)norm2(total) < 1e-6) {
+        Ls[0] = (float)1e-6 * H3{1.f, 1.f, 1.f};
+        uvw[0] = {0.f, 0.f, 0.f};
+      } else {
+        total = total * ((2.0f * kPI * area) / (float)kEmitSamples);
+      }
+      flux = total;
+      std::vector<float> vals(kEmitSamples);
+      for (int i = 0; i < kEmitSamples; ++i) vals[i] = norm(Ls[i]);
+      float avg = 0.f;
+      const std::vector<AliasBin> tab = alias_table(vals, &avg);
+      L.textured = 1;
+      L.emit_offset = (int32_t)emit.size();
+      for (int i = 0; i < kEmitSamples; ++i) {
+        EmitEntry e{};
+        e.prob = tab[i].prob;
+        e.left = tab[i].left;
+        e.right = tab[i].right;
+        put(e.uvw, uvw[i]);
+        put(e.L, Ls[i]);
+        const float gp = norm(Ls[i]) / avg / (float)kEmitSamples;  // TableSampler::GetPDF (TableSampler.h:122-124)
+        e.pdf = (gp * kEmitSamples) / area;                        // LightSampler.cpp:73
+        emit.push_back(e);
+      }
+    } else {
+      flux = rad * 2.0f * kPI * area;                              // LightSampler.cpp:62
+      put(L.radiance, flux / (2.0f * kPI * area));                 // LightSampler.cpp:78
+    }
+    flux_norm.push_back(norm(flux));
+    lights.push_back(L);
+  }
+  const int NL = (int)lights.size();
+  if (!NL) return;
+  float avg = 0.f;
+  const std::vector<AliasBin> tab = alias_table(flux_norm, &avg);
+  for (int i = 0; i < NL; ++i) {
+    lights[i].alias_prob = tab[i].prob;
+    lights[i].alias_left = tab[i].left;
+    lights[i].alias_right = tab[i].right;
+    lights[i].pdf_light = flux_norm[i] / avg / (float)NL;  // GetAreaLightPDF (LightSampler.h:87)
+  }
+}
+
+uint32_t next_pow2(uint64_t v) {
+  uint64_t p = 1;
+  while (p < v) p <<= 1;
+  return (uint32_t)std::min<uint64_t>(p, 1u << 31);
+}
+
+int run_iteration(fr_ctx* c) {
+  const uint32_t step = (uint32_t)(++c->iterations);
+  IterParams it{};
+  it.step = step;
+  it.photons = c->P;
+  it.width = c->W;
+  it.height = c->H;
+  it.alpha = c->alpha;
+  it.flags = c->flags;
+  cudaStream_t s = c->stream;
+  launch_eye_pass(c->sc, c->cam, it, c->rr_eye, c->hp, c->st, c->gi, c->err, s);
+  launch_photon_pass(c->sc, it, c->ph, c->counts, c->err, s);
+  launch_grid_setup(c->gi, c->sc, c->cell_scale, c->r0, s);
+  FR_CUDA(cudaMemsetAsync(c->grid.cell_count, 0, sizeof(uint32_t) * (size_t)c->grid.table, s));
+  launch_photon_count(c->ph, c->counts, c->P, kPhotonSlots, c->grid, c->gi, s);
+  launch_scan(c->grid.cell_count, c->grid.cell_start, c->grid.table + 1, c->scan, s);
+  launch_photon_scatter(c->ph, c->counts, c->P, kPhotonSlots, c->grid, s);
+  launch_gather_update(c->sc, it, c->hp, c->grid, c->gi, c->st, c->dbg_m, c->dbg_phi, s);
+  c->photons_total += c->P;
+  FR_CUDA(cudaGetLastError());
+  return FR_OK;
+}
+
+int check_device_error(fr_ctx* c) {
+  int e = 0;
+  FR_CUDA(cudaMemcpyAsync(&e, c->err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+  FR_CUDA(cudaStreamSynchronize(c->stream));
+  if (e & kErrStack) return fail(FR_ERR_DEVICE, "BVH traversal stack overflow (depth %d)", c->bvh_depth);
+  if (e) return fail(FR_ERR_DEVICE, "device error word %d", e);
+  return FR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* fr_last_error(void) { return g_error.c_str(); }
+
+int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr_sppm_params* params, fr_ctx** out) {
+  g_error.clear();
+  if (!out) return fail(FR_ERR_INVALID, "out is NULL");
+  *out = nullptr;
+  int rc = check_scene(scene);
+  if (rc) return rc;
+  if (!camera || camera->width <= 0 || camera->height <= 0 || (camera->type != 0 && camera->type != 1))
+    return fail(FR_ERR_INVALID, "camera: bad type or size");
+  if (!params || params->photons_per_iteration <= 0) return fail(FR_ERR_INVALID, "params: photons_per_iteration");
+  if (!(params->initial_radius > 0.0f)) return fail(FR_ERR_INVALID, "params: initial_radius");
+  if ((int64_t)camera->width * camera->height > (1 << 30)) return fail(FR_ERR_INVALID, "camera: too many pixels");
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return fail(FR_ERR_CUDA, "no CUDA device");
+
+  fr_ctx* c = new fr_ctx();
+  auto bail = [&](int code) {
+    delete c;
+    return code;
+  };
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(FR_ERR_CUDA, "cudaStreamCreate failed"));
+  c->W = camera->width;
+  c->H = camera->height;
+  c->P = params->photons_per_iteration;
+  c->alpha = params->alpha;
+  c->r0 = params->initial_radius;
+  c->flags = params->flags;
+  c->cell_scale = params->grid_cell_scale > 0.0f ? params->grid_cell_scale : 2.0f;
+  c->rr_eye[0] = (float)std::exp((double)(4 - 5));  // getHitpointInfo RR (SPPM.cpp:117)
+  c->rr_eye[1] = (float)std::exp((double)(4 - 6));
+  c->cam = setup_camera(*camera);
+  upload_byte_lut(c->stream);
+
+  // ---- geometry
+  const int T = scene->num_facets;
+  float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+  for (size_t i = 0; i < (size_t)T * 3; ++i)
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = std::min(lo[a], scene->positions[3 * i + a]);
+      hi[a] = std::max(hi[a], scene->positions[3 * i + a]);
+    }
+  const float diag = std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
+                               (hi[2] - lo[2]) * (hi[2] - lo[2]));
+  BVHResult bvh = build_bvh8(scene->positions, T, 1e-5f * diag + 1e-7f);
+  c->bvh_depth = bvh.depth;
+  if (bvh.depth * 7 + 1 > 64) return bail(fail(FR_ERR_INVALID, "BVH depth %d exceeds the traversal stack", bvh.depth));
+  std::vector<TriGPU> tris(T);
+  for (int k = 0; k < T; ++k) {
+    const int f = bvh.tri_order[k];
+    const float* P = scene->positions + 9 * (size_t)f;
+    TriGPU& t = tris[k];
+    for (int a = 0; a < 3; ++a) {
+      t.v0[a] = P[a];
+      t.e1[a] = P[3 + a] - P[a];
+      t.e2[a] = P[6 + a] - P[a];
+    }
+    int32_t fid = f;
+    std::memcpy(&t.v0[3], &fid, 4);
+    t.e1[3] = 0.f;
+    t.e2[3] = 0.f;
+  }
+  std::vector<FacetShade> shade(T);
+  for (int f = 0; f < T; ++f) {
+    FacetShade& s = shade[f];
+    const float* N = scene->normals + 9 * (size_t)f;
+    const float* U = scene->uvs + 6 * (size_t)f;
+    for (int a = 0; a < 3; ++a) { s.n0[a] = N[a]; s.n1[a] = N[3 + a]; s.n2[a] = N[6 + a]; }
+    s.uv0[0] = U[0]; s.uv0[1] = U[1]; s.uv1[0] = U[2]; s.uv1[1] = U[3]; s.uv2[0] = U[4]; s.uv2[1] = U[5];
+    s.attr = scene->material_ids[f];
+  }
+  std::vector<MaterialGPU> mats(scene->num_materials);
+  for (int m = 0; m < scene->num_materials; ++m) {
+    const fr_material_desc& d = scene->materials[m];
+    MaterialGPU& g = mats[m];
+    g.type = d.type;
+    g.flags = (d.sppm_surface ? kMatSPPM : 0) | (d.opaque ? kMatOpaque : 0);
+    g.tex_albedo = d.tex_albedo;
+    g.tex_rough = d.tex_roughness;
+    g.tex_bump = d.tex_bump;
+    for (int a = 0; a < 3; ++a) { g.albedo[a] = d.albedo[a]; g.radiance[a] = d.emission[a]; }
+    g.index = d.index;
+    g.roughness = d.roughness;
+    g.extinction = d.extinction;
+    g.reflectance = d.reflectance;
+  }
+  std::vector<LightGPU> lights;
+  std::vector<EmitEntry> emit;
+  build_lights(*scene, lights, emit);
+  if (lights.empty()) return bail(fail(FR_ERR_INVALID, "scene: no emissive facets"));
+
+  BVHNode8* d_nodes;
+  TriGPU* d_tris;
+  FacetShade* d_shade;
+  MaterialGPU* d_mats;
+  LightGPU* d_lights;
+  EmitEntry* d_emit;
+  if ((rc = c->upload(&d_nodes, bvh.nodes.data(), bvh.nodes.size())) ||
+      (rc = c->upload(&d_tris, tris.data(), tris.size())) || (rc = c->upload(&d_shade, shade.data(), shade.size())) ||
+      (rc = c->upload(&d_mats, mats.data(), mats.size())) ||
+      (rc = c->upload(&d_lights, lights.data(), lights.size())) ||
+      (rc = c->upload(&d_emit, emit.data(), emit.size())))
+    return bail(rc);
+  std::vector<TextureGPU> texs(scene->num_textures);
+  for (int t = 0; t < scene->num_textures; ++t) {
+    const fr_texture_desc& td = scene->textures[t];
+    uint32_t* d_tex;
+    const size_t n = (size_t)td.width * td.height;
+    if ((rc = c->alloc(&d_tex, n))) return bail(rc);
+    if (cudaMemcpyAsync(d_tex, td.texels, n * 4, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
+      return bail(fail(FR_ERR_CUDA, "texture upload"));
+    texs[t] = TextureGPU{d_tex, td.width, td.height, 0, 0};
+  }
+  TextureGPU* d_texs;
+  if ((rc = c->upload(&d_texs, texs.data(), texs.size()))) return bail(rc);
+  c->sc = SceneGPU{d_nodes, d_tris, d_shade, d_mats, d_texs, d_lights, d_emit,
+                   (int32_t)bvh.nodes.size(), T, T, (int32_t)lights.size(),
+                   {lo[0], lo[1], lo[2]}, {hi[0], hi[1], hi[2]}};
+
+  // ---- per-iteration buffers (all allocated here; iterations allocate nothing)
+  const size_t npix = (size_t)c->W * c->H;
+  const size_t nslots = (size_t)c->P * kPhotonSlots;
+  if ((rc = c->alloc(&c->hp.pos, npix)) || (rc = c->alloc(&c->hp.nrm, npix)) || (rc = c->alloc(&c->hp.out, npix)) ||
+      (rc = c->alloc(&c->hp.wgt, npix)) || (rc = c->alloc(&c->st.tau, 3 * npix)) || (rc = c->alloc(&c->st.n, npix)) ||
+      (rc = c->alloc(&c->st.r, npix)) || (rc = c->alloc(&c->st.g, npix)) || (rc = c->alloc(&c->ph.pos, nslots)) ||
+      (rc = c->alloc(&c->ph.flux, nslots)) || (rc = c->alloc(&c->ph.dir, nslots)) ||
+      (rc = c->alloc(&c->counts, (size_t)c->P)) || (rc = c->alloc(&c->gi, 1)) || (rc = c->alloc(&c->err, 1)) ||
+      (rc = c->alloc(&c->dbg_m, npix)) || (rc = c->alloc(&c->dbg_phi, npix)) || (rc = c->alloc(&c->image, npix)))
+    return bail(rc);
+  // Photon grid: one bucket per expected photon or better (a few photons per path).
+  c->grid.table = next_pow2(std::max<uint64_t>((uint64_t)c->P * 4, 1u << 16));
+  const size_t cap = nslots;
+  if ((rc = c->alloc(&c->grid.pos, cap)) || (rc = c->alloc(&c->grid.flux, cap)) || (rc = c->alloc(&c->grid.dir, cap)) ||
+      (rc = c->alloc(&c->grid.cell_count, (size_t)c->grid.table + 1)) ||
+      (rc = c->alloc(&c->grid.cell_start, (size_t)c->grid.table + 1)) || (rc = c->alloc(&c->grid.slot_key, nslots)) ||
+      (rc = c->alloc(&c->grid.slot_rank, nslots)))
+    return bail(rc);
+  const uint32_t words = scan_temp_words(c->grid.table + 1, c->scan);
+  uint32_t* sw;
+  if ((rc = c->alloc(&sw, words))) return bail(rc);
+  for (int l = 0; l < c->scan.levels; ++l) {
+    c->scan.level[l] = sw;
+    sw += c->scan.level_n[l] + 1;
+  }
+  // Initial state: initializeSharedPoints (SPPM.cpp:356-373) and empty photon slots.
+  std::vector<float> r(npix, c->r0);
+  if (cudaMemcpyAsync(c->st.r, r.data(), npix * 4, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
+    return bail(fail(FR_ERR_CUDA, "state upload"));
+  cudaMemsetAsync(c->st.tau, 0, 3 * npix * sizeof(double), c->stream);
+  cudaMemsetAsync(c->st.n, 0, npix * 4, c->stream);
+  cudaMemsetAsync(c->st.g, 0, npix * 4, c->stream);
+  cudaMemsetAsync(c->ph.dir, 0, nslots * sizeof(float4), c->stream);
+  cudaMemsetAsync(c->ph.pos, 0, nslots * sizeof(float4), c->stream);
+  cudaMemsetAsync(c->ph.flux, 0, nslots * sizeof(float4), c->stream);
+  cudaMemsetAsync(c->gi, 0, sizeof(GridInfo), c->stream);
+  cudaMemsetAsync(c->err, 0, sizeof(int), c->stream);
+  cudaMemsetAsync(c->hp.pos, 0, npix * sizeof(float4), c->stream);
+  if (cudaStreamSynchronize(c->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess)
+    return bail(fail(FR_ERR_CUDA, "initialisation failed"));
+  *out = c;
+  return FR_OK;
+}
+
+int fr_iterate(fr_ctx* c, int n) {
+  if (!c || n < 0) return fail(FR_ERR_INVALID, "fr_iterate: bad arguments");
+  for (int k = 0; k < n; ++k) {
+    const int rc = run_iteration(c);
+    if (rc) return rc;
+  }
+  return FR_OK;
+}
+
+int fr_synchronize(fr_ctx* c) {
+  if (!c) return fail(FR_ERR_INVALID, "fr_synchronize: NULL context");
+  FR_CUDA(cudaStreamSynchronize(c->stream));
+  FR_CUDA(cudaGetLastError());
+  return check_device_error(c);
+}
+
+int fr_resolve_dev(fr_ctx* c, float* rgba_dev) {
+  if (!c || !rgba_dev) return fail(FR_ERR_INVALID, "fr_resolve_dev: bad arguments");
+  launch_resolve(c->st, c->W * c->H, (double)c->photons_total, (double)c->iterations,
+                 reinterpret_cast<float4*>(rgba_dev), c->stream);
+  FR_CUDA(cudaGetLastError());
+  return FR_OK;
+}
+
+int fr_resolve(fr_ctx* c, float* rgba) {
+  if (!c || !rgba) return fail(FR_ERR_INVALID, "fr_resolve: bad arguments");
+  int rc = fr_resolve_dev(c, reinterpret_cast<float*>(c->image));
+  if (rc) return rc;
+  FR_CUDA(cudaMemcpyAsync(rgba, c->image, sizeof(float4) * (size_t)c->W * c->H, cudaMemcpyDeviceToHost, c->stream));
+  return fr_synchronize(c);
+}
+
+int fr_get_stats(fr_ctx* c, fr_stats* o) {
+  if (!c || !o) return fail(FR_ERR_INVALID, "fr_get_stats: bad arguments");
+  o->iterations = c->iterations;
+  o->photon_paths = c->photons_total;
+  o->pixels = (int64_t)c->W * c->H;
+  o->triangles = c->sc.num_tris;
+  o->bvh_nodes = c->sc.num_nodes;
+  o->photon_table = c->grid.table;
+  o->device_bytes = (double)c->device_bytes;
+  return FR_OK;
+}
+
+void* fr_stream(fr_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+void fr_destroy(fr_ctx* c) { delete c; }
+
+int fr_trace_closest(fr_ctx* c, const float* rays, int32_t n, int32_t* facet, float* tuv) {
+  if (!c || n < 0 || (n && (!rays || !facet || !tuv))) return fail(FR_ERR_INVALID, "fr_trace_closest: bad arguments");
+  if (!n) return FR_OK;
+  float *d_rays = nullptr, *d_tuv = nullptr;
+  int32_t* d_facet = nullptr;
+  FR_CUDA(cudaMalloc(&d_rays, sizeof(float) * 7 * (size_t)n));
+  FR_CUDA(cudaMalloc(&d_tuv, sizeof(float) * 3 * (size_t)n));
+  FR_CUDA(cudaMalloc(&d_facet, sizeof(int32_t) * (size_t)n));
+  cudaMemcpyAsync(d_rays, rays, sizeof(float) * 7 * (size_t)n, cudaMemcpyHostToDevice, c->stream);
+  launch_trace_closest(c->sc, d_rays, n, d_facet, d_tuv, c->err, c->stream);
+  cudaMemcpyAsync(facet, d_facet, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, c->stream);
+  cudaMemcpyAsync(tuv, d_tuv, sizeof(float) * 3 * (size_t)n, cudaMemcpyDeviceToHost, c->stream);
+  const int rc = fr_synchronize(c);
+  cudaFree(d_rays); cudaFree(d_tuv); cudaFree(d_facet);
+  return rc;
+}
+
+int fr_trace_any(fr_ctx* c, const float* rays, int32_t n, int32_t* hit) {
+  if (!c || n < 0 || (n && (!rays || !hit))) return fail(FR_ERR_INVALID, "fr_trace_any: bad arguments");
+  if (!n) return FR_OK;
+  float* d_rays = nullptr;
+  int32_t* d_hit = nullptr;
+  FR_CUDA(cudaMalloc(&d_rays, sizeof(float) * 8 * (size_t)n));
+  FR_CUDA(cudaMalloc(&d_hit, sizeof(int32_t) * (size_t)n));
+  cudaMemcpyAsync(d_rays, rays, sizeof(float) * 8 * (size_t)n, cudaMemcpyHostToDevice, c->stream);
+  launch_trace_any(c->sc, d_rays, n, d_hit, c->err, c->stream);
+  cudaMemcpyAsync(hit, d_hit, sizeof(int32_t) * (size_t)n, cudaMemcpyDeviceToHost, c->stream);
+  const int rc = fr_synchronize(c);
+  cudaFree(d_rays); cudaFree(d_hit);
+  return rc;
+}
+
+int fr_radius_query(fr_ctx* c, const float* hp, int32_t nh, const float* photons_xyz, int32_t np, float cell,
+                    int32_t* counts, uint32_t* pairs, uint32_t pair_capacity, uint32_t* pair_count) {
+  if (!c || nh < 0 || np < 0 || (nh && (!hp || !counts)) || (np && !photons_xyz) || !(cell > 0.0f) ||
+      (pairs && !pair_count))
+    return fail(FR_ERR_INVALID, "fr_radius_query: bad arguments");
+  if (!nh) return FR_OK;
+  // Flat photon list (one photon per "path", stride 1) through the same grid kernels.
+  std::vector<float4> pos(std::max(np, 1)), zero(std::max(np, 1), make_float4(0.f, 0.f, 0.f, 0.f));
+  float lo[3] = {1e30f, 1e30f, 1e30f};
+  for (int i = 0; i < np; ++i) {
+    pos[i] = make_float4(photons_xyz[3 * i], photons_xyz[3 * i + 1], photons_xyz[3 * i + 2], 1.0f);
+    for (int a = 0; a < 3; ++a) lo[a] = std::min(lo[a], photons_xyz[3 * i + a]);
+  }
+  for (int i = 0; i < nh; ++i)
+    for (int a = 0; a < 3; ++a) lo[a] = std::min(lo[a], hp[4 * i + a] - hp[4 * i + 3]);
+  std::vector<uint32_t> ones(std::max(np, 1), 1u);
+  PhotonSlots ph{};
+  PhotonGrid g{};
+  g.table = next_pow2(std::max<uint64_t>((uint64_t)np * 2, 1024));
+  GridInfo gi{};
+  gi.cell = cell;
+  gi.inv_cell = 1.0f / cell;
+  for (int a = 0; a < 3; ++a) gi.origin[a] = lo[a] - cell;
+  ScanTemp st{};
+  const uint32_t words = scan_temp_words(g.table + 1, st);
+  std::vector<void*> tmp;
+  auto dalloc = [&](size_t bytes) {
+    void* p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(bytes, 16)) != cudaSuccess) return (void*)nullptr;
+    tmp.push_back(p);
+    return p;
+  };
+  const size_t npp = (size_t)std::max(np, 1);
+  ph.pos = (float4*)dalloc(npp * 16); ph.flux = (float4*)dalloc(npp * 16); ph.dir = (float4*)dalloc(npp * 16);
+  g.pos = (float4*)dalloc(npp * 16); g.flux = (float4*)dalloc(npp * 16); g.dir = (float4*)dalloc(npp * 16);
+  g.cell_count = (uint32_t*)dalloc(4 * ((size_t)g.table + 1));
+  g.cell_start = (uint32_t*)dalloc(4 * ((size_t)g.table + 1));
+  g.slot_key = (uint32_t*)dalloc(4 * npp);
+  g.slot_rank = (uint32_t*)dalloc(4 * npp);
+  uint32_t* d_ones = (uint32_t*)dalloc(4 * npp);
+  uint32_t* sw = (uint32_t*)dalloc(4 * (size_t)words);
+  GridInfo* d_gi = (GridInfo*)dalloc(sizeof(GridInfo));
+  float4* d_hp = (float4*)dalloc(16 * (size_t)nh);
+  int32_t* d_m = (int32_t*)dalloc(4 * (size_t)nh);
+  uint32_t* d_pairs = pairs ? (uint32_t*)dalloc(8 * std::max<size_t>(pair_capacity, 1)) : nullptr;
+  uint32_t* d_pc = (uint32_t*)dalloc(4);
+  int rc = FR_OK;
+  for (void* p : tmp)
+    if (!p) rc = fail(FR_ERR_OOM, "fr_radius_query: cudaMalloc failed");
+  if (tmp.size() != (size_t)(17 + (pairs ? 1 : 0))) rc = fail(FR_ERR_OOM, "fr_radius_query: cudaMalloc failed");
+  if (!rc) {
+    for (int l = 0; l < st.levels; ++l) {
+      st.level[l] = sw;
+      sw += st.level_n[l] + 1;
+    }
+    cudaStream_t s = c->stream;
+    cudaMemcpyAsync(ph.pos, pos.data(), npp * 16, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(ph.flux, zero.data(), npp * 16, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(ph.dir, zero.data(), npp * 16, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_ones, ones.data(), npp * 4, cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_gi, &gi, sizeof(gi), cudaMemcpyHostToDevice, s);
+    cudaMemcpyAsync(d_hp, hp, 16 * (size_t)nh, cudaMemcpyHostToDevice, s);
+    cudaMemsetAsync(g.cell_count, 0, 4 * ((size_t)g.table + 1), s);
+    cudaMemsetAsync(d_pc, 0, 4, s);
+    launch_photon_count(ph, d_ones, np, 1, g, d_gi, s);
+    launch_scan(g.cell_count, g.cell_start, g.table + 1, st, s);
+    launch_photon_scatter(ph, d_ones, np, 1, g, s);
+    launch_radius_count(d_hp, nh, g, d_gi, d_m, d_pairs, pair_capacity, d_pc, s);
+    cudaMemcpyAsync(counts, d_m, 4 * (size_t)nh, cudaMemcpyDeviceToHost, s);
+    if (pairs) {
+      uint32_t total = 0;
+      cudaMemcpyAsync(&total, d_pc, 4, cudaMemcpyDeviceToHost, s);
+      cudaStreamSynchronize(s);
+      *pair_count = total;
+      const size_t take = std::min<uint32_t>(total, pair_capacity);
+      if (take) cudaMemcpyAsync(pairs, d_pairs, 8 * take, cudaMemcpyDeviceToHost, s);
+    }
+    rc = fr_synchronize(c);
+  }
+  for (void* p : tmp)
+    if (p) cudaFree(p);
+  return rc;
+}
+
+int fr_read_hitpoints(fr_ctx* c, float* pos_type, float* nrm_rough, float* out_mat, float* wgt_facet) {
+  if (!c) return fail(FR_ERR_INVALID, "fr_read_hitpoints: NULL context");
+  const size_t bytes = sizeof(float4) * (size_t)c->W * c->H;
+  if (pos_type) FR_CUDA(cudaMemcpyAsync(pos_type, c->hp.pos, bytes, cudaMemcpyDeviceToHost, c->stream));
+  if (nrm_rough) FR_CUDA(cudaMemcpyAsync(nrm_rough, c->hp.nrm, bytes, cudaMemcpyDeviceToHost, c->stream));
+  if (out_mat) FR_CUDA(cudaMemcpyAsync(out_mat, c->hp.out, bytes, cudaMemcpyDeviceToHost, c->stream));
+  if (wgt_facet) FR_CUDA(cudaMemcpyAsync(wgt_facet, c->hp.wgt, bytes, cudaMemcpyDeviceToHost, c->stream));
+  return fr_synchronize(c);
+}
+
+int fr_read_photon_slots(fr_ctx* c, float* pos, float* flux, float* dir, uint32_t* counts) {
+  if (!c) return fail(FR_ERR_INVALID, "fr_read_photon_slots: NULL context");
+  const size_t bytes = sizeof(float4) * (size_t)c->P * kPhotonSlots;
+  if (pos) FR_CUDA(cudaMemcpyAsync(pos, c->ph.pos, bytes, cudaMemcpyDeviceToHost, c->stream));
+  if (flux) FR_CUDA(cudaMemcpyAsync(flux, c->ph.flux, bytes, cudaMemcpyDeviceToHost, c->stream));
+  if (dir) FR_CUDA(cudaMemcpyAsync(dir, c->ph.dir, bytes, cudaMemcpyDeviceToHost, c->stream));
+  if (counts) FR_CUDA(cudaMemcpyAsync(counts, c->counts, 4 * (size_t)c->P, cudaMemcpyDeviceToHost, c->stream));
+  return fr_synchronize(c);
+}
+
+int fr_read_gather(fr_ctx* c, int32_t* m, float* phi4) {
+  if (!c) return fail(FR_ERR_INVALID, "fr_read_gather: NULL context");
+  const size_t n = (size_t)c->W * c->H;
+  if (m) FR_CUDA(cudaMemcpyAsync(m, c->dbg_m, 4 * n, cudaMemcpyDeviceToHost, c->stream));
+  if (phi4) FR_CUDA(cudaMemcpyAsync(phi4, c->dbg_phi, 16 * n, cudaMemcpyDeviceToHost, c->stream));
+  return fr_synchronize(c);
+}
+
+int fr_read_state(fr_ctx* c, double* tau, int32_t* n, float* r, int32_t* g) {
+  if (!c) return fail(FR_ERR_INVALID, "fr_read_state: NULL context");
+  const size_t np = (size_t)c->W * c->H;
+  if (tau) FR_CUDA(cudaMemcpyAsync(tau, c->st.tau, 24 * np, cudaMemcpyDeviceToHost, c->stream));
+  if (n) FR_CUDA(cudaMemcpyAsync(n, c->st.n, 4 * np, cudaMemcpyDeviceToHost, c->stream));
+  if (r) FR_CUDA(cudaMemcpyAsync(r, c->st.r, 4 * np, cudaMemcpyDeviceToHost, c->stream));
+  if (g) FR_CUDA(cudaMemcpyAsync(g, c->st.g, 4 * np, cudaMemcpyDeviceToHost, c->stream));
+  return fr_synchronize(c);
+}
+
+}  // extern "C"

@@ -1,0 +1,94 @@
+// Launch interface between the host library and the kernels (fr_kernels.cu).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+#include "fr_layout.h"
+
+namespace fr {
+
+// Hitpoint records of one iteration, one per pixel (SoA of float4):
+//   pos   xyz position,          w type (int bits: kHitNone/kHitHit/kHitOnlyDirect)
+//   nrm   xyz geometry normal,   w roughness
+//   out   xyz outgoing dir,      w material id (int bits)
+//   wgt   xyz pixel weight,      w facet id (int bits)
+struct HitpointBuf {
+  float4* pos;
+  float4* nrm;
+  float4* out;
+  float4* wgt;
+};
+
+// Photon slots: kPhotonSlots per path, persistent across iterations as the
+// reference's photon deques are (SPPM.cpp:753).
+//   pos  xyz position, w ray index of refraction
+//   flux xyz flux,     w pdf
+//   dir  xyz incoming direction, w 1 valid / 0 invalid
+struct PhotonSlots {
+  float4* pos;
+  float4* flux;
+  float4* dir;
+};
+
+// Photons sorted by cell of the hashed grid; dir.w holds the source slot id.
+struct PhotonGrid {
+  float4* pos;
+  float4* flux;
+  float4* dir;
+  uint32_t* cell_count;  // [table]  photons per bucket
+  uint32_t* cell_start;  // [table + 1] exclusive prefix of cell_count
+  uint32_t* slot_key;    // [paths * kPhotonSlots]  bucket of each valid slot
+  uint32_t* slot_rank;   // [paths * kPhotonSlots]  rank within its bucket
+  uint32_t table;        // bucket count, power of two
+};
+
+// Per-pixel progressive state (SharedHitPoint, SPPM.h:112-126): tau in FP64.
+struct PixelState {
+  double* tau;    // [3 * pixels]
+  int32_t* n;     // NumPhoton (int, truncating update, SPPM.cpp:447)
+  float* r;       // Radius
+  int32_t* g;     // NumGather
+};
+
+// Scratch shared by the kernels of one iteration.
+struct GridInfo {
+  float cell;        // cell edge for this iteration
+  float inv_cell;
+  float origin[3];
+  float r_sum;       // sum of radii of this iteration's hitpoints
+  uint32_t r_count;  // number of this iteration's hitpoints
+  uint32_t pad;
+};
+
+struct ScanTemp {
+  uint32_t* level[4];     // block sums per level
+  uint32_t level_n[4];
+  int levels;
+};
+
+void upload_byte_lut(cudaStream_t s);
+
+void launch_eye_pass(const SceneGPU& sc, const CameraGPU& cam, const IterParams& it, const float* rr_eye,
+                     HitpointBuf hp, PixelState st, GridInfo* gi, int* err, cudaStream_t s);
+void launch_photon_pass(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, uint32_t* counts, int* err,
+                        cudaStream_t s);
+void launch_grid_setup(GridInfo* gi, const SceneGPU& sc, float cell_scale, float r0, cudaStream_t s);
+// stride: slots per path (kPhotonSlots for the render loop, 1 for a flat photon list).
+void launch_photon_count(PhotonSlots ph, const uint32_t* counts, int paths, int stride, PhotonGrid g,
+                         const GridInfo* gi, cudaStream_t s);
+void launch_scan(uint32_t* data_in, uint32_t* data_out, uint32_t n, ScanTemp& tmp, cudaStream_t s);
+void launch_photon_scatter(PhotonSlots ph, const uint32_t* counts, int paths, int stride, PhotonGrid g,
+                           cudaStream_t s);
+// Words of block-sum scratch launch_scan needs for n elements; fills the level sizes of t.
+uint32_t scan_temp_words(uint32_t n, ScanTemp& t);
+void launch_gather_update(const SceneGPU& sc, const IterParams& it, HitpointBuf hp, PhotonGrid g, const GridInfo* gi,
+                          PixelState st, int32_t* dbg_m, float4* dbg_phi, cudaStream_t s);
+void launch_resolve(PixelState st, int pixels, double photons_total, double iterations, float4* out, cudaStream_t s);
+
+// Parity entry points.
+void launch_trace_closest(const SceneGPU& sc, const float* rays, int n, int32_t* facet, float* tuv, int* err,
+                          cudaStream_t s);
+void launch_trace_any(const SceneGPU& sc, const float* rays, int n, int32_t* hit, int* err, cudaStream_t s);
+void launch_radius_count(const float4* hp_pos_r, int nh, PhotonGrid g, const GridInfo* gi, int32_t* m,
+                         uint32_t* pairs, uint32_t pair_cap, uint32_t* pair_count, cudaStream_t s);
+
+}  // namespace fr

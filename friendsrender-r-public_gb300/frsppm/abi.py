@@ -1,0 +1,257 @@
+"""ctypes binding of the C-ABI in include/friendsrender.h (libfrsppm.so).
+
+``Renderer`` wraps one fr_ctx.  Loading fails loudly when the library is
+missing: there is no fallback implementation.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import build as _build
+
+FR_OK = 0
+
+_f3 = C.c_float * 3
+
+
+class MaterialDesc(C.Structure):
+    _fields_ = [('type', C.c_int32), ('sppm_surface', C.c_int32), ('opaque', C.c_int32),
+                ('tex_albedo', C.c_int32), ('tex_roughness', C.c_int32), ('tex_bump', C.c_int32),
+                ('albedo', _f3), ('emission', _f3), ('index', C.c_float), ('roughness', C.c_float),
+                ('extinction', C.c_float), ('reflectance', C.c_float)]
+
+
+class TextureDesc(C.Structure):
+    _fields_ = [('width', C.c_int32), ('height', C.c_int32), ('texels', C.c_void_p)]
+
+
+class SceneDesc(C.Structure):
+    _fields_ = [('num_facets', C.c_int32), ('positions', C.c_void_p), ('normals', C.c_void_p),
+                ('uvs', C.c_void_p), ('material_ids', C.c_void_p), ('num_materials', C.c_int32),
+                ('materials', C.POINTER(MaterialDesc)), ('num_textures', C.c_int32),
+                ('textures', C.POINTER(TextureDesc))]
+
+
+class CameraDesc(C.Structure):
+    _fields_ = [('type', C.c_int32), ('width', C.c_int32), ('height', C.c_int32), ('position', _f3),
+                ('target', _f3), ('fov_degrees', C.c_float), ('focal_length', C.c_float),
+                ('distance_to_lens', C.c_float), ('aspect', C.c_float), ('lens_width', C.c_float),
+                ('lens_height', C.c_float)]
+
+
+class SPPMParams(C.Structure):
+    _fields_ = [('photons_per_iteration', C.c_int32), ('alpha', C.c_float), ('initial_radius', C.c_float),
+                ('flags', C.c_uint32), ('grid_cell_scale', C.c_float)]
+
+
+class Stats(C.Structure):
+    _fields_ = [('iterations', C.c_int64), ('photon_paths', C.c_int64), ('pixels', C.c_int64),
+                ('triangles', C.c_int64), ('bvh_nodes', C.c_int64), ('photon_table', C.c_int64),
+                ('device_bytes', C.c_double)]
+
+
+# Every symbol include/friendsrender.h declares.
+EXPORTS = ['fr_last_error', 'fr_create', 'fr_iterate', 'fr_synchronize', 'fr_resolve', 'fr_resolve_dev',
+           'fr_get_stats', 'fr_stream', 'fr_destroy', 'fr_trace_closest', 'fr_trace_any', 'fr_radius_query',
+           'fr_read_hitpoints', 'fr_read_photon_slots', 'fr_read_gather', 'fr_read_state']
+
+_lib = None
+
+
+def load(path=None):
+    """Load libfrsppm.so (built in-tree by frsppm.build)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    path = path or _build.LIB
+    if not os.path.exists(path):
+        raise RuntimeError('libfrsppm.so not built (%s); run __graft_entry__.build()' % path)
+    lib = C.CDLL(path)
+    vp, i32, f32 = C.c_void_p, C.c_int32, C.c_float
+    lib.fr_last_error.restype = C.c_char_p
+    lib.fr_create.argtypes = [C.POINTER(SceneDesc), C.POINTER(CameraDesc), C.POINTER(SPPMParams), C.POINTER(vp)]
+    lib.fr_iterate.argtypes = [vp, C.c_int]
+    lib.fr_synchronize.argtypes = [vp]
+    lib.fr_resolve.argtypes = [vp, vp]
+    lib.fr_resolve_dev.argtypes = [vp, vp]
+    lib.fr_get_stats.argtypes = [vp, C.POINTER(Stats)]
+    lib.fr_stream.argtypes = [vp]
+    lib.fr_stream.restype = vp
+    lib.fr_destroy.argtypes = [vp]
+    lib.fr_destroy.restype = None
+    lib.fr_trace_closest.argtypes = [vp, vp, i32, vp, vp]
+    lib.fr_trace_any.argtypes = [vp, vp, i32, vp]
+    lib.fr_radius_query.argtypes = [vp, vp, i32, vp, i32, f32, vp, vp, C.c_uint32, vp]
+    lib.fr_read_hitpoints.argtypes = [vp, vp, vp, vp, vp]
+    lib.fr_read_photon_slots.argtypes = [vp, vp, vp, vp, vp]
+    lib.fr_read_gather.argtypes = [vp, vp, vp]
+    lib.fr_read_state.argtypes = [vp, vp, vp, vp, vp]
+    _lib = lib
+    return lib
+
+
+def _ptr(a):
+    return a.ctypes.data_as(C.c_void_p) if a is not None else None
+
+
+def _check(rc, what):
+    if rc != FR_OK:
+        msg = _lib.fr_last_error().decode() if _lib else ''
+        raise RuntimeError('%s failed (%d): %s' % (what, rc, msg))
+
+
+class Renderer:
+    """One fr_ctx: a scene (frsppm.scenes dict), camera and SPPM parameters."""
+
+    def __init__(self, scene, photons, alpha=0.9, radius=0.015, flags=0, cell_scale=0.0, camera=None):
+        lib = load()
+        self.scene = scene
+        cam = camera or scene['camera']
+        self._keep = []
+        pos = np.ascontiguousarray(scene['pos'], np.float32)
+        nrm = np.ascontiguousarray(scene['nrm'], np.float32)
+        uv = np.ascontiguousarray(scene['uv'], np.float32)
+        mat = np.ascontiguousarray(scene['mat'], np.int32)
+        texs = [np.ascontiguousarray(t, np.uint8) for t in scene['textures']]
+        self._keep += [pos, nrm, uv, mat] + texs
+        mats = (MaterialDesc * len(scene['materials']))()
+        for k, m in enumerate(scene['materials']):
+            d = mats[k]
+            d.type, d.sppm_surface, d.opaque = m['type'], int(m['sppm']), int(m['opaque'])
+            d.tex_albedo, d.tex_roughness, d.tex_bump = m['tex_albedo'], m['tex_roughness'], m['tex_bump']
+            d.albedo = _f3(*m['albedo'])
+            d.emission = _f3(*m['emission'])
+            d.index, d.roughness, d.extinction, d.reflectance = m['index'], m['roughness'], m['extinction'], m['reflectance']
+        tds = (TextureDesc * max(1, len(texs)))()
+        for k, t in enumerate(texs):
+            tds[k].width, tds[k].height = t.shape[1], t.shape[0]
+            tds[k].texels = t.ctypes.data
+        self._keep += [mats, tds]
+        sd = SceneDesc(len(pos), pos.ctypes.data, nrm.ctypes.data, uv.ctypes.data, mat.ctypes.data,
+                       len(scene['materials']), mats, len(texs), tds)
+        cd = CameraDesc()
+        cd.type, cd.width, cd.height = cam['type'], cam['width'], cam['height']
+        cd.position = _f3(*cam['pos'])
+        cd.target = _f3(*cam['target'])
+        cd.fov_degrees, cd.focal_length, cd.distance_to_lens = cam['fov'], cam['focal'], cam['dist']
+        cd.aspect = cam['aspect']
+        cd.lens_width = cd.lens_height = cam['lens']
+        pp = SPPMParams(int(photons), float(alpha), float(radius), int(flags), float(cell_scale))
+        self.width, self.height, self.photons = cam['width'], cam['height'], int(photons)
+        h = C.c_void_p()
+        _check(lib.fr_create(C.byref(sd), C.byref(cd), C.byref(pp), C.byref(h)), 'fr_create')
+        self.h = h
+
+    def close(self):
+        if getattr(self, 'h', None):
+            _lib.fr_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def iterate(self, n=1, sync=True):
+        _check(_lib.fr_iterate(self.h, int(n)), 'fr_iterate')
+        if sync:
+            self.synchronize()
+
+    def synchronize(self):
+        _check(_lib.fr_synchronize(self.h), 'fr_synchronize')
+
+    def stream(self):
+        return _lib.fr_stream(self.h)
+
+    def resolve(self):
+        out = np.empty((self.width * self.height, 4), np.float32)
+        _check(_lib.fr_resolve(self.h, _ptr(out)), 'fr_resolve')
+        return out
+
+    def resolve_dev(self, dev_ptr):
+        _check(_lib.fr_resolve_dev(self.h, C.c_void_p(dev_ptr)), 'fr_resolve_dev')
+
+    def stats(self):
+        s = Stats()
+        _check(_lib.fr_get_stats(self.h, C.byref(s)), 'fr_get_stats')
+        return {k: getattr(s, k) for k, _ in Stats._fields_}
+
+    def trace_closest(self, rays):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 7)
+        n = len(rays)
+        facet = np.empty(n, np.int32)
+        tuv = np.empty((n, 3), np.float32)
+        _check(_lib.fr_trace_closest(self.h, _ptr(rays), n, _ptr(facet), _ptr(tuv)), 'fr_trace_closest')
+        return facet, tuv
+
+    def trace_any(self, rays):
+        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        hit = np.empty(len(rays), np.int32)
+        _check(_lib.fr_trace_any(self.h, _ptr(rays), len(rays), _ptr(hit)), 'fr_trace_any')
+        return hit
+
+    def radius_query(self, hp_pos, hp_r, photons, cell, pairs_capacity=0):
+        hp = np.ascontiguousarray(np.concatenate([np.asarray(hp_pos, np.float32).reshape(-1, 3),
+                                                  np.asarray(hp_r, np.float32).reshape(-1, 1)], 1))
+        ph = np.ascontiguousarray(photons, np.float32).reshape(-1, 3)
+        counts = np.empty(len(hp), np.int32)
+        pairs = np.empty((max(pairs_capacity, 1), 2), np.uint32) if pairs_capacity else None
+        pc = np.zeros(1, np.uint32)
+        _check(_lib.fr_radius_query(self.h, _ptr(hp), len(hp), _ptr(ph), len(ph), float(cell), _ptr(counts),
+                                    _ptr(pairs), int(pairs_capacity), _ptr(pc) if pairs is not None else None),
+               'fr_radius_query')
+        if pairs is None:
+            return counts, None
+        return counts, pairs[:min(int(pc[0]), pairs_capacity)]
+
+    def read_hitpoints(self):
+        n = self.width * self.height
+        a = [np.empty((n, 4), np.float32) for _ in range(4)]
+        _check(_lib.fr_read_hitpoints(self.h, *[_ptr(x) for x in a]), 'fr_read_hitpoints')
+        pos, nrm, out, wgt = a
+        return dict(type=pos[:, 3].view(np.int32).copy(), pos=pos[:, :3].copy(), nrm=nrm[:, :3].copy(),
+                    rough=nrm[:, 3].copy(), out=out[:, :3].copy(), mat=out[:, 3].view(np.int32).copy(),
+                    w=wgt[:, :3].copy(), facet=wgt[:, 3].view(np.int32).copy())
+
+    def read_photon_slots(self):
+        n = self.photons * 32
+        a = [np.empty((n, 4), np.float32) for _ in range(3)]
+        counts = np.empty(self.photons, np.uint32)
+        _check(_lib.fr_read_photon_slots(self.h, *[_ptr(x) for x in a], _ptr(counts)), 'fr_read_photon_slots')
+        return a[0], a[1], a[2], counts
+
+    def compacted_photons(self):
+        """Photons of the last iteration in the compactor's order (path, slot):
+        (N, 11) {pos, flux, indir, index, pdf}, path ids and slot ids."""
+        pos, flux, d, counts = self.read_photon_slots()
+        paths = np.repeat(np.arange(self.photons), counts.astype(np.int64))
+        slots = np.concatenate([np.arange(c) for c in counts]) if len(counts) else np.zeros(0, int)
+        idx = paths * 32 + slots
+        ph = np.concatenate([pos[idx, :3], flux[idx, :3], d[idx, :3], pos[idx, 3:4], flux[idx, 3:4]], 1)
+        return ph, paths.astype(np.int32), slots.astype(np.int32)
+
+    def read_gather(self):
+        n = self.width * self.height
+        m = np.empty(n, np.int32)
+        phi = np.empty((n, 4), np.float32)
+        _check(_lib.fr_read_gather(self.h, _ptr(m), _ptr(phi)), 'fr_read_gather')
+        return m, phi[:, :3].copy()
+
+    def read_state(self):
+        n = self.width * self.height
+        tau = np.empty((n, 3), np.float64)
+        N = np.empty(n, np.int32)
+        r = np.empty(n, np.float32)
+        g = np.empty(n, np.int32)
+        _check(_lib.fr_read_state(self.h, _ptr(tau), _ptr(N), _ptr(r), _ptr(g)), 'fr_read_state')
+        return dict(tau=tau, n=N, r=r, g=g)

@@ -228,7 +228,7 @@ def height_field(b, rng, n, x0, x1, z0, z1, amp, mat_id, uv_scale=4.0):
 
 def mixed_materials(seed=CONFIG_SEED_BASE + 1, width=1280, height=720, n_spheres=200,
                     field_n=512, tex_size=1024, light_tex=512, n_lat=34, n_lon=36,
-                    aperture=0.02):
+                    aperture=0.02, extent=4.0):
     """Mixed-materials scene: ``n_spheres`` UV spheres (radius U(0.05,0.3)) over a
     ``field_n``^2 height field of seeded value noise.  Materials split equally
     across diffuse, specular, GGX conductor and GGX dielectric (IOR 1.5),
@@ -242,8 +242,9 @@ def mixed_materials(seed=CONFIG_SEED_BASE + 1, width=1280, height=720, n_spheres
     mats = [material('field', DIFFUSE, (0.7, 0.7, 0.7), tex_albedo=0, tex_roughness=1, tex_bump=2),
             material('light', DIFFUSE, (1, 1, 1), emission=(10.0, 9.0, 8.0), tex_albedo=3)]
     b = _Builder()
-    ext = 4.0
-    height_field(b, rng, field_n, -ext, ext, -ext, ext, 0.25, 0)
+    ext = float(extent)
+    k_s = ext / 4.0  # lengths below are for the 8x8 field and scale with it
+    height_field(b, rng, field_n, -ext, ext, -ext, ext, 0.25 * k_s, 0)
     for k in range(n_spheres):
         mtype = k % 4
         rough = float(rng.uniform(0.05, 0.5))
@@ -259,15 +260,15 @@ def mixed_materials(seed=CONFIG_SEED_BASE + 1, width=1280, height=720, n_spheres
             m = material(name, GGX_DIELECTRIC, (0.98, 0.98, 0.98), roughness=rough, index=1.5,
                          opaque=False, sppm=False)
         mats.append(m)
-        r = float(rng.uniform(0.05, 0.3))
+        r = float(rng.uniform(0.05, 0.3)) * k_s
         cx, cz = rng.uniform(-ext * 0.85, ext * 0.85, 2)
-        uv_sphere(b, (cx, 0.25 + r, cz), r, len(mats) - 1, n_lat, n_lon)
-    ly = 3.0
-    b.quad((-1, ly, -1), (1, ly, -1), (1, ly, 1), (-1, ly, 1), (0, -1, 0), 1)
+        uv_sphere(b, (cx, 0.25 * k_s + r, cz), r, len(mats) - 1, n_lat, n_lon)
+    ly, lh = 3.0 * k_s, 1.0 * k_s
+    b.quad((-lh, ly, -lh), (lh, ly, -lh), (lh, ly, lh), (-lh, ly, lh), (0, -1, 0), 1)
     scene = b.build()
     scene.update(materials=mats, textures=textures,
-                 camera=_camera(THINLENS, width, height, (0.0, 2.6, -7.5), (0.0, 0.2, 0.0), 30.0,
-                                focal=0.9, dist=1.0, lens=aperture))
+                 camera=_camera(THINLENS, width, height, (0.0, 2.6 * k_s, -7.5 * k_s), (0.0, 0.2 * k_s, 0.0),
+                                30.0, focal=0.9, dist=1.0, lens=aperture))
     return scene
 
 
@@ -276,7 +277,8 @@ def small_mixed(seed=CONFIG_SEED_BASE + 101, width=48, height=32, tex_size=64):
     material types, albedo/roughness/normal textures, textured light, thin
     lens) at a size the reference and the oracle finish in seconds."""
     return mixed_materials(seed=seed, width=width, height=height, n_spheres=12, field_n=24,
-                           tex_size=tex_size, light_tex=32, n_lat=10, n_lon=12, aperture=0.05)
+                           tex_size=tex_size, light_tex=32, n_lat=10, n_lon=12, aperture=0.05,
+                           extent=0.6)
 
 
 def scene_stats(scene):

@@ -1,0 +1,199 @@
+/*
+ * FriendsRender GB300 — C-ABI of the GPU SPPM render loop.
+ *
+ * Drop-in replacement for the per-iteration render loop of the reference's
+ * Render::StochasticProgressivePhotonMapping (SPPM/SPPM/SPPM.h:15-189):
+ * eye pass, photon pass, photon radius query and the N/tau/R update, run on
+ * one GPU.  Plain C types only; every buffer argument is a host pointer
+ * unless its name ends in _dev.  All calls return FR_OK (0) or an FR_ERR_*
+ * code and set a thread-local message readable with fr_last_error().
+ *
+ * Threading: a context is used by one thread at a time; it owns one CUDA
+ * stream.  Several contexts may coexist.
+ */
+#ifndef FRIENDSRENDER_H
+#define FRIENDSRENDER_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum {
+  FR_OK = 0,
+  FR_ERR_INVALID = 1,   /* bad argument or descriptor */
+  FR_ERR_CUDA = 2,      /* CUDA runtime error */
+  FR_ERR_OOM = 3,       /* device allocation failed */
+  FR_ERR_DEVICE = 4     /* a kernel reported an error (traversal stack) */
+};
+
+/* Surface types: the reference's Surface subclasses (SPPM/SPPM/material.h). */
+enum {
+  FR_MAT_DIFFUSE = 0,          /* DiffuseSurface  (material.h:163-177) */
+  FR_MAT_METAL = 1,            /* MetalSurface    (material.h:396-425) */
+  FR_MAT_GGX_CONDUCTOR = 2,    /* Roughconductor  (material.h:222-278) */
+  FR_MAT_GGX_DIELECTRIC = 3    /* GGXGlass        (material.h:280-394) */
+};
+
+enum { FR_CAMERA_PINHOLE = 0, FR_CAMERA_THINLENS = 1 };
+
+/* Replaces the reference's SceneMaterialManager plug-in result
+ * (SceneMaterial.h:13-16): an Attribute's Surface and SURFACE_PARAM
+ * (material.h:35-90) plus its map_Kd / map_d / map_bump textures
+ * (Scene.cpp:60-77).  Texture fields are indices into fr_scene_desc.textures
+ * or -1. */
+typedef struct fr_material_desc {
+  int32_t type;            /* FR_MAT_* */
+  int32_t sppm_surface;    /* SURFACE_PARAM::isSPPMSurface */
+  int32_t opaque;          /* SURFACE_PARAM::IfOpeque */
+  int32_t tex_albedo;      /* map_Kd: albedo, and emission of an emissive material */
+  int32_t tex_roughness;   /* map_d: roughness = clamp(0.5*r, 0.05, 0.8) */
+  int32_t tex_bump;        /* map_bump: normal map */
+  float albedo[3];         /* Kd */
+  float emission[3];       /* Ke; a material with Ke summing above 1e-5 makes its facets area lights */
+  float index;             /* SURFACE_PARAM::Index */
+  float roughness;         /* SURFACE_PARAM::Roughness */
+  float extinction;        /* SURFACE_PARAM::Extinction */
+  float reflectance;       /* SURFACE_PARAM::Reflectance */
+} fr_material_desc;
+
+/* RGBA8 texture, row j at texels + 4*width*j (stbi_load layout,
+ * TextureUtility.cpp:12-35). */
+typedef struct fr_texture_desc {
+  int32_t width, height;
+  const uint8_t* texels;
+} fr_texture_desc;
+
+/* Replaces Scene (Scene.h:55-93) as built by Scene::CreateScene
+ * (Scene.cpp:13-218): per facet three corner positions, normals and UVs and
+ * an attribute (material) index, in OBJ face order. */
+typedef struct fr_scene_desc {
+  int32_t num_facets;
+  const float* positions;       /* num_facets * 9 */
+  const float* normals;         /* num_facets * 9 */
+  const float* uvs;             /* num_facets * 6 */
+  const int32_t* material_ids;  /* num_facets */
+  int32_t num_materials;
+  const fr_material_desc* materials;
+  int32_t num_textures;
+  const fr_texture_desc* textures;
+} fr_scene_desc;
+
+/* Replaces iCamera (Camera.h:11-54) with PinholeCamera / ThinLensCamera.
+ * fov_degrees, focal_length and distance_to_lens are the constructor's Fov,
+ * F and DistanceToLens; lens_width/height <= 0 keep the reference default
+ * (the image-plane size, Camera.h:42-43). */
+typedef struct fr_camera_desc {
+  int32_t type;                 /* FR_CAMERA_* */
+  int32_t width, height;        /* render target size */
+  float position[3];
+  float target[3];
+  float fov_degrees;
+  float focal_length;
+  float distance_to_lens;
+  float aspect;
+  float lens_width, lens_height;
+} fr_camera_desc;
+
+enum {
+  /* Drop the reference's stale photon slot (SPPM.cpp:672): off by default, so
+   * the photon set of every iteration is the reference's. */
+  FR_FLAG_FIX_STALE_PHOTON_SLOT = 1u
+};
+
+typedef struct fr_sppm_params {
+  int32_t photons_per_iteration;  /* the reference's NumPhotonsPerStep */
+  float alpha;                    /* ppm_Alpha (SPPM.cpp:20), reference 0.9 */
+  float initial_radius;           /* FirstRadius (SPPM.cpp:21), reference 0.015 */
+  uint32_t flags;                 /* FR_FLAG_* */
+  float grid_cell_scale;          /* photon grid cell = scale * mean hitpoint radius; <= 0 selects 2 */
+} fr_sppm_params;
+
+typedef struct fr_stats {
+  int64_t iterations;         /* iterations run so far */
+  int64_t photon_paths;       /* photon paths emitted so far (TotalPhoton) */
+  int64_t pixels;
+  int64_t triangles;
+  int64_t bvh_nodes;
+  int64_t photon_table;       /* photon grid buckets */
+  double device_bytes;        /* device memory held by the context */
+} fr_stats;
+
+typedef struct fr_ctx fr_ctx;
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* fr_last_error(void);
+
+/* Uploads the scene (building its BVH and light tables on the host), sets up
+ * the camera and allocates all per-iteration buffers; nothing is allocated
+ * later.  Replaces the set-up part of RenderImage_FixStep /
+ * RenderImage_FixRenderTime (SPPM.cpp:682-766). */
+int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr_sppm_params* params,
+              fr_ctx** out);
+
+/* Enqueues n SPPM iterations on the context's stream (the loop body of
+ * RenderImage_FixRenderTime, SPPM.cpp:768-848, with a fixed photon count).
+ * Iteration k (counted from 1 over the context's life) uses the reference's
+ * seeds for step k.  Asynchronous; see fr_synchronize. */
+int fr_iterate(fr_ctx* ctx, int n);
+
+/* Waits for the context's stream and reports kernel errors. */
+int fr_synchronize(fr_ctx* ctx);
+
+/* Writes the image (reconstructImageFromSharedPoints, SPPM.cpp:473-493):
+ * width*height RGBA floats, pixel x + y*width.  rgba is a host pointer;
+ * fr_resolve_dev takes a device pointer and does not synchronize. */
+int fr_resolve(fr_ctx* ctx, float* rgba);
+int fr_resolve_dev(fr_ctx* ctx, float* rgba_dev);
+
+int fr_get_stats(fr_ctx* ctx, fr_stats* out);
+
+/* The context's cudaStream_t (as void*), for callers that record events on it. */
+void* fr_stream(fr_ctx* ctx);
+
+void fr_destroy(fr_ctx* ctx);
+
+/* ---------------------------------------------------------------- parity
+ * Entry points the parity tests drive; each synchronizes before returning. */
+
+/* Closest hit (Scene::GetOneFacetFromRay, Scene.cpp:224-237): rays are n x 7
+ * floats {origin, direction, index}; MinT = 1e-4, MaxT = FLT_MAX.
+ * facet[i] = -1 on a miss; tuv[i] = {t, u, v}. */
+int fr_trace_closest(fr_ctx* ctx, const float* rays, int32_t n, int32_t* facet, float* tuv);
+
+/* Any hit (findAnyElement, bvh8.h:643-707): rays are n x 8 floats
+ * {origin, direction, min_t, max_t}; hit[i] = 1 if a triangle is met with
+ * min_t < t <= max_t. */
+int fr_trace_any(fr_ctx* ctx, const float* rays, int32_t n, int32_t* hit);
+
+/* Radius query with the renderer's photon grid: for hitpoint h (position
+ * hp[4h..4h+2], radius hp[4h+3]) counts photons p with
+ * isIncludePoint(p, x - R, x + R) && |p - x|^2 < R^2 (kdtree.h:78-88,
+ * SPPM.cpp:424-432).  If pairs is not NULL it receives up to pair_capacity
+ * (hitpoint, photon) index pairs in any order and *pair_count the total. */
+int fr_radius_query(fr_ctx* ctx, const float* hp, int32_t num_hitpoints, const float* photons_xyz,
+                    int32_t num_photons, float cell, int32_t* counts, uint32_t* pairs, uint32_t pair_capacity,
+                    uint32_t* pair_count);
+
+/* Hitpoints of the last iteration (SoA, see HitpointBuf in the kernels):
+ * each array width*height*4 floats; any pointer may be NULL. */
+int fr_read_hitpoints(fr_ctx* ctx, float* pos_type, float* nrm_rough, float* out_mat, float* wgt_facet);
+
+/* Photon slots after the last iteration: paths * 32 entries of 4 floats each
+ * (pos+index, flux+pdf, dir+valid) and the per-path count of photons the
+ * compactor takes (SPPM.cpp:812-822). */
+int fr_read_photon_slots(fr_ctx* ctx, float* pos, float* flux, float* dir, uint32_t* counts);
+
+/* Per-pixel photon count M and flux sum of the last iteration's gather. */
+int fr_read_gather(fr_ctx* ctx, int32_t* m, float* phi4);
+
+/* Per-pixel progressive state: tau (3 doubles), N, R, NumGather. */
+int fr_read_state(fr_ctx* ctx, double* tau, int32_t* n, float* r, int32_t* g);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* FRIENDSRENDER_H */

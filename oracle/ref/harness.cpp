@@ -5,6 +5,7 @@
 //
 //   frref <scene_dir> facets <out_dir>
 //   frref <scene_dir> trace  <rays.bin> <out_dir>
+//   frref <scene_dir> any    <rays.bin> <out_dir>
 //   frref <scene_dir> render <photons_per_iter> <iterations> <out_dir>
 //
 // <scene_dir> holds meshData/scene.obj (+ .mtl, textures), materials.txt and
@@ -291,6 +292,28 @@ int main(int argc, char** argv) {
     }
     npy_i32(out_dir + "/hit_facet.npy", facet, {N});
     npy_f32(out_dir + "/hit_tuv.npy", tuv, {N, 3});
+    return 0;
+  }
+
+  if (mode == "any") {
+    // rays.bin: N x 8 float32 {org xyz, dir xyz, min_t, max_t} -> findAnyElement
+    // from the root (bvh8.h:643-707, AnyHit bvh8.h:767-769).
+    const std::string rays_path = argv[3];
+    out_dir = argv[4];
+    std::ifstream f(rays_path, std::ios::binary | std::ios::ate);
+    const size_t bytes = (size_t)f.tellg();
+    f.seekg(0);
+    std::vector<float> rays(bytes / 4);
+    f.read(reinterpret_cast<char*>(rays.data()), bytes);
+    const size_t N = rays.size() / 8;
+    std::vector<int32_t> hit(N);
+#pragma omp parallel for schedule(dynamic, 64)
+    for (long i = 0; i < (long)N; ++i) {
+      const float* r = &rays[i * 8];
+      Primitive::Ray ray(Vec3(r[0], r[1], r[2]), Vec3(r[3], r[4], r[5]), 1.0f, r[6], r[7]);
+      hit[i] = scene.m_Aobject->AnyHit(ray) ? 1 : 0;
+    }
+    npy_i32(out_dir + "/any_hit.npy", hit, {N});
     return 0;
   }
 

@@ -1,0 +1,124 @@
+"""Make the golden fixtures under tests/golden/ by running the reference's own
+SPPM code (oracle/_ref/frref, built by oracle/ref/Makefile from the reference
+sources) on small seeded scenes.
+
+    python tests/golden/make_golden.py
+
+Each fixture <name>.npz holds, for a scene from frsppm.scenes:
+  scene_sha                 digest of the scene arrays the fixture was made from
+  rays, hit_facet, hit_tuv  closest-hit queries (Scene::GetOneFacetFromRay)
+  any_rays, any_hit         any-hit queries (N_BVH8::AnyHit)
+  it{s}_*                   per iteration s = 1..iters: hitpoints, compacted
+                            photons (with path and slot), gather M and flux,
+                            per-pixel state after the update
+  image, meta               reconstructImageFromSharedPoints output and
+                            [total photons, iterations, threads]
+with the reference's ppm_Alpha = 0.9 and FirstRadius = 0.015 (SPPM.cpp:20-21).
+"""
+from __future__ import annotations
+
+import hashlib
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(REPO, 'friendsrender-r-public_gb300'))
+from frsppm import objio, scenes  # noqa: E402
+
+FRREF = os.path.join(REPO, 'oracle', '_ref', 'frref')
+
+FIXTURES = {
+    # name: (scene factory, photons per iteration, iterations)
+    'cornell32': (lambda: scenes.cornell_box(width=32, height=32), 2000, 3),
+    'mixed48x32': (lambda: scenes.small_mixed(), 2000, 3),
+}
+
+
+def scene_sha(scene):
+    h = hashlib.sha256()
+    for k in ('pos', 'nrm', 'uv', 'mat'):
+        h.update(np.ascontiguousarray(scene[k]).tobytes())
+    for t in scene['textures']:
+        h.update(np.ascontiguousarray(t).tobytes())
+    h.update(repr([sorted(m.items()) for m in scene['materials']]).encode())
+    h.update(repr(sorted(scene['camera'].items())).encode())
+    return h.hexdigest()
+
+
+def query_rays(scene, n, seed):
+    """Closest-hit rays: origins inside the scene bounds, uniform directions,
+    plus the camera position toward random scene points."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    lo, hi = scene['pos'].reshape(-1, 3).min(0), scene['pos'].reshape(-1, 3).max(0)
+    o = rng.uniform(lo, hi, (n, 3))
+    d = rng.normal(size=(n, 3))
+    cam = np.asarray(scene['camera']['pos'])
+    k = n // 4
+    o[:k] = cam
+    d[:k] = rng.uniform(lo, hi, (k, 3)) - cam
+    d /= np.linalg.norm(d, axis=1, keepdims=True)
+    return np.concatenate([o, d, np.ones((n, 1))], 1).astype(np.float32)
+
+
+def any_rays(scene, n, seed):
+    """Segments between two random points in the bounds: {org, dir, min_t, max_t}."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    lo, hi = scene['pos'].reshape(-1, 3).min(0), scene['pos'].reshape(-1, 3).max(0)
+    a = rng.uniform(lo, hi, (n, 3))
+    b = rng.uniform(lo, hi, (n, 3))
+    d = b - a
+    L = np.linalg.norm(d, axis=1, keepdims=True)
+    return np.concatenate([a, d / L, np.full((n, 1), 1e-4), L], 1).astype(np.float32)
+
+
+def run(args):
+    r = subprocess.run([FRREF] + args, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError('frref %s failed: %s' % (' '.join(args), r.stderr))
+
+
+def make(name, factory, photons, iters, out_dir=HERE):
+    scene = factory()
+    with tempfile.TemporaryDirectory() as d:
+        objio.write_scene(scene, d)
+        objio.write_materials_table(scene, os.path.join(d, 'materials.txt'))
+        objio.write_camera(scene, os.path.join(d, 'camera.txt'))
+        od = os.path.join(d, 'out')
+        os.makedirs(od)
+        run([d, 'facets', od])
+        for k, ref in (('facet_pos', 'pos'), ('facet_nrm', 'nrm'), ('facet_uv', 'uv'), ('facet_attr', 'mat')):
+            got = np.load(os.path.join(od, k + '.npy'))
+            if not np.array_equal(got, scene[ref]):
+                raise RuntimeError('%s: the reference loaded different %s' % (name, ref))
+        rays = query_rays(scene, 4096, 1)
+        rays.tofile(os.path.join(d, 'rays.bin'))
+        run([d, 'trace', os.path.join(d, 'rays.bin'), od])
+        arays = any_rays(scene, 4096, 2)
+        arays.tofile(os.path.join(d, 'arays.bin'))
+        run([d, 'any', os.path.join(d, 'arays.bin'), od])
+        run([d, 'render', str(photons), str(iters), od])
+        data = dict(scene_sha=np.array(scene_sha(scene)), photons=np.array(photons), iters=np.array(iters),
+                    rays=rays, hit_facet=np.load(os.path.join(od, 'hit_facet.npy')),
+                    hit_tuv=np.load(os.path.join(od, 'hit_tuv.npy')), any_rays=arays,
+                    any_hit=np.load(os.path.join(od, 'any_hit.npy')),
+                    image=np.load(os.path.join(od, 'image.npy')), meta=np.load(os.path.join(od, 'meta.npy')))
+        for s in range(1, iters + 1):
+            for k in ('hp_type', 'hp_facet', 'hp_pos', 'hp_nrm', 'hp_out', 'hp_w', 'hp_rough', 'ph', 'ph_path',
+                      'ph_slot', 'gather_m', 'gather_phi', 'sp_rad', 'sp_r', 'sp_n', 'sp_g'):
+                data['it%d_%s' % (s, k)] = np.load(os.path.join(od, 'it%d_%s.npy' % (s, k)))
+    path = os.path.join(out_dir, name + '.npz')
+    np.savez_compressed(path, **data)
+    return path
+
+
+if __name__ == '__main__':
+    if not os.path.exists(FRREF):
+        sys.exit('build the reference first: make -C oracle/ref')
+    for name, (factory, photons, iters) in FIXTURES.items():
+        p = make(name, factory, photons, iters)
+        print(p, os.path.getsize(p))
