@@ -649,9 +649,13 @@ int fr_radius_query(fr_ctx* c, const float* hp, int32_t nh, const float* photons
   ScanTemp st{};
   const uint32_t words = scan_temp_words(g.table + 1, st);
   std::vector<void*> tmp;
+  bool alloc_ok = true;
   auto dalloc = [&](size_t bytes) {
     void* p = nullptr;
-    if (cudaMalloc(&p, std::max<size_t>(bytes, 16)) != cudaSuccess) return (void*)nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(bytes, 16)) != cudaSuccess) {
+      alloc_ok = false;
+      return (void*)nullptr;
+    }
     tmp.push_back(p);
     return p;
   };
@@ -669,10 +673,7 @@ int fr_radius_query(fr_ctx* c, const float* hp, int32_t nh, const float* photons
   int32_t* d_m = (int32_t*)dalloc(4 * (size_t)nh);
   uint32_t* d_pairs = pairs ? (uint32_t*)dalloc(8 * std::max<size_t>(pair_capacity, 1)) : nullptr;
   uint32_t* d_pc = (uint32_t*)dalloc(4);
-  int rc = FR_OK;
-  for (void* p : tmp)
-    if (!p) rc = fail(FR_ERR_OOM, "fr_radius_query: cudaMalloc failed");
-  if (tmp.size() != (size_t)(17 + (pairs ? 1 : 0))) rc = fail(FR_ERR_OOM, "fr_radius_query: cudaMalloc failed");
+  int rc = alloc_ok ? FR_OK : fail(FR_ERR_OOM, "fr_radius_query: cudaMalloc failed");
   if (!rc) {
     for (int l = 0; l < st.levels; ++l) {
       st.level[l] = sw;
@@ -702,8 +703,7 @@ int fr_radius_query(fr_ctx* c, const float* hp, int32_t nh, const float* photons
     }
     rc = fr_synchronize(c);
   }
-  for (void* p : tmp)
-    if (p) cudaFree(p);
+  for (void* p : tmp) cudaFree(p);
   return rc;
 }
 

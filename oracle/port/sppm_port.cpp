@@ -1,0 +1,1229 @@
+// ORACLE — test infrastructure only.  Nothing in the product links, loads or
+// calls this file; tests/, smoke() and bench.py's CPU baseline use it as the
+// checker and the timed CPU reference.
+//
+// A CPU restatement (C++17 + OpenMP) of the reference's SPPM render loop,
+// SPPM/SPPM/SPPM.cpp of tabochans/FriendsRender-R-public, with the Philox
+// stream of the oracle overlay (oracle/ref/overlay/MT.h) in place of its
+// mt19937.  Its results are pinned to the reference's own outputs by the
+// golden fixtures (tests/golden/, made by running the reference).  Each
+// function names the reference lines it restates.
+//
+// Differences from the reference, all documented there too:
+//  * closest hit: the reference's BVH (bvh8.h) is replaced by a binary BVH;
+//    of equal-t hits the larger facet index wins (the reference keeps the one
+//    its traversal visits last, bvh8.h:591);
+//  * the photon kd-tree (kdtree.h) is a median-split kd-tree; the query keeps
+//    the reference's box test and sphere filter;
+//  * camera sampler: three draws from the pixel's own stream.
+#include <omp.h>
+
+#include <algorithm>
+#include <cfloat>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <memory>
+#include <vector>
+
+namespace port {
+
+constexpr float PI = 3.14159f;           // Vec.h:10
+constexpr float RAY_OFFSET = 1e-4f;      // Primitive.h:31
+constexpr float sMin = 1e-16f;           // Sampling.h:8
+constexpr int NUM_SAMPLE = 1000;         // LightSampler.h:17
+constexpr int SLOTS = 32;                // SPPM.cpp:753
+
+// ------------------------------------------------------------------ Vec3
+struct V {
+  float x = 0, y = 0, z = 0;
+  V() = default;
+  V(float a, float b, float c) : x(a), y(b), z(c) {}
+  float operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+};
+// Vec.h:179-243, 303-323
+inline V operator+(V a, V b) { return V(a.x + b.x, a.y + b.y, a.z + b.z); }
+inline V operator-(V a, V b) { return V(a.x - b.x, a.y - b.y, a.z - b.z); }
+inline V operator*(V a, V b) { return V(a.x * b.x, a.y * b.y, a.z * b.z); }
+inline V operator/(V a, V b) { return V(a.x / b.x, a.y / b.y, a.z / b.z); }
+inline V operator-(V a) { return V(-a.x, -a.y, -a.z); }
+inline V operator*(float s, V a) { return V(s * a.x, s * a.y, s * a.z); }
+inline V operator*(V a, float s) { return V(s * a.x, s * a.y, s * a.z); }
+inline V operator/(V a, float s) { return V(a.x / s, a.y / s, a.z / s); }
+inline float dot(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V cross(V a, V b) { return V(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+inline float norm2(V a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
+inline float norm(V a) { return std::sqrt(norm2(a)); }
+inline V normalized(V a) {
+  const float d = norm(a);
+  return V(a.x / d, a.y / d, a.z / d);
+}
+inline V vp(const float* p) { return V(p[0], p[1], p[2]); }
+
+// ------------------------------------------------------------------ RNG
+// Philox4x32-10 (Salmon et al., SC'11) keyed by the reference's integer seed.
+struct Rng {
+  uint32_t key, draw = 0, buf[4];
+  explicit Rng(uint32_t seed) : key(seed) {}
+  static void philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1, uint32_t o[4]) {
+    for (int r = 0; r < 10; ++r) {
+      if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
+      const uint64_t p0 = (uint64_t)0xD2511F53u * c0, p1 = (uint64_t)0xCD9E8D57u * c2;
+      const uint32_t n0 = (uint32_t)(p1 >> 32) ^ c1 ^ k0, n2 = (uint32_t)(p0 >> 32) ^ c3 ^ k1;
+      c0 = n0; c1 = (uint32_t)p1; c2 = n2; c3 = (uint32_t)p0;
+    }
+    o[0] = c0; o[1] = c1; o[2] = c2; o[3] = c3;
+  }
+  uint32_t u24() {
+    const uint32_t lane = draw & 3u;
+    if (!lane) philox(draw >> 2, 0, 0, 0, key, 0x5350504Du, buf);
+    ++draw;
+    return buf[lane] >> 8;
+  }
+  // RandomMT::genrand64_real1/real2 (MT.h:30-37)
+  double real() { return (double)((float)u24() * (1.0f / 16777216.0f)); }
+};
+
+// ------------------------------------------------------------------ scene
+struct Texture {
+  int w = 0, h = 0;
+  std::vector<float> c;  // RGBA, value / 255.0f (TextureUtility.cpp:28)
+};
+struct Material {
+  int type, sppm, opaque, tex_albedo, tex_rough, tex_bump;
+  V albedo, radiance;
+  float index, roughness, extinction, reflectance;
+};
+struct Facet {
+  V p[3], n[3];
+  float uv[3][2];
+  int attr;
+};
+struct AliasBin { float prob = 1.0f; int left = -1, right = -1; };
+struct Table {  // TableSampler<T> (TableSampler.h:9-169)
+  std::vector<AliasBin> bins;
+  std::vector<float> values;
+  float average = 0;
+  int n = 0;
+  // TableSampler::Init (TableSampler.h:44-120)
+  void init(const std::vector<float>& v) {
+    n = (int)v.size();
+    values = v;
+    bins.assign(n, AliasBin());
+    average = 0.0f;
+    for (int i = 0; i < n; ++i) average += std::max(0.0f, v[i]);
+    average /= n;
+    std::vector<std::pair<float, int>> bigger, smaller;
+    for (int i = 0; i < n; ++i) {
+      const float x = std::max(0.0f, v[i]);
+      if (x >= average) bigger.push_back({x / average, i});
+      else smaller.push_back({x / average, i});
+    }
+    size_t s = 0, b = 0;
+    for (int i = 0; i < n; ++i) {
+      if (s < smaller.size()) {
+        bins[i].left = smaller[s].second;
+        bins[i].prob = smaller[s].first;
+        ++s;
+        if (b < bigger.size()) {
+          bins[i].right = bigger[b].second;
+          bigger[b].first -= (1.0f - bins[i].prob);
+          if (bigger[b].first < 1.0f) smaller.push_back(bigger[b++]);
+        } else if (smaller.size() == s) {
+          bins[i].right = -1;
+          bins[i].prob = 1.0f;
+        } else {
+          bins[i].right = smaller[s].second;
+        }
+      } else {
+        bins[i].left = bigger[b].second;
+        bins[i].prob = 1.0f;
+        bigger[b].first -= 1.0f;
+        if (bigger[b].first < 1.0f) smaller.push_back(bigger[b++]);
+      }
+    }
+  }
+  float pdf(int i) const { return values[i] / average / (float)n; }  // TableSampler.h:122-124
+  // TableSampler::Sample (TableSampler.h:126-129)
+  int sample(Rng& mt) const {
+    const AliasBin& bin = bins[(size_t)((double)n * mt.real())];
+    return mt.real() < bin.prob ? bin.left : bin.right;
+  }
+};
+struct Light {
+  Facet f;
+  V flux;
+  bool textured;
+  Table table;
+  std::vector<V> uvw, L;
+};
+
+struct Camera {
+  int type, W, H;
+  V pos, dir, e1, e2;
+  float fov, pw, ph, lw, lh, F, dist;
+};
+
+struct Ray {
+  V o, d;
+  float index;
+};
+
+// --------------------------------------------------------------- texture
+// LinearSampler::Sample (TextureSampler.h:61-79)
+inline void tex_sample(const Texture& t, float u, float v, float out[4]) {
+  const int W = t.w, H = t.h;
+  const int x1 = std::abs(int(W * u)) % W;
+  const int y1 = std::abs(int(H * v)) % H;
+  const float* c00 = &t.c[4 * (size_t)(x1 + y1 * W)];
+  const float* c10 = &t.c[4 * (size_t)(std::min(W - 1, x1 + 1) + y1 * W)];
+  const float* c01 = &t.c[4 * (size_t)(x1 + std::min(H - 1, y1 + 1) * W)];
+  const float* c11 = &t.c[4 * (size_t)(std::min(W - 1, x1 + 1) + std::min(H - 1, y1 + 1) * W)];
+  const float w = (std::abs(u * W) - std::abs(int(W * u)));
+  const float h = (std::abs(v * H) - std::abs(int(H * v)));
+  for (int k = 0; k < 4; ++k) {
+    const float up = c00[k] * (float)(1.0 - w) + c10[k] * w;
+    const float down = c01[k] * (float)(1.0 - w) + c11[k] * w;
+    out[k] = up * (float)(1.0 - h) + down * h;
+  }
+}
+
+// ------------------------------------------------------------------- BVH
+struct BNode { float lo[3], hi[3]; int left, right, first, count; };
+struct BVH {
+  std::vector<BNode> nodes;
+  std::vector<int> idx;
+  void build(const std::vector<Facet>& F) {
+    const int T = (int)F.size();
+    idx.resize(T);
+    std::vector<V> cen(T);
+    for (int t = 0; t < T; ++t) {
+      idx[t] = t;
+      cen[t] = (F[t].p[0] + F[t].p[1] + F[t].p[2]) * (1.0f / 3.0f);
+    }
+    nodes.clear();
+    nodes.reserve(2 * (size_t)T);
+    rec(F, cen, 0, T);
+  }
+  int rec(const std::vector<Facet>& F, const std::vector<V>& cen, int first, int count) {
+    BNode n;
+    for (int a = 0; a < 3; ++a) { n.lo[a] = FLT_MAX; n.hi[a] = -FLT_MAX; }
+    float clo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, chi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int i = first; i < first + count; ++i) {
+      const Facet& f = F[idx[i]];
+      for (int k = 0; k < 3; ++k)
+        for (int a = 0; a < 3; ++a) { n.lo[a] = std::min(n.lo[a], f.p[k][a]); n.hi[a] = std::max(n.hi[a], f.p[k][a]); }
+      for (int a = 0; a < 3; ++a) { clo[a] = std::min(clo[a], cen[idx[i]][a]); chi[a] = std::max(chi[a], cen[idx[i]][a]); }
+    }
+    // Padded like the reference's triangle boxes (Intersect.cpp:572-573) so
+    // culling is conservative.
+    for (int a = 0; a < 3; ++a) { n.lo[a] -= 0.001f + std::fabs(n.lo[a]) * 1e-6f; n.hi[a] += 0.001f + std::fabs(n.hi[a]) * 1e-6f; }
+    n.left = n.right = -1;
+    n.first = first;
+    n.count = count;
+    const int id = (int)nodes.size();
+    nodes.push_back(n);
+    if (count <= 4) return id;
+    int axis = 0;
+    for (int a = 1; a < 3; ++a)
+      if (chi[a] - clo[a] > chi[axis] - clo[axis]) axis = a;
+    const int mid = first + count / 2;
+    std::nth_element(idx.begin() + first, idx.begin() + mid, idx.begin() + first + count,
+                     [&](int a, int b) { return cen[a][axis] < cen[b][axis]; });
+    const int l = rec(F, cen, first, mid - first);
+    const int r = rec(F, cen, mid, first + count - mid);
+    nodes[id].left = l;
+    nodes[id].right = r;
+    nodes[id].count = 0;
+    return id;
+  }
+};
+
+// Isc::Intersect(Ray, Triangle_ID) (Intersect.cpp:67-89)
+inline bool intersect(const Ray& ray, const Facet& p, float& t, float& u, float& v) {
+  const V dd = ray.d;
+  const V e1 = p.p[1] - p.p[0];
+  const V e2 = p.p[2] - p.p[0];
+  const V ps = cross(dd, e2);
+  const float a = dot(e1, ps);
+  if (a > -FLT_MIN && a < FLT_MIN) return false;
+  const float f = 1.0f / a;
+  const V s = ray.o - p.p[0];
+  u = f * dot(s, ps);
+  if (u < 0.0 || u > 1.0) return false;
+  const V q = cross(s, e1);
+  v = f * dot(dd, q);
+  if (v < 0.0 || u + v > 1.0) return false;
+  t = f * dot(e2, q);
+  return true;
+}
+
+inline bool box_hit(const BNode& n, const Ray& r, float tmin, float tmax) {
+  float t0 = tmin, t1 = tmax;
+  for (int a = 0; a < 3; ++a) {
+    const double inv = 1.0 / (double)r.d[a];
+    double ta = ((double)n.lo[a] - r.o[a]) * inv, tb = ((double)n.hi[a] - r.o[a]) * inv;
+    if (ta > tb) std::swap(ta, tb);
+    if (std::isnan(ta) || std::isnan(tb)) continue;
+    t0 = (float)std::max((double)t0, ta);
+    t1 = (float)std::min((double)t1, tb);
+  }
+  return t0 <= t1;
+}
+
+struct Hit { float t, u, v; int facet; };
+
+// N_BVH8::findClosestElement semantics (bvh8.h:568-641): nearest t > MinT.
+bool closest(const BVH& b, const std::vector<Facet>& F, const Ray& ray, Hit& h) {
+  float best = FLT_MAX;
+  int bf = -1;
+  float bu = 0, bv = 0;
+  int stack[128];
+  int sp = 0;
+  stack[sp++] = 0;
+  while (sp) {
+    const BNode& n = b.nodes[stack[--sp]];
+    if (!box_hit(n, ray, RAY_OFFSET, best)) continue;
+    if (n.left < 0) {
+      for (int i = n.first; i < n.first + n.count; ++i) {
+        const int f = b.idx[i];
+        float t, u, v;
+        if (intersect(ray, F[f], t, u, v) && t > RAY_OFFSET && (t < best || (t == best && f > bf))) {
+          best = t; bf = f; bu = u; bv = v;
+        }
+      }
+    } else {
+      stack[sp++] = n.right;
+      stack[sp++] = n.left;
+    }
+  }
+  if (bf < 0) return false;
+  h = Hit{best, bu, bv, bf};
+  return true;
+}
+
+// findAnyElement (bvh8.h:643-707)
+bool any_hit(const BVH& b, const std::vector<Facet>& F, const Ray& ray, float tmin, float tmax) {
+  int stack[128];
+  int sp = 0;
+  stack[sp++] = 0;
+  while (sp) {
+    const BNode& n = b.nodes[stack[--sp]];
+    if (!box_hit(n, ray, tmin, tmax)) continue;
+    if (n.left < 0) {
+      for (int i = n.first; i < n.first + n.count; ++i) {
+        float t, u, v;
+        if (intersect(ray, F[b.idx[i]], t, u, v) && tmax >= t && t > tmin) return true;
+      }
+    } else {
+      stack[sp++] = n.right;
+      stack[sp++] = n.left;
+    }
+  }
+  return false;
+}
+
+// ------------------------------------------------------------- sampling
+const V INVALID_DIR(1e-3, 1e-3, 1e-3);  // RayUtility.h:8
+inline bool valid_dir(V d) { return norm2(d) > 0.9999f; }  // RayUtility.cpp:36-38
+
+struct FP { V in, out, n; float from, to, rough, absorb, refl; };  // material.h:12-34
+
+inline void basis(V e1, V& e2, V& e3) {
+  if (std::abs(e1.x) > 0.000001) e2 = normalized(cross(V(0, 1, 0), e1));
+  else e2 = normalized(cross(V(1, 0, 0), e1));
+  e3 = normalized(cross(e1, e2));
+}
+
+// Sampling::Cos_Sampling (Sampling.cpp:7-28)
+V cos_sampling(Rng& mt, V normal, float* pdf) {
+  V e2, e3;
+  const V e1 = normal;
+  basis(e1, e2, e3);
+  const float ph = mt.real() * 2.0f * PI;
+  const float th = mt.real();
+  const float th2 = std::sqrt(th);
+  V r = e1 * (float)std::sqrt(1.000000001 - th) + e2 * (float)std::cos((double)ph) * th2 +
+        e3 * (float)std::sin((double)ph) * th2;
+  r = normalized(r);
+  if (pdf) *pdf = std::max(sMin, dot(r, normal) / PI);
+  return r;
+}
+// Sampling::Reflect_Sampling (Sampling.cpp:293-295)
+V reflect(V n, V in) { return normalized(in - 2.0f * (dot(n, in)) * n); }
+// Sampling::Fresnel_Reflectance (Sampling.cpp:297-313)
+float fresnel(V n, V in, float ni, float no) {
+  const float r12 = ni / no;
+  const float cosA = std::abs(dot(n, in));
+  const float sinA = std::sqrt(1.0000001f - cosA * cosA);
+  const float sinB = r12 * sinA;
+  if (sinB > 0.999999) return 1.0f;
+  const float cosB = std::sqrt(1.0000001f - sinB * sinB);
+  const float rp = (no * cosA - ni * cosB) / (no * cosA + ni * cosB);
+  const float rs = (ni * cosA - no * cosB) / (ni * cosA + no * cosB);
+  return (0.5f * rs * rs) + (0.5f * rp * rp);
+}
+// RUtil::Refract (RayUtility.cpp:10-17)
+V refract(V in, V n, float from, float into) {
+  const V NN = dot(in, n) < 0 ? n : -n;
+  const float eta = from / into;
+  const float LN = -dot(in, NN);
+  const float sq = std::max(0.0f, 1.0f - eta * eta * (1.0f - LN * LN));
+  return normalized(-NN * std::sqrt(sq) - eta * (-in - LN * NN));
+}
+inline bool is_reflect(V in, V out, V n) { return dot(n, in) * dot(n, out) < 0.0f; }  // RayUtility.cpp:34-36
+// RUtil::GetMicrofacetNormal_FromRefraction (RayUtility.cpp:21-33)
+V mfn_refraction(V in, V out, float from, float into) {
+  const float c = std::abs(dot(in, out));
+  const float eta = into / from;
+  const float isq = eta * eta - 2.0f * eta * c + 1.0f;
+  if (isq < 1e-8) return V(0, 0, 0);
+  const float ss = 1.0f / std::sqrt(isq);
+  const V h = normalized(-eta * ss * out + ss * in);
+  return into > from ? h : -h;
+}
+inline float powm2(float x) { return std::pow(x, -2.0f); }
+
+// Sampling::GGX_Sampling (Sampling.cpp:123-157)
+V ggx_sampling(Rng& mt, V normal, V in, float alpha, float* pdf) {
+  const V e1 = normal;
+  const float phi = mt.real() * 2.0f * PI;
+  const float e = mt.real();
+  const float cth = (float)std::sqrt((1.0 - e) / (e * (alpha * alpha - 1.0f) + 1.0f));
+  V e2, e3;
+  basis(e1, e2, e3);
+  const float cph = (float)std::cos((double)phi), sph = (float)std::sin((double)phi);
+  const float sth = std::sqrt(1.0f - cth * cth);
+  const V mN = normalized(e3 * sth * cph + e2 * sth * sph + e1 * cth);
+  if (dot(mN, in) > 0.0) { *pdf = sMin; return INVALID_DIR; }
+  const V r = reflect(mN, in);
+  if (dot(r, normal) < 0.0) { *pdf = sMin; return INVALID_DIR; }
+  const float wm_N = dot(mN, normal), wo_wm = dot(r, mN);
+  const double x = 1.0f - (1.0f - alpha * alpha) * wm_N * wm_N;
+  *pdf = (float)((alpha * alpha) / (PI * (x * x)) * wm_N / (4.0f * wo_wm));
+  return r;
+}
+// Sampling::GGX_Sampling_PDF (Sampling.cpp:158-180)
+float ggx_pdf(V out, V normal, V in, float a) {
+  if (!is_reflect(in, out, normal)) return sMin;
+  const V h = normalized(-in + out);
+  const float h_n = dot(h, normal);
+  if (h_n < 0.0f) return sMin;
+  if (-dot(in, h) < 0.0f) return sMin;
+  const float wo_h = dot(out, h);
+  if (wo_h < 0.0f) return sMin;
+  const float jc = 1.0f / (4.0f * wo_h);
+  return (a * a / PI * powm2(1.0f - (1.0f - a * a) * h_n * h_n)) * h_n * jc;
+}
+// Sampling::GGXGlass_Sampling (Sampling.cpp:181-248)
+V glass_sampling(Rng& mt, V normal, V in, float alpha, float Ii, float Io, float* pdf) {
+  constexpr float small = 1e-12f;
+  const V NN = dot(in, normal) < 0 ? normal : -normal;
+  *pdf = 1.0f;
+  const V e1 = NN;
+  const float phi = mt.real() * 2.0f * PI;
+  const float e = mt.real();
+  const float cth = (float)std::sqrt((1.0000001 - e) / (e * (alpha * alpha - 0.99999) + 1.0f));
+  V e2, e3;
+  basis(e1, e2, e3);
+  const float cph = (float)std::cos((double)phi), sph = (float)std::sin((double)phi);
+  const float sth = std::sqrt(1.00000001f - cth * cth);
+  const V mN = normalized(e3 * sth * cph + e2 * sth * sph + e1 * cth);
+  const float wi_wm = -dot(in, mN), wm_N = dot(mN, NN), wi_N = -dot(in, NN);
+  if (wi_N < small || wi_wm < small || wm_N < small) { *pdf = sMin; return INVALID_DIR; }
+  const float refl = fresnel(mN, in, Ii, Io);
+  const float y = 1.0f - (1.0f - alpha * alpha) * wm_N * wm_N;
+  if (refl > mt.real()) {
+    *pdf = refl;
+    const V r = reflect(mN, in);
+    const float wo_wm = dot(r, mN);
+    if (wo_wm < small) return INVALID_DIR;
+    if (dot(r, NN) * dot(in, NN) > small) { *pdf = sMin; return INVALID_DIR; }
+    *pdf = refl * (wm_N / (4.0f * wo_wm) * alpha * alpha / (PI * (y * y)));
+    return r;
+  }
+  const V r = refract(in, mN, Ii, Io);
+  const float wo_wm = -dot(r, mN), wo_N = -dot(r, NN);
+  if (wi_N * wo_N < small || wo_N < small || wo_wm < small) { *pdf = sMin; return INVALID_DIR; }
+  const double s = Ii * wi_wm + Io * wo_wm;
+  *pdf = (float)((1.0f - refl) * wm_N * (Io * Io * wo_wm / (s * s)) * alpha * alpha / (PI * (y * y)));
+  return r;
+}
+// Sampling::GGXGlass_Sampling_PDF (Sampling.cpp:249-288)
+float glass_pdf(V out, V normal, V in, float a, float Ii, float Io) {
+  if (is_reflect(in, out, normal)) {
+    const V h = normalized(-in + out);
+    const float h_n = dot(h, normal);
+    if (h_n < 0.0f) return sMin;
+    if (-dot(in, h) < 0.0f) return sMin;
+    const float wo_h = dot(out, h);
+    if (wo_h < 0.0f) return sMin;
+    const float refl = fresnel(h, in, Ii, Io);
+    const float jc = 1.0f / (4.0f * wo_h);
+    return refl * h_n * (a * a / PI * powm2(1.0f - (1.0f - a * a) * h_n * h_n)) * jc;
+  }
+  const V h = mfn_refraction(in, out, Ii, Io);
+  const float h_n = dot(h, normal);
+  if (h_n < 0.0f) return sMin;
+  const float wi_h = -dot(in, h);
+  if (wi_h < 0.0f) return sMin;
+  const float wo_h = -dot(out, h);
+  if (wo_h < 0.0f) return sMin;
+  const float refl = fresnel(h, in, Ii, Io);
+  const float jc = Io * Io * wo_h * powm2(Ii * wi_h + Io * wo_h);
+  return (1.0f - refl) * h_n * (a * a / PI * powm2(1.0f - (1.0f - a * a) * h_n * h_n)) * jc;
+}
+inline bool opaque_reflect(const FP& p) { return dot(p.in, -p.n) > 1e-4 && dot(p.out, p.n) > 1e-4; }  // material.h:139-141
+
+// Roughconductor::BRDF (material.h:227-274)
+float conductor_brdf(const FP& p) {
+  constexpr float small = 1e-10f;
+  if (dot(p.in, p.n) > -small || dot(p.out, p.n) < small) return 0.0f;
+  const float k = p.absorb, eta = p.to / p.from, alpha = p.rough;
+  const V h = normalized(-p.in + p.out);
+  const float ccs = dot(h, p.n);
+  if (ccs < small || dot(h, p.in) > -small || dot(h, p.out) < small) return 0.0f;
+  const float dd = 1.0001f - (1.0f - alpha * alpha) * ccs * ccs;
+  const float D = std::max(sMin, (alpha * alpha) / (PI * (dd * dd)));
+  const float lc = std::max(0.0f, std::min(0.9999f, dot(p.in, -p.n)));
+  const float lv = std::max(0.0f, std::min(0.9999f, dot(p.out, p.n)));
+  if (lc < sMin || lv < sMin) return 0.0f;
+  const float L_l = (-1.0f + std::sqrt(1.0f + alpha * alpha * (1.0f / (lc * lc) - 1.0))) * 0.5;
+  const float L_v = (-1.0f + std::sqrt(1.0f + alpha * alpha * (1.0f / (lv * lv) - 1.0))) * 0.5;
+  const float G = 1.0f / ((1.0f + L_l) * (1.0f + L_v));
+  const float fcos = dot(p.n, -p.in);
+  const float temp = eta * eta - k * k - (1.0f - fcos * fcos);
+  const float apb = std::sqrt(temp * temp + k * k * eta * eta);
+  const float a = std::sqrt((apb + temp) * 0.5);
+  const float tm1 = apb + fcos * fcos;
+  const float tm2 = a * 2.0f * fcos;
+  const float rs2 = (tm1 - tm2) / (tm1 + tm2);
+  const float tm3 = apb * fcos * fcos + (1.0f - fcos * fcos) * (1.0 - fcos * fcos);
+  const float tm4 = tm2 * (1.0f - fcos * fcos);
+  const float rp2 = rs2 * (tm3 - tm4) / (tm3 + tm4);
+  const float F = 0.5 * (rp2 + rs2);
+  const float fx = (4.0f * dot(p.in, -p.n) * dot(p.out, p.n));
+  return (F * G * D) / fx;
+}
+// GGXGlass::EstimateN (material.h:297-309)
+V estimate_n(V in, V out, float Ii, float Io) {
+  const float c = std::abs(dot(in, out));
+  const float eta = Io / Ii;
+  const float isq = eta * eta - 2.0f * eta * c + 1.0f;
+  if (isq < sMin) return V(0, 0, 0);
+  const float ss = 1.0f / std::sqrt(isq);
+  const V h = normalized(-eta * ss * out + ss * in);
+  return Io > Ii ? h : -h;
+}
+// GGXGlass::BRDF (material.h:314-390)
+float glass_brdf(const FP& p) {
+  constexpr float small = 1e-8f;
+  const bool refl = dot(p.n, p.in) * dot(p.n, p.out) < 0;
+  const float a = p.rough, Ii = p.from, Io = p.to;
+  if (refl) {
+    const V h = normalized(-p.in + p.out);
+    const float n_h = dot(p.n, h);
+    if (n_h < 0) return 0.0f;
+    const float D = (a * a) * powm2(1.0f - (1.0f - a * a) * n_h * n_h) / PI;
+    const float L_l = (-1.0f + std::sqrt(1.0001f + a * a * (powm2(dot(p.n, -p.in)) - 1.0f))) * 0.5f;
+    const float L_v = (-1.0f + std::sqrt(1.0001f + a * a * (powm2(dot(p.n, p.out)) - 1.0f))) * 0.5f;
+    const float G = 1.0f / (L_l + L_v + 1.0f);
+    const float F = fresnel(h, p.in, Ii, Io);
+    const float wo_n = std::max(0.0f, std::min(1.0f, dot(p.out, h)));
+    const float wi_n = std::max(0.0f, std::min(1.0f, -dot(p.in, h)));
+    if (wo_n < small || wi_n < small) return 0.0f;
+    return F * G * D / (4.0f * wo_n * wi_n);
+  }
+  const float eta = Io / Ii;
+  if (std::abs(eta - 1.0f) < small) return 1.0;
+  if (dot(p.in, p.out) < 0.0) return 0.0f;
+  const V h = estimate_n(p.in, p.out, p.from, p.to);
+  if (norm(h) < small) return 0.0f;
+  const float n_h = dot(h, p.n);
+  if (n_h < small) return 0.0f;
+  const float D = (a * a) * powm2(1.0f - (1.0f - a * a) * n_h * n_h) / PI;
+  const float L_l = (-1.0f + std::sqrt(1.0001f + a * a * (powm2(dot(p.n, -p.in)) - 1.0f))) * 0.5f;
+  const float L_v = (-1.0f + std::sqrt(1.0001f + a * a * (powm2(dot(p.n, -p.out)) - 1.0f))) * 0.5f;
+  const float G = 1.0f / (L_l + L_v + 1.0f);
+  const float F = fresnel(h, p.in, Ii, Io);
+  const float wi_wm = -dot(p.in, h), wo_wm = -dot(p.out, h);
+  const float wi_n = -dot(p.in, p.n), wo_n = -dot(p.out, p.n);
+  if (wo_wm < small || wi_wm < small) return 0.0f;
+  if (wi_n < small || wo_n < small) return 0.0f;
+  return (wi_wm * wo_wm) / (wi_n * wo_n) * (Io * Io) * (1.0f - F) * G * D * powm2(Ii * wo_wm + Io * wi_wm);
+}
+
+// Surface virtual interface (material.h:137-146) over the four surfaces.
+V surf_sample(int type, Rng& mt, const FP& p, float* pdf) {
+  switch (type) {
+    case 0: return cos_sampling(mt, p.n, pdf);                          // DiffuseSurface (material.h:165-167)
+    case 1: *pdf = 1.0f; return reflect(p.n, p.in);                     // MetalSurface (material.h:398-403)
+    case 2: return ggx_sampling(mt, p.n, p.in, p.rough, pdf);           // Roughconductor (material.h:224-226)
+    default: return glass_sampling(mt, p.n, p.in, p.rough, p.from, p.to, pdf);  // GGXGlass (material.h:311-313)
+  }
+}
+float surf_brdf(int type, const FP& p) {
+  switch (type) {
+    case 0: return opaque_reflect(p) ? 1.0f / PI : 0.0f;  // material.h:168-173
+    case 1: {                                             // material.h:404-415
+      if (!opaque_reflect(p)) return 0.0f;
+      const V r = reflect(p.n, p.in);
+      if (dot(r, p.out) > 1.0f - 1.0f / 1.0f) return 1.0f / (dot(p.out, p.n) + 0.00001);
+      return 0.0f;
+    }
+    case 2: return conductor_brdf(p);
+    default: return glass_brdf(p);
+  }
+}
+float surf_pdf(int type, const FP& p) {
+  switch (type) {
+    case 0: return std::max(sMin, dot(p.out, p.n) / PI);  // material.h:174-176
+    case 1: return dot(reflect(p.n, p.in), p.out) > 1.0f - 1.0f / 1.0f ? 1.0f : sMin;  // material.h:416-424
+    case 2: return ggx_pdf(p.out, p.n, p.in, p.rough);
+    default: return glass_pdf(p.out, p.n, p.in, p.rough, p.from, p.to);
+  }
+}
+
+// ------------------------------------------------------------- renderer
+struct Geometry {  // SPPM.h:56-68
+  V pos, normal;
+  float uvx, uvy;
+  const Material* m;
+  V albedo, radiance;
+  float rough, translucency;
+};
+struct HitPoint {  // SPPM.h:83-110
+  int type = 0;    // 0 NONE, 1 HIT, 2 ONLY_DIRECTLIGHT
+  V pos, normal, out, weight;
+  float rough = 0;
+  int facet = -1;
+  const Material* m = nullptr;
+};
+struct Photon { V pos, flux, dir; float index, pdf; bool valid = false; };  // SPPM.h:128-143
+struct Shared { V rad; int n = 0; float r = 0; int g = 0; };                 // SPPM.h:112-126
+
+struct KdNode { int photon, axis, left, right; };
+
+struct Renderer {
+  std::vector<Facet> F;
+  std::vector<Material> mats;
+  std::vector<Texture> texs;
+  std::vector<Light> lights;
+  Table light_table;
+  Camera cam;
+  BVH bvh;
+  int P = 0;
+  float alpha = 0.9f, r0 = 0.015f;
+  bool fix_stale = false;
+  int step = 0;
+  long long total_photons = 0;
+  std::vector<Shared> sp;
+  std::vector<HitPoint> hp;
+  std::vector<Photon> slots;  // P x SLOTS
+  std::vector<Photon> photons;
+  std::vector<int> ph_path, ph_slot;
+  std::vector<KdNode> kd;
+  std::vector<int> gather_m;
+  std::vector<V> gather_phi;
+
+  // calculateGeometry (SPPM.cpp:36-77)
+  void geometry(const Hit& h, Geometry& g) const {
+    const Facet& f = F[h.facet];
+    g.pos = h.u * (f.p[1] - f.p[0]) + h.v * (f.p[2] - f.p[0]) + f.p[0];
+    g.normal = normalized(h.u * (f.n[1] - f.n[0]) + h.v * (f.n[2] - f.n[0]) + f.n[0]);
+    g.uvx = h.u * (f.uv[1][0] - f.uv[0][0]) + h.v * (f.uv[2][0] - f.uv[0][0]) + f.uv[0][0];
+    g.uvy = h.u * (f.uv[1][1] - f.uv[0][1]) + h.v * (f.uv[2][1] - f.uv[0][1]) + f.uv[0][1];
+    const Material& m = mats[f.attr];
+    g.m = &m;
+    g.albedo = m.albedo;
+    g.radiance = m.radiance;
+    g.rough = m.roughness;
+    g.translucency = 0.0f;
+    if (norm2(g.radiance) > 1e-6) g.albedo = V(1, 1, 1);
+    float c[4];
+    if (m.tex_rough >= 0) {
+      tex_sample(texs[m.tex_rough], g.uvx, g.uvy, c);
+      g.rough = std::min(0.8f, std::max(0.05f, 0.5f * c[0]));
+    }
+    if (m.tex_albedo >= 0) {
+      tex_sample(texs[m.tex_albedo], g.uvx, g.uvy, c);
+      g.albedo = V(c[0], c[1], c[2]);
+      g.radiance = g.radiance * g.albedo;
+      g.translucency = 1.0 - c[3];
+    }
+    if (m.tex_bump >= 0) {
+      tex_sample(texs[m.tex_bump], g.uvx, g.uvy, c);  // GetNormalFromNormalmap (TextureUtility.cpp:161-164)
+      V nm = normalized(V(2.0f * c[0] - 1.0f, 2.0f * c[1] - 1.0f, 2.0f * c[2] - 1.0f));
+      nm = normalized(V(nm.x, nm.z, nm.y));
+      const V e2 = g.normal;
+      const V e1 = std::abs(e2.y) > 0.9 ? cross(e2, V(1, 0, 0)) : cross(e2, V(0, 1, 0));
+      const V e3 = normalized(cross(e1, e2));
+      // CreateMatrixFromColumns({e1, e2, e3}).inv() (Matrix.h:180-184, Matrix.cpp:22-34)
+      const float M[3][3] = {{e1.x, e2.x, e3.x}, {e1.y, e2.y, e3.y}, {e1.z, e2.z, e3.z}};
+      float C[3][3];
+      for (int r = 0; r < 3; ++r)
+        for (int col = 0; col < 3; ++col) {
+          float m2[2][2];
+          for (int i = 0, rr = 0; i < 3; ++i) {
+            if (i == r) continue;
+            for (int j = 0, cc = 0; j < 3; ++j) {
+              if (j == col) continue;
+              m2[rr][cc++] = M[i][j];
+            }
+            ++rr;
+          }
+          C[r][col] = (m2[0][0] * m2[1][1] - m2[0][1] * m2[1][0]) * ((r + col) % 2 ? -1 : 1);
+        }
+      const float det = M[0][0] * C[0][0] + M[1][0] * C[1][0] + M[2][0] * C[2][0];
+      const float ix = 1.0f / det;
+      V rows[3];
+      for (int i = 0; i < 3; ++i) rows[i] = V(ix * C[0][i], ix * C[1][i], ix * C[2][i]);
+      g.normal = normalized(V(dot(rows[0], nm), dot(rows[1], nm), dot(rows[2], nm)));
+    }
+  }
+
+  // Camera::SampleCameraRay (Camera.h:73-83 pinhole, 103-129 thin lens)
+  Ray camera_ray(float u, float v, Rng& mt, float& pdf) const {
+    const float s0 = mt.real(), s1 = mt.real(), s2 = mt.real();
+    if (cam.type == 0) {
+      const V off = V(s0, s1, s2) * V(cam.pw, cam.ph, 0) / V((float)cam.W, (float)cam.H, 1.0f);
+      const V image = cam.pos - cam.dir * cam.dist + (u - 0.5f + off.x) * cam.e1 * cam.pw + (v - 0.5f + off.y) * cam.e2 * cam.ph;
+      pdf = 1.0f;
+      return Ray{image, normalized(normalized(cam.pos - image)), 1.0f};
+    }
+    const float pdf_area = 1.0f / (cam.lw * cam.lh);
+    const V lens = cam.pos + (s0 - 0.5f) * cam.e1 * cam.lw + (s1 - 0.5f) * cam.e2 * cam.lh;
+    const V image = cam.pos - cam.dir * cam.dist + (u - 0.5f) * cam.e1 * cam.pw + (v - 0.5f) * cam.e2 * cam.ph;
+    const float A = cam.dist, B = (A * cam.F) / (A - cam.F);
+    const V target = image + (cam.pos - image) * (A + B) / A;
+    const float cs = dot(cam.dir, normalized(lens - image));
+    const float d2 = norm2(lens - image);
+    pdf = pdf_area * (d2 / cam.F / cam.F) / cs;
+    return Ray{lens, normalized(normalized(target - lens)), 1.0f};
+  }
+
+  static bool near1(float s) { return std::abs(s - 1.0f) < 0.00001; }  // SPPM.h:27-29
+
+  // getHitpointInfo (SPPM.cpp:98-306); stops at the first hitpoint (nothing
+  // after it reaches the image without an environment light).
+  HitPoint eye(int i) const {
+    const int W = cam.W, H = cam.H;
+    Rng mt((uint32_t)i + (uint32_t)(W * H) * (uint32_t)step);  // SPPM.cpp:334
+    const int w = i % W, h = i / W;
+    const float u = w / (float)W, v = h / (float)H;
+    float cam_pdf = 1.0f;
+    Ray cur = camera_ray(u, v, mt, cam_pdf), nxt = cur;
+    float PDF = 1.0f;
+    V thr(1, 1, 1);
+    int depth = 0;
+    HitPoint hp;
+    while (true) {
+      if (depth > 6) break;
+      if (depth > 4) {
+        const float rus = std::exp(4 - depth);
+        if (mt.real() > rus) break;
+        PDF *= rus;
+      }
+      Hit hit;
+      if (!closest(bvh, F, cur, hit)) {
+        hp.type = 2;
+        break;
+      }
+      Geometry g;
+      geometry(hit, g);
+      g.normal = dot(g.normal, cur.d) > 0 ? -g.normal : g.normal;
+      nxt.o = g.pos;
+      if (g.translucency > 0.5f) {
+        thr = thr * V(g.translucency, g.translucency, g.translucency);
+        cur.o = g.pos + cur.d * RAY_OFFSET;
+        continue;
+      }
+      if (g.m->sppm) {  // makeHitPoint (SPPM.cpp:79-96)
+        hp.type = 1;
+        hp.pos = g.pos;
+        hp.normal = g.normal;
+        hp.out = -cur.d;
+        hp.weight = (thr / PDF) / cam_pdf;
+        hp.rough = g.rough;
+        hp.facet = hit.facet;
+        hp.m = g.m;
+        return hp;
+      }
+      float Ii, Io;
+      if (near1(cur.index)) { Ii = 1.0f; Io = g.m->index; }
+      else { Ii = cur.index; Io = 1.0f; }
+      FP p{cur.d, nxt.d, g.normal, Ii, Io, g.rough, g.m->extinction, g.m->reflectance};
+      float pdf = 1.0f;
+      nxt.d = surf_sample(g.m->type, mt, p, &pdf);
+      if (!valid_dir(nxt.d)) break;
+      if (g.m->opaque) {
+        if (dot(nxt.d, g.normal) < 1e-6) break;
+      } else {
+        nxt.index = dot(nxt.d, g.normal) < 0.0f ? Io : cur.index;
+      }
+      p.out = nxt.d;
+      pdf = surf_pdf(g.m->type, p);
+      const V on = dot(g.normal, nxt.d) > 0 ? g.normal : -g.normal;
+      nxt.o = nxt.o + on * RAY_OFFSET;
+      const float brdf = surf_brdf(g.m->type, p);
+      const float cs = std::max(0.0f, std::min(1.0f, dot(nxt.d, on)));
+      if (brdf < 1e-8) break;
+      if (pdf < 0) break;
+      thr = thr * (g.albedo * cs * brdf);
+      PDF *= pdf;
+      cur = nxt;
+      ++depth;
+    }
+    return hp;
+  }
+
+  // createPhotonMap body for path i (SPPM.cpp:508-673)
+  void photon_path(int i) {
+    Rng mt((uint32_t)i + 135u + (uint32_t)step * (uint32_t)P);  // SPPM.cpp:520
+    Photon* arr = &slots[(size_t)i * SLOTS];
+    // generateLightRay (SPPM.cpp:453-471)
+    const Light& L = lights[light_table.sample(mt)];
+    V pos, rad;
+    float pdf_area;
+    const float area = 0.5f * norm(cross(L.f.p[1] - L.f.p[0], L.f.p[2] - L.f.p[0]));
+    if (L.textured) {  // SamplePointOnAreaLight (LightSampler.cpp:68-75)
+      const int e = L.table.sample(mt);
+      const V w = L.uvw[e];
+      pos = w.x * L.f.p[0] + w.y * L.f.p[1] + (1.0f - w.x - w.y) * L.f.p[2];
+      rad = L.L[e];
+      pdf_area = (L.table.pdf(e) * NUM_SAMPLE) / area;
+    } else {  // PointOnTriangle (Sampling.cpp:339-349), LightSampler.cpp:76-79
+      float u = mt.real(), v = mt.real();
+      if (v > u) { u *= 0.5f; v -= u; }
+      else { v *= 0.5f; u -= v; }
+      pdf_area = 2.0f / std::abs(norm(cross(L.f.p[1] - L.f.p[0], L.f.p[2] - L.f.p[0])));
+      pos = u * L.f.p[0] + v * L.f.p[1] + (1.0f - u - v) * L.f.p[2];
+      rad = L.flux / (2.0f * PI * area);
+    }
+    pdf_area *= light_table.pdf((int)(&L - &lights[0]));
+    const V ln = normalized(L.f.n[0] + L.f.n[1] + L.f.n[2]);
+    float pdf_dir = 1.0f;
+    const V od = cos_sampling(mt, ln, &pdf_dir);
+    rad = rad * std::min(1.0f, std::max(0.0f, dot(ln, od)));
+    Ray cur{pos + ln * RAY_OFFSET, normalized(od), 1.0f}, nxt = cur;
+    const V flux = rad;
+    float PDF = pdf_area * pdf_dir;
+    V thr(1, 1, 1);
+    arr[0] = Photon{cur.o, flux * thr * PI, cur.d, cur.index, PDF, true};
+    int k = 0, loop = 0, depth = 0;
+    while (true) {
+      if (loop++ > 32 || k >= 32 - 1) break;
+      if (thr.x < 1e-8 || thr.y < 1e-8 || thr.z < 1e-8) break;
+      Hit hit;
+      if (!closest(bvh, F, cur, hit)) break;
+      Geometry g;
+      geometry(hit, g);
+      g.normal = dot(g.normal, cur.d) > 0 ? -g.normal : g.normal;
+      nxt.o = g.pos;
+      if (norm2(g.radiance) > 0.00001) break;
+      if (g.translucency > 0.5f) {
+        thr = thr * V(g.translucency, g.translucency, g.translucency);
+        cur.o = g.pos + cur.d * RAY_OFFSET;
+        continue;
+      }
+      // russianRulette_PhotonMapping (SPPM.h:33-52)
+      if (depth > 16) break;
+      const V a = g.albedo;
+      const float pdf_rus = 0.98f * (a.x > a.y ? (a.x > a.z ? a.x : a.z) : (a.y > a.z ? a.y : a.z));
+      if (mt.real() > pdf_rus) break;
+      PDF *= pdf_rus;
+      float Ii, Io;
+      if (near1(cur.index)) { Ii = 1.0f; Io = g.m->index; }
+      else { Ii = cur.index; Io = 1.0f; }
+      FP p{cur.d, nxt.d, g.normal, Ii, Io, g.rough, g.m->extinction, g.m->reflectance};
+      if (g.m->sppm) arr[k++] = Photon{g.pos, flux * thr * g.albedo, cur.d, cur.index, PDF, true};
+      float pdf = 1.0f;
+      nxt.d = surf_sample(g.m->type, mt, p, &pdf);
+      if (!valid_dir(nxt.d)) break;
+      if (g.m->opaque) {
+        if (dot(nxt.d, g.normal) < 1e-6) break;
+      } else {
+        nxt.index = is_reflect(cur.d, nxt.d, g.normal) ? cur.index : Io;
+      }
+      p.out = nxt.d;
+      pdf = surf_pdf(g.m->type, p);
+      const V on = dot(g.normal, nxt.d) > 0 ? g.normal : -g.normal;
+      nxt.o = nxt.o + on * RAY_OFFSET;
+      const float brdf = surf_brdf(g.m->type, p);
+      const float cs = std::max(0.0f, std::min(1.0f, dot(nxt.d, on)));
+      if (brdf < 1e-8) break;
+      if (pdf < 0) break;
+      thr = thr * (g.albedo * cs * brdf);
+      PDF *= pdf;
+      cur = nxt;
+      ++depth;
+    }
+    // SPPM.cpp:672 (terminator one past the last stored photon).
+    const int term = fix_stale ? std::max(k, 1) : k + 1;
+    if (term < SLOTS) arr[term].valid = false;
+  }
+
+  // Median-split kd-tree over photons (replaces kdtree.h:348-431).
+  int kd_build(std::vector<int>& ids, int lo, int hi) {
+    if (lo >= hi) return -1;
+    float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    for (int i = lo; i < hi; ++i)
+      for (int a = 0; a < 3; ++a) {
+        mn[a] = std::min(mn[a], photons[ids[i]].pos[a]);
+        mx[a] = std::max(mx[a], photons[ids[i]].pos[a]);
+      }
+    int axis = 0;
+    for (int a = 1; a < 3; ++a)
+      if (mx[a] - mn[a] > mx[axis] - mn[axis]) axis = a;
+    const int mid = (lo + hi) / 2;
+    std::nth_element(ids.begin() + lo, ids.begin() + mid, ids.begin() + hi,
+                     [&](int a, int b) { return photons[a].pos[axis] < photons[b].pos[axis]; });
+    const int node = (int)kd.size();
+    kd.push_back(KdNode{ids[mid], axis, -1, -1});
+    const int l = kd_build(ids, lo, mid);
+    const int r = kd_build(ids, mid + 1, hi);
+    kd[node].left = l;
+    kd[node].right = r;
+    return node;
+  }
+
+  // GetElementsInsideBox (kdtree.h:457-482) then the sphere filter
+  // (SPPM.cpp:432); left subtree holds coordinates <= the split.
+  template <typename Fn>
+  void query(int node, V bmin, V bmax, V x, float R2, Fn&& fn) const {
+    if (node < 0) return;
+    const KdNode& n = kd[node];
+    const Photon& p = photons[n.photon];
+    bool in = true;
+    for (int a = 0; a < 3; ++a)
+      if (bmin[a] > p.pos[a] || bmax[a] < p.pos[a]) in = false;  // isIncludePoint (kdtree.h:78-88)
+    if (in && norm2(p.pos - x) < R2) fn(n.photon);
+    if (bmin[n.axis] <= p.pos[n.axis]) query(n.left, bmin, bmax, x, R2, fn);
+    if (bmax[n.axis] >= p.pos[n.axis]) query(n.right, bmin, bmax, x, R2, fn);
+  }
+
+  void iterate() {
+    ++step;
+    const int npix = cam.W * cam.H;
+    // Photon pass (SPPM.cpp:771-774, 798): slot 0 reset, then every path.
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int i = 0; i < P; ++i) {
+      slots[(size_t)i * SLOTS].valid = false;
+      photon_path(i);
+    }
+    // Compaction up to the first invalid slot (SPPM.cpp:812-822).
+    photons.clear(); ph_path.clear(); ph_slot.clear();
+    for (int i = 0; i < P; ++i)
+      for (int k = 0; k < SLOTS; ++k) {
+        const Photon& p = slots[(size_t)i * SLOTS + k];
+        if (!p.valid) break;
+        photons.push_back(p); ph_path.push_back(i); ph_slot.push_back(k);
+      }
+    kd.clear();
+    std::vector<int> ids(photons.size());
+    for (size_t i = 0; i < ids.size(); ++i) ids[i] = (int)i;
+    kd.reserve(ids.size());
+    kd_build(ids, 0, (int)ids.size());
+    // Eye pass (SPPM.cpp:776-779, 836).
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int i = 0; i < npix; ++i) hp[i] = eye(i);
+    // Gather and update (applyHitPointInfo, SPPM.cpp:395-451).
+#pragma omp parallel for schedule(dynamic, 64)
+    for (int v = 0; v < npix; ++v) {
+      const HitPoint& h = hp[v];
+      gather_m[v] = 0;
+      gather_phi[v] = V(0, 0, 0);
+      if (h.type != 1) continue;
+      Shared& s = sp[v];
+      const V bmin = h.pos - s.r * V(1, 1, 1), bmax = h.pos + s.r * V(1, 1, 1);
+      V add(0, 0, 0);
+      int m = 0;
+      query(kd.empty() ? -1 : 0, bmin, bmax, h.pos, s.r * s.r, [&](int j) {
+        const Photon& p = photons[j];
+        const float Ii = p.index;
+        const float Io = near1(p.index) ? h.m->index : 1.0f;
+        const V nn = dot(p.dir, h.normal) < 0 ? h.normal : -h.normal;
+        const FP fp{p.dir, h.out, nn, Ii, Io, h.rough, h.m->extinction, h.m->reflectance};
+        add = add + h.weight * surf_brdf(h.m->type, fp) * p.flux / p.pdf;
+        ++m;
+      });
+      gather_m[v] = m;
+      gather_phi[v] = add;
+      if (m > 0) {
+        const float a = s.n + alpha * m, b = (float)(s.n + m);
+        s.rad = (s.rad + add) * a / b;
+        s.r *= std::sqrt(a / b);
+        s.n += m * alpha;
+        s.g++;
+      }
+    }
+    total_photons += P;
+  }
+
+  // reconstructImageFromSharedPoints (SPPM.cpp:473-493)
+  void resolve(float* out) const {
+    const int npix = cam.W * cam.H;
+    for (int i = 0; i < npix; ++i) {
+      const Shared& s = sp[i];
+      const float d = ((float)total_photons * (s.g + 0.0001f) / (0.0001f + (float)step)) * PI * s.r * s.r;
+      const V L = s.rad / d;
+      out[4 * i] = std::pow(L.x, 1.0f / 1.2f);
+      out[4 * i + 1] = std::pow(L.y, 1.0f / 1.2f);
+      out[4 * i + 2] = std::pow(L.z, 1.0f / 1.2f);
+      out[4 * i + 3] = 1.0f;
+    }
+  }
+};
+
+// QRandSequence::HaltonCore (QRandSequence.h:10-25)
+float halton(int n, int B) {
+  float result = 0.0f;
+  if (n <= 0) return result;
+  const int keta = std::log2(n) / std::log2(B) + 1;
+  for (int i = 0; i < keta; ++i) {
+    result += (n % B) * std::pow(B, -(i + 1));
+    n /= B;
+  }
+  return result;
+}
+
+}  // namespace port
+
+using namespace port;
+
+extern "C" {
+
+struct port_material {
+  int32_t type, sppm, opaque, tex_albedo, tex_rough, tex_bump;
+  float albedo[3], emission[3], index, roughness, extinction, reflectance;
+};
+struct port_camera {
+  int32_t type, width, height;
+  float pos[3], target[3], fov, focal, dist, aspect, lens;
+};
+
+void* port_create(int32_t T, const float* pos, const float* nrm, const float* uv, const int32_t* mat, int32_t nm,
+                  const port_material* mats, int32_t nt, const int32_t* tex_wh, const uint8_t* const* texels,
+                  const port_camera* c, int32_t photons, float alpha, float r0, int32_t fix_stale) {
+  Renderer* r = new Renderer();
+  r->F.resize(T);
+  for (int t = 0; t < T; ++t) {
+    Facet& f = r->F[t];
+    for (int k = 0; k < 3; ++k) {
+      f.p[k] = vp(pos + 9 * (size_t)t + 3 * k);
+      f.n[k] = vp(nrm + 9 * (size_t)t + 3 * k);
+      f.uv[k][0] = uv[6 * (size_t)t + 2 * k];
+      f.uv[k][1] = uv[6 * (size_t)t + 2 * k + 1];
+    }
+    f.attr = mat[t];
+  }
+  for (int m = 0; m < nm; ++m) {
+    const port_material& d = mats[m];
+    r->mats.push_back(Material{d.type, d.sppm, d.opaque, d.tex_albedo, d.tex_rough, d.tex_bump, vp(d.albedo),
+                               vp(d.emission), d.index, d.roughness, d.extinction, d.reflectance});
+  }
+  for (int t = 0; t < nt; ++t) {
+    Texture tx;
+    tx.w = tex_wh[2 * t];
+    tx.h = tex_wh[2 * t + 1];
+    tx.c.resize(4 * (size_t)tx.w * tx.h);
+    for (size_t i = 0; i < tx.c.size(); ++i) tx.c[i] = texels[t][i] / 255.0f;
+    r->texs.push_back(std::move(tx));
+  }
+  // Scene::CreateScene lights (Scene.cpp:145-154), LightSampler (LightSampler.cpp:6-66).
+  std::vector<float> fl;
+  for (int t = 0; t < T; ++t) {
+    const Material& m = r->mats[r->F[t].attr];
+    if (!(m.radiance.x + m.radiance.y + m.radiance.z > 0.00001f)) continue;
+    Light L;
+    L.f = r->F[t];
+    const Facet& f = L.f;
+    const float area = 0.5f * norm(cross(f.p[1] - f.p[0], f.p[2] - f.p[0]));
+    if (m.tex_albedo >= 0) {
+      L.textured = true;
+      V total(0, 0, 0);
+      std::vector<float> vals;
+      for (int i = 0; i < NUM_SAMPLE; ++i) {
+        V w(i / (float)NUM_SAMPLE, halton(i, 2), halton(i, 3));
+        if (w.y > w.x) { w.x *= 0.5f; w.y -= w.x; }
+        else { w.y *= 0.5f; w.x -= w.y; }
+        const float u = w.x * f.uv[0][0] + w.y * f.uv[1][0] + (1.0f - w.x - w.y) * f.uv[2][0];
+        const float v = w.x * f.uv[0][1] + w.y * f.uv[1][1] + (1.0f - w.x - w.y) * f.uv[2][1];
+        float c4[4];
+        tex_sample(r->texs[m.tex_albedo], u, v, c4);
+        V l = V(c4[0], c4[1], c4[2]) * m.radiance;
+        if (norm2(l) < 0.01f) l = V(0, 0, 0);
+        L.uvw.push_back(w);
+        L.L.push_back(l);
+        total = total + l;
+      }
+      if (norm2(total) < 1e-6) {
+        L.L[0] = 1e-6 * V(1, 1, 1);
+        L.uvw[0] = V(0, 0, 0);
+      } else {
+        total = total * (2.0f * PI * area / (float)NUM_SAMPLE);
+      }
+      for (int i = 0; i < NUM_SAMPLE; ++i) vals.push_back(norm(L.L[i]));
+      L.table.init(vals);
+      L.flux = total;
+    } else {
+      L.textured = false;
+      L.flux = m.radiance * 2.0f * PI * area;
+    }
+    fl.push_back(norm(L.flux));
+    r->lights.push_back(std::move(L));
+  }
+  if (r->lights.empty()) { delete r; return nullptr; }
+  r->light_table.init(fl);
+  // iCamera constructor (Camera.h:132-151)
+  Camera& cam = r->cam;
+  cam.type = c->type;
+  cam.W = c->width;
+  cam.H = c->height;
+  cam.pos = vp(c->pos);
+  cam.dir = normalized(vp(c->target) - cam.pos);
+  cam.fov = PI * c->fov / 360.0f;
+  cam.pw = 2.0 * c->dist * std::tan((double)cam.fov) * c->aspect;
+  cam.ph = 2.0 * c->dist * std::tan((double)cam.fov);
+  cam.lw = c->lens > 0 ? c->lens : cam.pw;
+  cam.lh = c->lens > 0 ? c->lens : cam.ph;
+  cam.F = c->focal;
+  cam.dist = c->dist;
+  if (cam.dir.y > 0.99) { cam.e1 = V(1, 0, 0); cam.e2 = V(0, 0, 1); }
+  else { cam.e1 = normalized(cross(V(0, 1, 0), cam.dir)); cam.e2 = normalized(cross(cam.dir, cam.e1)); }
+  r->bvh.build(r->F);
+  r->P = photons;
+  r->alpha = alpha;
+  r->r0 = r0;
+  r->fix_stale = fix_stale != 0;
+  const int npix = cam.W * cam.H;
+  r->sp.assign(npix, Shared());
+  for (auto& s : r->sp) s.r = r0;  // initializeSharedPoints (SPPM.cpp:356-373)
+  r->hp.assign(npix, HitPoint());
+  r->slots.assign((size_t)photons * SLOTS, Photon());
+  r->gather_m.assign(npix, 0);
+  r->gather_phi.assign(npix, V());
+  return r;
+}
+
+void port_destroy(void* h) { delete static_cast<Renderer*>(h); }
+
+void port_set_threads(int32_t n) { omp_set_num_threads(n > 0 ? n : omp_get_num_procs()); }
+int32_t port_max_threads(void) { return omp_get_max_threads(); }
+
+void port_iterate(void* h, int32_t n) {
+  Renderer* r = static_cast<Renderer*>(h);
+  for (int k = 0; k < n; ++k) r->iterate();
+}
+
+// Photon pass only (for a bounded CPU timing sample).
+void port_photon_pass(void* h, int32_t first, int32_t count) {
+  Renderer* r = static_cast<Renderer*>(h);
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int i = first; i < first + count; ++i) r->photon_path(i);
+}
+
+void port_resolve(void* h, float* out) { static_cast<Renderer*>(h)->resolve(out); }
+
+void port_trace_closest(void* h, const float* rays, int32_t n, int32_t* facet, float* tuv) {
+  Renderer* r = static_cast<Renderer*>(h);
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int i = 0; i < n; ++i) {
+    const float* q = rays + 7 * (size_t)i;
+    Ray ray{vp(q), vp(q + 3), q[6]};
+    Hit hit;
+    if (closest(r->bvh, r->F, ray, hit)) {
+      facet[i] = hit.facet;
+      tuv[3 * i] = hit.t; tuv[3 * i + 1] = hit.u; tuv[3 * i + 2] = hit.v;
+    } else {
+      facet[i] = -1;
+      tuv[3 * i] = FLT_MAX; tuv[3 * i + 1] = 0; tuv[3 * i + 2] = 0;
+    }
+  }
+}
+
+void port_trace_any(void* h, const float* rays, int32_t n, int32_t* hit) {
+  Renderer* r = static_cast<Renderer*>(h);
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int i = 0; i < n; ++i) {
+    const float* q = rays + 8 * (size_t)i;
+    hit[i] = any_hit(r->bvh, r->F, Ray{vp(q), vp(q + 3), 1.0f}, q[6], q[7]) ? 1 : 0;
+  }
+}
+
+// Hitpoints of the last iteration: type, facet; pos/nrm/out/w (3 floats each), rough.
+void port_read_hitpoints(void* h, int32_t* type, int32_t* facet, float* pos, float* nrm, float* out, float* w,
+                         float* rough) {
+  Renderer* r = static_cast<Renderer*>(h);
+  for (size_t i = 0; i < r->hp.size(); ++i) {
+    const HitPoint& p = r->hp[i];
+    type[i] = p.type;
+    facet[i] = p.facet;
+    const V* src[4] = {&p.pos, &p.normal, &p.out, &p.weight};
+    float* dst[4] = {pos, nrm, out, w};
+    for (int k = 0; k < 4; ++k) { dst[k][3 * i] = src[k]->x; dst[k][3 * i + 1] = src[k]->y; dst[k][3 * i + 2] = src[k]->z; }
+    rough[i] = p.rough;
+  }
+}
+
+int64_t port_num_photons(void* h) { return (int64_t) static_cast<Renderer*>(h)->photons.size(); }
+
+// Compacted photons of the last iteration: N x 11 {pos, flux, dir, index, pdf}, path, slot.
+void port_read_photons(void* h, float* ph, int32_t* path, int32_t* slot) {
+  Renderer* r = static_cast<Renderer*>(h);
+  for (size_t i = 0; i < r->photons.size(); ++i) {
+    const Photon& p = r->photons[i];
+    float* d = ph + 11 * i;
+    d[0] = p.pos.x; d[1] = p.pos.y; d[2] = p.pos.z;
+    d[3] = p.flux.x; d[4] = p.flux.y; d[5] = p.flux.z;
+    d[6] = p.dir.x; d[7] = p.dir.y; d[8] = p.dir.z;
+    d[9] = p.index; d[10] = p.pdf;
+    path[i] = r->ph_path[i];
+    slot[i] = r->ph_slot[i];
+  }
+}
+
+void port_read_gather(void* h, int32_t* m, float* phi) {
+  Renderer* r = static_cast<Renderer*>(h);
+  for (size_t i = 0; i < r->gather_m.size(); ++i) {
+    m[i] = r->gather_m[i];
+    phi[3 * i] = r->gather_phi[i].x; phi[3 * i + 1] = r->gather_phi[i].y; phi[3 * i + 2] = r->gather_phi[i].z;
+  }
+}
+
+void port_read_state(void* h, float* rad, int32_t* n, float* rr, int32_t* g) {
+  Renderer* r = static_cast<Renderer*>(h);
+  for (size_t i = 0; i < r->sp.size(); ++i) {
+    const Shared& s = r->sp[i];
+    rad[3 * i] = s.rad.x; rad[3 * i + 1] = s.rad.y; rad[3 * i + 2] = s.rad.z;
+    n[i] = s.n;
+    rr[i] = s.r;
+    g[i] = s.g;
+  }
+}
+
+// Radius query over given hitpoints (x, y, z, R) and photons (x, y, z): counts.
+void port_radius_count(const float* hp, int32_t nh, const float* ph, int32_t np, int32_t* counts) {
+  Renderer r;
+  r.photons.resize(np);
+  for (int i = 0; i < np; ++i) r.photons[i].pos = vp(ph + 3 * (size_t)i);
+  std::vector<int> ids(np);
+  for (int i = 0; i < np; ++i) ids[i] = i;
+  r.kd.reserve(np);
+  r.kd_build(ids, 0, np);
+#pragma omp parallel for schedule(dynamic, 64)
+  for (int i = 0; i < nh; ++i) {
+    const V x = vp(hp + 4 * (size_t)i);
+    const float R = hp[4 * (size_t)i + 3];
+    int m = 0;
+    r.query(r.kd.empty() ? -1 : 0, x - R * V(1, 1, 1), x + R * V(1, 1, 1), x, R * R, [&](int) { ++m; });
+    counts[i] = m;
+  }
+}
+
+// Philox4x32-10 block, for known-answer tests.
+void port_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]) {
+  Rng::philox(ctr[0], ctr[1], ctr[2], ctr[3], key[0], key[1], out);
+}
+
+}  // extern "C"

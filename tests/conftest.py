@@ -7,7 +7,8 @@ import pytest
 REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 PKG = os.path.join(REPO, 'friendsrender-r-public_gb300')
 GOLDEN = os.path.join(REPO, 'tests', 'golden')
-for p in (PKG, REPO):
+ORACLE = os.path.join(REPO, 'oracle')
+for p in (PKG, REPO, ORACLE):
     if p not in sys.path:
         sys.path.insert(0, p)
 

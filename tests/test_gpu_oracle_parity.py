@@ -1,0 +1,68 @@
+"""GPU path against the oracle (the CPU restatement pinned to the reference)
+on larger seeded cases than the golden fixtures hold."""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    # name: (scene factory, photons, iterations, alpha, radius)
+    'cornell96': (lambda s: s.cornell_box(width=96, height=96), 20000, 4, 0.7, 0.02),
+    'mixed128x72': (lambda s: s.mixed_materials(width=128, height=72, n_spheres=24, field_n=48, tex_size=128,
+                                                light_tex=64, n_lat=12, n_lon=16, extent=0.8, aperture=0.05),
+                    20000, 3, 0.7, 0.02),
+}
+
+
+def _scene(name):
+    from frsppm import scenes
+    return CASES[name][0](scenes)
+
+
+@pytest.mark.parametrize('name', sorted(CASES))
+def test_gpu_matches_oracle(name):
+    import port_abi
+    from frsppm import abi
+    _, photons, iters, alpha, radius = CASES[name]
+    scene = _scene(name)
+    with abi.Renderer(scene, photons, alpha=alpha, radius=radius) as g, \
+            port_abi.PortRenderer(scene, photons, alpha=alpha, radius=radius) as c:
+        for s in range(iters):
+            g.iterate(1)
+            c.iterate(1)
+            hg, hc = g.read_hitpoints(), c.read_hitpoints()
+            np.testing.assert_array_equal(hg['type'] == 1, hc['type'] == 1)
+            h = hc['type'] == 1
+            np.testing.assert_array_equal(hg['facet'][h], hc['facet'][h])
+            np.testing.assert_array_equal(hg['pos'][h], hc['pos'][h])
+            pg, path_g, slot_g = g.compacted_photons()
+            pc, path_c, slot_c = c.compacted_photons()
+            np.testing.assert_array_equal(path_g, path_c)
+            np.testing.assert_array_equal(slot_g, slot_c)
+            np.testing.assert_array_equal(pg[:, :3], pc[:, :3])
+            mg, _ = g.read_gather()
+            mc, _ = c.read_gather()
+            np.testing.assert_array_equal(mg, mc)
+            sg, sc = g.read_state(), c.read_state()
+            np.testing.assert_array_equal(sg['n'], sc['n'])
+            np.testing.assert_array_equal(sg['r'], sc['r'])
+            assert np.abs(sg['tau'] - sc['tau']).max() <= 1e-4 * np.abs(sc['tau']).max()
+        ig, ic = g.resolve(), c.resolve()
+    assert np.abs(ig - ic).max() <= 1e-4 * np.abs(ic).max()
+    big = np.abs(ic) > 1e-3 * np.abs(ic[:, :3]).max()
+    assert (np.abs(ig - ic)[big] / np.abs(ic)[big]).max() < 1e-4
+
+
+def test_gpu_radius_query_matches_oracle_large():
+    """Counts at 200k photons / 50k hitpoints on surfaces, against the oracle's kd-tree."""
+    import port_abi
+    from frsppm import abi, scenes
+    rng = np.random.Generator(np.random.PCG64(11))
+    ph = rng.uniform(-2, 2, (200_000, 3)).astype(np.float32)
+    ph[:, 1] = rng.choice([0.0, 0.3, 1.7], len(ph))
+    hp = rng.uniform(-2, 2, (50_000, 3)).astype(np.float32)
+    hp[:, 1] = rng.choice([0.0, 0.3, 1.7], len(hp))
+    R = rng.uniform(0.002, 0.05, len(hp)).astype(np.float32)
+    with abi.Renderer(scenes.cornell_box(width=8, height=8), 16) as r:
+        got, _ = r.radius_query(hp, R, ph, 0.04)
+    np.testing.assert_array_equal(got, port_abi.radius_count(hp, R, ph))
