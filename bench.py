@@ -1,0 +1,300 @@
+"""Benchmark: SPPM iterations of the mixed-materials workload on GB300.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one SPPM iteration (eye pass over every pixel, photon pass of the
+iteration's photon paths, photon grid build, gather + N/tau/R update) of the
+mixed-materials scene: 997,444 triangles (200 seeded UV spheres + a 512^2
+value-noise height field), diffuse / specular / GGX conductor / GGX
+dielectric materials, 1024^2 albedo/roughness/normal textures, a 512^2
+textured area light, a 1280x720 thin-lens camera (aperture 0.02), 1M photon
+paths per iteration, alpha 0.7, initial radius 0.02.
+
+value: photon paths/s over all GPUs, inputs resident in HBM, CUDA events on
+the renderer's stream, L2 flushed (256 MB write) before every timed step.
+e2e: the same metric through the C-ABI with a host result buffer: every step
+is fr_iterate + fr_resolve into pinned host memory (the image, read back each
+step); the scene is uploaded once by fr_create (reported as setup).
+--impl reference: the CPU restatement of the reference path (oracle/port,
+pinned bit-exact to the reference's own outputs) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, 'friendsrender-r-public_gb300'))
+
+METRIC = 'photon paths/s; equal-time relMSE vs FP64 ref, guided vs plain SPPM, 1 GB300'
+UNIT = 'photon paths/s'
+PHOTONS = 1_000_000
+ALPHA, RADIUS = 0.7, 0.02
+WORKLOAD = ('mixed materials: 997,444 triangles (200 UV spheres + 512^2 height field), 4 surface types, '
+            '1024^2 RGBA8 albedo/roughness/normal textures, 512^2 textured light, 1280x720 thin lens '
+            'aperture 0.02, 1M photon paths/iteration, alpha 0.7, r0 0.02')
+
+
+def dist_env():
+    return int(os.environ.get('RANK', 0)), int(os.environ.get('WORLD_SIZE', 1)), int(os.environ.get('LOCAL_RANK', 0))
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons every 200 ms while active."""
+    Q = ('clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,'
+         'clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,'
+         'clocks_event_reasons.sw_power_cap')
+
+    def __init__(self, gpu):
+        self.gpu = gpu
+        self.p = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(['nvidia-smi', '-i', str(self.gpu), '--query-gpu=' + self.Q,
+                                       '--format=csv,noheader,nounits', '-lms', '200'],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.p = None
+        return self
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], 0.0, set()
+        names = ['hw_slowdown', 'hw_thermal_slowdown', 'sw_thermal_slowdown', 'sw_power_cap']
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(',')]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx = max(mx, float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[3:7]):
+                if v.lower() == 'active':
+                    reasons.add(n)
+        return {'sm_mhz': statistics.median(sm) if sm else None, 'sm_max_mhz': mx or None,
+                'reasons': sorted(reasons), 'samples': len(sm)}
+
+
+def measured_peaks():
+    p = os.path.join(REPO, 'MEASURED_PEAKS.json')
+    if os.path.exists(p):
+        d = json.load(open(p))
+        return d.get('hbm_gbs', 6800.0), 'measured'
+    return 6800.0, 'fallback'
+
+
+def cpu_baseline(scene, seconds_target=20.0):
+    """The oracle (CPU restatement of the reference path) on the host cores:
+    full iterations of the same workload, as many as fit ~seconds_target."""
+    sys.path.insert(0, os.path.join(REPO, 'oracle'))
+    import port_abi
+    port_abi.set_threads(os.cpu_count() or 1)
+    threads = port_abi.max_threads()
+    with port_abi.PortRenderer(scene, PHOTONS, alpha=ALPHA, radius=RADIUS) as r:
+        t0 = time.perf_counter()
+        r.iterate(1)
+        first = time.perf_counter() - t0
+        n = max(1, min(4, int(seconds_target / max(first, 1e-3)) - 1))
+        t0 = time.perf_counter()
+        r.iterate(n)
+        dt = time.perf_counter() - t0
+    return {'value': PHOTONS * n / dt, 'unit': UNIT, 'cores': threads, 'kind': 'port',
+            'sample': '%d full iterations of the workload (1M paths each) after 1 untimed, %d OpenMP threads, '
+                      '%.2f s' % (n, threads, dt)}
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return 0
+    from frsppm import scenes
+    sys.path.insert(0, os.path.join(REPO, 'oracle'))
+    import port_abi
+    port_abi.set_threads(os.cpu_count() or 1)
+    threads = port_abi.max_threads()
+    scene = scenes.mixed_materials()
+    # Each step is one iteration of the workload; the photon count per step is
+    # reduced when K + W full iterations would run past ~3 minutes.
+    budget = 150.0 / max(1, args.steps + args.warmup)
+    photons = PHOTONS
+    with port_abi.PortRenderer(scene, PHOTONS, alpha=ALPHA, radius=RADIUS) as r:
+        t0 = time.perf_counter()
+        r.iterate(1)
+        per_full = time.perf_counter() - t0
+    if per_full > budget:
+        photons = max(50_000, int(PHOTONS * budget / per_full))
+    with port_abi.PortRenderer(scene, photons, alpha=ALPHA, radius=RADIUS) as r:
+        for _ in range(args.warmup):
+            r.iterate(1)
+        t0 = time.perf_counter()
+        r.iterate(args.steps)
+        dt = time.perf_counter() - t0
+    value = photons * args.steps / dt
+    sample = ('%d iterations of %d photon paths each (full 1280x720 eye pass, grid, gather) after %d warm-up, '
+              '%d OpenMP threads' % (args.steps, photons, args.warmup, threads))
+    out = {'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
+           'warmup': args.warmup, 'ms_per_step': dt * 1000.0 / args.steps, 'higher_is_better': True,
+           'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded scene)',
+           'config': {'workload': WORKLOAD, 'photons_per_step': photons}, 'impl': 'reference',
+           'cpu_baseline': {'value': value, 'unit': UNIT, 'cores': threads, 'kind': 'port', 'sample': sample},
+           'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
+    print(json.dumps(out))
+    return 0
+
+
+def stage_bytes(stage, npix, hits, photons_stored, paths):
+    """Algorithmic DRAM bytes of one launch of a stage (the figures the
+    roofline's achieved GB/s is computed from)."""
+    if stage == 'eye':
+        return npix * (64 + 4)                     # hitpoint record write + radius read
+    if stage == 'photon':
+        return photons_stored * 48 + paths * 4     # photon slots written + per-path count
+    if stage == 'grid':
+        # count: photon position read + key/rank write; scatter: key/rank + 48 B read, 48 B write
+        return photons_stored * (16 + 8 + 8 + 48 + 48)
+    # gather/update: hitpoint record + radius read, each stored photon read once,
+    # tau (3 x f64) read+write, N/R/G read+write, M and flux debug write
+    return hits * (64 + 4 + 48 + 12 + 12 + 20) + photons_stored * 48
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument('--gpus', type=int, default=1)
+    ap.add_argument('--steps', type=int, default=10)
+    ap.add_argument('--warmup', type=int, default=3)
+    ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
+    ap.add_argument('--no-cpu-baseline', action='store_true')
+    ap.add_argument('--photons', type=int, default=PHOTONS)
+    args = ap.parse_args()
+    if args.impl == 'reference':
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+    from frsppm import abi, scenes
+
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group('nccl')
+    W = max(3, args.warmup)
+    scene = scenes.mixed_materials()
+    t0 = time.perf_counter()
+    r = abi.Renderer(scene, args.photons, alpha=ALPHA, radius=RADIUS)
+    setup_s = time.perf_counter() - t0
+    stats = r.stats()
+    npix = r.width * r.height
+    stream = torch.cuda.ExternalStream(r.stream())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device='cuda')
+    r.iterate(W)
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # ---- device-timed region
+    r.profile(True, max_iterations=args.steps)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    l0 = r.profile_read()[2]
+    r.profile(True, max_iterations=args.steps)
+    barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        for k in range(args.steps):
+            with torch.cuda.stream(stream):
+                flush.zero_()
+                evs[k][0].record(stream)
+            r.iterate(1, sync=False)
+            evs[k][1].record(stream)
+        stream.synchronize()
+    torch.cuda.synchronize()
+    barrier()
+    stage_ms, stage_n, l1 = r.profile_read()
+    r.profile(False)
+    total_ms = sum(a.elapsed_time(b) for a, b in evs)
+    if world > 1:
+        t = torch.tensor([total_ms], device='cuda')
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    launches = l1 - l0
+
+    # ---- photon / hitpoint counts of the last iteration (for the algorithmic bytes)
+    counts = np.empty(r.photons, np.uint32)
+    abi._check(abi._lib.fr_read_photon_slots(r.h, None, None, None, abi._ptr(counts)), 'fr_read_photon_slots')
+    stored = int(counts.sum())
+    hits = int((r.read_hitpoints()['type'] == 1).sum())
+
+    # ---- end to end through the C-ABI with a pinned host result buffer
+    host = torch.empty((npix, 4), dtype=torch.float32, pin_memory=True)
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r.iterate(1, sync=False)
+        abi._check(abi._lib.fr_resolve(r.h, abi.C.c_void_p(host.data_ptr())), 'fr_resolve')
+    e2e_s = time.perf_counter() - t0
+    if world > 1:
+        t = torch.tensor([e2e_s], device='cuda')
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    r.close()
+
+    if rank != 0:
+        return 0
+    value = world * args.photons * args.steps / (total_ms / 1000.0)
+    per = {k: stage_ms[k] / max(1, stage_n[k]) for k in stage_ms}
+    dom = max(per, key=per.get)
+    peak, peak_kind = measured_peaks()
+    bytes_dom = stage_bytes(dom, npix, hits, stored, args.photons)
+    achieved = bytes_dom / (per[dom] / 1000.0) / 1e9
+    out = {
+        'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps, 'warmup': W,
+        'ms_per_step': total_ms / args.steps, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
+        'dtype': 'f32', 'data': 'synthetic (seeded scene, random-init textures)',
+        'config': {'workload': WORKLOAD, 'photons_per_step': args.photons, 'pixels': npix,
+                   'triangles': stats['triangles'], 'l2': 'flushed (256 MB write) before every timed step',
+                   'parallelism': 'replicas' if world > 1 else 'single GPU'},
+        'hitpoint_updates_per_s': world * npix * args.steps / (total_ms / 1000.0),
+        'stage_ms_per_step': per,
+        'roofline': {'bound': 'hbm', 'kernel': dom, 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
+                     'frac': achieved / peak, 'traffic': None, 'peak_source': peak_kind,
+                     'algorithmic_bytes_per_launch': bytes_dom},
+        'e2e': {'value': world * args.photons * args.steps / e2e_s, 'unit': UNIT, 'h2d_bytes_per_step': 0,
+                'd2h_bytes_per_step': npix * 16, 'setup_s': setup_s,
+                'device_bytes': int(stats['device_bytes'])},
+        'gpu_launches': launches,
+        'clocks': clk.summary(),
+        'photons_stored_last_step': stored, 'hitpoints_last_step': hits,
+    }
+    if world == 1 and not args.no_cpu_baseline:
+        out['cpu_baseline'] = cpu_baseline(scene)
+    print(json.dumps(out))
+    return 0
+
+
+if __name__ == '__main__':
+    sys.exit(main())

@@ -178,6 +178,12 @@ struct fr_ctx {
   float4* dbg_phi = nullptr;
   float4* image = nullptr;
   int64_t iterations = 0, photons_total = 0;
+  int64_t launches = 0;  // kernels launched by fr_iterate so far
+  // Stage profiler: events recorded on the stream around each stage.
+  bool profiling = false;
+  std::vector<cudaEvent_t> ev_pool;
+  std::vector<std::pair<int, std::pair<cudaEvent_t, cudaEvent_t>>> ev_marks;  // (stage, (start, stop))
+  size_t ev_used = 0;
 
   template <typename T>
   int alloc(T** out, size_t count) {
@@ -199,6 +205,7 @@ struct fr_ctx {
   }
   ~fr_ctx() {
     if (stream) cudaStreamSynchronize(stream);
+    for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
     for (auto& b : bufs) cudaFree(b.p);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -343,6 +350,23 @@ uint32_t next_pow2(uint64_t v) {
   return (uint32_t)std::min<uint64_t>(p, 1u << 31);
 }
 
+// Records an event pair around one stage when profiling is on.
+struct StageMark {
+  fr_ctx* c;
+  int stage;
+  cudaEvent_t stop = nullptr;
+  StageMark(fr_ctx* ctx, int st) : c(ctx), stage(st) {
+    if (!c->profiling || c->ev_used + 2 > c->ev_pool.size()) return;
+    cudaEvent_t start = c->ev_pool[c->ev_used++];
+    stop = c->ev_pool[c->ev_used++];
+    cudaEventRecord(start, c->stream);
+    c->ev_marks.push_back({stage, {start, stop}});
+  }
+  ~StageMark() {
+    if (stop) cudaEventRecord(stop, c->stream);
+  }
+};
+
 int run_iteration(fr_ctx* c) {
   const uint32_t step = (uint32_t)(++c->iterations);
   IterParams it{};
@@ -353,14 +377,27 @@ int run_iteration(fr_ctx* c) {
   it.alpha = c->alpha;
   it.flags = c->flags;
   cudaStream_t s = c->stream;
-  launch_eye_pass(c->sc, c->cam, it, c->rr_eye, c->hp, c->st, c->gi, c->err, s);
-  launch_photon_pass(c->sc, it, c->ph, c->counts, c->err, s);
-  launch_grid_setup(c->gi, c->sc, c->cell_scale, c->r0, s);
-  FR_CUDA(cudaMemsetAsync(c->grid.cell_count, 0, sizeof(uint32_t) * (size_t)c->grid.table, s));
-  launch_photon_count(c->ph, c->counts, c->P, kPhotonSlots, c->grid, c->gi, s);
-  launch_scan(c->grid.cell_count, c->grid.cell_start, c->grid.table + 1, c->scan, s);
-  launch_photon_scatter(c->ph, c->counts, c->P, kPhotonSlots, c->grid, s);
-  launch_gather_update(c->sc, it, c->hp, c->grid, c->gi, c->st, c->dbg_m, c->dbg_phi, s);
+  {
+    StageMark m(c, FR_STAGE_EYE);
+    launch_eye_pass(c->sc, c->cam, it, c->rr_eye, c->hp, c->st, c->gi, c->err, s);
+  }
+  {
+    StageMark m(c, FR_STAGE_PHOTON);
+    launch_photon_pass(c->sc, it, c->ph, c->counts, c->err, s);
+  }
+  {
+    StageMark m(c, FR_STAGE_GRID);
+    launch_grid_setup(c->gi, c->sc, c->cell_scale, c->r0, s);
+    FR_CUDA(cudaMemsetAsync(c->grid.cell_count, 0, sizeof(uint32_t) * (size_t)c->grid.table, s));
+    launch_photon_count(c->ph, c->counts, c->P, kPhotonSlots, c->grid, c->gi, s);
+    c->launches += launch_scan(c->grid.cell_count, c->grid.cell_start, c->grid.table + 1, c->scan, s);
+    launch_photon_scatter(c->ph, c->counts, c->P, kPhotonSlots, c->grid, s);
+  }
+  {
+    StageMark m(c, FR_STAGE_GATHER);
+    launch_gather_update(c->sc, it, c->hp, c->grid, c->gi, c->st, c->dbg_m, c->dbg_phi, s);
+  }
+  c->launches += 6;  // eye, photon, grid setup, count, scatter, gather/update
   c->photons_total += c->P;
   FR_CUDA(cudaGetLastError());
   return FR_OK;
@@ -591,6 +628,40 @@ void* fr_stream(fr_ctx* c) { return c ? (void*)c->stream : nullptr; }
 
 void fr_destroy(fr_ctx* c) { delete c; }
 
+int fr_profile_enable(fr_ctx* c, int32_t on, int32_t max_iterations) {
+  if (!c) return fail(FR_ERR_INVALID, "fr_profile_enable: NULL context");
+  FR_CUDA(cudaStreamSynchronize(c->stream));
+  c->ev_marks.clear();
+  c->ev_used = 0;
+  c->profiling = on != 0;
+  const size_t need = on ? (size_t)std::max(1, max_iterations) * FR_STAGES * 2 : 0;
+  while (c->ev_pool.size() < need) {
+    cudaEvent_t e;
+    FR_CUDA(cudaEventCreate(&e));
+    c->ev_pool.push_back(e);
+  }
+  return FR_OK;
+}
+
+int fr_profile_read(fr_ctx* c, double* stage_ms, int64_t* stage_count, int64_t* launches) {
+  if (!c) return fail(FR_ERR_INVALID, "fr_profile_read: NULL context");
+  FR_CUDA(cudaStreamSynchronize(c->stream));
+  for (int k = 0; k < FR_STAGES; ++k) {
+    if (stage_ms) stage_ms[k] = 0.0;
+    if (stage_count) stage_count[k] = 0;
+  }
+  for (auto& m : c->ev_marks) {
+    float ms = 0.f;
+    FR_CUDA(cudaEventElapsedTime(&ms, m.second.first, m.second.second));
+    if (stage_ms) stage_ms[m.first] += ms;
+    if (stage_count) stage_count[m.first] += 1;
+  }
+  if (launches) *launches = c->launches;
+  c->ev_marks.clear();
+  c->ev_used = 0;
+  return FR_OK;
+}
+
 int fr_trace_closest(fr_ctx* c, const float* rays, int32_t n, int32_t* facet, float* tuv) {
   if (!c || n < 0 || (n && (!rays || !facet || !tuv))) return fail(FR_ERR_INVALID, "fr_trace_closest: bad arguments");
   if (!n) return FR_OK;
@@ -629,6 +700,11 @@ int fr_radius_query(fr_ctx* c, const float* hp, int32_t nh, const float* photons
       (pairs && !pair_count))
     return fail(FR_ERR_INVALID, "fr_radius_query: bad arguments");
   if (!nh) return FR_OK;
+  if (!np) {
+    std::fill(counts, counts + nh, 0);
+    if (pair_count) *pair_count = 0;
+    return FR_OK;
+  }
   // Flat photon list (one photon per "path", stride 1) through the same grid kernels.
   std::vector<float4> pos(std::max(np, 1)), zero(std::max(np, 1), make_float4(0.f, 0.f, 0.f, 0.f));
   float lo[3] = {1e30f, 1e30f, 1e30f};

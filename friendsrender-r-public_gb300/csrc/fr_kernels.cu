@@ -581,7 +581,8 @@ uint32_t scan_temp_words(uint32_t n, ScanTemp& t) {
   return words;
 }
 
-void launch_scan(uint32_t* in, uint32_t* out, uint32_t n, ScanTemp& t, cudaStream_t s) {
+int launch_scan(uint32_t* in, uint32_t* out, uint32_t n, ScanTemp& t, cudaStream_t s) {
+  int launches = 1;
   // Exclusive scan: tiles, then the tile sums (recursively), then the add-back.
   const uint32_t nb = (n + kScanTile - 1) / kScanTile;
   k_scan_tile<<<nb, kScanBlock, 0, s>>>(in, out, n, t.level[0]);
@@ -590,6 +591,7 @@ void launch_scan(uint32_t* in, uint32_t* out, uint32_t n, ScanTemp& t, cudaStrea
   while (cur_n > 1) {
     const uint32_t nb2 = (cur_n + kScanTile - 1) / kScanTile;
     k_scan_tile<<<nb2, kScanBlock, 0, s>>>(t.level[lvl], t.level[lvl], cur_n, t.level[lvl + 1]);
+    ++launches;
     cur_n = nb2;
     ++lvl;
   }
@@ -597,8 +599,13 @@ void launch_scan(uint32_t* in, uint32_t* out, uint32_t n, ScanTemp& t, cudaStrea
   for (int l = lvl - 2; l >= 0; --l) {
     const uint32_t nn = t.level_n[l];
     k_scan_add<<<(nn + kScanTile - 1) / kScanTile, kScanBlock, 0, s>>>(t.level[l], nn, t.level[l + 1]);
+    ++launches;
   }
-  if (nb > 1) k_scan_add<<<nb, kScanBlock, 0, s>>>(out, n, t.level[0]);
+  if (nb > 1) {
+    k_scan_add<<<nb, kScanBlock, 0, s>>>(out, n, t.level[0]);
+    ++launches;
+  }
+  return launches;
 }
 
 void launch_gather_update(const SceneGPU& sc, const IterParams& it, HitpointBuf hp, PhotonGrid g, const GridInfo* gi,

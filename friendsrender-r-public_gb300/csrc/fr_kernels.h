@@ -75,7 +75,8 @@ void launch_grid_setup(GridInfo* gi, const SceneGPU& sc, float cell_scale, float
 // stride: slots per path (kPhotonSlots for the render loop, 1 for a flat photon list).
 void launch_photon_count(PhotonSlots ph, const uint32_t* counts, int paths, int stride, PhotonGrid g,
                          const GridInfo* gi, cudaStream_t s);
-void launch_scan(uint32_t* data_in, uint32_t* data_out, uint32_t n, ScanTemp& tmp, cudaStream_t s);
+// Returns the number of kernels launched.
+int launch_scan(uint32_t* data_in, uint32_t* data_out, uint32_t n, ScanTemp& tmp, cudaStream_t s);
 void launch_photon_scatter(PhotonSlots ph, const uint32_t* counts, int paths, int stride, PhotonGrid g,
                            cudaStream_t s);
 // Words of block-sum scratch launch_scan needs for n elements; fills the level sizes of t.

@@ -56,7 +56,10 @@ class Stats(C.Structure):
 # Every symbol include/friendsrender.h declares.
 EXPORTS = ['fr_last_error', 'fr_create', 'fr_iterate', 'fr_synchronize', 'fr_resolve', 'fr_resolve_dev',
            'fr_get_stats', 'fr_stream', 'fr_destroy', 'fr_trace_closest', 'fr_trace_any', 'fr_radius_query',
-           'fr_read_hitpoints', 'fr_read_photon_slots', 'fr_read_gather', 'fr_read_state']
+           'fr_read_hitpoints', 'fr_read_photon_slots', 'fr_read_gather', 'fr_read_state', 'fr_profile_enable',
+           'fr_profile_read']
+
+STAGES = ('eye', 'photon', 'grid', 'gather')
 
 _lib = None
 
@@ -89,6 +92,8 @@ def load(path=None):
     lib.fr_read_photon_slots.argtypes = [vp, vp, vp, vp, vp]
     lib.fr_read_gather.argtypes = [vp, vp, vp]
     lib.fr_read_state.argtypes = [vp, vp, vp, vp, vp]
+    lib.fr_profile_enable.argtypes = [vp, i32, i32]
+    lib.fr_profile_read.argtypes = [vp, vp, vp, vp]
     _lib = lib
     return lib
 
@@ -172,6 +177,16 @@ class Renderer:
 
     def stream(self):
         return _lib.fr_stream(self.h)
+
+    def profile(self, on, max_iterations=256):
+        _check(_lib.fr_profile_enable(self.h, int(on), int(max_iterations)), 'fr_profile_enable')
+
+    def profile_read(self):
+        ms = np.zeros(len(STAGES), np.float64)
+        cnt = np.zeros(len(STAGES), np.int64)
+        launches = np.zeros(1, np.int64)
+        _check(_lib.fr_profile_read(self.h, _ptr(ms), _ptr(cnt), _ptr(launches)), 'fr_profile_read')
+        return dict(zip(STAGES, ms.tolist())), dict(zip(STAGES, cnt.tolist())), int(launches[0])
 
     def resolve(self):
         out = np.empty((self.width * self.height, 4), np.float32)

@@ -155,6 +155,16 @@ void* fr_stream(fr_ctx* ctx);
 
 void fr_destroy(fr_ctx* ctx);
 
+/* Stage profiler.  While enabled, fr_iterate records CUDA events on the
+ * context's stream around each stage of an iteration (FR_STAGE_*);
+ * fr_profile_read synchronizes, returns the summed milliseconds and the
+ * number of timed launches per stage, then clears them.  max_iterations
+ * bounds the iterations profiled between reads (events are created here).
+ * *launches is the number of kernels fr_iterate has launched so far. */
+enum { FR_STAGE_EYE = 0, FR_STAGE_PHOTON = 1, FR_STAGE_GRID = 2, FR_STAGE_GATHER = 3, FR_STAGES = 4 };
+int fr_profile_enable(fr_ctx* ctx, int32_t on, int32_t max_iterations);
+int fr_profile_read(fr_ctx* ctx, double* stage_ms, int64_t* stage_count, int64_t* launches);
+
 /* ---------------------------------------------------------------- parity
  * Entry points the parity tests drive; each synchronizes before returning. */
 
