@@ -463,7 +463,7 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
                                (hi[2] - lo[2]) * (hi[2] - lo[2]));
   BVHResult bvh = build_bvh8(scene->positions, T, 1e-5f * diag + 1e-7f);
   c->bvh_depth = bvh.depth;
-  if (bvh.depth * 7 + 1 > 64) return bail(fail(FR_ERR_INVALID, "BVH depth %d exceeds the traversal stack", bvh.depth));
+  if (bvh.depth * 7 + 1 > kTraversalStackEntries) return bail(fail(FR_ERR_INVALID, "BVH depth %d exceeds the traversal stack", bvh.depth));
   std::vector<TriGPU> tris(T);
   for (int k = 0; k < T; ++k) {
     const int f = bvh.tri_order[k];

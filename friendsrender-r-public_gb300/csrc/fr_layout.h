@@ -131,6 +131,9 @@ struct IterParams {
 
 constexpr uint32_t kFlagFixStaleSlot = 1u;  // drop the stale photon slot quirk (SPPM.cpp:672)
 
+// Entries of the per-thread traversal stack (a wide node pushes at most 7).
+constexpr int kTraversalStackEntries = 96;
+
 // Device error word bits.
 constexpr int kErrStack = 1;        // traversal stack overflow
 constexpr int kErrTableFull = 2;    // photon cell table overflow

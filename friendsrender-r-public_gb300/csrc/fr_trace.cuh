@@ -14,7 +14,7 @@
 
 namespace fr {
 
-constexpr int kTraversalStack = 64;
+constexpr int kTraversalStack = kTraversalStackEntries;
 
 struct Hit {
   float t, u, v;
