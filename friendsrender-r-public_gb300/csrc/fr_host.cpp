@@ -783,6 +783,15 @@ int fr_radius_query(fr_ctx* c, const float* hp, int32_t nh, const float* photons
   return rc;
 }
 
+int fr_radius_count_noalloc(const float* hp_dev, int32_t num_hitpoints, const float* photons_dev,
+                            int32_t num_photons, float cell, int32_t* counts_dev, void* stream) {
+  const char* msg = "";
+  const int rc = radius_count_noalloc(hp_dev, num_hitpoints, photons_dev, num_photons, cell, counts_dev,
+                                      static_cast<cudaStream_t>(stream), &msg);
+  if (rc) return fail(rc, "%s", msg);
+  return FR_OK;
+}
+
 int fr_read_hitpoints(fr_ctx* c, float* pos_type, float* nrm_rough, float* out_mat, float* wgt_facet) {
   if (!c) return fail(FR_ERR_INVALID, "fr_read_hitpoints: NULL context");
   const size_t bytes = sizeof(float4) * (size_t)c->W * c->H;

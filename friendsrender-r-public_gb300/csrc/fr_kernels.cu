@@ -16,6 +16,7 @@
 #include <cfloat>
 #include <cstdint>
 #include "fr_bsdf.cuh"
+#include "fr_grid.cuh"
 #include "fr_kernels.h"
 #include "fr_layout.h"
 #include "fr_math.cuh"
@@ -277,12 +278,6 @@ __global__ void __launch_bounds__(128) k_photon_pass(SceneGPU sc, IterParams it,
 }
 
 // ------------------------------------------------------------- photon grid
-__device__ __forceinline__ int cell_of(float p, float o, float inv) { return (int)floorf((p - o) * inv); }
-
-__device__ __forceinline__ uint32_t cell_hash(int x, int y, int z, uint32_t mask) {
-  return (((uint32_t)x * 73856093u) ^ ((uint32_t)y * 19349663u) ^ ((uint32_t)z * 83492791u)) & mask;
-}
-
 // Cell edge for this iteration from the mean radius of its hitpoints; resets
 // the accumulators for the next iteration's eye pass.
 __global__ void k_grid_setup(GridInfo* gi, SceneGPU sc, float cell_scale, float r0) {

@@ -92,4 +92,8 @@ void launch_trace_any(const SceneGPU& sc, const float* rays, int n, int32_t* hit
 void launch_radius_count(const float4* hp_pos_r, int nh, PhotonGrid g, const GridInfo* gi, int32_t* m,
                          uint32_t* pairs, uint32_t pair_cap, uint32_t* pair_count, cudaStream_t s);
 
+// Radius count with the fixed scratch of fr_noalloc.cu (allocates nothing).
+int radius_count_noalloc(const float* hp_dev, int32_t nh, const float* photons_dev, int32_t np, float cell,
+                         int32_t* counts_dev, cudaStream_t stream, const char** msg);
+
 }  // namespace fr

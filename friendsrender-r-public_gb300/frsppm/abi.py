@@ -57,7 +57,7 @@ class Stats(C.Structure):
 EXPORTS = ['fr_last_error', 'fr_create', 'fr_iterate', 'fr_synchronize', 'fr_resolve', 'fr_resolve_dev',
            'fr_get_stats', 'fr_stream', 'fr_destroy', 'fr_trace_closest', 'fr_trace_any', 'fr_radius_query',
            'fr_read_hitpoints', 'fr_read_photon_slots', 'fr_read_gather', 'fr_read_state', 'fr_profile_enable',
-           'fr_profile_read']
+           'fr_profile_read', 'fr_radius_count_noalloc']
 
 STAGES = ('eye', 'photon', 'grid', 'gather')
 
@@ -94,6 +94,7 @@ def load(path=None):
     lib.fr_read_state.argtypes = [vp, vp, vp, vp, vp]
     lib.fr_profile_enable.argtypes = [vp, i32, i32]
     lib.fr_profile_read.argtypes = [vp, vp, vp, vp]
+    lib.fr_radius_count_noalloc.argtypes = [vp, i32, vp, i32, f32, vp, vp]
     _lib = lib
     return lib
 

@@ -187,6 +187,26 @@ int fr_radius_query(fr_ctx* ctx, const float* hp, int32_t num_hitpoints, const f
                     int32_t num_photons, float cell, int32_t* counts, uint32_t* pairs, uint32_t pair_capacity,
                     uint32_t* pair_count);
 
+/* Radius count that allocates nothing.  No counterpart in the reference.
+ *
+ * For callers that cannot let the library call cudaMalloc: cudaMalloc and
+ * cudaFree synchronize the whole device (stalling work on other streams),
+ * and applications that hand out all device memory from their own pool at
+ * start-up cannot have a library allocate on its own.  Same query as
+ * fr_radius_query (counts only), with device pointers: hp_dev holds
+ * num_hitpoints x {x, y, z, R} floats, photons_dev num_photons x {x, y, z}
+ * floats, counts_dev receives num_hitpoints counts; the work is enqueued on
+ * `stream` (a cudaStream_t, NULL for the default stream) and not waited for.
+ * All intermediate buffers are fixed device arrays inside the library, sized
+ * for FR_NOALLOC_MAX_PHOTONS photons (about 10.5 MB, held by every GPU that
+ * loads the library until exit); more photons return FR_ERR_INVALID.  The
+ * first call on a device looks up those arrays' device addresses: make it
+ * before any stream capture.  Calls share the arrays (each call clears what
+ * must start at zero), so calls that overlap on the GPU race. */
+#define FR_NOALLOC_MAX_PHOTONS 262144
+int fr_radius_count_noalloc(const float* hp_dev, int32_t num_hitpoints, const float* photons_dev,
+                            int32_t num_photons, float cell, int32_t* counts_dev, void* stream);
+
 /* Hitpoints of the last iteration (SoA, see HitpointBuf in the kernels):
  * each array width*height*4 floats; any pointer may be NULL. */
 int fr_read_hitpoints(fr_ctx* ctx, float* pos_type, float* nrm_rough, float* out_mat, float* wgt_facet);
