@@ -4,9 +4,10 @@
 // Each function restates the reference's arithmetic in its own evaluation
 // order and precision.  Where the reference's expression is promoted to
 // double (a double literal or a double-returning libm call: sqrt, sincos) the
-// restatement computes in double too; where it calls powf(x, -2.0f) the
-// restatement uses pow_m2; pow(x, 2) is an exact square (the compiler folds
-// it in the reference's build).
+// restatement computes in double too, or reads a table of the exact result;
+// where it calls powf(x, -2.0f) the restatement uses pow_m2; pow(x, 2) is an
+// exact square (the compiler folds it in the reference's build); comparisons
+// of a float with a double constant use the equivalent float threshold.
 #pragma once
 #include "fr_layout.h"
 #include "fr_math.cuh"
@@ -27,27 +28,35 @@ struct FParam {
 
 // Orthonormal frame around e1 used by Cos/GGX sampling (Sampling.cpp:10-18, 132-138).
 __device__ __forceinline__ void frame(V3 e1, V3& e2, V3& e3) {
-  if ((double)fabsf(e1.x) > 0.000001) e2 = normalized(cross(v3(0.f, 1.f, 0.f), e1));
+  if (fabsf(e1.x) > kGt1e6) e2 = normalized(cross(v3(0.f, 1.f, 0.f), e1));
   else e2 = normalized(cross(v3(1.f, 0.f, 0.f), e1));
   e3 = normalized(cross(e1, e2));
 }
 
-// u * 2.0f * PI, which the reference evaluates in double and rounds once.
-__device__ __forceinline__ float two_pi_u(float u) { return (u * 2.0f) * kPI; }
+// Tables of the two double-precision functions of a single 24-bit draw u
+// that the sampling routines use, filled on the host with the host's libm:
+//   c_sincos_tab[u] = {(float)cos(x), (float)sin(x)}, x = (float)((u*2^-24) * 2 * PI)
+//                     (Sampling.cpp:65, 127, 191 evaluate u*2.0f*PI in double and round it once)
+//   c_sqrt1m_tab[u] = (float)sqrt(1.000000001 - u*2^-24)          (Sampling.cpp:24)
+// GB300's FP64 rate is 1/64 of FP32; a table read replaces ~50 FP64
+// instructions per bounce and returns the reference's exact floats.
+constexpr uint32_t kU24 = 1u << 24;
+__constant__ const float2* c_sincos_tab;
+__constant__ const float* c_sqrt1m_tab;
+
+__device__ __forceinline__ float unit24(uint32_t u) { return (float)u * (1.0f / 16777216.0f); }
 
 // Sampling::Cos_Sampling (Sampling.cpp:7-28)
 __device__ __forceinline__ V3 cos_sampling(Rng& rng, V3 normal, float* pdf) {
   V3 e2, e3;
   const V3 e1 = normal;
   frame(e1, e2, e3);
-  const float ph = two_pi_u(rng.next());
-  const float th = rng.next();
-  const float th2 = sqrtf(th);
-  double sd, cd;
-  sincos((double)ph, &sd, &cd);
-  const float c = (float)cd, s = (float)sd;
-  const float r1 = (float)sqrt(1.000000001 - (double)th);
-  V3 result = e1 * r1 + e2 * c * th2 + e3 * s * th2;
+  const uint32_t uph = rng.next_u24();
+  const uint32_t uth = rng.next_u24();
+  const float th2 = sqrtf(unit24(uth));
+  const float2 cs = __ldg(c_sincos_tab + uph);
+  const float r1 = __ldg(c_sqrt1m_tab + uth);
+  V3 result = e1 * r1 + e2 * cs.x * th2 + e3 * cs.y * th2;
   result = normalized(result);
   if (pdf) *pdf = fmaxf(kSMin, dot(result, normal) / kPI);
   return result;
@@ -62,7 +71,7 @@ __device__ __forceinline__ float fresnel_reflectance(V3 n, V3 in, float ni, floa
   const float cosA = fabsf(dot(n, in));
   const float sinA = sqrtf(1.0000001f - cosA * cosA);
   const float sinB = n1_div_n2 * sinA;
-  if ((double)sinB > 0.999999) return 1.0f;
+  if (sinB > kGt0_999999) return 1.0f;
   const float cosB = sqrtf(1.0000001f - sinB * sinB);
   const float rp = (no * cosA - ni * cosB) / (no * cosA + ni * cosB);
   const float rs = (ni * cosA - no * cosB) / (ni * cosA + no * cosB);
@@ -86,7 +95,7 @@ __device__ __forceinline__ V3 microfacet_from_refraction(V3 in, V3 out, float fr
   const float c = fabsf(dot(in, out));
   const float eta = into / from;
   const float isq = eta * eta - 2.0f * eta * c + 1.0f;
-  if ((double)isq < 1e-8) return v3(0.f, 0.f, 0.f);
+  if (isq < kLt1e8) return v3(0.f, 0.f, 0.f);
   const float ss = 1.0f / sqrtf(isq);
   const V3 h = normalized(-eta * ss * out + ss * in);
   return into > from ? h : -h;
@@ -95,20 +104,18 @@ __device__ __forceinline__ V3 microfacet_from_refraction(V3 in, V3 out, float fr
 // Sampling::GGX_Sampling (Sampling.cpp:123-157)
 __device__ __forceinline__ V3 ggx_sampling(Rng& rng, V3 normal, V3 in, float alpha, float* pdf) {
   const V3 e1 = normal;
-  const float phi = two_pi_u(rng.next());
+  const float2 cs = __ldg(c_sincos_tab + rng.next_u24());
   const float e = rng.next();
   const float den = e * (alpha * alpha - 1.0f) + 1.0f;
   const float cth = (float)sqrt((1.0 - (double)e) / (double)den);
   V3 e2, e3;
   frame(e1, e2, e3);
-  double sd, cd;
-  sincos((double)phi, &sd, &cd);
-  const float cph = (float)cd, sph = (float)sd;
+  const float cph = cs.x, sph = cs.y;
   const float sth = sqrtf(1.0f - cth * cth);
   const V3 mN = normalized(e3 * sth * cph + e2 * sth * sph + e1 * cth);
-  if ((double)dot(mN, in) > 0.0) { *pdf = kSMin; return invalid_dir(); }
+  if (dot(mN, in) > 0.0f) { *pdf = kSMin; return invalid_dir(); }
   const V3 result = reflect_sampling(mN, in);
-  if ((double)dot(result, normal) < 0.0) { *pdf = kSMin; return invalid_dir(); }
+  if (dot(result, normal) < 0.0f) { *pdf = kSMin; return invalid_dir(); }
   const float wm_N = dot(mN, normal);
   const float wo_wm = dot(result, mN);
   const float x = 1.0f - (1.0f - alpha * alpha) * wm_N * wm_N;
@@ -137,15 +144,13 @@ __device__ __forceinline__ V3 ggxglass_sampling(Rng& rng, V3 normal, V3 in, floa
   const V3 NN = dot(in, normal) < 0.0f ? normal : -normal;
   *pdf = 1.0f;
   const V3 e1 = NN;
-  const float phi = two_pi_u(rng.next());
+  const float2 cs = __ldg(c_sincos_tab + rng.next_u24());
   const float e = rng.next();
   const double den = (double)e * ((double)(alpha * alpha) - 0.99999) + 1.0;
   const float cth = (float)sqrt((1.0000001 - (double)e) / den);
   V3 e2, e3;
   frame(e1, e2, e3);
-  double sd, cd;
-  sincos((double)phi, &sd, &cd);
-  const float cph = (float)cd, sph = (float)sd;
+  const float cph = cs.x, sph = cs.y;
   const float sth = sqrtf(1.00000001f - cth * cth);
   const V3 mN = normalized(e3 * sth * cph + e2 * sth * sph + e1 * cth);
   const float wi_wm = -dot(in, mN);
@@ -206,7 +211,7 @@ __device__ __forceinline__ float ggxglass_sampling_pdf(V3 out, V3 normal, V3 in,
 
 // Surface::OpeqeReflect (material.h:139-141)
 __device__ __forceinline__ bool opaque_reflect(const FParam& p) {
-  return (double)dot(p.in, -p.n) > 1e-4 && (double)dot(p.out, p.n) > 1e-4;
+  return dot(p.in, -p.n) > kGt1e4 && dot(p.out, p.n) > kGt1e4;
 }
 
 // Roughconductor::BRDF (material.h:227-274)
@@ -275,7 +280,7 @@ __device__ __forceinline__ float ggxglass_brdf(const FParam& p) {
   }
   const float eta = Io / Ii;
   if (fabsf(eta - 1.0f) < kSmall) return 1.0f;
-  if ((double)dot(p.in, p.out) < 0.0) return 0.0f;
+  if (dot(p.in, p.out) < 0.0f) return 0.0f;
   const V3 h = ggxglass_estimate_n(p.in, p.out, p.from, p.to);
   if (norm(h) < kSmall) return 0.0f;
   const float n_h = dot(h, p.n);

@@ -11,7 +11,9 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/friendsrender.h"
@@ -148,6 +150,52 @@ std::vector<AliasBin> alias_table(const std::vector<float>& values, float* avera
 
 float facet_area(H3 p0, H3 p1, H3 p2) { return 0.5f * norm(cross(p1 - p0, p2 - p0)); }  // Normal_Facet.h:45-47
 
+// Exact-value tables of the sampling routines' double functions of one
+// 24-bit draw u (see fr_bsdf.cuh), computed with this host's libm — the
+// functions the reference calls — once per device and kept for the
+// process's life (192 MB of device memory).
+struct ExactTables {
+  float2* sincos = nullptr;
+  float* sqrt1m = nullptr;
+};
+std::mutex g_tables_mu;
+ExactTables g_tables[64];
+
+int exact_tables(int dev, ExactTables* out) {
+  if (dev < 0 || dev >= 64) return fail(FR_ERR_INVALID, "device %d out of range", dev);
+  std::lock_guard<std::mutex> lock(g_tables_mu);
+  ExactTables& t = g_tables[dev];
+  if (!t.sincos) {
+    const uint32_t n = 1u << 24;
+    std::vector<float2> sc(n);
+    std::vector<float> sq(n);
+    const unsigned nt = std::max(1u, std::min(32u, std::thread::hardware_concurrency()));
+    std::vector<std::thread> th;
+    for (unsigned w = 0; w < nt; ++w)
+      th.emplace_back([&, w]() {
+        for (uint32_t u = w; u < n; u += nt) {
+          const float uf = (float)u * (1.0f / 16777216.0f);
+          const float ph = (uf * 2.0f) * kPI;  // u*2.0f*PI (Sampling.cpp:65), rounded once
+          sc[u] = make_float2((float)std::cos((double)ph), (float)std::sin((double)ph));
+          sq[u] = (float)std::sqrt(1.000000001 - (double)uf);  // Sampling.cpp:24
+        }
+      });
+    for (auto& x : th) x.join();
+    float2* d_sc = nullptr;
+    float* d_sq = nullptr;
+    if (cudaMalloc(&d_sc, sizeof(float2) * n) != cudaSuccess || cudaMalloc(&d_sq, sizeof(float) * n) != cudaSuccess) {
+      cudaFree(d_sc);
+      return fail(FR_ERR_OOM, "exact tables: cudaMalloc failed");
+    }
+    FR_CUDA(cudaMemcpy(d_sc, sc.data(), sizeof(float2) * n, cudaMemcpyHostToDevice));
+    FR_CUDA(cudaMemcpy(d_sq, sq.data(), sizeof(float) * n, cudaMemcpyHostToDevice));
+    t.sincos = d_sc;
+    t.sqrt1m = d_sq;
+  }
+  *out = t;
+  return FR_OK;
+}
+
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
@@ -170,6 +218,8 @@ struct fr_ctx {
   PixelState st{};
   PhotonSlots ph{};
   uint32_t* counts = nullptr;
+  uint32_t* work = nullptr;      // photon-pass path counter
+  int photon_blocks = 0;         // resident blocks of the persistent photon pass
   PhotonGrid grid{};
   GridInfo* gi = nullptr;
   ScanTemp scan{};
@@ -383,7 +433,7 @@ int run_iteration(fr_ctx* c) {
   }
   {
     StageMark m(c, FR_STAGE_PHOTON);
-    launch_photon_pass(c->sc, it, c->ph, c->counts, c->err, s);
+    launch_photon_pass(c->sc, it, c->ph, c->counts, c->work, c->photon_blocks, c->err, s);
   }
   {
     StageMark m(c, FR_STAGE_GRID);
@@ -450,6 +500,13 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
   c->rr_eye[1] = (float)std::exp((double)(4 - 6));
   c->cam = setup_camera(*camera);
   upload_byte_lut(c->stream);
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return bail(fail(FR_ERR_CUDA, "device query failed"));
+  ExactTables tabs;
+  if ((rc = exact_tables(dev, &tabs))) return bail(rc);
+  upload_tables(tabs.sincos, tabs.sqrt1m, c->stream);
+  c->photon_blocks = std::max(1, photon_pass_blocks_per_sm()) * sms;
 
   // ---- geometry
   const int T = scene->num_facets;
@@ -543,7 +600,8 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
       (rc = c->alloc(&c->hp.wgt, npix)) || (rc = c->alloc(&c->st.tau, 3 * npix)) || (rc = c->alloc(&c->st.n, npix)) ||
       (rc = c->alloc(&c->st.r, npix)) || (rc = c->alloc(&c->st.g, npix)) || (rc = c->alloc(&c->ph.pos, nslots)) ||
       (rc = c->alloc(&c->ph.flux, nslots)) || (rc = c->alloc(&c->ph.dir, nslots)) ||
-      (rc = c->alloc(&c->counts, (size_t)c->P)) || (rc = c->alloc(&c->gi, 1)) || (rc = c->alloc(&c->err, 1)) ||
+      (rc = c->alloc(&c->counts, (size_t)c->P)) || (rc = c->alloc(&c->work, 1)) || (rc = c->alloc(&c->gi, 1)) ||
+      (rc = c->alloc(&c->err, 1)) ||
       (rc = c->alloc(&c->dbg_m, npix)) || (rc = c->alloc(&c->dbg_phi, npix)) || (rc = c->alloc(&c->image, npix)))
     return bail(rc);
   // Photon grid: one bucket per expected photon or better (a few photons per path).

@@ -13,6 +13,7 @@
 // reference's photon-first order; it lets the grid size its cells from this
 // iteration's hitpoint radii.
 #include <cuda_runtime.h>
+#include <algorithm>
 #include <cfloat>
 #include <cstdint>
 #include "fr_bsdf.cuh"
@@ -26,7 +27,7 @@ namespace fr {
 
 namespace {
 
-__device__ __forceinline__ bool near1(float s) { return (double)fabsf(s - 1.0f) < 0.00001; }  // SPPM.h:27-29
+__device__ __forceinline__ bool near1(float s) { return fabsf(s - 1.0f) < kLt1e5; }  // SPPM.h:27-29
 
 __device__ __forceinline__ float max3(V3 a) {
   return a.x > a.y ? (a.x > a.z ? a.x : a.z) : (a.y > a.z ? a.y : a.z);
@@ -124,7 +125,7 @@ __global__ void __launch_bounds__(128) k_eye_pass(SceneGPU sc, CameraGPU cam, It
       nxt_d = surface_sample(g.type, rng, p, &pdf);
       if (!is_valid_direction(nxt_d)) break;
       if (g.flags & kMatOpaque) {
-        if ((double)dot(nxt_d, g.normal) < 1e-6) break;
+        if (dot(nxt_d, g.normal) < kLt1e6) break;
       } else {
         const bool reflect = !(dot(nxt_d, g.normal) < 0.0f);
         nxt_ix = reflect ? cur_ix : Io;
@@ -135,7 +136,7 @@ __global__ void __launch_bounds__(128) k_eye_pass(SceneGPU sc, CameraGPU cam, It
       nxt_o = nxt_o + on * kRayOffset;
       const float brdf = surface_brdf(g.type, p);
       const float cs = fmaxf(0.0f, fminf(1.0f, dot(nxt_d, on)));
-      if ((double)brdf < 1e-8) break;
+      if (brdf < kLt1e8) break;
       if (pdf < 0.0f) break;
       thr = thr * (g.albedo * cs * brdf);
       PDF *= pdf;
@@ -159,75 +160,86 @@ __global__ void __launch_bounds__(128) k_eye_pass(SceneGPU sc, CameraGPU cam, It
 }
 
 // --------------------------------------------------------------- photon pass
-__global__ void __launch_bounds__(128) k_photon_pass(SceneGPU sc, IterParams it, PhotonSlots ph,
-                                                     uint32_t* counts, int* err) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= it.photons) return;
-  Rng rng((uint32_t)i + 135u + it.step * (uint32_t)it.photons);
-  const size_t base = (size_t)i * kPhotonSlots;
+// One photon path (createPhotonMap body, SPPM.cpp:508-673) as a state that
+// advances one loop iteration at a time, so a persistent thread can start a
+// new path as soon as its current one ends.
+struct PhotonPath {
+  Rng rng;
+  V3 cur_o, cur_d, nxt_o, nxt_d, thr, flux0;
+  float cur_ix, nxt_ix, PDF;
+  int k, loop, depth;
+  size_t base;
+  int idx;
 
-  // generateLightRay (SPPM.cpp:453-471)
-  const uint32_t lb = (uint32_t)(((uint64_t)(uint32_t)sc.num_lights * rng.next_u24()) >> 24);
-  const LightGPU& bin = sc.lights[lb];
-  const int li = rng.next() < bin.alias_prob ? bin.alias_left : bin.alias_right;
-  const LightGPU& L = sc.lights[li];
-  const V3 P0 = v3(L.p0), P1 = v3(L.p1), P2 = v3(L.p2);
-  V3 pos, rad;
-  float pdf_area;
-  if (L.textured) {
-    const EmitEntry* tab = sc.emit + L.emit_offset;
-    const uint32_t eb = (uint32_t)(((uint64_t)kEmitSamples * rng.next_u24()) >> 24);
-    const int ei = rng.next() < tab[eb].prob ? tab[eb].left : tab[eb].right;
-    const EmitEntry& e = tab[ei];
-    pos = e.uvw[0] * P0 + e.uvw[1] * P1 + (1.0f - e.uvw[0] - e.uvw[1]) * P2;
-    rad = v3(e.L);
-    pdf_area = e.pdf;
-  } else {
-    float u = rng.next(), v = rng.next();
-    if (v > u) { u *= 0.5f; v -= u; }
-    else { v *= 0.5f; u -= v; }
-    pos = u * P0 + v * P1 + (1.0f - u - v) * P2;
-    rad = v3(L.radiance);
-    pdf_area = L.pdf_point;
+  __device__ __forceinline__ PhotonPath() : rng(0u) {}
+
+  // generateLightRay (SPPM.cpp:453-471) and the light-surface photon (SPPM.cpp:530-540).
+  __device__ __forceinline__ void start(const SceneGPU& sc, const IterParams& it, const PhotonSlots& ph, int i) {
+    idx = i;
+    rng = Rng((uint32_t)i + 135u + it.step * (uint32_t)it.photons);
+    base = (size_t)i * kPhotonSlots;
+    const uint32_t lb = (uint32_t)(((uint64_t)(uint32_t)sc.num_lights * rng.next_u24()) >> 24);
+    const LightGPU& bin = sc.lights[lb];
+    const int li = rng.next() < bin.alias_prob ? bin.alias_left : bin.alias_right;
+    const LightGPU& L = sc.lights[li];
+    const V3 P0 = v3(L.p0), P1 = v3(L.p1), P2 = v3(L.p2);
+    V3 pos, rad;
+    float pdf_area;
+    if (L.textured) {
+      const EmitEntry* tab = sc.emit + L.emit_offset;
+      const uint32_t eb = (uint32_t)(((uint64_t)kEmitSamples * rng.next_u24()) >> 24);
+      const int ei = rng.next() < tab[eb].prob ? tab[eb].left : tab[eb].right;
+      const EmitEntry& e = tab[ei];
+      pos = e.uvw[0] * P0 + e.uvw[1] * P1 + (1.0f - e.uvw[0] - e.uvw[1]) * P2;
+      rad = v3(e.L);
+      pdf_area = e.pdf;
+    } else {
+      float u = rng.next(), v = rng.next();
+      if (v > u) { u *= 0.5f; v -= u; }
+      else { v *= 0.5f; u -= v; }
+      pos = u * P0 + v * P1 + (1.0f - u - v) * P2;
+      rad = v3(L.radiance);
+      pdf_area = L.pdf_point;
+    }
+    pdf_area *= L.pdf_light;
+    const V3 ln = v3(L.normal);
+    float pdf_dir = 1.0f;
+    const V3 d = cos_sampling(rng, ln, &pdf_dir);
+    rad = rad * fminf(1.0f, fmaxf(0.0f, dot(ln, d)));
+    cur_o = pos + ln * kRayOffset;
+    cur_d = normalized(d);
+    flux0 = rad;
+    PDF = pdf_area * pdf_dir;
+    thr = v3(1.f, 1.f, 1.f);
+    store_float4(ph.pos + base, cur_o, 1.0f);
+    store_float4(ph.flux + base, flux0 * thr * kPI, PDF);
+    store_float4(ph.dir + base, cur_d, 1.0f);
+    nxt_o = cur_o;
+    nxt_d = cur_d;
+    cur_ix = nxt_ix = 1.0f;
+    k = loop = depth = 0;
   }
-  pdf_area *= L.pdf_light;
-  const V3 ln = v3(L.normal);
-  float pdf_dir = 1.0f;
-  V3 d = cos_sampling(rng, ln, &pdf_dir);
-  rad = rad * fminf(1.0f, fmaxf(0.0f, dot(ln, d)));
-  V3 cur_o = pos + ln * kRayOffset;
-  V3 cur_d = normalized(d);
-  const V3 flux0 = rad;
 
-  float PDF = pdf_area * pdf_dir;
-  V3 thr = v3(1.f, 1.f, 1.f);
-  // Photon on the light surface in slot 0 (SPPM.cpp:530-540).
-  store_float4(ph.pos + base, cur_o, 1.0f);
-  store_float4(ph.flux + base, flux0 * thr * kPI, PDF);
-  store_float4(ph.dir + base, cur_d, 1.0f);
-
-  V3 nxt_o = cur_o, nxt_d = cur_d;
-  float cur_ix = 1.0f, nxt_ix = 1.0f;
-  int k = 0, loop = 0, depth = 0;
-  while (true) {
-    if (loop++ > 32 || k >= kPhotonSlots - 1) break;
-    if ((double)thr.x < 1e-8 || (double)thr.y < 1e-8 || (double)thr.z < 1e-8) break;
+  // One pass of the bounce loop (SPPM.cpp:548-671); false when the path ends.
+  __device__ __forceinline__ bool step(const SceneGPU& sc, const PhotonSlots& ph, int* err) {
+    if (loop++ > 32 || k >= kPhotonSlots - 1) return false;
+    if (thr.x < kLt1e8 || thr.y < kLt1e8 || thr.z < kLt1e8) return false;
     Hit hit;
-    if (!trace_closest(sc, cur_o, cur_d, kRayOffset, hit, err)) break;
+    if (!trace_closest(sc, cur_o, cur_d, kRayOffset, hit, err)) return false;
     Geom g;
     calc_geometry(sc, hit, g);
     g.normal = dot(g.normal, cur_d) > 0.0f ? -g.normal : g.normal;
     nxt_o = g.pos;
-    if ((double)norm2(g.radiance) > 0.00001) break;
+    if (norm2(g.radiance) > kGt1e5) return false;
     if (g.translucency > 0.5f) {
       thr = thr * v3(g.translucency, g.translucency, g.translucency);
       cur_o = g.pos + cur_d * kRayOffset;
-      continue;
+      return true;
     }
     // russianRulette_PhotonMapping (SPPM.h:33-52)
-    if (depth > 16) break;
+    if (depth > 16) return false;
     const float pdf_rus = 0.98f * max3(g.albedo);
-    if (rng.next() > pdf_rus) break;
+    if (rng.next() > pdf_rus) return false;
     PDF *= pdf_rus;
     float Ii, Io;
     if (near1(cur_ix)) { Ii = 1.0f; Io = g.index; }
@@ -242,9 +254,9 @@ __global__ void __launch_bounds__(128) k_photon_pass(SceneGPU sc, IterParams it,
     }
     float pdf = 1.0f;
     nxt_d = surface_sample(g.type, rng, p, &pdf);
-    if (!is_valid_direction(nxt_d)) break;
+    if (!is_valid_direction(nxt_d)) return false;
     if (g.flags & kMatOpaque) {
-      if ((double)dot(nxt_d, g.normal) < 1e-6) break;
+      if (dot(nxt_d, g.normal) < kLt1e6) return false;
     } else {
       nxt_ix = is_reflect(cur_d, nxt_d, g.normal) ? cur_ix : Io;
     }
@@ -254,27 +266,64 @@ __global__ void __launch_bounds__(128) k_photon_pass(SceneGPU sc, IterParams it,
     nxt_o = nxt_o + on * kRayOffset;
     const float brdf = surface_brdf(g.type, p);
     const float cs = fmaxf(0.0f, fminf(1.0f, dot(nxt_d, on)));
-    if ((double)brdf < 1e-8) break;
-    if (pdf < 0.0f) break;
+    if (brdf < kLt1e8) return false;
+    if (pdf < 0.0f) return false;
     thr = thr * (g.albedo * cs * brdf);
     PDF *= pdf;
     cur_o = nxt_o; cur_d = nxt_d; cur_ix = nxt_ix;
     ++depth;
+    return true;
   }
+
   // Terminator (SPPM.cpp:672): written one past the last stored photon, which
   // leaves slot k as it was; the compactor (SPPM.cpp:812-822) takes slots up to
   // the first invalid one, so a valid stale slot k joins this iteration.
-  uint32_t n;
-  if (it.flags & kFlagFixStaleSlot) {
-    const int term = k > 0 ? k : 1;
-    if (term < kPhotonSlots) ph.dir[base + term].w = 0.0f;
-    n = (uint32_t)term;
-  } else {
-    const int term = k + 1;
-    if (term < kPhotonSlots) ph.dir[base + term].w = 0.0f;
-    n = (k == 0 || ph.dir[base + k].w == 0.0f) ? (uint32_t)(k > 0 ? k : 1) : (uint32_t)(k + 1);
+  __device__ __forceinline__ void finish(const IterParams& it, const PhotonSlots& ph, uint32_t* counts) {
+    uint32_t n;
+    if (it.flags & kFlagFixStaleSlot) {
+      const int term = k > 0 ? k : 1;
+      if (term < kPhotonSlots) ph.dir[base + term].w = 0.0f;
+      n = (uint32_t)term;
+    } else {
+      const int term = k + 1;
+      if (term < kPhotonSlots) ph.dir[base + term].w = 0.0f;
+      n = (k == 0 || ph.dir[base + k].w == 0.0f) ? (uint32_t)(k > 0 ? k : 1) : (uint32_t)(k + 1);
+    }
+    counts[idx] = n;
   }
-  counts[i] = n;
+};
+
+// Persistent photon pass: every lane runs paths back to back, taking the next
+// path index (a warp-aggregated atomic on *work) as soon as its path ends, so
+// warps stay full however unequal the path lengths.
+__global__ void __launch_bounds__(128) k_photon_pass(SceneGPU sc, IterParams it, PhotonSlots ph,
+                                                     uint32_t* counts, uint32_t* work, int* err) {
+  const unsigned lane = threadIdx.x & 31u;
+  PhotonPath path;
+  bool active = false, done = false;
+  while (true) {
+    const unsigned need = __ballot_sync(0xffffffffu, !active && !done);
+    if (need) {
+      const int leader = __ffs(need) - 1;
+      uint32_t first = 0;
+      if ((int)lane == leader) first = atomicAdd(work, (uint32_t)__popc(need));
+      first = __shfl_sync(0xffffffffu, first, leader);
+      if (!active && !done) {
+        const uint32_t i = first + (uint32_t)__popc(need & ((1u << lane) - 1u));
+        if (i < (uint32_t)it.photons) {
+          path.start(sc, it, ph, (int)i);
+          active = true;
+        } else {
+          done = true;
+        }
+      }
+    }
+    if (__all_sync(0xffffffffu, done)) break;
+    if (active && !path.step(sc, ph, err)) {
+      path.finish(it, ph, counts);
+      active = false;
+    }
+  }
 }
 
 // ------------------------------------------------------------- photon grid
@@ -543,9 +592,23 @@ void launch_eye_pass(const SceneGPU& sc, const CameraGPU& cam, const IterParams&
   k_eye_pass<<<blocks_for(n, 128), 128, 0, s>>>(sc, cam, it, rr_eye[0], rr_eye[1], hp, st, gi, err);
 }
 
-void launch_photon_pass(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, uint32_t* counts, int* err,
-                        cudaStream_t s) {
-  k_photon_pass<<<blocks_for(it.photons, 128), 128, 0, s>>>(sc, it, ph, counts, err);
+void launch_photon_pass(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, uint32_t* counts, uint32_t* work,
+                        int resident_blocks, int* err, cudaStream_t s) {
+  const unsigned need = blocks_for(it.photons, 128);
+  const unsigned grid = resident_blocks > 0 ? std::min<unsigned>(need, (unsigned)resident_blocks) : need;
+  cudaMemsetAsync(work, 0, sizeof(uint32_t), s);
+  k_photon_pass<<<grid, 128, 0, s>>>(sc, it, ph, counts, work, err);
+}
+
+int photon_pass_blocks_per_sm() {
+  int b = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_photon_pass, 128, 0);
+  return b;
+}
+
+void upload_tables(const float2* sincos_tab, const float* sqrt1m_tab, cudaStream_t s) {
+  cudaMemcpyToSymbolAsync(c_sincos_tab, &sincos_tab, sizeof(sincos_tab), 0, cudaMemcpyHostToDevice, s);
+  cudaMemcpyToSymbolAsync(c_sqrt1m_tab, &sqrt1m_tab, sizeof(sqrt1m_tab), 0, cudaMemcpyHostToDevice, s);
 }
 
 void launch_grid_setup(GridInfo* gi, const SceneGPU& sc, float cell_scale, float r0, cudaStream_t s) {

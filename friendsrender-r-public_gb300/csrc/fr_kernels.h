@@ -69,8 +69,12 @@ void upload_byte_lut(cudaStream_t s);
 
 void launch_eye_pass(const SceneGPU& sc, const CameraGPU& cam, const IterParams& it, const float* rr_eye,
                      HitpointBuf hp, PixelState st, GridInfo* gi, int* err, cudaStream_t s);
-void launch_photon_pass(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, uint32_t* counts, int* err,
-                        cudaStream_t s);
+// Persistent photon pass: resident_blocks blocks of 128 threads (0: one block per 128 paths).
+void launch_photon_pass(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, uint32_t* counts, uint32_t* work,
+                        int resident_blocks, int* err, cudaStream_t s);
+int photon_pass_blocks_per_sm();
+// Points the kernels at the exact-value tables (see fr_bsdf.cuh).
+void upload_tables(const float2* sincos_tab, const float* sqrt1m_tab, cudaStream_t s);
 void launch_grid_setup(GridInfo* gi, const SceneGPU& sc, float cell_scale, float r0, cudaStream_t s);
 // stride: slots per path (kPhotonSlots for the render loop, 1 for a flat photon list).
 void launch_photon_count(PhotonSlots ph, const uint32_t* counts, int paths, int stride, PhotonGrid g,

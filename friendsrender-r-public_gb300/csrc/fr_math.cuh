@@ -37,6 +37,20 @@ __device__ __forceinline__ V3 normalized(V3 a) {
 }
 __device__ __forceinline__ float comp(V3 a, int i) { return i == 0 ? a.x : (i == 1 ? a.y : a.z); }
 
+// Float thresholds for the reference's float-against-double comparisons.
+// For a float g and a double constant d that is not a float, (double)g > d
+// exactly when g > rd(d), and (double)g < d exactly when g < ru(d), where
+// rd/ru round d down/up to a float.  Comparing in float keeps the decisions
+// bit-identical without the FP64 pipe.
+constexpr float kGt1e4 = 0x1.a36e2ep-14f;      // (double)g > 1e-4
+constexpr float kGt1e5 = 0x1.4f8b58p-17f;      // (double)g > 1e-5
+constexpr float kLt1e5 = 0x1.4f8b5ap-17f;      // (double)g < 1e-5
+constexpr float kGt1e6 = 0x1.0c6f7ap-20f;      // (double)g > 1e-6
+constexpr float kLt1e6 = 0x1.0c6f7cp-20f;      // (double)g < 1e-6
+constexpr float kLt1e8 = 0x1.5798f0p-27f;      // (double)g < 1e-8
+constexpr float kGt0_999999 = 0x1.ffffdep-1f;  // (double)g > 0.999999
+constexpr float kGt0_9 = 0x1.ccccccp-1f;       // (double)g > 0.9
+
 // x^-2 for a float x, rounded once from the exact double square: the value
 // the reference's powf(x, -2.0f) returns.
 __device__ __forceinline__ float pow_m2(float x) {

@@ -239,7 +239,7 @@ __device__ __forceinline__ void calc_geometry(const SceneGPU& sc, const Hit& h, 
   g.extinction = m.extinction;
   g.reflectance = m.reflectance;
   g.translucency = 0.0f;
-  if ((double)norm2(g.radiance) > 1e-6) g.albedo = v3(1.f, 1.f, 1.f);
+  if (norm2(g.radiance) > kGt1e6) g.albedo = v3(1.f, 1.f, 1.f);
   if (m.tex_rough >= 0) {
     const F4 c = tex_bilinear(sc.texs[m.tex_rough], g.uvx, g.uvy);
     g.rough = fminf(0.8f, fmaxf(0.05f, 0.5f * c.x));
@@ -257,7 +257,7 @@ __device__ __forceinline__ void calc_geometry(const SceneGPU& sc, const Hit& h, 
     const V3 nm = normalized(v3(2.0f * c.x - 1.0f, 2.0f * c.y - 1.0f, 2.0f * c.z - 1.0f));
     const V3 nrm = normalized(v3(nm.x, nm.z, nm.y));
     const V3 e2 = g.normal;
-    const V3 e1 = (double)fabsf(e2.y) > 0.9 ? cross(e2, v3(1.f, 0.f, 0.f)) : cross(e2, v3(0.f, 1.f, 0.f));
+    const V3 e1 = fabsf(e2.y) > kGt0_9 ? cross(e2, v3(1.f, 0.f, 0.f)) : cross(e2, v3(0.f, 1.f, 0.f));
     const V3 e3 = normalized(cross(e1, e2));
     // M[i][j] = component i of column j.
     const float M[3][3] = {{e1.x, e2.x, e3.x}, {e1.y, e2.y, e3.y}, {e1.z, e2.z, e3.z}};
