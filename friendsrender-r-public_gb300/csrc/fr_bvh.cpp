@@ -9,6 +9,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstring>
 #include <limits>
 #include <thread>
@@ -156,20 +157,22 @@ BVHResult build_bvh8(const float* positions, int num_tris, float pad_abs) {
   const int root = b.build(0, num_tris, 0);
 
   BVHResult out;
-  out.tri_order = b.perm;
-  // Collapse: each wide node takes up to 8 binary descendants, opening the
-  // largest-area inner child first.
-  struct Job { int bnode; int wide; };
+  // Collapse breadth first: each wide node takes up to 8 binary descendants,
+  // opening the largest-area inner child first; its internal children get
+  // consecutive node indices and its leaves consecutive triangle slots.
+  struct Job { int bnode; int wide; int depth; };
   std::vector<Job> jobs;
+  size_t head = 0;
   out.nodes.emplace_back();
-  jobs.push_back({root, 0});
+  jobs.push_back({root, 0, 1});
   auto pad = [&](float v, bool up) {
     const float d = pad_abs + std::fabs(v) * 1e-6f;
     return up ? v + d : v - d;
   };
-  while (!jobs.empty()) {
-    const Job j = jobs.back();
-    jobs.pop_back();
+  int maxd = 1;
+  while (head < jobs.size()) {
+    const Job j = jobs[head++];
+    maxd = std::max(maxd, j.depth);
     std::vector<int> kids;
     const BNode& bn = b.nodes[j.bnode];
     if (bn.left < 0) {
@@ -191,41 +194,38 @@ BVHResult build_bvh8(const float* positions, int num_tris, float pad_abs) {
         kids.push_back(r);
       }
     }
-    BVHNode8 node;
+    BVHNodeW node;
     std::memset(&node, 0, sizeof(node));
     for (int c = 0; c < 8; ++c) {
       node.lox[c] = node.loy[c] = node.loz[c] = std::numeric_limits<float>::infinity();
       node.hix[c] = node.hiy[c] = node.hiz[c] = -std::numeric_limits<float>::infinity();
-      node.child[c] = kEmptyChild;
     }
+    int ninternal = 0;
+    for (int c = 0; c < (int)kids.size(); ++c)
+      if (b.nodes[kids[c]].left >= 0) ++ninternal;
+    node.child_base = (uint32_t)out.nodes.size();
+    node.tri_base = (uint32_t)out.tri_order.size();
+    for (int i = 0; i < ninternal; ++i) out.nodes.emplace_back();
+    int next_internal = 0;
+    uint32_t tri_off = 0;
     for (int c = 0; c < (int)kids.size(); ++c) {
       const BNode& k = b.nodes[kids[c]];
-      if (k.left < 0 && k.count == 0) continue;
       node.lox[c] = pad(k.box.lo[0], false); node.hix[c] = pad(k.box.hi[0], true);
       node.loy[c] = pad(k.box.lo[1], false); node.hiy[c] = pad(k.box.hi[1], true);
       node.loz[c] = pad(k.box.lo[2], false); node.hiz[c] = pad(k.box.hi[2], true);
-      if (k.left < 0) {
-        node.child[c] = kLeafBit | ((uint32_t)(k.count - 1) << kLeafCountShift) | (uint32_t)k.first;
+      if (k.left >= 0) {
+        node.imask |= 1u << c;
+        node.meta[c] = 0x80;
+        jobs.push_back({kids[c], (int)node.child_base + next_internal++, j.depth + 1});
       } else {
-        const int wide = (int)out.nodes.size();
-        out.nodes.emplace_back();
-        node.child[c] = (uint32_t)wide;
-        jobs.push_back({kids[c], wide});
+        node.meta[c] = (uint8_t)(0x80u | ((uint32_t)(k.count - 1) << 5) | tri_off);
+        for (int t = 0; t < k.count; ++t) out.tri_order.push_back(b.perm[k.first + t]);
+        tri_off += (uint32_t)k.count;
       }
     }
     out.nodes[j.wide] = node;
   }
-  // Depth of the wide tree (bounds the traversal stack).
-  std::vector<int> depth(out.nodes.size(), 0);
-  int maxd = 0;
-  for (size_t i = 0; i < out.nodes.size(); ++i) {
-    maxd = std::max(maxd, depth[i]);
-    for (int c = 0; c < 8; ++c) {
-      const uint32_t ch = out.nodes[i].child[c];
-      if (ch != kEmptyChild && !(ch & kLeafBit)) depth[ch] = depth[i] + 1;
-    }
-  }
-  out.depth = maxd + 1;
+  out.depth = maxd;
   return out;
 }
 

@@ -5,7 +5,7 @@
 namespace fr {
 
 struct BVHResult {
-  std::vector<BVHNode8> nodes;  // node 0 is the root
+  std::vector<BVHNodeW> nodes;  // node 0 is the root
   std::vector<int> tri_order;   // leaf order -> facet index
   int depth = 0;                // levels of the wide tree
 };

@@ -218,8 +218,8 @@ struct fr_ctx {
   PixelState st{};
   PhotonSlots ph{};
   uint32_t* counts = nullptr;
-  uint32_t* work = nullptr;      // photon-pass path counter
-  int photon_blocks = 0;         // resident blocks of the persistent photon pass
+  PhotonWave wave{};             // wavefront photon-pass state
+  int photon_blocks = 0;         // grid of the wavefront round kernels
   PhotonGrid grid{};
   GridInfo* gi = nullptr;
   ScanTemp scan{};
@@ -433,7 +433,7 @@ int run_iteration(fr_ctx* c) {
   }
   {
     StageMark m(c, FR_STAGE_PHOTON);
-    launch_photon_pass(c->sc, it, c->ph, c->counts, c->work, c->photon_blocks, c->err, s);
+    launch_photon_pass(c->sc, it, c->ph, c->counts, c->wave, c->photon_blocks, c->err, s);
   }
   {
     StageMark m(c, FR_STAGE_GRID);
@@ -447,7 +447,7 @@ int run_iteration(fr_ctx* c) {
     StageMark m(c, FR_STAGE_GATHER);
     launch_gather_update(c->sc, it, c->hp, c->grid, c->gi, c->st, c->dbg_m, c->dbg_phi, s);
   }
-  c->launches += 6;  // eye, photon, grid setup, count, scatter, gather/update
+  c->launches += 5 + 2 + 2 * kWaveRounds;  // eye, photon emit/rounds/tail, grid setup, count, scatter, gather
   c->photons_total += c->P;
   FR_CUDA(cudaGetLastError());
   return FR_OK;
@@ -565,7 +565,7 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
   build_lights(*scene, lights, emit);
   if (lights.empty()) return bail(fail(FR_ERR_INVALID, "scene: no emissive facets"));
 
-  BVHNode8* d_nodes;
+  BVHNodeW* d_nodes;
   TriGPU* d_tris;
   FacetShade* d_shade;
   MaterialGPU* d_mats;
@@ -600,7 +600,11 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
       (rc = c->alloc(&c->hp.wgt, npix)) || (rc = c->alloc(&c->st.tau, 3 * npix)) || (rc = c->alloc(&c->st.n, npix)) ||
       (rc = c->alloc(&c->st.r, npix)) || (rc = c->alloc(&c->st.g, npix)) || (rc = c->alloc(&c->ph.pos, nslots)) ||
       (rc = c->alloc(&c->ph.flux, nslots)) || (rc = c->alloc(&c->ph.dir, nslots)) ||
-      (rc = c->alloc(&c->counts, (size_t)c->P)) || (rc = c->alloc(&c->work, 1)) || (rc = c->alloc(&c->gi, 1)) ||
+      (rc = c->alloc(&c->counts, (size_t)c->P)) || (rc = c->alloc(&c->wave.a, (size_t)c->P)) ||
+      (rc = c->alloc(&c->wave.b, (size_t)c->P)) || (rc = c->alloc(&c->wave.c, (size_t)c->P)) ||
+      (rc = c->alloc(&c->wave.d, (size_t)c->P)) || (rc = c->alloc(&c->wave.hit, (size_t)c->P)) ||
+      (rc = c->alloc(&c->wave.queue[0], (size_t)c->P)) || (rc = c->alloc(&c->wave.queue[1], (size_t)c->P)) ||
+      (rc = c->alloc(&c->wave.qcount, (size_t)kWaveRounds + 2)) || (rc = c->alloc(&c->gi, 1)) ||
       (rc = c->alloc(&c->err, 1)) ||
       (rc = c->alloc(&c->dbg_m, npix)) || (rc = c->alloc(&c->dbg_phi, npix)) || (rc = c->alloc(&c->image, npix)))
     return bail(rc);

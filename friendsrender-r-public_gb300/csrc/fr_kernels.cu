@@ -2,7 +2,9 @@
 //
 // One iteration (StochasticProgressivePhotonMapping, SPPM/SPPM/SPPM.cpp:768-848):
 //   k_eye_pass       createHitpoints + getHitpointInfo  (SPPM.cpp:98-353)
-//   k_photon_pass    createPhotonMap + generateLightRay (SPPM.cpp:453-680)
+//   k_pw_emit / k_pw_trace / k_pw_shade / k_pw_tail
+//                    createPhotonMap + generateLightRay (SPPM.cpp:453-680)
+//                    as a wavefront over queues of live paths
 //   k_grid_setup / k_photon_count / scan / k_photon_scatter
 //                    photon cell grid, replacing the photon kd-tree
 //                    (SPPM.cpp:809-833, kdtree.h:348-431)
@@ -160,169 +162,267 @@ __global__ void __launch_bounds__(128) k_eye_pass(SceneGPU sc, CameraGPU cam, It
 }
 
 // --------------------------------------------------------------- photon pass
-// One photon path (createPhotonMap body, SPPM.cpp:508-673) as a state that
-// advances one loop iteration at a time, so a persistent thread can start a
-// new path as soon as its current one ends.
-struct PhotonPath {
-  Rng rng;
-  V3 cur_o, cur_d, nxt_o, nxt_d, thr, flux0;
-  float cur_ix, nxt_ix, PDF;
+// createPhotonMap (SPPM.cpp:495-680) as a wavefront.  k_pw_emit starts every
+// path (generateLightRay, SPPM.cpp:453-471, and the light-surface photon,
+// SPPM.cpp:530-540); then rounds of k_pw_trace (closest hit of every live
+// path) and k_pw_shade (the rest of one pass of the bounce loop,
+// SPPM.cpp:548-671) over a compacted queue of live paths; k_pw_tail finishes
+// the few paths still alive after the last round.  Every path keeps its own
+// Philox stream, so the order in which paths are processed changes nothing.
+//
+// Path state between kernels (one entry per path):
+//   a: origin.xyz, ray index of refraction     b: direction.xyz, PDF
+//   c: throughput.xyz, flux0.x                 d: flux0.yz, draw counter, k | loop << 8 | depth << 16
+// At the top of each loop pass the reference's NextRay equals CurrentRay
+// (SPPM.cpp:669), so only the current ray is kept.
+struct PhotonState {
+  V3 o, d, thr, flux0;
+  float ix, PDF;
+  uint32_t draw;
   int k, loop, depth;
-  size_t base;
-  int idx;
-
-  __device__ __forceinline__ PhotonPath() : rng(0u) {}
-
-  // generateLightRay (SPPM.cpp:453-471) and the light-surface photon (SPPM.cpp:530-540).
-  __device__ __forceinline__ void start(const SceneGPU& sc, const IterParams& it, const PhotonSlots& ph, int i) {
-    idx = i;
-    rng = Rng((uint32_t)i + 135u + it.step * (uint32_t)it.photons);
-    base = (size_t)i * kPhotonSlots;
-    const uint32_t lb = (uint32_t)(((uint64_t)(uint32_t)sc.num_lights * rng.next_u24()) >> 24);
-    const LightGPU& bin = sc.lights[lb];
-    const int li = rng.next() < bin.alias_prob ? bin.alias_left : bin.alias_right;
-    const LightGPU& L = sc.lights[li];
-    const V3 P0 = v3(L.p0), P1 = v3(L.p1), P2 = v3(L.p2);
-    V3 pos, rad;
-    float pdf_area;
-    if (L.textured) {
-      const EmitEntry* tab = sc.emit + L.emit_offset;
-      const uint32_t eb = (uint32_t)(((uint64_t)kEmitSamples * rng.next_u24()) >> 24);
-      const int ei = rng.next() < tab[eb].prob ? tab[eb].left : tab[eb].right;
-      const EmitEntry& e = tab[ei];
-      pos = e.uvw[0] * P0 + e.uvw[1] * P1 + (1.0f - e.uvw[0] - e.uvw[1]) * P2;
-      rad = v3(e.L);
-      pdf_area = e.pdf;
-    } else {
-      float u = rng.next(), v = rng.next();
-      if (v > u) { u *= 0.5f; v -= u; }
-      else { v *= 0.5f; u -= v; }
-      pos = u * P0 + v * P1 + (1.0f - u - v) * P2;
-      rad = v3(L.radiance);
-      pdf_area = L.pdf_point;
-    }
-    pdf_area *= L.pdf_light;
-    const V3 ln = v3(L.normal);
-    float pdf_dir = 1.0f;
-    const V3 d = cos_sampling(rng, ln, &pdf_dir);
-    rad = rad * fminf(1.0f, fmaxf(0.0f, dot(ln, d)));
-    cur_o = pos + ln * kRayOffset;
-    cur_d = normalized(d);
-    flux0 = rad;
-    PDF = pdf_area * pdf_dir;
-    thr = v3(1.f, 1.f, 1.f);
-    store_float4(ph.pos + base, cur_o, 1.0f);
-    store_float4(ph.flux + base, flux0 * thr * kPI, PDF);
-    store_float4(ph.dir + base, cur_d, 1.0f);
-    nxt_o = cur_o;
-    nxt_d = cur_d;
-    cur_ix = nxt_ix = 1.0f;
-    k = loop = depth = 0;
-  }
-
-  // One pass of the bounce loop (SPPM.cpp:548-671); false when the path ends.
-  __device__ __forceinline__ bool step(const SceneGPU& sc, const PhotonSlots& ph, int* err) {
-    if (loop++ > 32 || k >= kPhotonSlots - 1) return false;
-    if (thr.x < kLt1e8 || thr.y < kLt1e8 || thr.z < kLt1e8) return false;
-    Hit hit;
-    if (!trace_closest(sc, cur_o, cur_d, kRayOffset, hit, err)) return false;
-    Geom g;
-    calc_geometry(sc, hit, g);
-    g.normal = dot(g.normal, cur_d) > 0.0f ? -g.normal : g.normal;
-    nxt_o = g.pos;
-    if (norm2(g.radiance) > kGt1e5) return false;
-    if (g.translucency > 0.5f) {
-      thr = thr * v3(g.translucency, g.translucency, g.translucency);
-      cur_o = g.pos + cur_d * kRayOffset;
-      return true;
-    }
-    // russianRulette_PhotonMapping (SPPM.h:33-52)
-    if (depth > 16) return false;
-    const float pdf_rus = 0.98f * max3(g.albedo);
-    if (rng.next() > pdf_rus) return false;
-    PDF *= pdf_rus;
-    float Ii, Io;
-    if (near1(cur_ix)) { Ii = 1.0f; Io = g.index; }
-    else { Ii = cur_ix; Io = 1.0f; }
-    FParam p{cur_d, nxt_d, g.normal, Ii, Io, g.rough, g.extinction, g.reflectance};
-    if (g.flags & kMatSPPM) {
-      const size_t s = base + k;
-      store_float4(ph.pos + s, g.pos, cur_ix);
-      store_float4(ph.flux + s, flux0 * thr * g.albedo, PDF);
-      store_float4(ph.dir + s, cur_d, 1.0f);
-      ++k;
-    }
-    float pdf = 1.0f;
-    nxt_d = surface_sample(g.type, rng, p, &pdf);
-    if (!is_valid_direction(nxt_d)) return false;
-    if (g.flags & kMatOpaque) {
-      if (dot(nxt_d, g.normal) < kLt1e6) return false;
-    } else {
-      nxt_ix = is_reflect(cur_d, nxt_d, g.normal) ? cur_ix : Io;
-    }
-    p.out = nxt_d;
-    pdf = surface_pdf(g.type, p);
-    const V3 on = dot(g.normal, nxt_d) > 0.0f ? g.normal : -g.normal;
-    nxt_o = nxt_o + on * kRayOffset;
-    const float brdf = surface_brdf(g.type, p);
-    const float cs = fmaxf(0.0f, fminf(1.0f, dot(nxt_d, on)));
-    if (brdf < kLt1e8) return false;
-    if (pdf < 0.0f) return false;
-    thr = thr * (g.albedo * cs * brdf);
-    PDF *= pdf;
-    cur_o = nxt_o; cur_d = nxt_d; cur_ix = nxt_ix;
-    ++depth;
-    return true;
-  }
-
-  // Terminator (SPPM.cpp:672): written one past the last stored photon, which
-  // leaves slot k as it was; the compactor (SPPM.cpp:812-822) takes slots up to
-  // the first invalid one, so a valid stale slot k joins this iteration.
-  __device__ __forceinline__ void finish(const IterParams& it, const PhotonSlots& ph, uint32_t* counts) {
-    uint32_t n;
-    if (it.flags & kFlagFixStaleSlot) {
-      const int term = k > 0 ? k : 1;
-      if (term < kPhotonSlots) ph.dir[base + term].w = 0.0f;
-      n = (uint32_t)term;
-    } else {
-      const int term = k + 1;
-      if (term < kPhotonSlots) ph.dir[base + term].w = 0.0f;
-      n = (k == 0 || ph.dir[base + k].w == 0.0f) ? (uint32_t)(k > 0 ? k : 1) : (uint32_t)(k + 1);
-    }
-    counts[idx] = n;
-  }
 };
 
-// Persistent photon pass: every lane runs paths back to back, taking the next
-// path index (a warp-aggregated atomic on *work) as soon as its path ends, so
-// warps stay full however unequal the path lengths.
-__global__ void __launch_bounds__(128) k_photon_pass(SceneGPU sc, IterParams it, PhotonSlots ph,
-                                                     uint32_t* counts, uint32_t* work, int* err) {
+__device__ __forceinline__ uint32_t photon_seed(const IterParams& it, int i) {
+  return (uint32_t)i + 135u + it.step * (uint32_t)it.photons;  // SPPM.cpp:520
+}
+
+__device__ __forceinline__ void load_state(const PhotonWave& w, int i, PhotonState& s) {
+  const float4 a = w.a[i], b = w.b[i], c = w.c[i], d = w.d[i];
+  s.o = v3(a.x, a.y, a.z); s.ix = a.w;
+  s.d = v3(b.x, b.y, b.z); s.PDF = b.w;
+  s.thr = v3(c.x, c.y, c.z);
+  s.flux0 = v3(c.w, d.x, d.y);
+  s.draw = __float_as_uint(d.z);
+  const uint32_t m = __float_as_uint(d.w);
+  s.k = (int)(m & 0xFFu); s.loop = (int)((m >> 8) & 0xFFu); s.depth = (int)(m >> 16);
+}
+
+__device__ __forceinline__ void store_state(const PhotonWave& w, int i, const PhotonState& s) {
+  w.a[i] = make_float4(s.o.x, s.o.y, s.o.z, s.ix);
+  w.b[i] = make_float4(s.d.x, s.d.y, s.d.z, s.PDF);
+  w.c[i] = make_float4(s.thr.x, s.thr.y, s.thr.z, s.flux0.x);
+  w.d[i] = make_float4(s.flux0.y, s.flux0.z, __uint_as_float(s.draw),
+                       __uint_as_float((uint32_t)s.k | ((uint32_t)s.loop << 8) | ((uint32_t)s.depth << 16)));
+}
+
+// generateLightRay (SPPM.cpp:453-471) and the light-surface photon in slot 0.
+__device__ __forceinline__ void photon_start(const SceneGPU& sc, const IterParams& it, const PhotonSlots& ph, int i,
+                                             PhotonState& s) {
+  Rng rng(photon_seed(it, i));
+  const size_t base = (size_t)i * kPhotonSlots;
+  const uint32_t lb = (uint32_t)(((uint64_t)(uint32_t)sc.num_lights * rng.next_u24()) >> 24);
+  const LightGPU& bin = sc.lights[lb];
+  const int li = rng.next() < bin.alias_prob ? bin.alias_left : bin.alias_right;
+  const LightGPU& L = sc.lights[li];
+  const V3 P0 = v3(L.p0), P1 = v3(L.p1), P2 = v3(L.p2);
+  V3 pos, rad;
+  float pdf_area;
+  if (L.textured) {
+    const EmitEntry* tab = sc.emit + L.emit_offset;
+    const uint32_t eb = (uint32_t)(((uint64_t)kEmitSamples * rng.next_u24()) >> 24);
+    const int ei = rng.next() < tab[eb].prob ? tab[eb].left : tab[eb].right;
+    const EmitEntry& e = tab[ei];
+    pos = e.uvw[0] * P0 + e.uvw[1] * P1 + (1.0f - e.uvw[0] - e.uvw[1]) * P2;
+    rad = v3(e.L);
+    pdf_area = e.pdf;
+  } else {
+    float u = rng.next(), v = rng.next();
+    if (v > u) { u *= 0.5f; v -= u; }
+    else { v *= 0.5f; u -= v; }
+    pos = u * P0 + v * P1 + (1.0f - u - v) * P2;
+    rad = v3(L.radiance);
+    pdf_area = L.pdf_point;
+  }
+  pdf_area *= L.pdf_light;
+  const V3 ln = v3(L.normal);
+  float pdf_dir = 1.0f;
+  const V3 d = cos_sampling(rng, ln, &pdf_dir);
+  rad = rad * fminf(1.0f, fmaxf(0.0f, dot(ln, d)));
+  s.o = pos + ln * kRayOffset;
+  s.d = normalized(d);
+  s.flux0 = rad;
+  s.PDF = pdf_area * pdf_dir;
+  s.thr = v3(1.f, 1.f, 1.f);
+  store_float4(ph.pos + base, s.o, 1.0f);
+  store_float4(ph.flux + base, s.flux0 * s.thr * kPI, s.PDF);
+  store_float4(ph.dir + base, s.d, 1.0f);
+  s.ix = 1.0f;
+  s.k = s.loop = s.depth = 0;
+  s.draw = rng.draw;
+}
+
+// Checks at the top of each pass of the bounce loop (SPPM.cpp:549-554);
+// false ends the path.
+__device__ __forceinline__ bool photon_top(PhotonState& s) {
+  if (s.loop++ > 32 || s.k >= kPhotonSlots - 1) return false;
+  return !(s.thr.x < kLt1e8 || s.thr.y < kLt1e8 || s.thr.z < kLt1e8);
+}
+
+// The rest of one pass after the closest hit (SPPM.cpp:556-670); false ends
+// the path.
+__device__ __forceinline__ bool photon_shade(const SceneGPU& sc, const IterParams& it, const PhotonSlots& ph, int i,
+                                             PhotonState& s, const Hit& hit) {
+  Rng rng(photon_seed(it, i));
+  rng.seek(s.draw);
+  const size_t base = (size_t)i * kPhotonSlots;
+  Geom g;
+  calc_geometry(sc, hit, g);
+  g.normal = dot(g.normal, s.d) > 0.0f ? -g.normal : g.normal;
+  V3 nxt_o = g.pos;
+  if (norm2(g.radiance) > kGt1e5) return false;
+  if (g.translucency > 0.5f) {
+    s.thr = s.thr * v3(g.translucency, g.translucency, g.translucency);
+    s.o = g.pos + s.d * kRayOffset;
+    return true;
+  }
+  // russianRulette_PhotonMapping (SPPM.h:33-52)
+  if (s.depth > 16) return false;
+  const float pdf_rus = 0.98f * max3(g.albedo);
+  if (rng.next() > pdf_rus) return false;
+  s.PDF *= pdf_rus;
+  float Ii, Io;
+  if (near1(s.ix)) { Ii = 1.0f; Io = g.index; }
+  else { Ii = s.ix; Io = 1.0f; }
+  FParam p{s.d, s.d, g.normal, Ii, Io, g.rough, g.extinction, g.reflectance};
+  if (g.flags & kMatSPPM) {
+    const size_t slot = base + s.k;
+    store_float4(ph.pos + slot, g.pos, s.ix);
+    store_float4(ph.flux + slot, s.flux0 * s.thr * g.albedo, s.PDF);
+    store_float4(ph.dir + slot, s.d, 1.0f);
+    ++s.k;
+  }
+  float pdf = 1.0f;
+  const V3 nd = surface_sample(g.type, rng, p, &pdf);
+  s.draw = rng.draw;
+  if (!is_valid_direction(nd)) return false;
+  float nix = s.ix;
+  if (g.flags & kMatOpaque) {
+    if (dot(nd, g.normal) < kLt1e6) return false;
+  } else {
+    nix = is_reflect(s.d, nd, g.normal) ? s.ix : Io;
+  }
+  p.out = nd;
+  pdf = surface_pdf(g.type, p);
+  const V3 on = dot(g.normal, nd) > 0.0f ? g.normal : -g.normal;
+  nxt_o = nxt_o + on * kRayOffset;
+  const float brdf = surface_brdf(g.type, p);
+  const float cs = fmaxf(0.0f, fminf(1.0f, dot(nd, on)));
+  if (brdf < kLt1e8) return false;
+  if (pdf < 0.0f) return false;
+  s.thr = s.thr * (g.albedo * cs * brdf);
+  s.PDF *= pdf;
+  s.o = nxt_o; s.d = nd; s.ix = nix;
+  ++s.depth;
+  return true;
+}
+
+// Terminator (SPPM.cpp:672): written one past the last stored photon, which
+// leaves slot k as it was; the compactor (SPPM.cpp:812-822) takes slots up to
+// the first invalid one, so a valid stale slot k joins this iteration.
+__device__ __forceinline__ void photon_finish(const IterParams& it, const PhotonSlots& ph, uint32_t* counts, int i,
+                                              int k) {
+  const size_t base = (size_t)i * kPhotonSlots;
+  uint32_t n;
+  if (it.flags & kFlagFixStaleSlot) {
+    const int term = k > 0 ? k : 1;
+    if (term < kPhotonSlots) ph.dir[base + term].w = 0.0f;
+    n = (uint32_t)term;
+  } else {
+    const int term = k + 1;
+    if (term < kPhotonSlots) ph.dir[base + term].w = 0.0f;
+    n = (k == 0 || ph.dir[base + k].w == 0.0f) ? (uint32_t)(k > 0 ? k : 1) : (uint32_t)(k + 1);
+  }
+  counts[i] = n;
+}
+
+// Appends i to a queue with one atomic per warp.
+__device__ __forceinline__ void queue_push(uint32_t* queue, uint32_t* count, bool push, uint32_t i) {
+  const unsigned m = __ballot_sync(__activemask(), push);
+  if (!m) return;
   const unsigned lane = threadIdx.x & 31u;
-  PhotonPath path;
-  bool active = false, done = false;
-  while (true) {
-    const unsigned need = __ballot_sync(0xffffffffu, !active && !done);
-    if (need) {
-      const int leader = __ffs(need) - 1;
-      uint32_t first = 0;
-      if ((int)lane == leader) first = atomicAdd(work, (uint32_t)__popc(need));
-      first = __shfl_sync(0xffffffffu, first, leader);
-      if (!active && !done) {
-        const uint32_t i = first + (uint32_t)__popc(need & ((1u << lane) - 1u));
-        if (i < (uint32_t)it.photons) {
-          path.start(sc, it, ph, (int)i);
-          active = true;
-        } else {
-          done = true;
-        }
+  const int leader = __ffs(m) - 1;
+  uint32_t base = 0;
+  if ((int)lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
+  base = __shfl_sync(__activemask(), base, leader);
+  if (push) queue[base + __popc(m & ((1u << lane) - 1u))] = i;
+}
+
+__global__ void __launch_bounds__(128) k_pw_emit(SceneGPU sc, IterParams it, PhotonSlots ph, PhotonWave w,
+                                                 uint32_t* counts) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = i < it.photons;
+  PhotonState s;
+  bool go = false;
+  if (live) {
+    photon_start(sc, it, ph, i, s);
+    go = photon_top(s);
+    if (go) store_state(w, i, s);
+    else photon_finish(it, ph, counts, i, s.k);
+  }
+  queue_push(w.queue[0], w.qcount + 0, live && go, (uint32_t)i);
+}
+
+__global__ void __launch_bounds__(128) k_pw_trace(SceneGPU sc, PhotonWave w, int round, int* err) {
+  const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
+  const uint32_t* q = w.queue[round & 1];
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const uint32_t i = q[j];
+    const float4 a = w.a[i], b = w.b[i];
+    Hit h;
+    if (trace_closest(sc, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), kRayOffset, h, err))
+      w.hit[i] = make_float4(h.u, h.v, __int_as_float(h.tri), __int_as_float(h.facet));
+    else
+      w.hit[i] = make_float4(0.f, 0.f, __int_as_float(-1), __int_as_float(-1));
+  }
+}
+
+__global__ void __launch_bounds__(128) k_pw_shade(SceneGPU sc, IterParams it, PhotonSlots ph, PhotonWave w,
+                                                  uint32_t* counts, int round) {
+  const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
+  const uint32_t* q = w.queue[round & 1];
+  uint32_t* qn = w.queue[(round + 1) & 1];
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t n_round = (n + stride - 1) / stride * stride;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n_round; j += stride) {
+    bool keep = false;
+    uint32_t i = 0;
+    if (j < n) {
+      i = q[j];
+      PhotonState s;
+      load_state(w, (int)i, s);
+      const float4 hv = w.hit[i];
+      bool alive = false;
+      if (__float_as_int(hv.z) >= 0) {
+        Hit h;
+        h.t = 0.f; h.u = hv.x; h.v = hv.y; h.tri = __float_as_int(hv.z); h.facet = __float_as_int(hv.w);
+        alive = photon_shade(sc, it, ph, (int)i, s, h) && photon_top(s);
+      }
+      if (alive) {
+        store_state(w, (int)i, s);
+        keep = true;
+      } else {
+        photon_finish(it, ph, counts, (int)i, s.k);
       }
     }
-    if (__all_sync(0xffffffffu, done)) break;
-    if (active && !path.step(sc, ph, err)) {
-      path.finish(it, ph, counts);
-      active = false;
+    queue_push(qn, w.qcount + round + 1, keep, i);
+  }
+}
+
+// Paths alive after the last wavefront round, each run to its end.
+__global__ void __launch_bounds__(128) k_pw_tail(SceneGPU sc, IterParams it, PhotonSlots ph, PhotonWave w,
+                                                 uint32_t* counts, int round, int* err) {
+  const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
+  const uint32_t* q = w.queue[round & 1];
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const int i = (int)q[j];
+    PhotonState s;
+    load_state(w, i, s);
+    while (true) {
+      Hit h;
+      if (!trace_closest(sc, s.o, s.d, kRayOffset, h, err)) break;
+      if (!photon_shade(sc, it, ph, i, s, h) || !photon_top(s)) break;
     }
+    photon_finish(it, ph, counts, i, s.k);
   }
 }
 
@@ -592,17 +692,21 @@ void launch_eye_pass(const SceneGPU& sc, const CameraGPU& cam, const IterParams&
   k_eye_pass<<<blocks_for(n, 128), 128, 0, s>>>(sc, cam, it, rr_eye[0], rr_eye[1], hp, st, gi, err);
 }
 
-void launch_photon_pass(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, uint32_t* counts, uint32_t* work,
+void launch_photon_pass(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, uint32_t* counts, PhotonWave w,
                         int resident_blocks, int* err, cudaStream_t s) {
-  const unsigned need = blocks_for(it.photons, 128);
-  const unsigned grid = resident_blocks > 0 ? std::min<unsigned>(need, (unsigned)resident_blocks) : need;
-  cudaMemsetAsync(work, 0, sizeof(uint32_t), s);
-  k_photon_pass<<<grid, 128, 0, s>>>(sc, it, ph, counts, work, err);
+  const unsigned grid = std::max(1, resident_blocks);
+  cudaMemsetAsync(w.qcount, 0, sizeof(uint32_t) * (kWaveRounds + 2), s);
+  k_pw_emit<<<blocks_for(it.photons, 128), 128, 0, s>>>(sc, it, ph, w, counts);
+  for (int r = 0; r < kWaveRounds; ++r) {
+    k_pw_trace<<<grid, 128, 0, s>>>(sc, w, r, err);
+    k_pw_shade<<<grid, 128, 0, s>>>(sc, it, ph, w, counts, r);
+  }
+  k_pw_tail<<<grid, 128, 0, s>>>(sc, it, ph, w, counts, kWaveRounds, err);
 }
 
 int photon_pass_blocks_per_sm() {
   int b = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_photon_pass, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pw_trace, 128, 0);
   return b;
 }
 

@@ -41,6 +41,16 @@ struct PhotonGrid {
   uint32_t table;        // bucket count, power of two
 };
 
+// Wavefront photon pass: per-path state, hit records and the two queues of
+// live paths (see fr_kernels.cu).  qcount[r] counts the paths of round r.
+constexpr int kWaveRounds = 8;
+struct PhotonWave {
+  float4 *a, *b, *c, *d;  // path state
+  float4* hit;            // u, v, triangle, facet (triangle -1: miss)
+  uint32_t* queue[2];
+  uint32_t* qcount;       // kWaveRounds + 2 counters
+};
+
 // Per-pixel progressive state (SharedHitPoint, SPPM.h:112-126): tau in FP64.
 struct PixelState {
   double* tau;    // [3 * pixels]
@@ -69,8 +79,8 @@ void upload_byte_lut(cudaStream_t s);
 
 void launch_eye_pass(const SceneGPU& sc, const CameraGPU& cam, const IterParams& it, const float* rr_eye,
                      HitpointBuf hp, PixelState st, GridInfo* gi, int* err, cudaStream_t s);
-// Persistent photon pass: resident_blocks blocks of 128 threads (0: one block per 128 paths).
-void launch_photon_pass(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, uint32_t* counts, uint32_t* work,
+// Wavefront photon pass; resident_blocks is the grid of the round kernels.
+void launch_photon_pass(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, uint32_t* counts, PhotonWave w,
                         int resident_blocks, int* err, cudaStream_t s);
 int photon_pass_blocks_per_sm();
 // Points the kernels at the exact-value tables (see fr_bsdf.cuh).

@@ -74,22 +74,32 @@ struct CameraGPU {
   float plane_w, plane_h, lens_w, lens_h, F, dist;
 };
 
-// 8-wide BVH node: child boxes as float SoA, child references.
-// child[c]: internal node index, or kLeafBit | (count-1) << 27 | first triangle,
-// or kEmptyChild.
-constexpr uint32_t kLeafBit = 0x80000000u;
-constexpr uint32_t kEmptyChild = 0xFFFFFFFFu;
-constexpr int kLeafCountShift = 27;
-constexpr uint32_t kLeafFirstMask = (1u << kLeafCountShift) - 1u;
-constexpr int kMaxLeafTris = 16;
-
-struct alignas(64) BVHNode8 {
+// 8-wide BVH node (224 bytes, fourteen 16-byte loads): child boxes as float
+// SoA, then the child bookkeeping.  Internal children are stored contiguously
+// from child_base in slot order; the triangles of leaf children contiguously
+// from tri_base.
+//   meta[c] == 0                : empty slot
+//   imask bit c set             : internal child child_base + popc(imask & ((1<<c)-1))
+//   otherwise (meta[c] & 0x80)  : leaf of ((meta[c] >> 5) & 3) + 1 triangles at
+//                                 tri_base + (meta[c] & 31)
+struct alignas(16) BVHNodeW {
   float lox[8], loy[8], loz[8];
   float hix[8], hiy[8], hiz[8];
-  uint32_t child[8];
-  uint32_t pad[8];
+  uint32_t child_base;
+  uint32_t tri_base;
+  uint32_t imask;
+  uint32_t pad0;
+  uint8_t meta[8];
+  uint32_t pad1[2];
 };
-static_assert(sizeof(BVHNode8) == 256, "node is two 128-byte lines");
+static_assert(sizeof(BVHNodeW) == 224, "node is fourteen 16-byte words");
+
+// Traversal-stack reference: an internal node index, or a leaf run
+// kLeafBit | (count-1) << kLeafCountShift | first triangle.
+constexpr uint32_t kLeafBit = 0x80000000u;
+constexpr int kLeafCountShift = 27;
+constexpr uint32_t kLeafFirstMask = (1u << kLeafCountShift) - 1u;
+constexpr int kMaxLeafTris = 4;
 
 // Triangle in leaf order: v0, e1 = v1 - v0, e2 = v2 - v0 (the exact floats
 // the reference's Moller-Trumbore test forms, Intersect.cpp:67-89);
@@ -109,7 +119,7 @@ struct alignas(16) FacetShade {
 static_assert(sizeof(FacetShade) == 64, "facet record is 64 bytes");
 
 struct SceneGPU {
-  const BVHNode8* nodes;
+  const BVHNodeW* nodes;
   const TriGPU* tris;
   const FacetShade* shade;
   const MaterialGPU* mats;

@@ -87,6 +87,11 @@ struct Rng {
   uint32_t buf[4];
 
   __device__ __forceinline__ explicit Rng(uint32_t seed) : key(seed), draw(0) {}
+  // Continue the stream at draw n (the buffered block is refilled on demand).
+  __device__ __forceinline__ void seek(uint32_t n) {
+    draw = n;
+    if (n & 3u) philox4x32_10(n >> 2, 0u, 0u, 0u, key, kPhiloxKeyHi, buf);
+  }
   __device__ __forceinline__ uint32_t next_u24() {
     const uint32_t lane = draw & 3u;
     if (lane == 0) philox4x32_10(draw >> 2, 0u, 0u, 0u, key, kPhiloxKeyHi, buf);

@@ -50,8 +50,9 @@ __device__ __forceinline__ TriGPU load_tri(const TriGPU* tris, int i) {
   return t;
 }
 
-struct RayBoxPre {
-  float idx, idy, idz, ox, oy, oz;  // inverse direction and origin * inverse direction
+struct RayPre {
+  float idx, idy, idz;  // inverse direction
+  float ox, oy, oz;     // origin
 };
 
 __device__ __forceinline__ float safe_inv(float d) {
@@ -59,52 +60,82 @@ __device__ __forceinline__ float safe_inv(float d) {
   return 1.0f / (fabsf(d) < m ? copysignf(m, d) : d);
 }
 
-// Test the 8 children of a node; returns a bit mask of entered children and
-// their entry distances.
-__device__ __forceinline__ uint32_t node_hits(const BVHNode8* nodes, uint32_t ni, const RayBoxPre& r, float tmin,
-                                              float tmax, float tn[8], uint32_t ch[8]) {
-  const float4* p = reinterpret_cast<const float4*>(nodes + ni);
+// Entry distances of the 8 children of a node, as sort keys (float bits of
+// the entry distance with the slot in the low 3 bits; entry distances are
+// positive, so the integer order is the distance order), and the node's child
+// bookkeeping.  Missed and empty children get 0xFFFFFFFF.
+struct NodeVisit {
+  uint32_t key[8];
+  uint32_t child_base, tri_base, imask;
+  uint32_t meta_lo, meta_hi;
+};
+
+__device__ __forceinline__ void visit_node(const BVHNodeW* nodes, uint32_t ni, const RayPre& r, float tmin,
+                                           float tmax, NodeVisit& nv) {
+  const float4* q = reinterpret_cast<const float4*>(nodes + ni);
   float lx[8], ly[8], lz[8], hx[8], hy[8], hz[8];
-  {
-    float4 q;
-    q = __ldg(p + 0); lx[0] = q.x; lx[1] = q.y; lx[2] = q.z; lx[3] = q.w;
-    q = __ldg(p + 1); lx[4] = q.x; lx[5] = q.y; lx[6] = q.z; lx[7] = q.w;
-    q = __ldg(p + 2); ly[0] = q.x; ly[1] = q.y; ly[2] = q.z; ly[3] = q.w;
-    q = __ldg(p + 3); ly[4] = q.x; ly[5] = q.y; ly[6] = q.z; ly[7] = q.w;
-    q = __ldg(p + 4); lz[0] = q.x; lz[1] = q.y; lz[2] = q.z; lz[3] = q.w;
-    q = __ldg(p + 5); lz[4] = q.x; lz[5] = q.y; lz[6] = q.z; lz[7] = q.w;
-    q = __ldg(p + 6); hx[0] = q.x; hx[1] = q.y; hx[2] = q.z; hx[3] = q.w;
-    q = __ldg(p + 7); hx[4] = q.x; hx[5] = q.y; hx[6] = q.z; hx[7] = q.w;
-    q = __ldg(p + 8); hy[0] = q.x; hy[1] = q.y; hy[2] = q.z; hy[3] = q.w;
-    q = __ldg(p + 9); hy[4] = q.x; hy[5] = q.y; hy[6] = q.z; hy[7] = q.w;
-    q = __ldg(p + 10); hz[0] = q.x; hz[1] = q.y; hz[2] = q.z; hz[3] = q.w;
-    q = __ldg(p + 11); hz[4] = q.x; hz[5] = q.y; hz[6] = q.z; hz[7] = q.w;
-    const uint4 c0 = __ldg(reinterpret_cast<const uint4*>(p + 12));
-    const uint4 c1 = __ldg(reinterpret_cast<const uint4*>(p + 13));
-    ch[0] = c0.x; ch[1] = c0.y; ch[2] = c0.z; ch[3] = c0.w;
-    ch[4] = c1.x; ch[5] = c1.y; ch[6] = c1.z; ch[7] = c1.w;
+#define FR_LD8(arr, i0)                                   \
+  {                                                       \
+    const float4 a_ = __ldg(q + (i0)), b_ = __ldg(q + (i0) + 1); \
+    arr[0] = a_.x; arr[1] = a_.y; arr[2] = a_.z; arr[3] = a_.w;   \
+    arr[4] = b_.x; arr[5] = b_.y; arr[6] = b_.z; arr[7] = b_.w;   \
   }
-  uint32_t mask = 0;
+  FR_LD8(lx, 0) FR_LD8(ly, 2) FR_LD8(lz, 4) FR_LD8(hx, 6) FR_LD8(hy, 8) FR_LD8(hz, 10)
+#undef FR_LD8
+  const uint4 m0 = __ldg(reinterpret_cast<const uint4*>(q + 12));
+  const uint4 m1 = __ldg(reinterpret_cast<const uint4*>(q + 13));
+  nv.child_base = m0.x;
+  nv.tri_base = m0.y;
+  nv.imask = m0.z;
+  nv.meta_lo = m1.x;
+  nv.meta_hi = m1.y;
+  // t = (b - o) * idir, with the products fused (the boxes are padded far
+  // beyond the rounding of the fused form).
+  const float ox = r.ox * r.idx, oy = r.oy * r.idy, oz = r.oz * r.idz;
 #pragma unroll
   for (int c = 0; c < 8; ++c) {
-    // Boxes are padded on the host, so fused rounding here only moves the
-    // slab bounds by far less than the padding.
-    const float ax = fmaf(lx[c], r.idx, -r.ox), bx = fmaf(hx[c], r.idx, -r.ox);
-    const float ay = fmaf(ly[c], r.idy, -r.oy), by = fmaf(hy[c], r.idy, -r.oy);
-    const float az = fmaf(lz[c], r.idz, -r.oz), bz = fmaf(hz[c], r.idz, -r.oz);
+    const float ax = fmaf(lx[c], r.idx, -ox), bx = fmaf(hx[c], r.idx, -ox);
+    const float ay = fmaf(ly[c], r.idy, -oy), by = fmaf(hy[c], r.idy, -oy);
+    const float az = fmaf(lz[c], r.idz, -oz), bz = fmaf(hz[c], r.idz, -oz);
     const float t0 = fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fmaxf(fminf(az, bz), tmin));
     const float t1 = fminf(fminf(fmaxf(ax, bx), fmaxf(ay, by)), fminf(fmaxf(az, bz), tmax));
-    tn[c] = t0;
-    if (t0 <= t1 && ch[c] != kEmptyChild) mask |= 1u << c;
+    const uint32_t mw = c < 4 ? m1.x : m1.y;
+    const bool valid = ((mw >> (8 * (c & 3))) & 0xFFu) != 0u;
+    nv.key[c] = (valid && t0 <= t1) ? ((__float_as_uint(t0) & ~7u) | (uint32_t)c) : 0xFFFFFFFFu;
   }
-  return mask;
+}
+
+// Ascending order of the 8 keys (19-comparator sorting network), in registers.
+__device__ __forceinline__ void sort8(uint32_t k[8]) {
+#define FR_CX(i, j)                              \
+  {                                              \
+    const uint32_t a_ = min(k[i], k[j]);         \
+    k[j] = max(k[i], k[j]);                      \
+    k[i] = a_;                                   \
+  }
+  FR_CX(0, 1) FR_CX(2, 3) FR_CX(4, 5) FR_CX(6, 7) FR_CX(0, 2) FR_CX(1, 3) FR_CX(4, 6) FR_CX(5, 7)
+  FR_CX(1, 2) FR_CX(5, 6) FR_CX(0, 4) FR_CX(3, 7) FR_CX(1, 5) FR_CX(2, 6) FR_CX(1, 4) FR_CX(3, 6)
+  FR_CX(2, 4) FR_CX(3, 5) FR_CX(3, 4)
+#undef FR_CX
+}
+
+// Stack reference of slot c of a visited node.
+__device__ __forceinline__ uint32_t child_ref(const NodeVisit& nv, uint32_t c) {
+  if ((nv.imask >> c) & 1u) return nv.child_base + (uint32_t)__popc(nv.imask & ((1u << c) - 1u));
+  const uint32_t m = ((c < 4 ? nv.meta_lo : nv.meta_hi) >> (8 * (c & 3))) & 0xFFu;
+  return kLeafBit | (((m >> 5) & 3u) << kLeafCountShift) | (nv.tri_base + (m & 31u));
+}
+
+__device__ __forceinline__ RayPre ray_pre(V3 org, V3 dir) {
+  RayPre r;
+  r.idx = safe_inv(dir.x); r.idy = safe_inv(dir.y); r.idz = safe_inv(dir.z);
+  r.ox = org.x; r.oy = org.y; r.oz = org.z;
+  return r;
 }
 
 // Closest hit on (tmin, +inf).  Returns false on a miss; sets *err on stack overflow.
 __device__ bool trace_closest(const SceneGPU& sc, V3 org, V3 dir, float tmin, Hit& hit, int* err) {
-  RayBoxPre r;
-  r.idx = safe_inv(dir.x); r.idy = safe_inv(dir.y); r.idz = safe_inv(dir.z);
-  r.ox = org.x * r.idx; r.oy = org.y * r.idy; r.oz = org.z * r.idz;
+  const RayPre r = ray_pre(org, dir);
   float tbest = FLT_MAX;
   int32_t best_tri = -1, best_facet = -1;
   float bu = 0.0f, bv = 0.0f;
@@ -115,35 +146,23 @@ __device__ bool trace_closest(const SceneGPU& sc, V3 org, V3 dir, float tmin, Hi
   while (true) {
     if (tref <= tbest) {
       if (!(ref & kLeafBit)) {
-        float tn[8];
-        uint32_t ch[8];
-        uint32_t mask = node_hits(sc.nodes, ref, r, tmin, tbest, tn, ch);
-        // Visit the nearest entered child next; stack the others far to near.
-        int n = 0;
-        uint32_t ord_c[8];
-        float ord_t[8];
-        while (mask) {
-          const int c = __ffs(mask) - 1;
-          mask &= mask - 1;
-          float t = tn[c];
-          uint32_t cc = ch[c];
-          int j = n++;
-          while (j > 0 && ord_t[j - 1] < t) {
-            ord_t[j] = ord_t[j - 1];
-            ord_c[j] = ord_c[j - 1];
-            --j;
-          }
-          ord_t[j] = t;
-          ord_c[j] = cc;
-        }
-        if (n > 0) {
+        NodeVisit nv;
+        visit_node(sc.nodes, ref, r, tmin, tbest, nv);
+        sort8(nv.key);
+        if (nv.key[0] != 0xFFFFFFFFu) {
+          // Nearest child next; the others stacked far to near.
+          int n = 1;
+#pragma unroll
+          for (int k = 1; k < 8; ++k) n += nv.key[k] != 0xFFFFFFFFu;
           if (sp + n - 1 > kTraversalStack) {
             atomicOr(err, kErrStack);
             return false;
           }
-          for (int k = 0; k < n - 1; ++k) stack[sp++] = make_uint2(ord_c[k], __float_as_uint(ord_t[k]));
-          ref = ord_c[n - 1];
-          tref = ord_t[n - 1];
+#pragma unroll
+          for (int k = 7; k >= 1; --k)
+            if (k < n) stack[sp++] = make_uint2(child_ref(nv, nv.key[k] & 7u), nv.key[k] & ~7u);
+          ref = child_ref(nv, nv.key[0] & 7u);
+          tref = __uint_as_float(nv.key[0] & ~7u);
           continue;
         }
       } else {
@@ -173,26 +192,24 @@ __device__ bool trace_closest(const SceneGPU& sc, V3 org, V3 dir, float tmin, Hi
 
 // Any hit with t in (tmin, tmax] (findAnyElement, bvh8.h:643-707).
 __device__ bool trace_any(const SceneGPU& sc, V3 org, V3 dir, float tmin, float tmax, int* err) {
-  RayBoxPre r;
-  r.idx = safe_inv(dir.x); r.idy = safe_inv(dir.y); r.idz = safe_inv(dir.z);
-  r.ox = org.x * r.idx; r.oy = org.y * r.idy; r.oz = org.z * r.idz;
+  const RayPre r = ray_pre(org, dir);
   uint32_t stack[kTraversalStack];
   int sp = 0;
   uint32_t ref = 0;
   while (true) {
     if (!(ref & kLeafBit)) {
-      float tn[8];
-      uint32_t ch[8];
-      uint32_t mask = node_hits(sc.nodes, ref, r, tmin, tmax, tn, ch);
-      if (sp + __popc(mask) > kTraversalStack) {
+      NodeVisit nv;
+      visit_node(sc.nodes, ref, r, tmin, tmax, nv);
+      int n = 0;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) n += nv.key[k] != 0xFFFFFFFFu;
+      if (sp + n > kTraversalStack) {
         atomicOr(err, kErrStack);
         return false;
       }
-      while (mask) {
-        const int c = __ffs(mask) - 1;
-        mask &= mask - 1;
-        stack[sp++] = ch[c];
-      }
+#pragma unroll
+      for (int k = 0; k < 8; ++k)
+        if (nv.key[k] != 0xFFFFFFFFu) stack[sp++] = child_ref(nv, (uint32_t)k);
     } else {
       const int first = (int)(ref & kLeafFirstMask);
       const int count = (int)((ref >> kLeafCountShift) & 0xFu) + 1;
