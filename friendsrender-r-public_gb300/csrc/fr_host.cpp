@@ -218,7 +218,7 @@ struct fr_ctx {
   PixelState st{};
   PhotonSlots ph{};
   uint32_t* counts = nullptr;
-  PhotonWave wave{};             // wavefront photon-pass state
+  PathWave wave{};               // wavefront state, shared by the eye and photon passes
   int photon_blocks = 0;         // grid of the wavefront round kernels
   PhotonGrid grid{};
   GridInfo* gi = nullptr;
@@ -429,11 +429,14 @@ int run_iteration(fr_ctx* c) {
   cudaStream_t s = c->stream;
   {
     StageMark m(c, FR_STAGE_EYE);
-    launch_eye_pass(c->sc, c->cam, it, c->rr_eye, c->hp, c->st, c->gi, c->err, s);
+    FR_CUDA(cudaMemsetAsync(c->wave.qcount, 0, sizeof(uint32_t) * 2 * (kWaveRounds + 2), s));
+    launch_eye_pass(c->sc, c->cam, it, c->rr_eye, c->hp, c->st, c->gi, c->wave, c->photon_blocks, c->err, s);
   }
   {
     StageMark m(c, FR_STAGE_PHOTON);
-    launch_photon_pass(c->sc, it, c->ph, c->counts, c->wave, c->photon_blocks, c->err, s);
+    PathWave pw = c->wave;
+    pw.qcount += kWaveRounds + 2;
+    launch_photon_pass(c->sc, it, c->ph, c->counts, pw, c->photon_blocks, c->err, s);
   }
   {
     StageMark m(c, FR_STAGE_GRID);
@@ -447,7 +450,8 @@ int run_iteration(fr_ctx* c) {
     StageMark m(c, FR_STAGE_GATHER);
     launch_gather_update(c->sc, it, c->hp, c->grid, c->gi, c->st, c->dbg_m, c->dbg_phi, s);
   }
-  c->launches += 5 + 2 + 2 * kWaveRounds;  // eye, photon emit/rounds/tail, grid setup, count, scatter, gather
+  // eye and photon passes (start, rounds, tail), grid setup, count, scatter, gather
+  c->launches += 4 + 2 * (2 + 2 * kWaveRounds);
   c->photons_total += c->P;
   FR_CUDA(cudaGetLastError());
   return FR_OK;
@@ -596,15 +600,16 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
   // ---- per-iteration buffers (all allocated here; iterations allocate nothing)
   const size_t npix = (size_t)c->W * c->H;
   const size_t nslots = (size_t)c->P * kPhotonSlots;
+  const size_t wave_n = std::max(npix, (size_t)c->P);
   if ((rc = c->alloc(&c->hp.pos, npix)) || (rc = c->alloc(&c->hp.nrm, npix)) || (rc = c->alloc(&c->hp.out, npix)) ||
       (rc = c->alloc(&c->hp.wgt, npix)) || (rc = c->alloc(&c->st.tau, 3 * npix)) || (rc = c->alloc(&c->st.n, npix)) ||
       (rc = c->alloc(&c->st.r, npix)) || (rc = c->alloc(&c->st.g, npix)) || (rc = c->alloc(&c->ph.pos, nslots)) ||
       (rc = c->alloc(&c->ph.flux, nslots)) || (rc = c->alloc(&c->ph.dir, nslots)) ||
-      (rc = c->alloc(&c->counts, (size_t)c->P)) || (rc = c->alloc(&c->wave.a, (size_t)c->P)) ||
-      (rc = c->alloc(&c->wave.b, (size_t)c->P)) || (rc = c->alloc(&c->wave.c, (size_t)c->P)) ||
-      (rc = c->alloc(&c->wave.d, (size_t)c->P)) || (rc = c->alloc(&c->wave.hit, (size_t)c->P)) ||
-      (rc = c->alloc(&c->wave.queue[0], (size_t)c->P)) || (rc = c->alloc(&c->wave.queue[1], (size_t)c->P)) ||
-      (rc = c->alloc(&c->wave.qcount, (size_t)kWaveRounds + 2)) || (rc = c->alloc(&c->gi, 1)) ||
+      (rc = c->alloc(&c->counts, (size_t)c->P)) || (rc = c->alloc(&c->wave.a, wave_n)) ||
+      (rc = c->alloc(&c->wave.b, wave_n)) || (rc = c->alloc(&c->wave.c, wave_n)) ||
+      (rc = c->alloc(&c->wave.d, wave_n)) || (rc = c->alloc(&c->wave.hit, wave_n)) ||
+      (rc = c->alloc(&c->wave.queue[0], wave_n)) || (rc = c->alloc(&c->wave.queue[1], wave_n)) ||
+      (rc = c->alloc(&c->wave.qcount, 2 * ((size_t)kWaveRounds + 2))) || (rc = c->alloc(&c->gi, 1)) ||
       (rc = c->alloc(&c->err, 1)) ||
       (rc = c->alloc(&c->dbg_m, npix)) || (rc = c->alloc(&c->dbg_phi, npix)) || (rc = c->alloc(&c->image, npix)))
     return bail(rc);

@@ -1,8 +1,10 @@
 // SPPM iteration kernels for sm_103a.
 //
 // One iteration (StochasticProgressivePhotonMapping, SPPM/SPPM/SPPM.cpp:768-848):
-//   k_eye_pass       createHitpoints + getHitpointInfo  (SPPM.cpp:98-353)
-//   k_pw_emit / k_pw_trace / k_pw_shade / k_pw_tail
+//   k_ew_start / k_wave_trace / k_ew_shade / k_ew_tail
+//                    createHitpoints + getHitpointInfo  (SPPM.cpp:98-353)
+//                    as a wavefront over queues of live paths
+//   k_pw_emit / k_wave_trace / k_pw_shade / k_pw_tail
 //                    createPhotonMap + generateLightRay (SPPM.cpp:453-680)
 //                    as a wavefront over queues of live paths
 //   k_grid_setup / k_photon_count / scan / k_photon_scatter
@@ -65,91 +67,120 @@ __device__ __forceinline__ void camera_ray(const CameraGPU& c, float u, float v,
 }
 
 // ------------------------------------------------------------------ eye pass
-__global__ void __launch_bounds__(128) k_eye_pass(SceneGPU sc, CameraGPU cam, IterParams it, float rr5, float rr6,
-                                                  HitpointBuf hp, PixelState st, GridInfo* gi, int* err) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int npix = it.width * it.height;
-  int hit_type = kHitNone;
-  float radius = 0.0f;
-  if (i < npix) {
-    const int w = i % it.width, h = i / it.width;
-    const float u = (float)w / (float)it.width;
-    const float v = (float)h / (float)it.height;
-    Rng rng((uint32_t)i + (uint32_t)npix * it.step);
-    const float s0 = rng.next(), s1 = rng.next(), s2 = rng.next();
-    V3 org, dir;
-    float cam_pdf;
-    camera_ray(cam, u, v, s0, s1, s2, org, dir, cam_pdf);
+// createHitpoints + getHitpointInfo (SPPM.cpp:98-353) as a wavefront: k_ew_start
+// makes every camera ray, rounds of k_wave_trace and k_ew_shade advance the
+// live paths, k_ew_tail finishes the rest.  A path ends at its first SPPM
+// surface (makeHitPoint, SPPM.cpp:79-96): with no IBL nothing after the first
+// hitpoint reaches the image.
+//
+// Path state between kernels (one entry per pixel):
+//   a: origin.xyz, ray index of refraction   b: direction.xyz, PDF
+//   c: throughput.xyz, camera PDF            d: draw counter, depth
+struct EyeState {
+  V3 o, d, thr;
+  float ix, PDF, cam_pdf;
+  uint32_t draw;
+  int depth;
+};
 
-    V3 cur_o = org, cur_d = dir, nxt_o = org, nxt_d = dir;
-    float cur_ix = 1.0f, nxt_ix = 1.0f;
-    float PDF = 1.0f;
-    V3 thr = v3(1.f, 1.f, 1.f);
-    int depth = 0;
-    while (true) {
-      if (depth > 6) break;
-      if (depth > 4) {
-        const float rus = depth == 5 ? rr5 : rr6;
-        if (rng.next() > rus) break;
-        PDF *= rus;
-      }
-      Hit hit;
-      if (!trace_closest(sc, cur_o, cur_d, kRayOffset, hit, err)) {
-        hit_type = kHitOnlyDirect;  // miss: ONLY_DIRECTLIGHT with no IBL (SPPM.cpp:290-300)
-        break;
-      }
-      Geom g;
-      calc_geometry(sc, hit, g);
-      g.normal = dot(g.normal, cur_d) > 0.0f ? -g.normal : g.normal;
-      nxt_o = g.pos;
-      if (g.translucency > 0.5f) {
-        thr = thr * v3(g.translucency, g.translucency, g.translucency);
-        cur_o = g.pos + cur_d * kRayOffset;
-        continue;
-      }
-      if (g.flags & kMatSPPM) {
-        // makeHitPoint (SPPM.cpp:79-96); with no IBL nothing after the first
-        // hitpoint reaches the image, so the path stops here.
-        const V3 wgt = (thr / PDF) / cam_pdf;
-        store_float4(hp.pos + i, g.pos, __int_as_float(kHitHit));
-        store_float4(hp.nrm + i, g.normal, g.rough);
-        store_float4(hp.out + i, -cur_d, __int_as_float(g.mat));
-        store_float4(hp.wgt + i, wgt, __int_as_float(hit.facet));
-        hit_type = kHitHit;
-        radius = st.r[i];
-        break;
-      }
-      float Ii, Io;
-      if (near1(cur_ix)) { Ii = 1.0f; Io = g.index; }
-      else { Ii = cur_ix; Io = 1.0f; }
-      FParam p{cur_d, nxt_d, g.normal, Ii, Io, g.rough, g.extinction, g.reflectance};
-      float pdf = 1.0f;
-      nxt_d = surface_sample(g.type, rng, p, &pdf);
-      if (!is_valid_direction(nxt_d)) break;
-      if (g.flags & kMatOpaque) {
-        if (dot(nxt_d, g.normal) < kLt1e6) break;
-      } else {
-        const bool reflect = !(dot(nxt_d, g.normal) < 0.0f);
-        nxt_ix = reflect ? cur_ix : Io;
-      }
-      p.out = nxt_d;
-      pdf = surface_pdf(g.type, p);
-      const V3 on = dot(g.normal, nxt_d) > 0.0f ? g.normal : -g.normal;
-      nxt_o = nxt_o + on * kRayOffset;
-      const float brdf = surface_brdf(g.type, p);
-      const float cs = fmaxf(0.0f, fminf(1.0f, dot(nxt_d, on)));
-      if (brdf < kLt1e8) break;
-      if (pdf < 0.0f) break;
-      thr = thr * (g.albedo * cs * brdf);
-      PDF *= pdf;
-      cur_o = nxt_o; cur_d = nxt_d; cur_ix = nxt_ix;
-      ++depth;
-    }
-    if (hit_type != kHitHit) store_float4(hp.pos + i, v3(0.f, 0.f, 0.f), __int_as_float(hit_type));
+__device__ __forceinline__ uint32_t eye_seed(const IterParams& it, int i) {
+  return (uint32_t)i + (uint32_t)(it.width * it.height) * it.step;  // SPPM.cpp:334
+}
+
+__device__ __forceinline__ void load_eye(const PathWave& w, int i, EyeState& s) {
+  const float4 a = w.a[i], b = w.b[i], c = w.c[i], d = w.d[i];
+  s.o = v3(a.x, a.y, a.z); s.ix = a.w;
+  s.d = v3(b.x, b.y, b.z); s.PDF = b.w;
+  s.thr = v3(c.x, c.y, c.z); s.cam_pdf = c.w;
+  s.draw = __float_as_uint(d.x);
+  s.depth = __float_as_int(d.y);
+}
+
+__device__ __forceinline__ void store_eye(const PathWave& w, int i, const EyeState& s) {
+  w.a[i] = make_float4(s.o.x, s.o.y, s.o.z, s.ix);
+  w.b[i] = make_float4(s.d.x, s.d.y, s.d.z, s.PDF);
+  w.c[i] = make_float4(s.thr.x, s.thr.y, s.thr.z, s.cam_pdf);
+  w.d[i] = make_float4(__uint_as_float(s.draw), __int_as_float(s.depth), 0.f, 0.f);
+}
+
+// Top of the bounce loop (SPPM.cpp:99-122): depth cap and Russian roulette
+// with p = exp(4 - depth) above depth 4.  false ends the path.
+__device__ __forceinline__ bool eye_top(EyeState& s, Rng& rng, float rr5, float rr6) {
+  if (s.depth > 6) return false;
+  if (s.depth > 4) {
+    const float rus = s.depth == 5 ? rr5 : rr6;
+    if (rng.next() > rus) return false;
+    s.PDF *= rus;
   }
-  // Radii of this iteration's hitpoints, for the grid's cell size.
-  float rs = radius;
-  unsigned cnt = hit_type == kHitHit ? 1u : 0u;
+  return true;
+}
+
+// The rest of one pass after the closest hit (SPPM.cpp:123-305).  Returns
+// kHitHit after writing a hitpoint, kHitNone when the path ends without one,
+// and -1 when it goes on.
+__device__ __forceinline__ int eye_shade(const SceneGPU& sc, const HitpointBuf& hp, int i, EyeState& s, Rng& rng,
+                                         const Hit& hit, float rr5, float rr6) {
+  Geom g;
+  calc_geometry(sc, hit, g);
+  g.normal = dot(g.normal, s.d) > 0.0f ? -g.normal : g.normal;
+  V3 nxt_o = g.pos;
+  if (g.translucency > 0.5f) {
+    s.thr = s.thr * v3(g.translucency, g.translucency, g.translucency);
+    s.o = g.pos + s.d * kRayOffset;
+    return eye_top(s, rng, rr5, rr6) ? -1 : kHitNone;
+  }
+  if (g.flags & kMatSPPM) {
+    const V3 wgt = (s.thr / s.PDF) / s.cam_pdf;
+    store_float4(hp.pos + i, g.pos, __int_as_float(kHitHit));
+    store_float4(hp.nrm + i, g.normal, g.rough);
+    store_float4(hp.out + i, -s.d, __int_as_float(g.mat));
+    store_float4(hp.wgt + i, wgt, __int_as_float(hit.facet));
+    return kHitHit;
+  }
+  float Ii, Io;
+  if (near1(s.ix)) { Ii = 1.0f; Io = g.index; }
+  else { Ii = s.ix; Io = 1.0f; }
+  FParam p{s.d, s.d, g.normal, Ii, Io, g.rough, g.extinction, g.reflectance};
+  float pdf = 1.0f;
+  const V3 nd = surface_sample(g.type, rng, p, &pdf);
+  if (!is_valid_direction(nd)) return kHitNone;
+  float nix = s.ix;
+  if (g.flags & kMatOpaque) {
+    if (dot(nd, g.normal) < kLt1e6) return kHitNone;
+  } else {
+    const bool reflect = !(dot(nd, g.normal) < 0.0f);
+    nix = reflect ? s.ix : Io;
+  }
+  p.out = nd;
+  pdf = surface_pdf(g.type, p);
+  const V3 on = dot(g.normal, nd) > 0.0f ? g.normal : -g.normal;
+  nxt_o = nxt_o + on * kRayOffset;
+  const float brdf = surface_brdf(g.type, p);
+  const float cs = fmaxf(0.0f, fminf(1.0f, dot(nd, on)));
+  if (brdf < kLt1e8) return kHitNone;
+  if (pdf < 0.0f) return kHitNone;
+  s.thr = s.thr * (g.albedo * cs * brdf);
+  s.PDF *= pdf;
+  s.o = nxt_o; s.d = nd; s.ix = nix;
+  ++s.depth;
+  return eye_top(s, rng, rr5, rr6) ? -1 : kHitNone;
+}
+
+// End of an eye path: the hit code of a pixel without a hitpoint, and the
+// radius of this iteration's hitpoints summed per warp for the grid's cell
+// size.  Every lane of the warp calls it.
+__device__ __forceinline__ void eye_finish(const HitpointBuf& hp, const PixelState& st, GridInfo* gi, bool ended,
+                                           int i, int hit_type) {
+  float rs = 0.0f;
+  unsigned cnt = 0;
+  if (ended) {
+    if (hit_type == kHitHit) {
+      rs = st.r[i];
+      cnt = 1;
+    } else {
+      store_float4(hp.pos + i, v3(0.f, 0.f, 0.f), __int_as_float(hit_type));
+    }
+  }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     rs += __shfl_down_sync(0xffffffffu, rs, o);
@@ -158,6 +189,131 @@ __global__ void __launch_bounds__(128) k_eye_pass(SceneGPU sc, CameraGPU cam, It
   if ((threadIdx.x & 31) == 0 && cnt) {
     atomicAdd(&gi->r_sum, rs);
     atomicAdd(&gi->r_count, cnt);
+  }
+}
+
+// Appends i to a queue with one atomic per warp.
+__device__ __forceinline__ void queue_push(uint32_t* queue, uint32_t* count, bool push, uint32_t i) {
+  const unsigned m = __ballot_sync(__activemask(), push);
+  if (!m) return;
+  const unsigned lane = threadIdx.x & 31u;
+  const int leader = __ffs(m) - 1;
+  uint32_t base = 0;
+  if ((int)lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
+  base = __shfl_sync(__activemask(), base, leader);
+  if (push) queue[base + __popc(m & ((1u << lane) - 1u))] = i;
+}
+
+__global__ void __launch_bounds__(128) k_ew_start(CameraGPU cam, IterParams it, PathWave w) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  const bool live = i < it.width * it.height;
+  if (live) {
+    const int px = i % it.width, py = i / it.width;
+    const float u = (float)px / (float)it.width;
+    const float v = (float)py / (float)it.height;
+    Rng rng(eye_seed(it, i));
+    const float s0 = rng.next(), s1 = rng.next(), s2 = rng.next();
+    EyeState s;
+    camera_ray(cam, u, v, s0, s1, s2, s.o, s.d, s.cam_pdf);
+    s.ix = 1.0f;
+    s.PDF = 1.0f;
+    s.thr = v3(1.f, 1.f, 1.f);
+    s.depth = 0;
+    s.draw = rng.draw;
+    store_eye(w, i, s);
+  }
+  queue_push(w.queue[0], w.qcount + 0, live, (uint32_t)i);
+}
+
+// Closest hit of every path in queue `round` (eye or photon wave).
+__global__ void __launch_bounds__(128) k_wave_trace(SceneGPU sc, PathWave w, int round, int* err) {
+  const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
+  const uint32_t* q = w.queue[round & 1];
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const uint32_t i = q[j];
+    const float4 a = w.a[i], b = w.b[i];
+    Hit h;
+    if (trace_closest(sc, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), kRayOffset, h, err))
+      w.hit[i] = make_float4(h.u, h.v, __int_as_float(h.tri), __int_as_float(h.facet));
+    else
+      w.hit[i] = make_float4(0.f, 0.f, __int_as_float(-1), __int_as_float(-1));
+  }
+}
+
+__device__ __forceinline__ bool wave_hit(const PathWave& w, uint32_t i, Hit& h) {
+  const float4 hv = w.hit[i];
+  h.t = 0.f; h.u = hv.x; h.v = hv.y; h.tri = __float_as_int(hv.z); h.facet = __float_as_int(hv.w);
+  return h.tri >= 0;
+}
+
+__global__ void __launch_bounds__(128) k_ew_shade(SceneGPU sc, IterParams it, float rr5, float rr6, PathWave w,
+                                                  HitpointBuf hp, PixelState st, GridInfo* gi, int round) {
+  const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
+  const uint32_t* q = w.queue[round & 1];
+  uint32_t* qn = w.queue[(round + 1) & 1];
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t n_round = (n + stride - 1) / stride * stride;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n_round; j += stride) {
+    bool keep = false, ended = false;
+    int hit_type = kHitNone;
+    uint32_t i = 0;
+    if (j < n) {
+      i = q[j];
+      EyeState s;
+      load_eye(w, (int)i, s);
+      Hit h;
+      if (!wave_hit(w, i, h)) {
+        hit_type = kHitOnlyDirect;  // miss: ONLY_DIRECTLIGHT with no IBL (SPPM.cpp:290-300)
+        ended = true;
+      } else {
+        Rng rng(eye_seed(it, (int)i));
+        rng.seek(s.draw);
+        const int r = eye_shade(sc, hp, (int)i, s, rng, h, rr5, rr6);
+        if (r < 0) {
+          s.draw = rng.draw;
+          store_eye(w, (int)i, s);
+          keep = true;
+        } else {
+          hit_type = r;
+          ended = true;
+        }
+      }
+    }
+    eye_finish(hp, st, gi, ended, (int)i, hit_type);
+    queue_push(qn, w.qcount + round + 1, keep, i);
+  }
+}
+
+// Eye paths alive after the last wavefront round, each run to its end.
+__global__ void __launch_bounds__(128) k_ew_tail(SceneGPU sc, IterParams it, float rr5, float rr6, PathWave w,
+                                                 HitpointBuf hp, PixelState st, GridInfo* gi, int round, int* err) {
+  const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
+  const uint32_t* q = w.queue[round & 1];
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t n_round = (n + stride - 1) / stride * stride;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n_round; j += stride) {
+    int hit_type = kHitNone;
+    int i = 0;
+    if (j < n) {
+      i = (int)q[j];
+      EyeState s;
+      load_eye(w, i, s);
+      Rng rng(eye_seed(it, i));
+      rng.seek(s.draw);
+      while (true) {
+        Hit h;
+        if (!trace_closest(sc, s.o, s.d, kRayOffset, h, err)) {
+          hit_type = kHitOnlyDirect;
+          break;
+        }
+        const int r = eye_shade(sc, hp, i, s, rng, h, rr5, rr6);
+        if (r >= 0) {
+          hit_type = r;
+          break;
+        }
+      }
+    }
+    eye_finish(hp, st, gi, j < n, i, hit_type);
   }
 }
 
@@ -186,7 +342,7 @@ __device__ __forceinline__ uint32_t photon_seed(const IterParams& it, int i) {
   return (uint32_t)i + 135u + it.step * (uint32_t)it.photons;  // SPPM.cpp:520
 }
 
-__device__ __forceinline__ void load_state(const PhotonWave& w, int i, PhotonState& s) {
+__device__ __forceinline__ void load_state(const PathWave& w, int i, PhotonState& s) {
   const float4 a = w.a[i], b = w.b[i], c = w.c[i], d = w.d[i];
   s.o = v3(a.x, a.y, a.z); s.ix = a.w;
   s.d = v3(b.x, b.y, b.z); s.PDF = b.w;
@@ -197,7 +353,7 @@ __device__ __forceinline__ void load_state(const PhotonWave& w, int i, PhotonSta
   s.k = (int)(m & 0xFFu); s.loop = (int)((m >> 8) & 0xFFu); s.depth = (int)(m >> 16);
 }
 
-__device__ __forceinline__ void store_state(const PhotonWave& w, int i, const PhotonState& s) {
+__device__ __forceinline__ void store_state(const PathWave& w, int i, const PhotonState& s) {
   w.a[i] = make_float4(s.o.x, s.o.y, s.o.z, s.ix);
   w.b[i] = make_float4(s.d.x, s.d.y, s.d.z, s.PDF);
   w.c[i] = make_float4(s.thr.x, s.thr.y, s.thr.z, s.flux0.x);
@@ -335,19 +491,7 @@ __device__ __forceinline__ void photon_finish(const IterParams& it, const Photon
   counts[i] = n;
 }
 
-// Appends i to a queue with one atomic per warp.
-__device__ __forceinline__ void queue_push(uint32_t* queue, uint32_t* count, bool push, uint32_t i) {
-  const unsigned m = __ballot_sync(__activemask(), push);
-  if (!m) return;
-  const unsigned lane = threadIdx.x & 31u;
-  const int leader = __ffs(m) - 1;
-  uint32_t base = 0;
-  if ((int)lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
-  base = __shfl_sync(__activemask(), base, leader);
-  if (push) queue[base + __popc(m & ((1u << lane) - 1u))] = i;
-}
-
-__global__ void __launch_bounds__(128) k_pw_emit(SceneGPU sc, IterParams it, PhotonSlots ph, PhotonWave w,
+__global__ void __launch_bounds__(128) k_pw_emit(SceneGPU sc, IterParams it, PhotonSlots ph, PathWave w,
                                                  uint32_t* counts) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   const bool live = i < it.photons;
@@ -362,21 +506,7 @@ __global__ void __launch_bounds__(128) k_pw_emit(SceneGPU sc, IterParams it, Pho
   queue_push(w.queue[0], w.qcount + 0, live && go, (uint32_t)i);
 }
 
-__global__ void __launch_bounds__(128) k_pw_trace(SceneGPU sc, PhotonWave w, int round, int* err) {
-  const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
-  const uint32_t* q = w.queue[round & 1];
-  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
-    const uint32_t i = q[j];
-    const float4 a = w.a[i], b = w.b[i];
-    Hit h;
-    if (trace_closest(sc, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), kRayOffset, h, err))
-      w.hit[i] = make_float4(h.u, h.v, __int_as_float(h.tri), __int_as_float(h.facet));
-    else
-      w.hit[i] = make_float4(0.f, 0.f, __int_as_float(-1), __int_as_float(-1));
-  }
-}
-
-__global__ void __launch_bounds__(128) k_pw_shade(SceneGPU sc, IterParams it, PhotonSlots ph, PhotonWave w,
+__global__ void __launch_bounds__(128) k_pw_shade(SceneGPU sc, IterParams it, PhotonSlots ph, PathWave w,
                                                   uint32_t* counts, int round) {
   const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
   const uint32_t* q = w.queue[round & 1];
@@ -390,13 +520,8 @@ __global__ void __launch_bounds__(128) k_pw_shade(SceneGPU sc, IterParams it, Ph
       i = q[j];
       PhotonState s;
       load_state(w, (int)i, s);
-      const float4 hv = w.hit[i];
-      bool alive = false;
-      if (__float_as_int(hv.z) >= 0) {
-        Hit h;
-        h.t = 0.f; h.u = hv.x; h.v = hv.y; h.tri = __float_as_int(hv.z); h.facet = __float_as_int(hv.w);
-        alive = photon_shade(sc, it, ph, (int)i, s, h) && photon_top(s);
-      }
+      Hit h;
+      const bool alive = wave_hit(w, i, h) && photon_shade(sc, it, ph, (int)i, s, h) && photon_top(s);
       if (alive) {
         store_state(w, (int)i, s);
         keep = true;
@@ -409,7 +534,7 @@ __global__ void __launch_bounds__(128) k_pw_shade(SceneGPU sc, IterParams it, Ph
 }
 
 // Paths alive after the last wavefront round, each run to its end.
-__global__ void __launch_bounds__(128) k_pw_tail(SceneGPU sc, IterParams it, PhotonSlots ph, PhotonWave w,
+__global__ void __launch_bounds__(128) k_pw_tail(SceneGPU sc, IterParams it, PhotonSlots ph, PathWave w,
                                                  uint32_t* counts, int round, int* err) {
   const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
   const uint32_t* q = w.queue[round & 1];
@@ -687,18 +812,24 @@ void upload_byte_lut(cudaStream_t s) {
 }
 
 void launch_eye_pass(const SceneGPU& sc, const CameraGPU& cam, const IterParams& it, const float* rr_eye,
-                     HitpointBuf hp, PixelState st, GridInfo* gi, int* err, cudaStream_t s) {
+                     HitpointBuf hp, PixelState st, GridInfo* gi, PathWave w, int resident_blocks, int* err,
+                     cudaStream_t s) {
   const int n = it.width * it.height;
-  k_eye_pass<<<blocks_for(n, 128), 128, 0, s>>>(sc, cam, it, rr_eye[0], rr_eye[1], hp, st, gi, err);
+  const unsigned grid = std::max(1, resident_blocks);
+  k_ew_start<<<blocks_for(n, 128), 128, 0, s>>>(cam, it, w);
+  for (int r = 0; r < kWaveRounds; ++r) {
+    k_wave_trace<<<grid, 128, 0, s>>>(sc, w, r, err);
+    k_ew_shade<<<grid, 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, r);
+  }
+  k_ew_tail<<<grid, 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, kWaveRounds, err);
 }
 
-void launch_photon_pass(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, uint32_t* counts, PhotonWave w,
+void launch_photon_pass(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, uint32_t* counts, PathWave w,
                         int resident_blocks, int* err, cudaStream_t s) {
   const unsigned grid = std::max(1, resident_blocks);
-  cudaMemsetAsync(w.qcount, 0, sizeof(uint32_t) * (kWaveRounds + 2), s);
   k_pw_emit<<<blocks_for(it.photons, 128), 128, 0, s>>>(sc, it, ph, w, counts);
   for (int r = 0; r < kWaveRounds; ++r) {
-    k_pw_trace<<<grid, 128, 0, s>>>(sc, w, r, err);
+    k_wave_trace<<<grid, 128, 0, s>>>(sc, w, r, err);
     k_pw_shade<<<grid, 128, 0, s>>>(sc, it, ph, w, counts, r);
   }
   k_pw_tail<<<grid, 128, 0, s>>>(sc, it, ph, w, counts, kWaveRounds, err);
@@ -706,7 +837,7 @@ void launch_photon_pass(const SceneGPU& sc, const IterParams& it, PhotonSlots ph
 
 int photon_pass_blocks_per_sm() {
   int b = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pw_trace, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wave_trace, 128, 0);
   return b;
 }
 

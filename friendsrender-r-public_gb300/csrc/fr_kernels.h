@@ -41,14 +41,19 @@ struct PhotonGrid {
   uint32_t table;        // bucket count, power of two
 };
 
-// Wavefront photon pass: per-path state, hit records and the two queues of
-// live paths (see fr_kernels.cu).  qcount[r] counts the paths of round r.
-constexpr int kWaveRounds = 8;
-struct PhotonWave {
+// Wavefront passes: per-path state, hit records and the two queues of live
+// paths (see fr_kernels.cu), shared by the eye and the photon pass.  qcount[r]
+// counts the paths of round r; each pass has its own kWaveRounds + 2 counters,
+// zeroed once per iteration.
+#ifndef FR_WAVE_ROUNDS
+#define FR_WAVE_ROUNDS 8
+#endif
+constexpr int kWaveRounds = FR_WAVE_ROUNDS;
+struct PathWave {
   float4 *a, *b, *c, *d;  // path state
   float4* hit;            // u, v, triangle, facet (triangle -1: miss)
   uint32_t* queue[2];
-  uint32_t* qcount;       // kWaveRounds + 2 counters
+  uint32_t* qcount;
 };
 
 // Per-pixel progressive state (SharedHitPoint, SPPM.h:112-126): tau in FP64.
@@ -77,10 +82,12 @@ struct ScanTemp {
 
 void upload_byte_lut(cudaStream_t s);
 
+// Wavefront eye pass; resident_blocks is the grid of the round kernels.
 void launch_eye_pass(const SceneGPU& sc, const CameraGPU& cam, const IterParams& it, const float* rr_eye,
-                     HitpointBuf hp, PixelState st, GridInfo* gi, int* err, cudaStream_t s);
+                     HitpointBuf hp, PixelState st, GridInfo* gi, PathWave w, int resident_blocks, int* err,
+                     cudaStream_t s);
 // Wavefront photon pass; resident_blocks is the grid of the round kernels.
-void launch_photon_pass(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, uint32_t* counts, PhotonWave w,
+void launch_photon_pass(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, uint32_t* counts, PathWave w,
                         int resident_blocks, int* err, cudaStream_t s);
 int photon_pass_blocks_per_sm();
 // Points the kernels at the exact-value tables (see fr_bsdf.cuh).
