@@ -4,11 +4,13 @@
 // Each function restates the reference's arithmetic in its own evaluation
 // order and precision.  Where the reference's expression is promoted to
 // double (a double literal or a double-returning libm call: sqrt, sincos) the
-// restatement computes in double too, or reads a table of the exact result;
-// where it calls powf(x, -2.0f) the restatement uses pow_m2; pow(x, 2) is an
-// exact square (the compiler folds it in the reference's build); comparisons
-// of a float with a double constant use the equivalent float threshold.
+// restatement returns the same float without FP64 arithmetic in all but rare
+// cases (fr_exact.cuh), or reads a table of the exact result; where it calls
+// powf(x, -2.0f) the restatement uses pow_m2; pow(x, 2) is an exact square
+// (the compiler folds it in the reference's build); comparisons of a float
+// with a double constant use the equivalent float threshold.
 #pragma once
+#include "fr_exact.cuh"
 #include "fr_layout.h"
 #include "fr_math.cuh"
 
@@ -107,7 +109,7 @@ __device__ __forceinline__ V3 ggx_sampling(Rng& rng, V3 normal, V3 in, float alp
   const float2 cs = __ldg(c_sincos_tab + rng.next_u24());
   const float e = rng.next();
   const float den = e * (alpha * alpha - 1.0f) + 1.0f;
-  const float cth = (float)sqrt((1.0 - (double)e) / (double)den);
+  const float cth = ggx_cth(e, den);
   V3 e2, e3;
   frame(e1, e2, e3);
   const float cph = cs.x, sph = cs.y;
@@ -119,8 +121,7 @@ __device__ __forceinline__ V3 ggx_sampling(Rng& rng, V3 normal, V3 in, float alp
   const float wm_N = dot(mN, normal);
   const float wo_wm = dot(result, mN);
   const float x = 1.0f - (1.0f - alpha * alpha) * wm_N * wm_N;
-  const double p = (double)(alpha * alpha) / ((double)kPI * ((double)x * (double)x)) * (double)wm_N / (double)(4.0f * wo_wm);
-  *pdf = (float)p;
+  *pdf = ggx_pdf(alpha * alpha, x, wm_N, 4.0f * wo_wm, kPI);
   return result;
 }
 
@@ -146,8 +147,7 @@ __device__ __forceinline__ V3 ggxglass_sampling(Rng& rng, V3 normal, V3 in, floa
   const V3 e1 = NN;
   const float2 cs = __ldg(c_sincos_tab + rng.next_u24());
   const float e = rng.next();
-  const double den = (double)e * ((double)(alpha * alpha) - 0.99999) + 1.0;
-  const float cth = (float)sqrt((1.0000001 - (double)e) / den);
+  const float cth = glass_cth(e, alpha * alpha);
   V3 e2, e3;
   frame(e1, e2, e3);
   const float cph = cs.x, sph = cs.y;
@@ -177,9 +177,7 @@ __device__ __forceinline__ V3 ggxglass_sampling(Rng& rng, V3 normal, V3 in, floa
   const float A = (1.0f - reflectance) * wm_N;
   const float B = io * io * wo_wm;
   const float s = ii * wi_wm + io * wo_wm;
-  const double q = (double)B / ((double)s * (double)s);
-  const double p = (double)A * q * (double)alpha * (double)alpha / (double)(kPI * (y * y));
-  *pdf = (float)p;
+  *pdf = glass_pdf(A, B, s, alpha, kPI * (y * y));
   return result;
 }
 
@@ -229,20 +227,20 @@ __device__ __forceinline__ float roughconductor_brdf(const FParam& p) {
   const float lc = fmaxf(0.0f, fminf(0.9999f, dot(p.in, -p.n)));
   const float lv = fmaxf(0.0f, fminf(0.9999f, dot(p.out, p.n)));
   if (lc < kSMin || lv < kSMin) return 0.0f;
-  const float L_l = (float)((-1.0f + sqrt(1.0f + (double)(alpha * alpha) * ((double)(1.0f / (lc * lc)) - 1.0))) * 0.5);
-  const float L_v = (float)((-1.0f + sqrt(1.0f + (double)(alpha * alpha) * ((double)(1.0f / (lv * lv)) - 1.0))) * 0.5);
+  const float L_l = conductor_lambda(alpha * alpha, 1.0f / (lc * lc));
+  const float L_v = conductor_lambda(alpha * alpha, 1.0f / (lv * lv));
   const float G = 1.0f / ((1.0f + L_l) * (1.0f + L_v));
   const float fcos = dot(p.n, -p.in);
   const float temp = eta * eta - k * k - (1.0f - fcos * fcos);
   const float apb = sqrtf(temp * temp + k * k * eta * eta);
-  const float a = (float)sqrt((double)(apb + temp) * 0.5);
+  const float a = sqrt_half(apb + temp);
   const float tm1 = apb + fcos * fcos;
   const float tm2 = a * 2.0f * fcos;
   const float rs2 = (tm1 - tm2) / (tm1 + tm2);
-  const float tm3 = (float)((double)(apb * fcos * fcos) + (double)(1.0f - fcos * fcos) * (1.0 - (double)(fcos * fcos)));
+  const float tm3 = conductor_tm3(apb * fcos * fcos, 1.0f - fcos * fcos, fcos * fcos);
   const float tm4 = tm2 * (1.0f - fcos * fcos);
   const float rp2 = rs2 * (tm3 - tm4) / (tm3 + tm4);
-  const float F = (float)(0.5 * (double)(rp2 + rs2));
+  const float F = 0.5f * (rp2 + rs2);  // (float)(0.5 * (double)x) rounds 0.5 * x once, as this does
   const float fx = (4.0f * dot(p.in, -p.n) * dot(p.out, p.n));
   return (F * G * D) / fx;
 }
@@ -315,7 +313,7 @@ __device__ __forceinline__ float surface_brdf(int type, const FParam& p) {
     case 1: {
       if (!opaque_reflect(p)) return 0.0f;
       const V3 ref = reflect_sampling(p.n, p.in);
-      if (dot(ref, p.out) > 1.0f - 1.0f / kDeltaPDF) return (float)((double)kDeltaPDF / ((double)dot(p.out, p.n) + 0.00001));
+      if (dot(ref, p.out) > 1.0f - 1.0f / kDeltaPDF) return metal_brdf(dot(p.out, p.n), kDeltaPDF);
       return 0.0f;
     }
     case 2: return roughconductor_brdf(p);

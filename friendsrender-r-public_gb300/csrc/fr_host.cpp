@@ -859,6 +859,13 @@ int fr_radius_count_noalloc(const float* hp_dev, int32_t num_hitpoints, const fl
   return FR_OK;
 }
 
+int fr_check_exact_math(uint64_t samples, uint32_t seed, uint64_t* mismatches, uint64_t* fast_paths) {
+  if (!mismatches || !fast_paths) return fail(FR_ERR_INVALID, "fr_check_exact_math: NULL output");
+  const char* msg = "";
+  if (check_exact_math(samples, seed, mismatches, fast_paths, &msg)) return fail(FR_ERR_CUDA, "fr_check_exact_math: %s", msg);
+  return FR_OK;
+}
+
 int fr_read_hitpoints(fr_ctx* c, float* pos_type, float* nrm_rough, float* out_mat, float* wgt_facet) {
   if (!c) return fail(FR_ERR_INVALID, "fr_read_hitpoints: NULL context");
   const size_t bytes = sizeof(float4) * (size_t)c->W * c->H;

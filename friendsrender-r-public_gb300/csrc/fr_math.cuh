@@ -51,13 +51,6 @@ constexpr float kLt1e8 = 0x1.5798f0p-27f;      // (double)g < 1e-8
 constexpr float kGt0_999999 = 0x1.ffffdep-1f;  // (double)g > 0.999999
 constexpr float kGt0_9 = 0x1.ccccccp-1f;       // (double)g > 0.9
 
-// x^-2 for a float x, rounded once from the exact double square: the value
-// the reference's powf(x, -2.0f) returns.
-__device__ __forceinline__ float pow_m2(float x) {
-  const double xd = (double)x;
-  return (float)(1.0 / (xd * xd));
-}
-
 // ---------------------------------------------------------------- Philox
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).  A stream is keyed by the
 // reference's integer seed; draw n is lane n%4 of block n/4; a draw is the

@@ -57,7 +57,7 @@ class Stats(C.Structure):
 EXPORTS = ['fr_last_error', 'fr_create', 'fr_iterate', 'fr_synchronize', 'fr_resolve', 'fr_resolve_dev',
            'fr_get_stats', 'fr_stream', 'fr_destroy', 'fr_trace_closest', 'fr_trace_any', 'fr_radius_query',
            'fr_read_hitpoints', 'fr_read_photon_slots', 'fr_read_gather', 'fr_read_state', 'fr_profile_enable',
-           'fr_profile_read', 'fr_radius_count_noalloc']
+           'fr_profile_read', 'fr_radius_count_noalloc', 'fr_check_exact_math']
 
 STAGES = ('eye', 'photon', 'grid', 'gather')
 
@@ -95,6 +95,7 @@ def load(path=None):
     lib.fr_profile_enable.argtypes = [vp, i32, i32]
     lib.fr_profile_read.argtypes = [vp, vp, vp, vp]
     lib.fr_radius_count_noalloc.argtypes = [vp, i32, vp, i32, f32, vp, vp]
+    lib.fr_check_exact_math.argtypes = [C.c_uint64, C.c_uint32, vp, vp]
     _lib = lib
     return lib
 
@@ -271,3 +272,16 @@ class Renderer:
         g = np.empty(n, np.int32)
         _check(_lib.fr_read_state(self.h, _ptr(tau), _ptr(N), _ptr(r), _ptr(g)), 'fr_read_state')
         return dict(tau=tau, n=N, r=r, g=g)
+
+
+EXACT_FUNCTIONS = ('pow_m2', 'ggx_cth', 'ggx_pdf', 'glass_cth', 'glass_pdf', 'metal_brdf', 'conductor_lambda',
+                   'conductor_tm3', 'sqrt_half')
+
+
+def check_exact_math(samples, seed=1):
+    """fr_check_exact_math: {function: (fast-path count, mismatches)}."""
+    lib = load()
+    mm = np.zeros(len(EXACT_FUNCTIONS), np.uint64)
+    fp = np.zeros(len(EXACT_FUNCTIONS), np.uint64)
+    _check(lib.fr_check_exact_math(int(samples), int(seed), _ptr(mm), _ptr(fp)), 'fr_check_exact_math')
+    return {n: (int(fp[k]), int(mm[k])) for k, n in enumerate(EXACT_FUNCTIONS)}

@@ -207,6 +207,18 @@ int fr_radius_query(fr_ctx* ctx, const float* hp, int32_t num_hitpoints, const f
 int fr_radius_count_noalloc(const float* hp_dev, int32_t num_hitpoints, const float* photons_dev,
                             int32_t num_photons, float cell, int32_t* counts_dev, void* stream);
 
+/* No reference counterpart: a device self-check of the kernels' float
+ * replacements for the reference's double-precision expressions.  Evaluates
+ * each of FR_EXACT_FUNCTIONS functions on `samples` seeded random inputs both
+ * ways and returns, per function, how often the float path produced a value
+ * (fast_paths) and how often that value differed from the double expression's
+ * (mismatches, 0 when the replacement is exact).  Functions, in order: pow_m2,
+ * GGX sampling cos(theta), GGX sampling pdf, GGX glass cos(theta), GGX glass
+ * refraction pdf, metal BRDF, conductor masking term, conductor tm3, conductor
+ * square root. */
+#define FR_EXACT_FUNCTIONS 9
+int fr_check_exact_math(uint64_t samples, uint32_t seed, uint64_t* mismatches, uint64_t* fast_paths);
+
 /* Hitpoints of the last iteration (SoA, see HitpointBuf in the kernels):
  * each array width*height*4 floats; any pointer may be NULL. */
 int fr_read_hitpoints(fr_ctx* ctx, float* pos_type, float* nrm_rough, float* out_mat, float* wgt_facet);
