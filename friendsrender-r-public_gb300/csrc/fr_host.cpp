@@ -220,6 +220,7 @@ struct fr_ctx {
   uint32_t* counts = nullptr;
   PathWave wave{};               // wavefront state, shared by the eye and photon passes
   int photon_blocks = 0;         // grid of the wavefront round kernels
+  int gather_blocks = 0;         // grid of the gather (one warp per hitpoint)
   PhotonGrid grid{};
   GridInfo* gi = nullptr;
   ScanTemp scan{};
@@ -429,7 +430,8 @@ int run_iteration(fr_ctx* c) {
   cudaStream_t s = c->stream;
   {
     StageMark m(c, FR_STAGE_EYE);
-    FR_CUDA(cudaMemsetAsync(c->wave.qcount, 0, sizeof(uint32_t) * 2 * (kWaveRounds + 2), s));
+    // Queue counters of both passes and the hitpoint-list count.
+    FR_CUDA(cudaMemsetAsync(c->wave.qcount, 0, sizeof(uint32_t) * (2 * (kWaveRounds + 2) + 1), s));
     launch_eye_pass(c->sc, c->cam, it, c->rr_eye, c->hp, c->st, c->gi, c->wave, c->photon_blocks, c->err, s);
   }
   {
@@ -448,7 +450,9 @@ int run_iteration(fr_ctx* c) {
   }
   {
     StageMark m(c, FR_STAGE_GATHER);
-    launch_gather_update(c->sc, it, c->hp, c->grid, c->gi, c->st, c->dbg_m, c->dbg_phi, s);
+    FR_CUDA(cudaMemsetAsync(c->dbg_m, 0, sizeof(int32_t) * (size_t)c->W * c->H, s));
+    FR_CUDA(cudaMemsetAsync(c->dbg_phi, 0, sizeof(float4) * (size_t)c->W * c->H, s));
+    launch_gather_update(c->sc, it, c->hp, c->grid, c->gi, c->st, c->dbg_m, c->dbg_phi, c->gather_blocks, s);
   }
   // eye and photon passes (start, rounds, tail), grid setup, count, scatter, gather
   c->launches += 4 + 2 * (2 + 2 * kWaveRounds);
@@ -511,6 +515,7 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
   if ((rc = exact_tables(dev, &tabs))) return bail(rc);
   upload_tables(tabs.sincos, tabs.sqrt1m, c->stream);
   c->photon_blocks = std::max(1, photon_pass_blocks_per_sm()) * sms;
+  c->gather_blocks = std::max(1, gather_blocks_per_sm()) * sms;
 
   // ---- geometry
   const int T = scene->num_facets;
@@ -609,10 +614,12 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
       (rc = c->alloc(&c->wave.b, wave_n)) || (rc = c->alloc(&c->wave.c, wave_n)) ||
       (rc = c->alloc(&c->wave.d, wave_n)) || (rc = c->alloc(&c->wave.hit, wave_n)) ||
       (rc = c->alloc(&c->wave.queue[0], wave_n)) || (rc = c->alloc(&c->wave.queue[1], wave_n)) ||
-      (rc = c->alloc(&c->wave.qcount, 2 * ((size_t)kWaveRounds + 2))) || (rc = c->alloc(&c->gi, 1)) ||
+      (rc = c->alloc(&c->wave.qcount, 2 * ((size_t)kWaveRounds + 2) + 1)) || (rc = c->alloc(&c->hp.list, npix)) ||
+      (rc = c->alloc(&c->gi, 1)) ||
       (rc = c->alloc(&c->err, 1)) ||
       (rc = c->alloc(&c->dbg_m, npix)) || (rc = c->alloc(&c->dbg_phi, npix)) || (rc = c->alloc(&c->image, npix)))
     return bail(rc);
+  c->hp.list_count = c->wave.qcount + 2 * (kWaveRounds + 2);
   // Photon grid: one bucket per expected photon or better (a few photons per path).
   c->grid.table = next_pow2(std::max<uint64_t>((uint64_t)c->P * 4, 1u << 16));
   const size_t cap = nslots;

@@ -10,7 +10,7 @@
 //   k_grid_setup / k_photon_count / scan / k_photon_scatter
 //                    photon cell grid, replacing the photon kd-tree
 //                    (SPPM.cpp:809-833, kdtree.h:348-431)
-//   k_gather_update  applyHitPointInfo                  (SPPM.cpp:395-451)
+//   k_gather         applyHitPointInfo                  (SPPM.cpp:395-451)
 //   k_resolve        reconstructImageFromSharedPoints   (SPPM.cpp:473-493)
 // The eye and photon passes draw from independent per-pixel / per-path
 // streams, so running the eye pass first gives the same numbers as the
@@ -166,9 +166,21 @@ __device__ __forceinline__ int eye_shade(const SceneGPU& sc, const HitpointBuf& 
   return eye_top(s, rng, rr5, rr6) ? -1 : kHitNone;
 }
 
-// End of an eye path: the hit code of a pixel without a hitpoint, and the
-// radius of this iteration's hitpoints summed per warp for the grid's cell
-// size.  Every lane of the warp calls it.
+// Appends i to a queue with one atomic per warp.
+__device__ __forceinline__ void queue_push(uint32_t* queue, uint32_t* count, bool push, uint32_t i) {
+  const unsigned m = __ballot_sync(__activemask(), push);
+  if (!m) return;
+  const unsigned lane = threadIdx.x & 31u;
+  const int leader = __ffs(m) - 1;
+  uint32_t base = 0;
+  if ((int)lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
+  base = __shfl_sync(__activemask(), base, leader);
+  if (push) queue[base + __popc(m & ((1u << lane) - 1u))] = i;
+}
+
+// End of an eye path: the hit code of a pixel without a hitpoint, the list
+// of this iteration's hitpoints, and their radius summed per warp for the
+// grid's cell size.  Every lane of the warp calls it.
 __device__ __forceinline__ void eye_finish(const HitpointBuf& hp, const PixelState& st, GridInfo* gi, bool ended,
                                            int i, int hit_type) {
   float rs = 0.0f;
@@ -181,6 +193,7 @@ __device__ __forceinline__ void eye_finish(const HitpointBuf& hp, const PixelSta
       store_float4(hp.pos + i, v3(0.f, 0.f, 0.f), __int_as_float(hit_type));
     }
   }
+  queue_push(hp.list, hp.list_count, cnt != 0, (uint32_t)i);
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
     rs += __shfl_down_sync(0xffffffffu, rs, o);
@@ -190,18 +203,6 @@ __device__ __forceinline__ void eye_finish(const HitpointBuf& hp, const PixelSta
     atomicAdd(&gi->r_sum, rs);
     atomicAdd(&gi->r_count, cnt);
   }
-}
-
-// Appends i to a queue with one atomic per warp.
-__device__ __forceinline__ void queue_push(uint32_t* queue, uint32_t* count, bool push, uint32_t i) {
-  const unsigned m = __ballot_sync(__activemask(), push);
-  if (!m) return;
-  const unsigned lane = threadIdx.x & 31u;
-  const int leader = __ffs(m) - 1;
-  uint32_t base = 0;
-  if ((int)lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
-  base = __shfl_sync(__activemask(), base, leader);
-  if (push) queue[base + __popc(m & ((1u << lane) - 1u))] = i;
 }
 
 __global__ void __launch_bounds__(128) k_ew_start(CameraGPU cam, IterParams it, PathWave w) {
@@ -690,56 +691,126 @@ __device__ __forceinline__ void for_each_photon_in_ball(const PhotonGrid& g, con
       }
 }
 
-__global__ void __launch_bounds__(128) k_gather_update(SceneGPU sc, IterParams it, HitpointBuf hp, PhotonGrid g,
-                                                       const GridInfo* gip, PixelState st, int32_t* dbg_m,
-                                                       float4* dbg_phi) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= it.width * it.height) return;
-  const float4 hp0 = hp.pos[i];
-  if (__float_as_int(hp0.w) != kHitHit) {
-    if (dbg_m) { dbg_m[i] = 0; dbg_phi[i] = make_float4(0.f, 0.f, 0.f, 0.f); }
-    return;
-  }
+// applyHitPointInfo (SPPM.cpp:395-451) with one warp per hitpoint of the
+// hitpoint list.  The warp's lanes take one overlapping cell each, scan the
+// cells' photon counts, and then share out the candidates of all cells, 32 at
+// a time, so every lane tests and (if inside the ball) shades its own photon.
+// Per-lane Kahan FP32 sums are added in a fixed butterfly order; the N/tau/R
+// update follows with tau in FP64.
+__global__ void __launch_bounds__(256) k_gather(SceneGPU sc, IterParams it, HitpointBuf hp, PhotonGrid g,
+                                               const GridInfo* gip, PixelState st, int32_t* dbg_m, float4* dbg_phi) {
+  const unsigned lane = threadIdx.x & 31u;
+  const uint32_t n = *(volatile const uint32_t*)hp.list_count;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
   const GridInfo gi = *gip;
-  const float4 hn = hp.nrm[i], ho = hp.out[i], hw = hp.wgt[i];
-  const V3 x = v3(hp0.x, hp0.y, hp0.z), n = v3(hn.x, hn.y, hn.z), out = v3(ho.x, ho.y, ho.z);
-  const V3 W = v3(hw.x, hw.y, hw.z);
-  const MaterialGPU& m = sc.mats[__float_as_int(ho.w)];
-  const int type = m.type;
-  const float R = st.r[i];
-  int M = 0;
-  // Compensated (Kahan) FP32 sum of this iteration's flux.
-  float sx = 0.f, sy = 0.f, sz = 0.f, cx = 0.f, cy = 0.f, cz = 0.f;
-  for_each_photon_in_ball(g, gi, x, R, [&](uint32_t j, float4 p4) {
-    const float4 f4 = __ldg(g.flux + j);
-    const float4 d4 = __ldg(g.dir + j);
-    const V3 indir = v3(d4.x, d4.y, d4.z);
-    const float Ii = p4.w;
-    const float Io = near1(p4.w) ? m.index : 1.0f;
-    const V3 nn = dot(indir, n) < 0.0f ? n : -n;
-    const FParam p{indir, out, nn, Ii, Io, hn.w, m.extinction, m.reflectance};
-    const float brdf = surface_brdf(type, p);
-    const V3 add = W * brdf * v3(f4.x, f4.y, f4.z) / f4.w;
-    float y, t;
-    y = add.x - cx; t = sx + y; cx = (t - sx) - y; sx = t;
-    y = add.y - cy; t = sy + y; cy = (t - sy) - y; sy = t;
-    y = add.z - cz; t = sz + y; cz = (t - sz) - y; sz = t;
-    ++M;
-  });
-  if (dbg_m) { dbg_m[i] = M; dbg_phi[i] = make_float4(sx, sy, sz, 0.f); }
-  if (M > 0) {
-    // N/tau/R update (SPPM.cpp:444-449); tau kept in FP64.
-    const int N = st.n[i];
-    const float a = (float)N + it.alpha * (float)M;
-    const float b = (float)(N + M);
-    double* tau = st.tau + 3 * (size_t)i;
-    const double ad = (double)a, bd = (double)b;
-    tau[0] = (tau[0] + (double)sx) * ad / bd;
-    tau[1] = (tau[1] + (double)sy) * ad / bd;
-    tau[2] = (tau[2] + (double)sz) * ad / bd;
-    st.r[i] = R * sqrtf(a / b);
-    st.n[i] = (int)((float)N + (float)M * it.alpha);
-    st.g[i] += 1;
+  const float inv = gi.inv_cell;
+  const uint32_t mask = g.table - 1u;
+  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n; w += nwarps) {
+    const uint32_t i = hp.list[w];
+    const float4 hp0 = hp.pos[i], hn = hp.nrm[i], ho = hp.out[i], hw = hp.wgt[i];
+    const V3 x = v3(hp0.x, hp0.y, hp0.z), nrm = v3(hn.x, hn.y, hn.z), out = v3(ho.x, ho.y, ho.z);
+    const MaterialGPU& mat = sc.mats[__float_as_int(ho.w)];
+    const int type = mat.type;
+    const float R = st.r[i];
+    const V3 bmin = x - R * v3(1.f, 1.f, 1.f);
+    const V3 bmax = x + R * v3(1.f, 1.f, 1.f);
+    const float R2 = R * R;
+    const int x0 = cell_of(bmin.x, gi.origin[0], inv), nx = cell_of(bmax.x, gi.origin[0], inv) - x0 + 1;
+    const int y0 = cell_of(bmin.y, gi.origin[1], inv), ny = cell_of(bmax.y, gi.origin[1], inv) - y0 + 1;
+    const int z0 = cell_of(bmin.z, gi.origin[2], inv), nz = cell_of(bmax.z, gi.origin[2], inv) - z0 + 1;
+    const int ncell = nx * ny * nz;
+    int M = 0;
+    float sx = 0.f, sy = 0.f, sz = 0.f, kx = 0.f, ky = 0.f, kz = 0.f;
+    for (int c0 = 0; c0 < ncell; c0 += 32) {
+      const int c = c0 + (int)lane;
+      int cx = 0, cy = 0, cz = 0;
+      uint32_t cb = 0, cn = 0;
+      if (c < ncell) {
+        const int q = c / nx;
+        cx = x0 + (c - q * nx);
+        cy = y0 + q % ny;
+        cz = z0 + q / ny;
+        const uint32_t h = cell_hash(cx, cy, cz, mask);
+        cb = __ldg(g.cell_start + h);
+        cn = __ldg(g.cell_start + h + 1) - cb;
+      }
+      uint32_t incl = cn;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
+        if ((int)lane >= o) incl += t;
+      }
+      const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
+      for (uint32_t t0 = 0; t0 < total; t0 += 32) {
+        const uint32_t k = t0 + lane;
+        // Source lane: the first whose inclusive count exceeds k.
+        int src = 0;
+#pragma unroll
+        for (int step = 16; step; step >>= 1) {
+          const uint32_t v = __shfl_sync(0xffffffffu, incl, src + step - 1);
+          if (v <= k) src += step;
+        }
+        const uint32_t sb = __shfl_sync(0xffffffffu, cb, src);
+        const uint32_t se = __shfl_sync(0xffffffffu, incl, src) - __shfl_sync(0xffffffffu, cn, src);
+        const int scx = __shfl_sync(0xffffffffu, cx, src);
+        const int scy = __shfl_sync(0xffffffffu, cy, src);
+        const int scz = __shfl_sync(0xffffffffu, cz, src);
+        if (k >= total) continue;
+        const uint32_t j = sb + (k - se);
+        const float4 p4 = __ldg(g.pos + j);
+        // Query box (kdtree.h:78-88, SPPM.cpp:424-428), ball (SPPM.cpp:432),
+        // and the photon's own cell only (hash collisions share buckets).
+        if (cell_of(p4.x, gi.origin[0], inv) != scx || cell_of(p4.y, gi.origin[1], inv) != scy ||
+            cell_of(p4.z, gi.origin[2], inv) != scz)
+          continue;
+        if (bmin.x > p4.x || bmax.x < p4.x || bmin.y > p4.y || bmax.y < p4.y || bmin.z > p4.z || bmax.z < p4.z)
+          continue;
+        if (!(norm2(v3(p4.x, p4.y, p4.z) - x) < R2)) continue;
+        const float4 f4 = __ldg(g.flux + j);
+        const float4 d4 = __ldg(g.dir + j);
+        const V3 indir = v3(d4.x, d4.y, d4.z);
+        const float Ii = p4.w;
+        const float Io = near1(p4.w) ? mat.index : 1.0f;
+        const V3 nn = dot(indir, nrm) < 0.0f ? nrm : -nrm;
+        const FParam p{indir, out, nn, Ii, Io, hn.w, mat.extinction, mat.reflectance};
+        const float brdf = surface_brdf(type, p);
+        const V3 add = v3(hw.x, hw.y, hw.z) * brdf * v3(f4.x, f4.y, f4.z) / f4.w;
+        float y, t;
+        y = add.x - kx; t = sx + y; kx = (t - sx) - y; sx = t;
+        y = add.y - ky; t = sy + y; ky = (t - sy) - y; sy = t;
+        y = add.z - kz; t = sz + y; kz = (t - sz) - y; sz = t;
+        ++M;
+      }
+    }
+    M = __reduce_add_sync(0xffffffffu, M);
+    float vx = sx - kx, vy = sy - ky, vz = sz - kz;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      vx += __shfl_xor_sync(0xffffffffu, vx, o);
+      vy += __shfl_xor_sync(0xffffffffu, vy, o);
+      vz += __shfl_xor_sync(0xffffffffu, vz, o);
+    }
+    vx = __shfl_sync(0xffffffffu, vx, 0);
+    vy = __shfl_sync(0xffffffffu, vy, 0);
+    vz = __shfl_sync(0xffffffffu, vz, 0);
+    if (lane == 0 && dbg_m) {
+      dbg_m[i] = M;
+      dbg_phi[i] = make_float4(vx, vy, vz, 0.f);
+    }
+    if (M > 0 && lane < 3) {
+      // N/tau/R update (SPPM.cpp:444-449); lane c updates tau component c.
+      const int N = st.n[i];
+      const float a = (float)N + it.alpha * (float)M;
+      const float b = (float)(N + M);
+      double* tau = st.tau + 3 * (size_t)i + lane;
+      const float v = lane == 0 ? vx : (lane == 1 ? vy : vz);
+      *tau = (*tau + (double)v) * (double)a / (double)b;
+      if (lane == 0) {
+        st.r[i] = R * sqrtf(a / b);
+        st.n[i] = (int)((float)N + (float)M * it.alpha);
+        st.g[i] += 1;
+      }
+    }
   }
 }
 
@@ -902,9 +973,14 @@ int launch_scan(uint32_t* in, uint32_t* out, uint32_t n, ScanTemp& t, cudaStream
 }
 
 void launch_gather_update(const SceneGPU& sc, const IterParams& it, HitpointBuf hp, PhotonGrid g, const GridInfo* gi,
-                          PixelState st, int32_t* dbg_m, float4* dbg_phi, cudaStream_t s) {
-  const int n = it.width * it.height;
-  k_gather_update<<<blocks_for(n, 128), 128, 0, s>>>(sc, it, hp, g, gi, st, dbg_m, dbg_phi);
+                          PixelState st, int32_t* dbg_m, float4* dbg_phi, int resident_blocks, cudaStream_t s) {
+  k_gather<<<std::max(1, resident_blocks), 256, 0, s>>>(sc, it, hp, g, gi, st, dbg_m, dbg_phi);
+}
+
+int gather_blocks_per_sm() {
+  int b = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_gather, 256, 0);
+  return b;
 }
 
 void launch_resolve(PixelState st, int pixels, double photons_total, double iterations, float4* out, cudaStream_t s) {

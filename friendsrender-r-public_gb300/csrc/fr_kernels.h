@@ -16,6 +16,8 @@ struct HitpointBuf {
   float4* nrm;
   float4* out;
   float4* wgt;
+  uint32_t* list;        // pixels holding a hitpoint this iteration, in no set order
+  uint32_t* list_count;  // zeroed before the eye pass
 };
 
 // Photon slots: kPhotonSlots per path, persistent across iterations as the
@@ -102,8 +104,10 @@ void launch_photon_scatter(PhotonSlots ph, const uint32_t* counts, int paths, in
                            cudaStream_t s);
 // Words of block-sum scratch launch_scan needs for n elements; fills the level sizes of t.
 uint32_t scan_temp_words(uint32_t n, ScanTemp& t);
+// One warp per listed hitpoint; resident_blocks blocks of 256 threads.
 void launch_gather_update(const SceneGPU& sc, const IterParams& it, HitpointBuf hp, PhotonGrid g, const GridInfo* gi,
-                          PixelState st, int32_t* dbg_m, float4* dbg_phi, cudaStream_t s);
+                          PixelState st, int32_t* dbg_m, float4* dbg_phi, int resident_blocks, cudaStream_t s);
+int gather_blocks_per_sm();
 void launch_resolve(PixelState st, int pixels, double photons_total, double iterations, float4* out, cudaStream_t s);
 
 // Parity entry points.
