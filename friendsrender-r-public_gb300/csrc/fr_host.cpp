@@ -218,7 +218,10 @@ struct fr_ctx {
   PixelState st{};
   PhotonSlots ph{};
   uint32_t* counts = nullptr;
-  PathWave wave{};               // wavefront state, shared by the eye and photon passes
+  PathWave wave{};               // photon-pass wavefront state
+  PathWave eye_wave{};           // eye-pass wavefront state (the passes run concurrently)
+  cudaStream_t side = nullptr;   // the eye pass's stream, forked from and joined to `stream`
+  cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   int photon_blocks = 0;         // grid of the wavefront round kernels
   int gather_blocks = 0;         // grid of the gather (one warp per hitpoint)
   PhotonGrid grid{};
@@ -256,8 +259,12 @@ struct fr_ctx {
   }
   ~fr_ctx() {
     if (stream) cudaStreamSynchronize(stream);
+    if (side) cudaStreamSynchronize(side);
     for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
     for (auto& b : bufs) cudaFree(b.p);
+    if (fork_ev) cudaEventDestroy(fork_ev);
+    if (join_ev) cudaEventDestroy(join_ev);
+    if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -405,18 +412,23 @@ uint32_t next_pow2(uint64_t v) {
 struct StageMark {
   fr_ctx* c;
   int stage;
+  cudaStream_t s;
   cudaEvent_t stop = nullptr;
-  StageMark(fr_ctx* ctx, int st) : c(ctx), stage(st) {
+  StageMark(fr_ctx* ctx, int st, cudaStream_t stream) : c(ctx), stage(st), s(stream) {
     if (!c->profiling || c->ev_used + 2 > c->ev_pool.size()) return;
     cudaEvent_t start = c->ev_pool[c->ev_used++];
     stop = c->ev_pool[c->ev_used++];
-    cudaEventRecord(start, c->stream);
+    cudaEventRecord(start, s);
     c->ev_marks.push_back({stage, {start, stop}});
   }
   ~StageMark() {
-    if (stop) cudaEventRecord(stop, c->stream);
+    if (stop) cudaEventRecord(stop, s);
   }
 };
+
+// Per-iteration counters: both passes' round queues, the hitpoint list and
+// both passes' shade queues.
+constexpr size_t kCounters = 2 * (kWaveRounds + 2) + 1 + 2 * kWaveRounds * kShadeQueues;
 
 int run_iteration(fr_ctx* c) {
   const uint32_t step = (uint32_t)(++c->iterations);
@@ -428,20 +440,27 @@ int run_iteration(fr_ctx* c) {
   it.alpha = c->alpha;
   it.flags = c->flags;
   cudaStream_t s = c->stream;
+  // Queue counters of both passes and the hitpoint-list count.
+  FR_CUDA(cudaMemsetAsync(c->eye_wave.qcount, 0, sizeof(uint32_t) * kCounters, s));
+  // The eye pass (side stream) and the photon pass (main stream) share
+  // nothing but the error word, so they run concurrently: each fills the
+  // SMs that the other's last, nearly empty rounds leave idle.  The grid
+  // needs both (cell size from the hitpoint radii).
+  FR_CUDA(cudaEventRecord(c->fork_ev, s));
+  FR_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
   {
-    StageMark m(c, FR_STAGE_EYE);
-    // Queue counters of both passes and the hitpoint-list count.
-    FR_CUDA(cudaMemsetAsync(c->wave.qcount, 0, sizeof(uint32_t) * (2 * (kWaveRounds + 2) + 1), s));
-    launch_eye_pass(c->sc, c->cam, it, c->rr_eye, c->hp, c->st, c->gi, c->wave, c->photon_blocks, c->err, s);
+    StageMark m(c, FR_STAGE_EYE, c->side);
+    launch_eye_pass(c->sc, c->cam, it, c->rr_eye, c->hp, c->st, c->gi, c->eye_wave, c->photon_blocks, c->err,
+                    c->side);
   }
+  FR_CUDA(cudaEventRecord(c->join_ev, c->side));
   {
-    StageMark m(c, FR_STAGE_PHOTON);
-    PathWave pw = c->wave;
-    pw.qcount += kWaveRounds + 2;
-    launch_photon_pass(c->sc, it, c->ph, c->counts, pw, c->photon_blocks, c->err, s);
+    StageMark m(c, FR_STAGE_PHOTON, s);
+    launch_photon_pass(c->sc, it, c->ph, c->counts, c->wave, c->photon_blocks, c->err, s);
   }
+  FR_CUDA(cudaStreamWaitEvent(s, c->join_ev, 0));
   {
-    StageMark m(c, FR_STAGE_GRID);
+    StageMark m(c, FR_STAGE_GRID, s);
     launch_grid_setup(c->gi, c->sc, c->cell_scale, c->r0, s);
     FR_CUDA(cudaMemsetAsync(c->grid.cell_count, 0, sizeof(uint32_t) * (size_t)c->grid.table, s));
     launch_photon_count(c->ph, c->counts, c->P, kPhotonSlots, c->grid, c->gi, s);
@@ -449,13 +468,13 @@ int run_iteration(fr_ctx* c) {
     launch_photon_scatter(c->ph, c->counts, c->P, kPhotonSlots, c->grid, s);
   }
   {
-    StageMark m(c, FR_STAGE_GATHER);
+    StageMark m(c, FR_STAGE_GATHER, s);
     FR_CUDA(cudaMemsetAsync(c->dbg_m, 0, sizeof(int32_t) * (size_t)c->W * c->H, s));
     FR_CUDA(cudaMemsetAsync(c->dbg_phi, 0, sizeof(float4) * (size_t)c->W * c->H, s));
     launch_gather_update(c->sc, it, c->hp, c->grid, c->gi, c->st, c->dbg_m, c->dbg_phi, c->gather_blocks, s);
   }
-  // eye and photon passes (start, rounds, tail), grid setup, count, scatter, gather
-  c->launches += 4 + 2 * (2 + 2 * kWaveRounds);
+  // eye and photon passes (start, rounds of trace/sort/shade, tail), grid setup, count, scatter, gather
+  c->launches += 4 + 2 * (2 + 3 * kWaveRounds);
   c->photons_total += c->P;
   FR_CUDA(cudaGetLastError());
   return FR_OK;
@@ -495,8 +514,11 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
     delete c;
     return code;
   };
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess)
-    return bail(fail(FR_ERR_CUDA, "cudaStreamCreate failed"));
+  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming) != cudaSuccess)
+    return bail(fail(FR_ERR_CUDA, "cudaStreamCreate/cudaEventCreate failed"));
   c->W = camera->width;
   c->H = camera->height;
   c->P = params->photons_per_iteration;
@@ -605,7 +627,7 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
   // ---- per-iteration buffers (all allocated here; iterations allocate nothing)
   const size_t npix = (size_t)c->W * c->H;
   const size_t nslots = (size_t)c->P * kPhotonSlots;
-  const size_t wave_n = std::max(npix, (size_t)c->P);
+  const size_t wave_n = (size_t)c->P;
   if ((rc = c->alloc(&c->hp.pos, npix)) || (rc = c->alloc(&c->hp.nrm, npix)) || (rc = c->alloc(&c->hp.out, npix)) ||
       (rc = c->alloc(&c->hp.wgt, npix)) || (rc = c->alloc(&c->st.tau, 3 * npix)) || (rc = c->alloc(&c->st.n, npix)) ||
       (rc = c->alloc(&c->st.r, npix)) || (rc = c->alloc(&c->st.g, npix)) || (rc = c->alloc(&c->ph.pos, nslots)) ||
@@ -614,12 +636,26 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
       (rc = c->alloc(&c->wave.b, wave_n)) || (rc = c->alloc(&c->wave.c, wave_n)) ||
       (rc = c->alloc(&c->wave.d, wave_n)) || (rc = c->alloc(&c->wave.hit, wave_n)) ||
       (rc = c->alloc(&c->wave.queue[0], wave_n)) || (rc = c->alloc(&c->wave.queue[1], wave_n)) ||
-      (rc = c->alloc(&c->wave.qcount, 2 * ((size_t)kWaveRounds + 2) + 1)) || (rc = c->alloc(&c->hp.list, npix)) ||
+      (rc = c->alloc(&c->eye_wave.a, npix)) || (rc = c->alloc(&c->eye_wave.b, npix)) ||
+      (rc = c->alloc(&c->eye_wave.c, npix)) || (rc = c->alloc(&c->eye_wave.d, npix)) ||
+      (rc = c->alloc(&c->eye_wave.hit, npix)) || (rc = c->alloc(&c->eye_wave.queue[0], npix)) ||
+      (rc = c->alloc(&c->eye_wave.queue[1], npix)) ||
+      (rc = c->alloc(&c->wave.qcount, kCounters)) || (rc = c->alloc(&c->hp.list, npix)) ||
+      (rc = c->alloc(&c->wave.mq, (size_t)kShadeQueues * wave_n)) ||
+      (rc = c->alloc(&c->eye_wave.mq, (size_t)kShadeQueues * npix)) ||
       (rc = c->alloc(&c->gi, 1)) ||
       (rc = c->alloc(&c->err, 1)) ||
       (rc = c->alloc(&c->dbg_m, npix)) || (rc = c->alloc(&c->dbg_phi, npix)) || (rc = c->alloc(&c->image, npix)))
     return bail(rc);
-  c->hp.list_count = c->wave.qcount + 2 * (kWaveRounds + 2);
+  // Counters (one memset per iteration): eye rounds, photon rounds, the
+  // hitpoint list, eye and photon shade queues.
+  c->eye_wave.qcount = c->wave.qcount;
+  c->wave.qcount += kWaveRounds + 2;
+  c->hp.list_count = c->eye_wave.qcount + 2 * (kWaveRounds + 2);
+  c->eye_wave.mcount = c->hp.list_count + 1;
+  c->wave.mcount = c->eye_wave.mcount + kWaveRounds * kShadeQueues;
+  c->eye_wave.cap = (uint32_t)npix;
+  c->wave.cap = (uint32_t)wave_n;
   // Photon grid: one bucket per expected photon or better (a few photons per path).
   c->grid.table = next_pow2(std::max<uint64_t>((uint64_t)c->P * 4, 1u << 16));
   const size_t cap = nslots;

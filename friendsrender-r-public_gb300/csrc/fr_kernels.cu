@@ -241,6 +241,55 @@ __global__ void __launch_bounds__(128) k_wave_trace(SceneGPU sc, PathWave w, int
   }
 }
 
+// The paths of queue `round` sorted into the queues of their hit surface's
+// type (misses last), so that each warp of the shade kernel runs one
+// surface's code.
+__global__ void __launch_bounds__(256) k_wave_sort(SceneGPU sc, PathWave w, int round) {
+  const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
+  const uint32_t* q = w.queue[round & 1];
+  uint32_t* mc = w.mcount + round * kShadeQueues;
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const uint32_t n_round = (n + stride - 1) / stride * stride;
+  const unsigned lane = threadIdx.x & 31u;
+  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n_round; j += stride) {
+    int type = -1;
+    uint32_t i = 0;
+    if (j < n) {
+      i = q[j];
+      const int facet = __float_as_int(w.hit[i].w);
+      type = facet >= 0 ? sc.mats[sc.shade[facet].attr].type : kShadeQueues - 1;
+    }
+    // One atomic per surface type present in the warp.
+    const unsigned peers = __match_any_sync(0xffffffffu, type);
+    if (type >= 0) {
+      const int leader = __ffs(peers) - 1;
+      uint32_t base = 0;
+      if ((int)lane == leader) base = atomicAdd(mc + type, (uint32_t)__popc(peers));
+      base = __shfl_sync(peers, base, leader);
+      w.mq[(size_t)type * w.cap + base + __popc(peers & ((1u << lane) - 1u))] = i;
+    }
+  }
+}
+
+// Entry k of this round's shade work: the queues of the surface types one
+// after another.
+struct ShadeQueues {
+  uint32_t off[kShadeQueues + 1];
+  __device__ __forceinline__ ShadeQueues(const PathWave& w, int round) {
+    off[0] = 0;
+#pragma unroll
+    for (int t = 0; t < kShadeQueues; ++t)
+      off[t + 1] = off[t] + *(volatile uint32_t*)(w.mcount + round * kShadeQueues + t);
+  }
+  __device__ __forceinline__ uint32_t total() const { return off[kShadeQueues]; }
+  __device__ __forceinline__ uint32_t path(const PathWave& w, uint32_t k) const {
+    int t = 0;
+#pragma unroll
+    for (int u = 1; u < kShadeQueues; ++u) t += k >= off[u];
+    return w.mq[(size_t)t * w.cap + (k - off[t])];
+  }
+};
+
 __device__ __forceinline__ bool wave_hit(const PathWave& w, uint32_t i, Hit& h) {
   const float4 hv = w.hit[i];
   h.t = 0.f; h.u = hv.x; h.v = hv.y; h.tri = __float_as_int(hv.z); h.facet = __float_as_int(hv.w);
@@ -249,8 +298,8 @@ __device__ __forceinline__ bool wave_hit(const PathWave& w, uint32_t i, Hit& h) 
 
 __global__ void __launch_bounds__(128) k_ew_shade(SceneGPU sc, IterParams it, float rr5, float rr6, PathWave w,
                                                   HitpointBuf hp, PixelState st, GridInfo* gi, int round) {
-  const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
-  const uint32_t* q = w.queue[round & 1];
+  const ShadeQueues sq(w, round);
+  const uint32_t n = sq.total();
   uint32_t* qn = w.queue[(round + 1) & 1];
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t n_round = (n + stride - 1) / stride * stride;
@@ -259,7 +308,7 @@ __global__ void __launch_bounds__(128) k_ew_shade(SceneGPU sc, IterParams it, fl
     int hit_type = kHitNone;
     uint32_t i = 0;
     if (j < n) {
-      i = q[j];
+      i = sq.path(w, j);
       EyeState s;
       load_eye(w, (int)i, s);
       Hit h;
@@ -509,8 +558,8 @@ __global__ void __launch_bounds__(128) k_pw_emit(SceneGPU sc, IterParams it, Pho
 
 __global__ void __launch_bounds__(128) k_pw_shade(SceneGPU sc, IterParams it, PhotonSlots ph, PathWave w,
                                                   uint32_t* counts, int round) {
-  const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
-  const uint32_t* q = w.queue[round & 1];
+  const ShadeQueues sq(w, round);
+  const uint32_t n = sq.total();
   uint32_t* qn = w.queue[(round + 1) & 1];
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t n_round = (n + stride - 1) / stride * stride;
@@ -518,7 +567,7 @@ __global__ void __launch_bounds__(128) k_pw_shade(SceneGPU sc, IterParams it, Ph
     bool keep = false;
     uint32_t i = 0;
     if (j < n) {
-      i = q[j];
+      i = sq.path(w, j);
       PhotonState s;
       load_state(w, (int)i, s);
       Hit h;
@@ -887,9 +936,11 @@ void launch_eye_pass(const SceneGPU& sc, const CameraGPU& cam, const IterParams&
                      cudaStream_t s) {
   const int n = it.width * it.height;
   const unsigned grid = std::max(1, resident_blocks);
+  const unsigned sort_grid = std::max(1u, std::min(blocks_for(n, 256), 4 * grid));
   k_ew_start<<<blocks_for(n, 128), 128, 0, s>>>(cam, it, w);
   for (int r = 0; r < kWaveRounds; ++r) {
     k_wave_trace<<<grid, 128, 0, s>>>(sc, w, r, err);
+    k_wave_sort<<<sort_grid, 256, 0, s>>>(sc, w, r);
     k_ew_shade<<<grid, 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, r);
   }
   k_ew_tail<<<grid, 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, kWaveRounds, err);
@@ -898,9 +949,11 @@ void launch_eye_pass(const SceneGPU& sc, const CameraGPU& cam, const IterParams&
 void launch_photon_pass(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, uint32_t* counts, PathWave w,
                         int resident_blocks, int* err, cudaStream_t s) {
   const unsigned grid = std::max(1, resident_blocks);
+  const unsigned sort_grid = std::max(1u, std::min(blocks_for(it.photons, 256), 4 * grid));
   k_pw_emit<<<blocks_for(it.photons, 128), 128, 0, s>>>(sc, it, ph, w, counts);
   for (int r = 0; r < kWaveRounds; ++r) {
     k_wave_trace<<<grid, 128, 0, s>>>(sc, w, r, err);
+    k_wave_sort<<<sort_grid, 256, 0, s>>>(sc, w, r);
     k_pw_shade<<<grid, 128, 0, s>>>(sc, it, ph, w, counts, r);
   }
   k_pw_tail<<<grid, 128, 0, s>>>(sc, it, ph, w, counts, kWaveRounds, err);

@@ -43,19 +43,23 @@ struct PhotonGrid {
   uint32_t table;        // bucket count, power of two
 };
 
-// Wavefront passes: per-path state, hit records and the two queues of live
-// paths (see fr_kernels.cu), shared by the eye and the photon pass.  qcount[r]
-// counts the paths of round r; each pass has its own kWaveRounds + 2 counters,
-// zeroed once per iteration.
+// Wavefront passes (see fr_kernels.cu): per-path state, hit records, the two
+// queues of live paths and the per-surface-type queues that the trace kernel
+// sorts each round's hits into for the shade kernel.  qcount[r] counts the
+// paths of round r; every counter is zeroed once per iteration.
 #ifndef FR_WAVE_ROUNDS
 #define FR_WAVE_ROUNDS 8
 #endif
 constexpr int kWaveRounds = FR_WAVE_ROUNDS;
+constexpr int kShadeQueues = 5;  // one per surface type, then misses
 struct PathWave {
   float4 *a, *b, *c, *d;  // path state
   float4* hit;            // u, v, triangle, facet (triangle -1: miss)
-  uint32_t* queue[2];
-  uint32_t* qcount;
+  uint32_t* queue[2];     // live paths of the current and the next round
+  uint32_t* qcount;       // kWaveRounds + 2 counters
+  uint32_t* mq;           // kShadeQueues queues of `cap` entries: this round's hits by surface type
+  uint32_t* mcount;       // kWaveRounds * kShadeQueues counters
+  uint32_t cap;
 };
 
 // Per-pixel progressive state (SharedHitPoint, SPPM.h:112-126): tau in FP64.
