@@ -166,25 +166,76 @@ __device__ __forceinline__ int eye_shade(const SceneGPU& sc, const HitpointBuf& 
   return eye_top(s, rng, rr5, rr6) ? -1 : kHitNone;
 }
 
-// Appends i to a queue with one atomic per warp.
-__device__ __forceinline__ void queue_push(uint32_t* queue, uint32_t* count, bool push, uint32_t i) {
-  const unsigned m = __ballot_sync(__activemask(), push);
-  if (!m) return;
-  const unsigned lane = threadIdx.x & 31u;
-  const int leader = __ffs(m) - 1;
-  uint32_t base = 0;
-  if ((int)lane == leader) base = atomicAdd(count, (uint32_t)__popc(m));
-  base = __shfl_sync(__activemask(), base, leader);
-  if (push) queue[base + __popc(m & ((1u << lane) - 1u))] = i;
+// Appends i to queue t of T (queue t starts at q + t * cap, its length is
+// count[t]) when 0 <= t < T, with one global atomic per queue per block: the
+// counters are few addresses that every block of a launch updates.  Every
+// thread of the block calls it, the same number of times.
+template <int T>
+__device__ __forceinline__ void block_append(uint32_t* q, size_t cap, uint32_t* count, int t, uint32_t i) {
+  __shared__ uint32_t s_warp[32][T];
+  __shared__ uint32_t s_base[T];
+  const unsigned lane = threadIdx.x & 31u, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+  unsigned mine = 0;
+#pragma unroll
+  for (int u = 0; u < T; ++u) {
+    const unsigned m = __ballot_sync(0xffffffffu, t == u);
+    if (t == u) mine = m;
+    if (lane == 0) s_warp[wid][u] = (uint32_t)__popc(m);
+  }
+  __syncthreads();
+  if (threadIdx.x < (unsigned)T) {
+    const int u = (int)threadIdx.x;
+    uint32_t run = 0;
+    for (unsigned v = 0; v < nw; ++v) {
+      const uint32_t c = s_warp[v][u];
+      s_warp[v][u] = run;
+      run += c;
+    }
+    s_base[u] = run ? atomicAdd(count + u, run) : 0u;
+  }
+  __syncthreads();
+  if (t >= 0 && t < T) q[(size_t)t * cap + s_base[t] + s_warp[wid][t] + (uint32_t)__popc(mine & ((1u << lane) - 1u))] = i;
+  __syncthreads();
+}
+
+// Sum over the block of v and n into *sum and *cnt (one atomic pair per
+// block).  Every thread of the block calls it.
+__device__ __forceinline__ void block_add(float* sum, uint32_t* cnt, float v, uint32_t n) {
+  __shared__ float s_v[32];
+  __shared__ uint32_t s_n[32];
+  const unsigned lane = threadIdx.x & 31u, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    v += __shfl_down_sync(0xffffffffu, v, o);
+    n += __shfl_down_sync(0xffffffffu, n, o);
+  }
+  if (lane == 0) {
+    s_v[wid] = v;
+    s_n[wid] = n;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    float tv = 0.0f;
+    uint32_t tn = 0;
+    for (unsigned k = 0; k < nw; ++k) {
+      tv += s_v[k];
+      tn += s_n[k];
+    }
+    if (tn) {
+      atomicAdd(sum, tv);
+      atomicAdd(cnt, tn);
+    }
+  }
+  __syncthreads();
 }
 
 // End of an eye path: the hit code of a pixel without a hitpoint, the list
-// of this iteration's hitpoints, and their radius summed per warp for the
-// grid's cell size.  Every lane of the warp calls it.
+// of this iteration's hitpoints, and their radius summed for the grid's cell
+// size.  Every thread of the block calls it.
 __device__ __forceinline__ void eye_finish(const HitpointBuf& hp, const PixelState& st, GridInfo* gi, bool ended,
                                            int i, int hit_type) {
   float rs = 0.0f;
-  unsigned cnt = 0;
+  uint32_t cnt = 0;
   if (ended) {
     if (hit_type == kHitHit) {
       rs = st.r[i];
@@ -193,22 +244,18 @@ __device__ __forceinline__ void eye_finish(const HitpointBuf& hp, const PixelSta
       store_float4(hp.pos + i, v3(0.f, 0.f, 0.f), __int_as_float(hit_type));
     }
   }
-  queue_push(hp.list, hp.list_count, cnt != 0, (uint32_t)i);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    rs += __shfl_down_sync(0xffffffffu, rs, o);
-    cnt += __shfl_down_sync(0xffffffffu, cnt, o);
-  }
-  if ((threadIdx.x & 31) == 0 && cnt) {
-    atomicAdd(&gi->r_sum, rs);
-    atomicAdd(&gi->r_count, cnt);
-  }
+  block_append<1>(hp.list, 0, hp.list_count, cnt ? 0 : -1, (uint32_t)i);
+  block_add(&gi->r_sum, &gi->r_count, rs, cnt);
 }
 
+// Every pixel's path is live after its camera ray, so the first queue is
+// the identity (no atomics).
 __global__ void __launch_bounds__(128) k_ew_start(CameraGPU cam, IterParams it, PathWave w) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool live = i < it.width * it.height;
-  if (live) {
+  const int npix = it.width * it.height;
+  if (i == 0) w.qcount[0] = (uint32_t)npix;
+  if (i < npix) {
+    w.queue[0][i] = (uint32_t)i;
     const int px = i % it.width, py = i / it.width;
     const float u = (float)px / (float)it.width;
     const float v = (float)py / (float)it.height;
@@ -223,7 +270,6 @@ __global__ void __launch_bounds__(128) k_ew_start(CameraGPU cam, IterParams it, 
     s.draw = rng.draw;
     store_eye(w, i, s);
   }
-  queue_push(w.queue[0], w.qcount + 0, live, (uint32_t)i);
 }
 
 // Closest hit of every path in queue `round` (eye or photon wave).
@@ -250,7 +296,6 @@ __global__ void __launch_bounds__(256) k_wave_sort(SceneGPU sc, PathWave w, int 
   uint32_t* mc = w.mcount + round * kShadeQueues;
   const uint32_t stride = gridDim.x * blockDim.x;
   const uint32_t n_round = (n + stride - 1) / stride * stride;
-  const unsigned lane = threadIdx.x & 31u;
   for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n_round; j += stride) {
     int type = -1;
     uint32_t i = 0;
@@ -259,15 +304,7 @@ __global__ void __launch_bounds__(256) k_wave_sort(SceneGPU sc, PathWave w, int 
       const int facet = __float_as_int(w.hit[i].w);
       type = facet >= 0 ? sc.mats[sc.shade[facet].attr].type : kShadeQueues - 1;
     }
-    // One atomic per surface type present in the warp.
-    const unsigned peers = __match_any_sync(0xffffffffu, type);
-    if (type >= 0) {
-      const int leader = __ffs(peers) - 1;
-      uint32_t base = 0;
-      if ((int)lane == leader) base = atomicAdd(mc + type, (uint32_t)__popc(peers));
-      base = __shfl_sync(peers, base, leader);
-      w.mq[(size_t)type * w.cap + base + __popc(peers & ((1u << lane) - 1u))] = i;
-    }
+    block_append<kShadeQueues>(w.mq, w.cap, mc, type, i);
   }
 }
 
@@ -330,7 +367,7 @@ __global__ void __launch_bounds__(128) k_ew_shade(SceneGPU sc, IterParams it, fl
       }
     }
     eye_finish(hp, st, gi, ended, (int)i, hit_type);
-    queue_push(qn, w.qcount + round + 1, keep, i);
+    block_append<1>(qn, 0, w.qcount + round + 1, keep ? 0 : -1, i);
   }
 }
 
@@ -541,19 +578,20 @@ __device__ __forceinline__ void photon_finish(const IterParams& it, const Photon
   counts[i] = n;
 }
 
+// A new path passes the bounce loop's first checks (loop 0, no photon
+// stored, throughput 1), so every path is live and the first queue is the
+// identity (no atomics).
 __global__ void __launch_bounds__(128) k_pw_emit(SceneGPU sc, IterParams it, PhotonSlots ph, PathWave w,
                                                  uint32_t* counts) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool live = i < it.photons;
-  PhotonState s;
-  bool go = false;
-  if (live) {
+  if (i == 0) w.qcount[0] = (uint32_t)it.photons;
+  if (i < it.photons) {
+    PhotonState s;
     photon_start(sc, it, ph, i, s);
-    go = photon_top(s);
-    if (go) store_state(w, i, s);
-    else photon_finish(it, ph, counts, i, s.k);
+    photon_top(s);  // loop 0 -> 1; true for a new path
+    store_state(w, i, s);
+    w.queue[0][i] = (uint32_t)i;
   }
-  queue_push(w.queue[0], w.qcount + 0, live && go, (uint32_t)i);
 }
 
 __global__ void __launch_bounds__(128) k_pw_shade(SceneGPU sc, IterParams it, PhotonSlots ph, PathWave w,
@@ -579,7 +617,7 @@ __global__ void __launch_bounds__(128) k_pw_shade(SceneGPU sc, IterParams it, Ph
         photon_finish(it, ph, counts, (int)i, s.k);
       }
     }
-    queue_push(qn, w.qcount + round + 1, keep, i);
+    block_append<1>(qn, 0, w.qcount + round + 1, keep ? 0 : -1, i);
   }
 }
 
