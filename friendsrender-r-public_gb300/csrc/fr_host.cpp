@@ -474,7 +474,7 @@ int run_iteration(fr_ctx* c) {
     launch_gather_update(c->sc, it, c->hp, c->grid, c->gi, c->st, c->dbg_m, c->dbg_phi, c->gather_blocks, s);
   }
   // eye and photon passes (start, rounds of trace/sort/shade, tail), grid setup, count, scatter, gather
-  c->launches += 4 + 2 * (2 + 3 * kWaveRounds);
+  c->launches += 4 + (2 + 3 * kEyeRounds) + (2 + 3 * kPhotonRounds);
   c->photons_total += c->P;
   FR_CUDA(cudaGetLastError());
   return FR_OK;

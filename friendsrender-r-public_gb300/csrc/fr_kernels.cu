@@ -976,12 +976,12 @@ void launch_eye_pass(const SceneGPU& sc, const CameraGPU& cam, const IterParams&
   const unsigned grid = std::max(1, resident_blocks);
   const unsigned sort_grid = std::max(1u, std::min(blocks_for(n, 256), 4 * grid));
   k_ew_start<<<blocks_for(n, 128), 128, 0, s>>>(cam, it, w);
-  for (int r = 0; r < kWaveRounds; ++r) {
+  for (int r = 0; r < kEyeRounds; ++r) {
     k_wave_trace<<<grid, 128, 0, s>>>(sc, w, r, err);
     k_wave_sort<<<sort_grid, 256, 0, s>>>(sc, w, r);
     k_ew_shade<<<grid, 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, r);
   }
-  k_ew_tail<<<grid, 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, kWaveRounds, err);
+  k_ew_tail<<<grid, 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, kEyeRounds, err);
 }
 
 void launch_photon_pass(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, uint32_t* counts, PathWave w,
@@ -989,12 +989,12 @@ void launch_photon_pass(const SceneGPU& sc, const IterParams& it, PhotonSlots ph
   const unsigned grid = std::max(1, resident_blocks);
   const unsigned sort_grid = std::max(1u, std::min(blocks_for(it.photons, 256), 4 * grid));
   k_pw_emit<<<blocks_for(it.photons, 128), 128, 0, s>>>(sc, it, ph, w, counts);
-  for (int r = 0; r < kWaveRounds; ++r) {
+  for (int r = 0; r < kPhotonRounds; ++r) {
     k_wave_trace<<<grid, 128, 0, s>>>(sc, w, r, err);
     k_wave_sort<<<sort_grid, 256, 0, s>>>(sc, w, r);
     k_pw_shade<<<grid, 128, 0, s>>>(sc, it, ph, w, counts, r);
   }
-  k_pw_tail<<<grid, 128, 0, s>>>(sc, it, ph, w, counts, kWaveRounds, err);
+  k_pw_tail<<<grid, 128, 0, s>>>(sc, it, ph, w, counts, kPhotonRounds, err);
 }
 
 int photon_pass_blocks_per_sm() {

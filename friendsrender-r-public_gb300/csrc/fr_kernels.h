@@ -47,10 +47,18 @@ struct PhotonGrid {
 // queues of live paths and the per-surface-type queues that the trace kernel
 // sorts each round's hits into for the shade kernel.  qcount[r] counts the
 // paths of round r; every counter is zeroed once per iteration.
-#ifndef FR_WAVE_ROUNDS
-#define FR_WAVE_ROUNDS 8
+// Rounds of trace/sort/shade before the tail kernel takes the paths still
+// alive.  Later rounds carry few paths and cost a launch sequence each, while
+// the tail advances a path by a bounce at the latency of one trace and shade.
+#ifndef FR_EYE_ROUNDS
+#define FR_EYE_ROUNDS 8
 #endif
-constexpr int kWaveRounds = FR_WAVE_ROUNDS;
+#ifndef FR_PHOTON_ROUNDS
+#define FR_PHOTON_ROUNDS 5
+#endif
+constexpr int kEyeRounds = FR_EYE_ROUNDS;
+constexpr int kPhotonRounds = FR_PHOTON_ROUNDS;
+constexpr int kWaveRounds = kEyeRounds > kPhotonRounds ? kEyeRounds : kPhotonRounds;  // counter layout
 constexpr int kShadeQueues = 5;  // one per surface type, then misses
 struct PathWave {
   float4 *a, *b, *c, *d;  // path state
