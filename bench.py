@@ -165,19 +165,24 @@ def run_reference(args):
     return 0
 
 
-def stage_bytes(stage, npix, hits, photons_stored, paths):
-    """Algorithmic DRAM bytes of one launch of a stage (the figures the
-    roofline's achieved GB/s is computed from)."""
-    if stage == 'eye':
-        return npix * (64 + 4)                     # hitpoint record write + radius read
-    if stage == 'photon':
-        return photons_stored * 48 + paths * 4     # photon slots written + per-path count
-    if stage == 'grid':
-        # count: photon position read + key/rank write; scatter: key/rank + 48 B read, 48 B write
-        return photons_stored * (16 + 8 + 8 + 48 + 48)
-    # gather/update: hitpoint record + radius read, each stored photon read once,
-    # tau (3 x f64) read+write, N/R/G read+write, M and flux debug write
-    return hits * (64 + 4 + 48 + 12 + 12 + 20) + photons_stored * 48
+# Algorithmic bytes of one traced ray in k_wave_trace, the dominant kernel:
+# the queue entry (4 B), the ray (origin + index of refraction, direction +
+# PDF: 32 B) read and the hit record (16 B) written.  The BVH and triangle
+# reads are re-reads of a resident scene, not per-ray algorithmic traffic.
+TRACE_BYTES_PER_RAY = 52
+TRACE_TRAFFIC_PROFILE = os.path.join(REPO, 'profiles', 'k_wave_trace_traffic_mixed_materials_1M.md')
+
+
+def trace_traffic_per_launch():
+    """DRAM bytes (read + write) per k_wave_trace launch from the committed
+    ncu capture of this workload, or None."""
+    try:
+        for line in open(TRACE_TRAFFIC_PROFILE):
+            if line.startswith('bytes_per_launch:'):
+                return float(line.split(':', 1)[1])
+    except OSError:
+        pass
+    return None
 
 
 def main():
@@ -242,7 +247,9 @@ def main():
         total_ms = float(t.item())
     launches = l1 - l0
 
-    # ---- photon / hitpoint counts of the last iteration (for the algorithmic bytes)
+    # ---- rays traced and photons stored in the last timed iteration
+    eye_q, photon_q = r.wave_counts()
+    rays = int(eye_q[:-1].sum()) + int(photon_q[:-1].sum())
     counts = np.empty(r.photons, np.uint32)
     abi._check(abi._lib.fr_read_photon_slots(r.h, None, None, None, abi._ptr(counts)), 'fr_read_photon_slots')
     stored = int(counts.sum())
@@ -266,11 +273,12 @@ def main():
     if rank != 0:
         return 0
     value = world * args.photons * args.steps / (total_ms / 1000.0)
-    per = {k: stage_ms[k] / max(1, stage_n[k]) for k in stage_ms}
-    dom = max(per, key=per.get)
+    per = {k: stage_ms[k] / args.steps for k in stage_ms}
     peak, peak_kind = measured_peaks()
-    bytes_dom = stage_bytes(dom, npix, hits, stored, args.photons)
-    achieved = bytes_dom / (per[dom] / 1000.0) / 1e9
+    trace_launches = (stage_n['eye_trace'] + stage_n['photon_trace']) / args.steps
+    trace_s = (stage_ms['eye_trace'] + stage_ms['photon_trace']) / 1000.0 / args.steps
+    bytes_per_launch = rays * TRACE_BYTES_PER_RAY / trace_launches
+    achieved = bytes_per_launch / (trace_s / trace_launches) / 1e9
     out = {
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps, 'warmup': W,
         'ms_per_step': total_ms / args.steps, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
@@ -280,9 +288,12 @@ def main():
                    'parallelism': 'replicas' if world > 1 else 'single GPU'},
         'hitpoint_updates_per_s': world * npix * args.steps / (total_ms / 1000.0),
         'stage_ms_per_step': per,
-        'roofline': {'bound': 'hbm', 'kernel': dom, 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
-                     'frac': achieved / peak, 'traffic': None, 'peak_source': peak_kind,
-                     'algorithmic_bytes_per_launch': bytes_dom},
+        'roofline': {'bound': 'hbm', 'kernel': 'k_wave_trace', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
+                     'frac': achieved / peak, 'traffic': trace_traffic_per_launch(), 'peak_source': peak_kind,
+                     'algorithmic_bytes_per_launch': bytes_per_launch, 'launches_per_step': trace_launches,
+                     'note': 'latency-bound BVH traversal; eye and photon launches overlap in time'},
+        'traversal': {'kernel': 'k_wave_trace', 'rays_per_step': rays, 'rays_per_s': rays / trace_s,
+                      'tail_paths_per_step': int(eye_q[-1]) + int(photon_q[-1])},
         'e2e': {'value': world * args.photons * args.steps / e2e_s, 'unit': UNIT, 'h2d_bytes_per_step': 0,
                 'd2h_bytes_per_step': npix * 16, 'setup_s': setup_s,
                 'device_bytes': int(stats['device_bytes'])},

@@ -448,15 +448,36 @@ int run_iteration(fr_ctx* c) {
   // needs both (cell size from the hitpoint radii).
   FR_CUDA(cudaEventRecord(c->fork_ev, s));
   FR_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
+  const int grid = c->photon_blocks;
   {
-    StageMark m(c, FR_STAGE_EYE, c->side);
-    launch_eye_pass(c->sc, c->cam, it, c->rr_eye, c->hp, c->st, c->gi, c->eye_wave, c->photon_blocks, c->err,
-                    c->side);
+    cudaStream_t e = c->side;
+    StageMark m(c, FR_STAGE_EYE, e);
+    const int sort_grid = (int)std::min<size_t>(((size_t)c->W * c->H + 255) / 256, 4 * (size_t)grid);
+    launch_ew_start(c->cam, it, c->eye_wave, e);
+    for (int r = 0; r < kEyeRounds; ++r) {
+      {
+        StageMark t(c, FR_STAGE_EYE_TRACE, e);
+        launch_wave_trace(c->sc, c->eye_wave, r, grid, c->err, e);
+      }
+      launch_wave_sort(c->sc, c->eye_wave, r, sort_grid, e);
+      launch_ew_shade(c->sc, it, c->rr_eye, c->eye_wave, c->hp, c->st, c->gi, r, grid, e);
+    }
+    launch_ew_tail(c->sc, it, c->rr_eye, c->eye_wave, c->hp, c->st, c->gi, kEyeRounds, grid, c->err, e);
   }
   FR_CUDA(cudaEventRecord(c->join_ev, c->side));
   {
     StageMark m(c, FR_STAGE_PHOTON, s);
-    launch_photon_pass(c->sc, it, c->ph, c->counts, c->wave, c->photon_blocks, c->err, s);
+    const int sort_grid = (int)std::min<size_t>(((size_t)c->P + 255) / 256, 4 * (size_t)grid);
+    launch_pw_emit(c->sc, it, c->ph, c->wave, c->counts, s);
+    for (int r = 0; r < kPhotonRounds; ++r) {
+      {
+        StageMark t(c, FR_STAGE_PHOTON_TRACE, s);
+        launch_wave_trace(c->sc, c->wave, r, grid, c->err, s);
+      }
+      launch_wave_sort(c->sc, c->wave, r, sort_grid, s);
+      launch_pw_shade(c->sc, it, c->ph, c->wave, c->counts, r, grid, s);
+    }
+    launch_pw_tail(c->sc, it, c->ph, c->wave, c->counts, kPhotonRounds, grid, c->err, s);
   }
   FR_CUDA(cudaStreamWaitEvent(s, c->join_ev, 0));
   {
@@ -744,7 +765,8 @@ int fr_profile_enable(fr_ctx* c, int32_t on, int32_t max_iterations) {
   c->ev_marks.clear();
   c->ev_used = 0;
   c->profiling = on != 0;
-  const size_t need = on ? (size_t)std::max(1, max_iterations) * FR_STAGES * 2 : 0;
+  // Marks per iteration: the four stages and every trace round of both passes.
+  const size_t need = on ? (size_t)std::max(1, max_iterations) * (4 + kEyeRounds + kPhotonRounds) * 2 : 0;
   while (c->ev_pool.size() < need) {
     cudaEvent_t e;
     FR_CUDA(cudaEventCreate(&e));
@@ -907,6 +929,20 @@ int fr_check_exact_math(uint64_t samples, uint32_t seed, uint64_t* mismatches, u
   const char* msg = "";
   if (check_exact_math(samples, seed, mismatches, fast_paths, &msg)) return fail(FR_ERR_CUDA, "fr_check_exact_math: %s", msg);
   return FR_OK;
+}
+
+static_assert(kWaveRounds <= FR_MAX_WAVE_ROUNDS, "round counters exceed FR_MAX_WAVE_ROUNDS");
+
+int fr_read_wave_counts(fr_ctx* c, uint32_t* eye_counts, uint32_t* photon_counts, int32_t* eye_rounds,
+                        int32_t* photon_rounds) {
+  if (!c || !eye_counts || !photon_counts) return fail(FR_ERR_INVALID, "fr_read_wave_counts: bad arguments");
+  FR_CUDA(cudaMemcpyAsync(eye_counts, c->eye_wave.qcount, sizeof(uint32_t) * (kEyeRounds + 1), cudaMemcpyDeviceToHost,
+                          c->stream));
+  FR_CUDA(cudaMemcpyAsync(photon_counts, c->wave.qcount, sizeof(uint32_t) * (kPhotonRounds + 1),
+                          cudaMemcpyDeviceToHost, c->stream));
+  if (eye_rounds) *eye_rounds = kEyeRounds;
+  if (photon_rounds) *photon_rounds = kPhotonRounds;
+  return fr_synchronize(c);
 }
 
 int fr_read_hitpoints(fr_ctx* c, float* pos_type, float* nrm_rough, float* out_mat, float* wgt_facet) {

@@ -969,32 +969,41 @@ void upload_byte_lut(cudaStream_t s) {
   cudaMemcpyToSymbolAsync(c_byte_to_unit, lut, sizeof(lut), 0, cudaMemcpyHostToDevice, s);
 }
 
-void launch_eye_pass(const SceneGPU& sc, const CameraGPU& cam, const IterParams& it, const float* rr_eye,
-                     HitpointBuf hp, PixelState st, GridInfo* gi, PathWave w, int resident_blocks, int* err,
-                     cudaStream_t s) {
-  const int n = it.width * it.height;
-  const unsigned grid = std::max(1, resident_blocks);
-  const unsigned sort_grid = std::max(1u, std::min(blocks_for(n, 256), 4 * grid));
-  k_ew_start<<<blocks_for(n, 128), 128, 0, s>>>(cam, it, w);
-  for (int r = 0; r < kEyeRounds; ++r) {
-    k_wave_trace<<<grid, 128, 0, s>>>(sc, w, r, err);
-    k_wave_sort<<<sort_grid, 256, 0, s>>>(sc, w, r);
-    k_ew_shade<<<grid, 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, r);
-  }
-  k_ew_tail<<<grid, 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, kEyeRounds, err);
+void launch_ew_start(const CameraGPU& cam, const IterParams& it, PathWave w, cudaStream_t s) {
+  k_ew_start<<<blocks_for((size_t)it.width * it.height, 128), 128, 0, s>>>(cam, it, w);
 }
 
-void launch_photon_pass(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, uint32_t* counts, PathWave w,
-                        int resident_blocks, int* err, cudaStream_t s) {
-  const unsigned grid = std::max(1, resident_blocks);
-  const unsigned sort_grid = std::max(1u, std::min(blocks_for(it.photons, 256), 4 * grid));
+void launch_wave_trace(const SceneGPU& sc, PathWave w, int round, int grid, int* err, cudaStream_t s) {
+  k_wave_trace<<<std::max(1, grid), 128, 0, s>>>(sc, w, round, err);
+}
+
+void launch_wave_sort(const SceneGPU& sc, PathWave w, int round, int grid, cudaStream_t s) {
+  k_wave_sort<<<std::max(1, grid), 256, 0, s>>>(sc, w, round);
+}
+
+void launch_ew_shade(const SceneGPU& sc, const IterParams& it, const float* rr_eye, PathWave w, HitpointBuf hp,
+                     PixelState st, GridInfo* gi, int round, int grid, cudaStream_t s) {
+  k_ew_shade<<<std::max(1, grid), 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, round);
+}
+
+void launch_ew_tail(const SceneGPU& sc, const IterParams& it, const float* rr_eye, PathWave w, HitpointBuf hp,
+                    PixelState st, GridInfo* gi, int round, int grid, int* err, cudaStream_t s) {
+  k_ew_tail<<<std::max(1, grid), 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, round, err);
+}
+
+void launch_pw_emit(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, PathWave w, uint32_t* counts,
+                    cudaStream_t s) {
   k_pw_emit<<<blocks_for(it.photons, 128), 128, 0, s>>>(sc, it, ph, w, counts);
-  for (int r = 0; r < kPhotonRounds; ++r) {
-    k_wave_trace<<<grid, 128, 0, s>>>(sc, w, r, err);
-    k_wave_sort<<<sort_grid, 256, 0, s>>>(sc, w, r);
-    k_pw_shade<<<grid, 128, 0, s>>>(sc, it, ph, w, counts, r);
-  }
-  k_pw_tail<<<grid, 128, 0, s>>>(sc, it, ph, w, counts, kPhotonRounds, err);
+}
+
+void launch_pw_shade(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, PathWave w, uint32_t* counts,
+                     int round, int grid, cudaStream_t s) {
+  k_pw_shade<<<std::max(1, grid), 128, 0, s>>>(sc, it, ph, w, counts, round);
+}
+
+void launch_pw_tail(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, PathWave w, uint32_t* counts,
+                    int round, int grid, int* err, cudaStream_t s) {
+  k_pw_tail<<<std::max(1, grid), 128, 0, s>>>(sc, it, ph, w, counts, round, err);
 }
 
 int photon_pass_blocks_per_sm() {

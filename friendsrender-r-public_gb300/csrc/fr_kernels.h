@@ -96,13 +96,22 @@ struct ScanTemp {
 
 void upload_byte_lut(cudaStream_t s);
 
-// Wavefront eye pass; resident_blocks is the grid of the round kernels.
-void launch_eye_pass(const SceneGPU& sc, const CameraGPU& cam, const IterParams& it, const float* rr_eye,
-                     HitpointBuf hp, PixelState st, GridInfo* gi, PathWave w, int resident_blocks, int* err,
-                     cudaStream_t s);
-// Wavefront photon pass; resident_blocks is the grid of the round kernels.
-void launch_photon_pass(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, uint32_t* counts, PathWave w,
-                        int resident_blocks, int* err, cudaStream_t s);
+// Wavefront passes, launched round by round by the host: a start kernel,
+// rounds of trace / sort / shade over the live-path queue, and a tail
+// kernel.  `grid` is the block count of the persistent-style round kernels.
+void launch_ew_start(const CameraGPU& cam, const IterParams& it, PathWave w, cudaStream_t s);
+void launch_wave_trace(const SceneGPU& sc, PathWave w, int round, int grid, int* err, cudaStream_t s);
+void launch_wave_sort(const SceneGPU& sc, PathWave w, int round, int grid, cudaStream_t s);
+void launch_ew_shade(const SceneGPU& sc, const IterParams& it, const float* rr_eye, PathWave w, HitpointBuf hp,
+                     PixelState st, GridInfo* gi, int round, int grid, cudaStream_t s);
+void launch_ew_tail(const SceneGPU& sc, const IterParams& it, const float* rr_eye, PathWave w, HitpointBuf hp,
+                    PixelState st, GridInfo* gi, int round, int grid, int* err, cudaStream_t s);
+void launch_pw_emit(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, PathWave w, uint32_t* counts,
+                    cudaStream_t s);
+void launch_pw_shade(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, PathWave w, uint32_t* counts,
+                     int round, int grid, cudaStream_t s);
+void launch_pw_tail(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, PathWave w, uint32_t* counts,
+                    int round, int grid, int* err, cudaStream_t s);
 int photon_pass_blocks_per_sm();
 // Points the kernels at the exact-value tables (see fr_bsdf.cuh).
 void upload_tables(const float2* sincos_tab, const float* sqrt1m_tab, cudaStream_t s);

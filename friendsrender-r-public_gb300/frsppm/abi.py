@@ -57,9 +57,10 @@ class Stats(C.Structure):
 EXPORTS = ['fr_last_error', 'fr_create', 'fr_iterate', 'fr_synchronize', 'fr_resolve', 'fr_resolve_dev',
            'fr_get_stats', 'fr_stream', 'fr_destroy', 'fr_trace_closest', 'fr_trace_any', 'fr_radius_query',
            'fr_read_hitpoints', 'fr_read_photon_slots', 'fr_read_gather', 'fr_read_state', 'fr_profile_enable',
-           'fr_profile_read', 'fr_radius_count_noalloc', 'fr_check_exact_math']
+           'fr_profile_read', 'fr_radius_count_noalloc', 'fr_check_exact_math',
+           'fr_read_wave_counts']
 
-STAGES = ('eye', 'photon', 'grid', 'gather')
+STAGES = ('eye', 'photon', 'grid', 'gather', 'eye_trace', 'photon_trace')
 
 _lib = None
 
@@ -96,6 +97,7 @@ def load(path=None):
     lib.fr_profile_read.argtypes = [vp, vp, vp, vp]
     lib.fr_radius_count_noalloc.argtypes = [vp, i32, vp, i32, f32, vp, vp]
     lib.fr_check_exact_math.argtypes = [C.c_uint64, C.c_uint32, vp, vp]
+    lib.fr_read_wave_counts.argtypes = [vp, vp, vp, vp, vp]
     _lib = lib
     return lib
 
@@ -256,6 +258,16 @@ class Renderer:
         idx = paths * 32 + slots
         ph = np.concatenate([pos[idx, :3], flux[idx, :3], d[idx, :3], pos[idx, 3:4], flux[idx, 3:4]], 1)
         return ph, paths.astype(np.int32), slots.astype(np.int32)
+
+    def wave_counts(self):
+        """Paths traced per round of the last iteration's eye and photon
+        passes, and (last entry) the paths handed to each tail kernel."""
+        e = np.zeros(17, np.uint32)
+        p = np.zeros(17, np.uint32)
+        er = np.zeros(1, np.int32)
+        pr = np.zeros(1, np.int32)
+        _check(_lib.fr_read_wave_counts(self.h, _ptr(e), _ptr(p), _ptr(er), _ptr(pr)), 'fr_read_wave_counts')
+        return e[:er[0] + 1].copy(), p[:pr[0] + 1].copy()
 
     def read_gather(self):
         n = self.width * self.height

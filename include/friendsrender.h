@@ -155,13 +155,24 @@ void* fr_stream(fr_ctx* ctx);
 
 void fr_destroy(fr_ctx* ctx);
 
-/* Stage profiler.  While enabled, fr_iterate records CUDA events on the
- * context's stream around each stage of an iteration (FR_STAGE_*);
- * fr_profile_read synchronizes, returns the summed milliseconds and the
- * number of timed launches per stage, then clears them.  max_iterations
- * bounds the iterations profiled between reads (events are created here).
- * *launches is the number of kernels fr_iterate has launched so far. */
-enum { FR_STAGE_EYE = 0, FR_STAGE_PHOTON = 1, FR_STAGE_GRID = 2, FR_STAGE_GATHER = 3, FR_STAGES = 4 };
+/* Stage profiler.  While enabled, fr_iterate records CUDA events around each
+ * stage of an iteration and around each trace-round kernel (FR_STAGE_*), on
+ * the stream the stage runs on (the eye pass has a stream of its own, joined
+ * to the context's stream before the grid stage, so the eye and photon stages
+ * overlap in time); fr_profile_read synchronizes, returns the summed
+ * milliseconds and the number of timed intervals per stage, then clears them.
+ * max_iterations bounds the iterations profiled between reads (events are
+ * created here).  *launches is the number of kernels fr_iterate has launched
+ * so far. */
+enum {
+  FR_STAGE_EYE = 0,          /* eye pass (its own stream, concurrent with the photon pass) */
+  FR_STAGE_PHOTON = 1,       /* photon pass */
+  FR_STAGE_GRID = 2,         /* photon grid build */
+  FR_STAGE_GATHER = 3,       /* gather and N/tau/R update */
+  FR_STAGE_EYE_TRACE = 4,    /* the eye pass's trace-round kernels (inside FR_STAGE_EYE) */
+  FR_STAGE_PHOTON_TRACE = 5, /* the photon pass's trace-round kernels (inside FR_STAGE_PHOTON) */
+  FR_STAGES = 6
+};
 int fr_profile_enable(fr_ctx* ctx, int32_t on, int32_t max_iterations);
 int fr_profile_read(fr_ctx* ctx, double* stage_ms, int64_t* stage_count, int64_t* launches);
 
@@ -218,6 +229,14 @@ int fr_radius_count_noalloc(const float* hp_dev, int32_t num_hitpoints, const fl
  * square root. */
 #define FR_EXACT_FUNCTIONS 9
 int fr_check_exact_math(uint64_t samples, uint32_t seed, uint64_t* mismatches, uint64_t* fast_paths);
+
+/* No reference counterpart: the wavefront queue lengths of the last
+ * iteration.  eye_counts[r] / photon_counts[r] is the number of paths traced
+ * in round r (r < *eye_rounds / *photon_rounds) and, at r = rounds, the number
+ * handed to the tail kernel; arrays of FR_MAX_WAVE_ROUNDS + 1 entries. */
+#define FR_MAX_WAVE_ROUNDS 16
+int fr_read_wave_counts(fr_ctx* ctx, uint32_t* eye_counts, uint32_t* photon_counts, int32_t* eye_rounds,
+                        int32_t* photon_rounds);
 
 /* Hitpoints of the last iteration (SoA, see HitpointBuf in the kernels):
  * each array width*height*4 floats; any pointer may be NULL. */
