@@ -284,7 +284,8 @@ def main():
         'ms_per_step': total_ms / args.steps, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
         'dtype': 'f32', 'data': 'synthetic (seeded scene, random-init textures)',
         'config': {'workload': WORKLOAD, 'photons_per_step': args.photons, 'pixels': npix,
-                   'triangles': stats['triangles'], 'l2': 'flushed (256 MB write) before every timed step',
+                   'triangles': stats['triangles'], 'bvh_nodes': stats['bvh_nodes'],
+                   'l2': 'flushed (256 MB write) before every timed step',
                    'parallelism': 'replicas' if world > 1 else 'single GPU'},
         'hitpoint_updates_per_s': world * npix * args.steps / (total_ms / 1000.0),
         'stage_ms_per_step': per,

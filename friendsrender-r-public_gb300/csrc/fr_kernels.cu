@@ -891,7 +891,11 @@ __global__ void __launch_bounds__(256) k_gather(SceneGPU sc, IterParams it, Hitp
       const float b = (float)(N + M);
       double* tau = st.tau + 3 * (size_t)i + lane;
       const float v = lane == 0 ? vx : (lane == 1 ? vy : vz);
-      *tau = (*tau + (double)v) * (double)a / (double)b;
+      // The ratio a / b as a float-float (within 2^-46 of a / b; an FP64
+      // divide is about ten FP64 instructions on GB300), then one FP64 add
+      // and multiply per component.
+      const xf::ff q = xf::div_f(xf::ff{a, 0.0f}, b);
+      *tau = (*tau + (double)v) * ((double)q.h + (double)q.l);
       if (lane == 0) {
         st.r[i] = R * sqrtf(a / b);
         st.n[i] = (int)((float)N + (float)M * it.alpha);
