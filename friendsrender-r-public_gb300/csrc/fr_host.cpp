@@ -426,9 +426,9 @@ struct StageMark {
   }
 };
 
-// Per-iteration counters: both passes' round queues, the hitpoint list and
-// both passes' shade queues.
-constexpr size_t kCounters = 2 * (kWaveRounds + 2) + 1 + 2 * kWaveRounds * kShadeQueues;
+// Per-iteration counters: both passes' round queues, the hitpoint list,
+// both passes' shade queues and trace fetch counters.
+constexpr size_t kCounters = 2 * (kWaveRounds + 2) + 1 + 2 * kWaveRounds * kShadeQueues + 2 * kWaveRounds;
 
 int run_iteration(fr_ctx* c) {
   const uint32_t step = (uint32_t)(++c->iterations);
@@ -457,7 +457,7 @@ int run_iteration(fr_ctx* c) {
     for (int r = 0; r < kEyeRounds; ++r) {
       {
         StageMark t(c, FR_STAGE_EYE_TRACE, e);
-        launch_wave_trace(c->sc, c->eye_wave, r, grid, c->err, e);
+        launch_wave_trace(c->sc, c->eye_wave, r, grid, r == 0, c->err, e);
       }
       launch_wave_sort(c->sc, c->eye_wave, r, sort_grid, e);
       launch_ew_shade(c->sc, it, c->rr_eye, c->eye_wave, c->hp, c->st, c->gi, r, grid, e);
@@ -472,7 +472,7 @@ int run_iteration(fr_ctx* c) {
     for (int r = 0; r < kPhotonRounds; ++r) {
       {
         StageMark t(c, FR_STAGE_PHOTON_TRACE, s);
-        launch_wave_trace(c->sc, c->wave, r, grid, c->err, s);
+        launch_wave_trace(c->sc, c->wave, r, grid, false, c->err, s);
       }
       launch_wave_sort(c->sc, c->wave, r, sort_grid, s);
       launch_pw_shade(c->sc, it, c->ph, c->wave, c->counts, r, grid, s);
@@ -669,12 +669,14 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
       (rc = c->alloc(&c->dbg_m, npix)) || (rc = c->alloc(&c->dbg_phi, npix)) || (rc = c->alloc(&c->image, npix)))
     return bail(rc);
   // Counters (one memset per iteration): eye rounds, photon rounds, the
-  // hitpoint list, eye and photon shade queues.
+  // hitpoint list, eye and photon shade queues, eye and photon trace fetches.
   c->eye_wave.qcount = c->wave.qcount;
   c->wave.qcount += kWaveRounds + 2;
   c->hp.list_count = c->eye_wave.qcount + 2 * (kWaveRounds + 2);
   c->eye_wave.mcount = c->hp.list_count + 1;
   c->wave.mcount = c->eye_wave.mcount + kWaveRounds * kShadeQueues;
+  c->eye_wave.tfetch = c->wave.mcount + kWaveRounds * kShadeQueues;
+  c->wave.tfetch = c->eye_wave.tfetch + kWaveRounds;
   c->eye_wave.cap = (uint32_t)npix;
   c->wave.cap = (uint32_t)wave_n;
   // Photon grid: one bucket per expected photon or better (a few photons per path).

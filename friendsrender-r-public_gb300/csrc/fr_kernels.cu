@@ -272,8 +272,9 @@ __global__ void __launch_bounds__(128) k_ew_start(CameraGPU cam, IterParams it, 
   }
 }
 
-// Closest hit of every path in queue `round` (eye or photon wave).
-__global__ void __launch_bounds__(128) k_wave_trace(SceneGPU sc, PathWave w, int round, int* err) {
+// Closest hit of every path in queue `round`, for queues of coherent rays
+// (camera rays in pixel order): each warp takes 32 consecutive entries.
+__global__ void __launch_bounds__(128) k_wave_trace_static(SceneGPU sc, PathWave w, int round, int* err) {
   const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
   const uint32_t* q = w.queue[round & 1];
   for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
@@ -284,6 +285,120 @@ __global__ void __launch_bounds__(128) k_wave_trace(SceneGPU sc, PathWave w, int
       w.hit[i] = make_float4(h.u, h.v, __int_as_float(h.tri), __int_as_float(h.facet));
     else
       w.hit[i] = make_float4(0.f, 0.f, __int_as_float(-1), __int_as_float(-1));
+  }
+}
+
+// Closest hit of every path in queue `round` (eye or photon wave), with
+// dynamic ray fetch: a lane whose ray is done takes the next queue entry at
+// once instead of idling until the warp's slowest ray ends.  A warp claims
+// queue entries 32 at a time with one atomic and hands them to its idle lanes.
+// The traversal is trace_closest's (fr_trace.cuh), one node visit or leaf per
+// loop pass, so the hits are the same.
+__global__ void __launch_bounds__(128) k_wave_trace(SceneGPU sc, PathWave w, int round, int* err) {
+  const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
+  const uint32_t* q = w.queue[round & 1];
+  uint32_t* fetch = w.tfetch + round;
+  const unsigned lane = threadIdx.x & 31u;
+  const unsigned below = (1u << lane) - 1u;
+  // Warp-uniform batch of claimed queue entries [pool, pool + left).
+  uint32_t pool = 0, left = 0;
+  bool exhausted = false;
+  // Per-lane traversal state.
+  bool active = false;
+  uint32_t i = 0;
+  V3 org = v3(0.f, 0.f, 0.f), dir = org;
+  RayPre r{};
+  float tbest = FLT_MAX, bu = 0.f, bv = 0.f, tref = 0.f;
+  int32_t best_tri = -1, best_facet = -1;
+  uint32_t ref = 0;
+  int sp = 0;
+  uint2 stack[kTraversalStack];
+  while (true) {
+    unsigned idle = __ballot_sync(0xffffffffu, !active);
+    while (idle && !exhausted) {
+      if (left == 0) {
+        uint32_t b = 0;
+        if (lane == 0) b = atomicAdd(fetch, 32u);
+        b = __shfl_sync(0xffffffffu, b, 0);
+        if (b >= n) {
+          exhausted = true;
+          break;
+        }
+        pool = b;
+        left = min(32u, n - b);
+      }
+      const unsigned take = min((unsigned)__popc(idle), left);
+      const unsigned rank = (unsigned)__popc(idle & below);
+      if (!active && rank < take) {
+        i = q[pool + rank];
+        const float4 a4 = w.a[i], b4 = w.b[i];
+        org = v3(a4.x, a4.y, a4.z);
+        dir = v3(b4.x, b4.y, b4.z);
+        r = ray_pre(org, dir);
+        tbest = FLT_MAX;
+        best_tri = best_facet = -1;
+        bu = bv = 0.f;
+        ref = 0;
+        tref = kRayOffset;
+        sp = 0;
+        active = true;
+      }
+      pool += take;
+      left -= take;
+      idle = __ballot_sync(0xffffffffu, !active);
+    }
+    if (!__any_sync(0xffffffffu, active)) break;
+    if (!active) continue;
+    // One pass of trace_closest's loop.
+    bool pop = true;
+    if (tref <= tbest) {
+      if (!(ref & kLeafBit)) {
+        NodeVisit nv;
+        visit_node(sc.nodes, ref, r, kRayOffset, tbest, nv);
+        sort8(nv.key);
+        if (nv.key[0] != 0xFFFFFFFFu) {
+          int cnt = 1;
+#pragma unroll
+          for (int k = 1; k < 8; ++k) cnt += nv.key[k] != 0xFFFFFFFFu;
+          if (sp + cnt - 1 > kTraversalStack) {
+            atomicOr(err, kErrStack);
+            best_tri = -1;
+            sp = 0;
+          } else {
+#pragma unroll
+            for (int k = 7; k >= 1; --k)
+              if (k < cnt) stack[sp++] = make_uint2(child_ref(nv, nv.key[k] & 7u), nv.key[k] & ~7u);
+            ref = child_ref(nv, nv.key[0] & 7u);
+            tref = __uint_as_float(nv.key[0] & ~7u);
+            pop = false;
+          }
+        }
+      } else {
+        const int first = (int)(ref & kLeafFirstMask);
+        const int count = (int)((ref >> kLeafCountShift) & 0xFu) + 1;
+        for (int k = 0; k < count; ++k) {
+          const TriGPU tr = load_tri(sc.tris, first + k);
+          float t, u, v;
+          if (intersect_triangle(org, dir, tr, t, u, v) && t > kRayOffset) {
+            const int32_t facet = __float_as_int(tr.v0[3]);
+            if (t < tbest || (t == tbest && facet > best_facet)) {
+              tbest = t; bu = u; bv = v; best_tri = first + k; best_facet = facet;
+            }
+          }
+        }
+      }
+    }
+    if (pop) {
+      if (sp == 0) {
+        w.hit[i] = best_tri >= 0 ? make_float4(bu, bv, __int_as_float(best_tri), __int_as_float(best_facet))
+                                 : make_float4(0.f, 0.f, __int_as_float(-1), __int_as_float(-1));
+        active = false;
+      } else {
+        const uint2 e = stack[--sp];
+        ref = e.x;
+        tref = __uint_as_float(e.y);
+      }
+    }
   }
 }
 
@@ -977,8 +1092,11 @@ void launch_ew_start(const CameraGPU& cam, const IterParams& it, PathWave w, cud
   k_ew_start<<<blocks_for((size_t)it.width * it.height, 128), 128, 0, s>>>(cam, it, w);
 }
 
-void launch_wave_trace(const SceneGPU& sc, PathWave w, int round, int grid, int* err, cudaStream_t s) {
-  k_wave_trace<<<std::max(1, grid), 128, 0, s>>>(sc, w, round, err);
+void launch_wave_trace(const SceneGPU& sc, PathWave w, int round, int grid, bool coherent, int* err, cudaStream_t s) {
+  if (coherent)
+    k_wave_trace_static<<<std::max(1, grid), 128, 0, s>>>(sc, w, round, err);
+  else
+    k_wave_trace<<<std::max(1, grid), 128, 0, s>>>(sc, w, round, err);
 }
 
 void launch_wave_sort(const SceneGPU& sc, PathWave w, int round, int grid, cudaStream_t s) {

@@ -67,6 +67,7 @@ struct PathWave {
   uint32_t* qcount;       // kWaveRounds + 2 counters
   uint32_t* mq;           // kShadeQueues queues of `cap` entries: this round's hits by surface type
   uint32_t* mcount;       // kWaveRounds * kShadeQueues counters
+  uint32_t* tfetch;       // kWaveRounds counters: queue entries claimed by the trace kernel
   uint32_t cap;
 };
 
@@ -100,7 +101,9 @@ void upload_byte_lut(cudaStream_t s);
 // rounds of trace / sort / shade over the live-path queue, and a tail
 // kernel.  `grid` is the block count of the persistent-style round kernels.
 void launch_ew_start(const CameraGPU& cam, const IterParams& it, PathWave w, cudaStream_t s);
-void launch_wave_trace(const SceneGPU& sc, PathWave w, int round, int grid, int* err, cudaStream_t s);
+// coherent: the queue holds rays in an order that neighbouring lanes should
+// keep (camera rays in pixel order); otherwise lanes fetch rays dynamically.
+void launch_wave_trace(const SceneGPU& sc, PathWave w, int round, int grid, bool coherent, int* err, cudaStream_t s);
 void launch_wave_sort(const SceneGPU& sc, PathWave w, int round, int grid, cudaStream_t s);
 void launch_ew_shade(const SceneGPU& sc, const IterParams& it, const float* rr_eye, PathWave w, HitpointBuf hp,
                      PixelState st, GridInfo* gi, int round, int grid, cudaStream_t s);
