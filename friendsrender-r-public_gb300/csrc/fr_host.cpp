@@ -535,8 +535,13 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
     delete c;
     return code;
   };
-  if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess ||
-      cudaStreamCreateWithFlags(&c->side, cudaStreamNonBlocking) != cudaSuccess ||
+  // The photon pass (main stream) is the iteration's critical path; the eye
+  // pass (side stream) runs at a lower priority and fills the SMs the photon
+  // pass leaves idle.
+  int prio_low = 0, prio_high = 0;
+  cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
+  if (cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio_high) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, prio_low) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming) != cudaSuccess)
     return bail(fail(FR_ERR_CUDA, "cudaStreamCreate/cudaEventCreate failed"));

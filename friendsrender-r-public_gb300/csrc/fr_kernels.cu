@@ -737,11 +737,23 @@ __global__ void __launch_bounds__(128) k_pw_shade(SceneGPU sc, IterParams it, Ph
 }
 
 // Paths alive after the last wavefront round, each run to its end.
+// At most kTailPathsPerWarp paths share a warp: a tail path's bounces are a
+// chain of dependent traversals, and the fewer divergent paths a warp carries,
+// the sooner each of its paths advances.
+#ifndef FR_TAIL_PATHS_PER_WARP
+#define FR_TAIL_PATHS_PER_WARP 16
+#endif
+constexpr uint32_t kTailPathsPerWarp = FR_TAIL_PATHS_PER_WARP;
+
 __global__ void __launch_bounds__(128) k_pw_tail(SceneGPU sc, IterParams it, PhotonSlots ph, PathWave w,
                                                  uint32_t* counts, int round, int* err) {
   const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
   const uint32_t* q = w.queue[round & 1];
-  for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+  const uint32_t lane = threadIdx.x & 31u;
+  if (lane >= kTailPathsPerWarp) return;
+  const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  for (uint32_t j = warp * kTailPathsPerWarp + lane; j < n; j += nwarps * kTailPathsPerWarp) {
     const int i = (int)q[j];
     PhotonState s;
     load_state(w, i, s);
@@ -893,21 +905,31 @@ __device__ __forceinline__ void for_each_photon_in_ball(const PhotonGrid& g, con
       }
 }
 
-// applyHitPointInfo (SPPM.cpp:395-451) with one warp per hitpoint of the
-// hitpoint list.  The warp's lanes take one overlapping cell each, scan the
-// cells' photon counts, and then share out the candidates of all cells, 32 at
-// a time, so every lane tests and (if inside the ball) shades its own photon.
+// applyHitPointInfo (SPPM.cpp:395-451) with one group of G lanes per hitpoint
+// of the hitpoint list (32 / G hitpoints per warp at a time: a hitpoint's
+// work is a chain of dependent loads, so several in flight per warp hide
+// it).  The group's lanes take one overlapping cell each, scan the cells'
+// photon counts, and then share out the candidates of all cells, G at a time,
+// so every lane tests and (if inside the ball) shades its own photon.
 // Per-lane Kahan FP32 sums are added in a fixed butterfly order; the N/tau/R
 // update follows with tau in FP64.
+#ifndef FR_GATHER_GROUP
+#define FR_GATHER_GROUP 16
+#endif
+constexpr int kGatherGroup = FR_GATHER_GROUP;
+
 __global__ void __launch_bounds__(256) k_gather(SceneGPU sc, IterParams it, HitpointBuf hp, PhotonGrid g,
                                                const GridInfo* gip, PixelState st, int32_t* dbg_m, float4* dbg_phi) {
+  constexpr int G = kGatherGroup;
   const unsigned lane = threadIdx.x & 31u;
+  const unsigned gl = lane & (G - 1);                        // lane within the group
+  const unsigned gmask = (G == 32 ? 0xffffffffu : ((1u << G) - 1u) << (lane & ~(unsigned)(G - 1)));
   const uint32_t n = *(volatile const uint32_t*)hp.list_count;
-  const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
+  const uint32_t ngroups = (gridDim.x * blockDim.x) / G;
   const GridInfo gi = *gip;
   const float inv = gi.inv_cell;
   const uint32_t mask = g.table - 1u;
-  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < n; w += nwarps) {
+  for (uint32_t w = (blockIdx.x * blockDim.x + threadIdx.x) / G; w < n; w += ngroups) {
     const uint32_t i = hp.list[w];
     const float4 hp0 = hp.pos[i], hn = hp.nrm[i], ho = hp.out[i], hw = hp.wgt[i];
     const V3 x = v3(hp0.x, hp0.y, hp0.z), nrm = v3(hn.x, hn.y, hn.z), out = v3(ho.x, ho.y, ho.z);
@@ -923,8 +945,8 @@ __global__ void __launch_bounds__(256) k_gather(SceneGPU sc, IterParams it, Hitp
     const int ncell = nx * ny * nz;
     int M = 0;
     float sx = 0.f, sy = 0.f, sz = 0.f, kx = 0.f, ky = 0.f, kz = 0.f;
-    for (int c0 = 0; c0 < ncell; c0 += 32) {
-      const int c = c0 + (int)lane;
+    for (int c0 = 0; c0 < ncell; c0 += G) {
+      const int c = c0 + (int)gl;
       int cx = 0, cy = 0, cz = 0;
       uint32_t cb = 0, cn = 0;
       if (c < ncell) {
@@ -938,25 +960,25 @@ __global__ void __launch_bounds__(256) k_gather(SceneGPU sc, IterParams it, Hitp
       }
       uint32_t incl = cn;
 #pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t t = __shfl_up_sync(0xffffffffu, incl, o);
-        if ((int)lane >= o) incl += t;
+      for (int o = 1; o < G; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(gmask, incl, o, G);
+        if ((int)gl >= o) incl += t;
       }
-      const uint32_t total = __shfl_sync(0xffffffffu, incl, 31);
-      for (uint32_t t0 = 0; t0 < total; t0 += 32) {
-        const uint32_t k = t0 + lane;
+      const uint32_t total = __shfl_sync(gmask, incl, G - 1, G);
+      for (uint32_t t0 = 0; t0 < total; t0 += G) {
+        const uint32_t k = t0 + gl;
         // Source lane: the first whose inclusive count exceeds k.
         int src = 0;
 #pragma unroll
-        for (int step = 16; step; step >>= 1) {
-          const uint32_t v = __shfl_sync(0xffffffffu, incl, src + step - 1);
+        for (int step = G / 2; step; step >>= 1) {
+          const uint32_t v = __shfl_sync(gmask, incl, src + step - 1, G);
           if (v <= k) src += step;
         }
-        const uint32_t sb = __shfl_sync(0xffffffffu, cb, src);
-        const uint32_t se = __shfl_sync(0xffffffffu, incl, src) - __shfl_sync(0xffffffffu, cn, src);
-        const int scx = __shfl_sync(0xffffffffu, cx, src);
-        const int scy = __shfl_sync(0xffffffffu, cy, src);
-        const int scz = __shfl_sync(0xffffffffu, cz, src);
+        const uint32_t sb = __shfl_sync(gmask, cb, src, G);
+        const uint32_t se = __shfl_sync(gmask, incl, src, G) - __shfl_sync(gmask, cn, src, G);
+        const int scx = __shfl_sync(gmask, cx, src, G);
+        const int scy = __shfl_sync(gmask, cy, src, G);
+        const int scz = __shfl_sync(gmask, cz, src, G);
         if (k >= total) continue;
         const uint32_t j = sb + (k - se);
         const float4 p4 = __ldg(g.pos + j);
@@ -984,34 +1006,34 @@ __global__ void __launch_bounds__(256) k_gather(SceneGPU sc, IterParams it, Hitp
         ++M;
       }
     }
-    M = __reduce_add_sync(0xffffffffu, M);
     float vx = sx - kx, vy = sy - ky, vz = sz - kz;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      vx += __shfl_xor_sync(0xffffffffu, vx, o);
-      vy += __shfl_xor_sync(0xffffffffu, vy, o);
-      vz += __shfl_xor_sync(0xffffffffu, vz, o);
+    for (int o = G / 2; o > 0; o >>= 1) {
+      M += __shfl_xor_sync(gmask, M, o, G);
+      vx += __shfl_xor_sync(gmask, vx, o, G);
+      vy += __shfl_xor_sync(gmask, vy, o, G);
+      vz += __shfl_xor_sync(gmask, vz, o, G);
     }
-    vx = __shfl_sync(0xffffffffu, vx, 0);
-    vy = __shfl_sync(0xffffffffu, vy, 0);
-    vz = __shfl_sync(0xffffffffu, vz, 0);
-    if (lane == 0 && dbg_m) {
+    vx = __shfl_sync(gmask, vx, 0, G);
+    vy = __shfl_sync(gmask, vy, 0, G);
+    vz = __shfl_sync(gmask, vz, 0, G);
+    if (gl == 0 && dbg_m) {
       dbg_m[i] = M;
       dbg_phi[i] = make_float4(vx, vy, vz, 0.f);
     }
-    if (M > 0 && lane < 3) {
-      // N/tau/R update (SPPM.cpp:444-449); lane c updates tau component c.
+    if (M > 0 && gl < 3) {
+      // N/tau/R update (SPPM.cpp:444-449); group lane c updates tau component c.
       const int N = st.n[i];
       const float a = (float)N + it.alpha * (float)M;
       const float b = (float)(N + M);
-      double* tau = st.tau + 3 * (size_t)i + lane;
-      const float v = lane == 0 ? vx : (lane == 1 ? vy : vz);
+      double* tau = st.tau + 3 * (size_t)i + gl;
+      const float v = gl == 0 ? vx : (gl == 1 ? vy : vz);
       // The ratio a / b as a float-float (within 2^-46 of a / b; an FP64
       // divide is about ten FP64 instructions on GB300), then one FP64 add
       // and multiply per component.
       const xf::ff q = xf::div_f(xf::ff{a, 0.0f}, b);
       *tau = (*tau + (double)v) * ((double)q.h + (double)q.l);
-      if (lane == 0) {
+      if (gl == 0) {
         st.r[i] = R * sqrtf(a / b);
         st.n[i] = (int)((float)N + (float)M * it.alpha);
         st.g[i] += 1;
@@ -1125,7 +1147,16 @@ void launch_pw_shade(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, P
 
 void launch_pw_tail(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, PathWave w, uint32_t* counts,
                     int round, int grid, int* err, cudaStream_t s) {
-  k_pw_tail<<<std::max(1, grid), 128, 0, s>>>(sc, it, ph, w, counts, round, err);
+  static int tail_blocks = -1;  // resident blocks of k_pw_tail on this device
+  if (tail_blocks < 0) {
+    int b = 0, dev = 0, sms = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pw_tail, 128, 0);
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    tail_blocks = std::max(1, b * sms);
+  }
+  (void)grid;
+  k_pw_tail<<<tail_blocks, 128, 0, s>>>(sc, it, ph, w, counts, round, err);
 }
 
 int photon_pass_blocks_per_sm() {
