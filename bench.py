@@ -12,6 +12,8 @@ paths per iteration, alpha 0.7, initial radius 0.02.
 
 value: photon paths/s over all GPUs, inputs resident in HBM, CUDA events on
 the renderer's stream, L2 flushed (256 MB write) before every timed step.
+Stage times and the roofline come from a second, profiled run of the same
+steps (CUDA events around every stage and trace launch).
 e2e: the same metric through the C-ABI with a host result buffer: every step
 is fr_iterate + fr_resolve into pinned host memory (the image, read back each
 step); the scene is uploaded once by fr_create (reported as setup).
@@ -221,11 +223,9 @@ def main():
         if world > 1:
             torch.distributed.barrier()
 
-    # ---- device-timed region
-    r.profile(True, max_iterations=args.steps)
+    # ---- device-timed region (iterations replay the captured iteration graph)
     evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
     l0 = r.profile_read()[2]
-    r.profile(True, max_iterations=args.steps)
     barrier()
     torch.cuda.synchronize()
     with ClockSampler(local) as clk:
@@ -238,14 +238,25 @@ def main():
         stream.synchronize()
     torch.cuda.synchronize()
     barrier()
-    stage_ms, stage_n, l1 = r.profile_read()
-    r.profile(False)
+    l1 = r.profile_read()[2]
     total_ms = sum(a.elapsed_time(b) for a, b in evs)
     if world > 1:
         t = torch.tensor([total_ms], device='cuda')
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         total_ms = float(t.item())
     launches = l1 - l0
+
+    # ---- the same steps again with the stage profiler's CUDA events (stage and
+    # trace-kernel durations for the roofline; launched directly, not as a graph)
+    r.profile(True, max_iterations=args.steps)
+    torch.cuda.synchronize()
+    for k in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        r.iterate(1, sync=False)
+    stream.synchronize()
+    stage_ms, stage_n, _ = r.profile_read()
+    r.profile(False)
 
     # ---- rays traced and photons stored in the last timed iteration
     eye_q, photon_q = r.wave_counts()

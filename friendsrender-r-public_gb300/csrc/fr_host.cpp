@@ -223,6 +223,11 @@ struct fr_ctx {
   cudaStream_t side = nullptr;   // the eye pass's stream, forked from and joined to `stream`
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   int photon_blocks = 0;         // grid of the wavefront round kernels
+  int tail_blocks = 0;           // grid of the photon tail kernel
+  uint32_t* step_dev = nullptr;  // device iteration counter (IterParams::step)
+  cudaGraph_t graph = nullptr;   // one captured iteration
+  cudaGraphExec_t graph_exec = nullptr;
+  int64_t graph_launches = 0;    // kernels per replay of the graph
   int gather_blocks = 0;         // grid of the gather (one warp per hitpoint)
   PhotonGrid grid{};
   GridInfo* gi = nullptr;
@@ -264,6 +269,8 @@ struct fr_ctx {
     for (auto& b : bufs) cudaFree(b.p);
     if (fork_ev) cudaEventDestroy(fork_ev);
     if (join_ev) cudaEventDestroy(join_ev);
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (graph) cudaGraphDestroy(graph);
     if (side) cudaStreamDestroy(side);
     if (stream) cudaStreamDestroy(stream);
   }
@@ -430,16 +437,18 @@ struct StageMark {
 // both passes' shade queues and trace fetch counters.
 constexpr size_t kCounters = 2 * (kWaveRounds + 2) + 1 + 2 * kWaveRounds * kShadeQueues + 2 * kWaveRounds;
 
-int run_iteration(fr_ctx* c) {
-  const uint32_t step = (uint32_t)(++c->iterations);
+// Enqueues one iteration (the kernels read the iteration number from
+// c->step_dev, which the first kernel advances).
+int enqueue_iteration(fr_ctx* c) {
   IterParams it{};
-  it.step = step;
+  it.step = c->step_dev;
   it.photons = c->P;
   it.width = c->W;
   it.height = c->H;
   it.alpha = c->alpha;
   it.flags = c->flags;
   cudaStream_t s = c->stream;
+  launch_next_step(c->step_dev, s);
   // Queue counters of both passes and the hitpoint-list count.
   FR_CUDA(cudaMemsetAsync(c->eye_wave.qcount, 0, sizeof(uint32_t) * kCounters, s));
   // The eye pass (side stream) and the photon pass (main stream) share
@@ -477,7 +486,7 @@ int run_iteration(fr_ctx* c) {
       launch_wave_sort(c->sc, c->wave, r, sort_grid, s);
       launch_pw_shade(c->sc, it, c->ph, c->wave, c->counts, r, grid, s);
     }
-    launch_pw_tail(c->sc, it, c->ph, c->wave, c->counts, kPhotonRounds, grid, c->err, s);
+    launch_pw_tail(c->sc, it, c->ph, c->wave, c->counts, kPhotonRounds, c->tail_blocks, c->err, s);
   }
   FR_CUDA(cudaStreamWaitEvent(s, c->join_ev, 0));
   {
@@ -494,10 +503,41 @@ int run_iteration(fr_ctx* c) {
     FR_CUDA(cudaMemsetAsync(c->dbg_phi, 0, sizeof(float4) * (size_t)c->W * c->H, s));
     launch_gather_update(c->sc, it, c->hp, c->grid, c->gi, c->st, c->dbg_m, c->dbg_phi, c->gather_blocks, s);
   }
-  // eye and photon passes (start, rounds of trace/sort/shade, tail), grid setup, count, scatter, gather
-  c->launches += 4 + (2 + 3 * kEyeRounds) + (2 + 3 * kPhotonRounds);
-  c->photons_total += c->P;
+  // iteration counter, eye and photon passes (start, rounds of
+  // trace/sort/shade, tail), grid setup, count, scatter, gather
+  c->launches += 5 + (2 + 3 * kEyeRounds) + (2 + 3 * kPhotonRounds);
   FR_CUDA(cudaGetLastError());
+  return FR_OK;
+}
+
+// One iteration: a replay of the captured iteration graph, or (while the
+// stage profiler records events) direct launches.
+int run_iteration(fr_ctx* c) {
+  if (c->profiling) {
+    const int rc = enqueue_iteration(c);
+    if (rc) return rc;
+  } else {
+    if (!c->graph_exec) {
+      const int64_t before = c->launches;
+      FR_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      const int rc = enqueue_iteration(c);
+      cudaGraph_t g = nullptr;
+      const cudaError_t ec = cudaStreamEndCapture(c->stream, &g);
+      if (rc) {
+        if (g) cudaGraphDestroy(g);
+        return rc;
+      }
+      if (ec != cudaSuccess) return fail(FR_ERR_CUDA, "iteration capture: %s", cudaGetErrorString(ec));
+      c->graph = g;
+      FR_CUDA(cudaGraphInstantiate(&c->graph_exec, c->graph, 0));
+      c->graph_launches = c->launches - before;
+      c->launches = before;
+    }
+    FR_CUDA(cudaGraphLaunch(c->graph_exec, c->stream));
+    c->launches += c->graph_launches;
+  }
+  ++c->iterations;
+  c->photons_total += c->P;
   return FR_OK;
 }
 
@@ -563,6 +603,7 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
   if ((rc = exact_tables(dev, &tabs))) return bail(rc);
   upload_tables(tabs.sincos, tabs.sqrt1m, c->stream);
   c->photon_blocks = std::max(1, photon_pass_blocks_per_sm()) * sms;
+  c->tail_blocks = std::max(1, pw_tail_blocks_per_sm()) * sms;
   c->gather_blocks = std::max(1, gather_blocks_per_sm()) * sms;
 
   // ---- geometry
@@ -669,7 +710,7 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
       (rc = c->alloc(&c->wave.qcount, kCounters)) || (rc = c->alloc(&c->hp.list, npix)) ||
       (rc = c->alloc(&c->wave.mq, (size_t)kShadeQueues * wave_n)) ||
       (rc = c->alloc(&c->eye_wave.mq, (size_t)kShadeQueues * npix)) ||
-      (rc = c->alloc(&c->gi, 1)) ||
+      (rc = c->alloc(&c->gi, 1)) || (rc = c->alloc(&c->step_dev, 1)) ||
       (rc = c->alloc(&c->err, 1)) ||
       (rc = c->alloc(&c->dbg_m, npix)) || (rc = c->alloc(&c->dbg_phi, npix)) || (rc = c->alloc(&c->image, npix)))
     return bail(rc);
@@ -710,6 +751,7 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
   cudaMemsetAsync(c->ph.pos, 0, nslots * sizeof(float4), c->stream);
   cudaMemsetAsync(c->ph.flux, 0, nslots * sizeof(float4), c->stream);
   cudaMemsetAsync(c->gi, 0, sizeof(GridInfo), c->stream);
+  cudaMemsetAsync(c->step_dev, 0, sizeof(uint32_t), c->stream);
   cudaMemsetAsync(c->err, 0, sizeof(int), c->stream);
   cudaMemsetAsync(c->hp.pos, 0, npix * sizeof(float4), c->stream);
   if (cudaStreamSynchronize(c->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess)
@@ -988,6 +1030,107 @@ int fr_read_state(fr_ctx* c, double* tau, int32_t* n, float* r, int32_t* g) {
   if (r) FR_CUDA(cudaMemcpyAsync(r, c->st.r, 4 * np, cudaMemcpyDeviceToHost, c->stream));
   if (g) FR_CUDA(cudaMemcpyAsync(g, c->st.g, 4 * np, cudaMemcpyDeviceToHost, c->stream));
   return fr_synchronize(c);
+}
+
+int fr_update(fr_ctx* c, const int32_t* m, const float* phi) {
+  if (!c || !m || !phi) return fail(FR_ERR_INVALID, "fr_update: bad arguments");
+  const size_t np = (size_t)c->W * c->H;
+  std::vector<float4> phi4(np);
+  for (size_t i = 0; i < np; ++i) phi4[i] = make_float4(phi[3 * i], phi[3 * i + 1], phi[3 * i + 2], 0.0f);
+  FR_CUDA(cudaMemcpyAsync(c->dbg_m, m, sizeof(int32_t) * np, cudaMemcpyHostToDevice, c->stream));
+  FR_CUDA(cudaMemcpyAsync(c->dbg_phi, phi4.data(), sizeof(float4) * np, cudaMemcpyHostToDevice, c->stream));
+  launch_update(c->st, c->dbg_m, c->dbg_phi, (int)np, c->alpha, c->stream);
+  return fr_synchronize(c);
+}
+
+// ------------------------------------------------------------ checkpoint
+// State between iterations: the iteration count and photon total (they key
+// the random streams and the resolve), the per-pixel state and the photon
+// slots (a slot stored in an earlier iteration can join a later iteration's
+// photon set, SPPM.cpp:672).  Layout: a fixed header, then tau, N, R,
+// NumGather, slot positions, fluxes and directions, each as on the device.
+namespace {
+struct StateHeader {
+  char magic[8];  // "FRSPPMS1"
+  int32_t width, height, photons, flags;
+  float alpha, initial_radius;
+  int32_t triangles, reserved;
+  int64_t iterations, photons_total;
+};
+static_assert(sizeof(StateHeader) == 56, "checkpoint header is 56 bytes");
+constexpr char kStateMagic[8] = {'F', 'R', 'S', 'P', 'P', 'M', 'S', '1'};
+
+struct StatePart {
+  void* dev;
+  size_t bytes;
+};
+
+std::vector<StatePart> state_parts(fr_ctx* c) {
+  const size_t np = (size_t)c->W * c->H, ns = (size_t)c->P * kPhotonSlots;
+  return {{c->st.tau, 24 * np}, {c->st.n, 4 * np},       {c->st.r, 4 * np},
+          {c->st.g, 4 * np},    {c->ph.pos, 16 * ns},    {c->ph.flux, 16 * ns}, {c->ph.dir, 16 * ns}};
+}
+
+size_t state_bytes(fr_ctx* c) {
+  size_t n = sizeof(StateHeader);
+  for (const StatePart& p : state_parts(c)) n += p.bytes;
+  return n;
+}
+}  // namespace
+
+int fr_save_state(fr_ctx* c, void* buf, size_t* size) {
+  if (!c || !size) return fail(FR_ERR_INVALID, "fr_save_state: bad arguments");
+  const size_t need = state_bytes(c);
+  if (!buf) {
+    *size = need;
+    return FR_OK;
+  }
+  if (*size < need) return fail(FR_ERR_INVALID, "fr_save_state: buffer of %zu bytes, %zu needed", *size, need);
+  StateHeader h{};
+  std::memcpy(h.magic, kStateMagic, 8);
+  h.width = c->W;
+  h.height = c->H;
+  h.photons = c->P;
+  h.flags = (int32_t)c->flags;
+  h.alpha = c->alpha;
+  h.initial_radius = c->r0;
+  h.triangles = c->sc.num_tris;
+  h.iterations = c->iterations;
+  h.photons_total = c->photons_total;
+  std::memcpy(buf, &h, sizeof h);
+  char* p = static_cast<char*>(buf) + sizeof h;
+  for (const StatePart& part : state_parts(c)) {
+    FR_CUDA(cudaMemcpyAsync(p, part.dev, part.bytes, cudaMemcpyDeviceToHost, c->stream));
+    p += part.bytes;
+  }
+  *size = need;
+  return fr_synchronize(c);
+}
+
+int fr_load_state(fr_ctx* c, const void* buf, size_t size) {
+  if (!c || !buf) return fail(FR_ERR_INVALID, "fr_load_state: bad arguments");
+  if (size < sizeof(StateHeader)) return fail(FR_ERR_INVALID, "fr_load_state: %zu bytes, no header", size);
+  StateHeader h;
+  std::memcpy(&h, buf, sizeof h);
+  if (std::memcmp(h.magic, kStateMagic, 8) != 0) return fail(FR_ERR_INVALID, "fr_load_state: not a checkpoint");
+  if (h.width != c->W || h.height != c->H || h.photons != c->P || h.flags != (int32_t)c->flags ||
+      h.alpha != c->alpha || h.initial_radius != c->r0 || h.triangles != c->sc.num_tris)
+    return fail(FR_ERR_INVALID, "fr_load_state: checkpoint of another configuration (%dx%d, %d paths)", h.width,
+                h.height, h.photons);
+  if (h.iterations < 0 || h.photons_total < 0) return fail(FR_ERR_INVALID, "fr_load_state: bad counters");
+  if (size != state_bytes(c)) return fail(FR_ERR_INVALID, "fr_load_state: %zu bytes, %zu expected", size, state_bytes(c));
+  FR_CUDA(cudaStreamSynchronize(c->stream));
+  const char* p = static_cast<const char*>(buf) + sizeof h;
+  for (const StatePart& part : state_parts(c)) {
+    FR_CUDA(cudaMemcpyAsync(part.dev, p, part.bytes, cudaMemcpyHostToDevice, c->stream));
+    p += part.bytes;
+  }
+  const uint32_t step = (uint32_t)h.iterations;
+  FR_CUDA(cudaMemcpyAsync(c->step_dev, &step, sizeof step, cudaMemcpyHostToDevice, c->stream));
+  FR_CUDA(cudaStreamSynchronize(c->stream));
+  c->iterations = h.iterations;
+  c->photons_total = h.photons_total;
+  return FR_OK;
 }
 
 }  // extern "C"

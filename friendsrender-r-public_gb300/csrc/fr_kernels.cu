@@ -66,6 +66,10 @@ __device__ __forceinline__ void camera_ray(const CameraGPU& c, float u, float v,
   }
 }
 
+// Advances the device iteration counter: the first kernel of an iteration, so
+// that a captured iteration graph replays unchanged.
+__global__ void k_next_step(uint32_t* step) { *step += 1u; }
+
 // ------------------------------------------------------------------ eye pass
 // createHitpoints + getHitpointInfo (SPPM.cpp:98-353) as a wavefront: k_ew_start
 // makes every camera ray, rounds of k_wave_trace and k_ew_shade advance the
@@ -84,7 +88,7 @@ struct EyeState {
 };
 
 __device__ __forceinline__ uint32_t eye_seed(const IterParams& it, int i) {
-  return (uint32_t)i + (uint32_t)(it.width * it.height) * it.step;  // SPPM.cpp:334
+  return (uint32_t)i + (uint32_t)(it.width * it.height) * *it.step;  // SPPM.cpp:334
 }
 
 __device__ __forceinline__ void load_eye(const PathWave& w, int i, EyeState& s) {
@@ -541,7 +545,7 @@ struct PhotonState {
 };
 
 __device__ __forceinline__ uint32_t photon_seed(const IterParams& it, int i) {
-  return (uint32_t)i + 135u + it.step * (uint32_t)it.photons;  // SPPM.cpp:520
+  return (uint32_t)i + 135u + *it.step * (uint32_t)it.photons;  // SPPM.cpp:520
 }
 
 __device__ __forceinline__ void load_state(const PathWave& w, int i, PhotonState& s) {
@@ -905,6 +909,14 @@ __device__ __forceinline__ void for_each_photon_in_ball(const PhotonGrid& g, con
       }
 }
 
+// tau <- (tau + phi) * a / b (SPPM.cpp:445), tau in FP64.  The ratio a / b is a
+// float-float (within 2^-46 of a / b; an FP64 divide is about ten FP64
+// instructions on GB300), then one FP64 add and multiply.
+__device__ __forceinline__ double tau_update(double tau, float phi, float a, float b) {
+  const xf::ff q = xf::div_f(xf::ff{a, 0.0f}, b);
+  return (tau + (double)phi) * ((double)q.h + (double)q.l);
+}
+
 // applyHitPointInfo (SPPM.cpp:395-451) with one group of G lanes per hitpoint
 // of the hitpoint list (32 / G hitpoints per warp at a time: a hitpoint's
 // work is a chain of dependent loads, so several in flight per warp hide
@@ -1028,11 +1040,7 @@ __global__ void __launch_bounds__(256) k_gather(SceneGPU sc, IterParams it, Hitp
       const float b = (float)(N + M);
       double* tau = st.tau + 3 * (size_t)i + gl;
       const float v = gl == 0 ? vx : (gl == 1 ? vy : vz);
-      // The ratio a / b as a float-float (within 2^-46 of a / b; an FP64
-      // divide is about ten FP64 instructions on GB300), then one FP64 add
-      // and multiply per component.
-      const xf::ff q = xf::div_f(xf::ff{a, 0.0f}, b);
-      *tau = (*tau + (double)v) * ((double)q.h + (double)q.l);
+      *tau = tau_update(*tau, v, a, b);
       if (gl == 0) {
         st.r[i] = R * sqrtf(a / b);
         st.n[i] = (int)((float)N + (float)M * it.alpha);
@@ -1040,6 +1048,26 @@ __global__ void __launch_bounds__(256) k_gather(SceneGPU sc, IterParams it, Hitp
       }
     }
   }
+}
+
+// The N/tau/R update alone (SPPM.cpp:444-449) from given per-pixel photon
+// counts m and flux sums phi; the same arithmetic as the gather's update.
+__global__ void k_update(PixelState st, const int32_t* m, const float4* phi, int pixels, float alpha) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= pixels) return;
+  const int M = m[i];
+  if (M <= 0) return;
+  const int N = st.n[i];
+  const float a = (float)N + alpha * (float)M;
+  const float b = (float)(N + M);
+  const float4 v = phi[i];
+  double* tau = st.tau + 3 * (size_t)i;
+  tau[0] = tau_update(tau[0], v.x, a, b);
+  tau[1] = tau_update(tau[1], v.y, a, b);
+  tau[2] = tau_update(tau[2], v.z, a, b);
+  st.r[i] = st.r[i] * sqrtf(a / b);
+  st.n[i] = (int)((float)N + (float)M * alpha);
+  st.g[i] += 1;
 }
 
 // ---------------------------------------------------------------- resolve
@@ -1110,6 +1138,14 @@ void upload_byte_lut(cudaStream_t s) {
   cudaMemcpyToSymbolAsync(c_byte_to_unit, lut, sizeof(lut), 0, cudaMemcpyHostToDevice, s);
 }
 
+void launch_next_step(uint32_t* step, cudaStream_t s) { k_next_step<<<1, 1, 0, s>>>(step); }
+
+int pw_tail_blocks_per_sm() {
+  int b = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pw_tail, 128, 0);
+  return b;
+}
+
 void launch_ew_start(const CameraGPU& cam, const IterParams& it, PathWave w, cudaStream_t s) {
   k_ew_start<<<blocks_for((size_t)it.width * it.height, 128), 128, 0, s>>>(cam, it, w);
 }
@@ -1147,16 +1183,7 @@ void launch_pw_shade(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, P
 
 void launch_pw_tail(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, PathWave w, uint32_t* counts,
                     int round, int grid, int* err, cudaStream_t s) {
-  static int tail_blocks = -1;  // resident blocks of k_pw_tail on this device
-  if (tail_blocks < 0) {
-    int b = 0, dev = 0, sms = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pw_tail, 128, 0);
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    tail_blocks = std::max(1, b * sms);
-  }
-  (void)grid;
-  k_pw_tail<<<tail_blocks, 128, 0, s>>>(sc, it, ph, w, counts, round, err);
+  k_pw_tail<<<std::max(1, grid), 128, 0, s>>>(sc, it, ph, w, counts, round, err);
 }
 
 int photon_pass_blocks_per_sm() {
@@ -1234,6 +1261,10 @@ int gather_blocks_per_sm() {
   int b = 0;
   cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_gather, 256, 0);
   return b;
+}
+
+void launch_update(PixelState st, const int32_t* m, const float4* phi, int pixels, float alpha, cudaStream_t s) {
+  k_update<<<blocks_for(pixels, 256), 256, 0, s>>>(st, m, phi, pixels, alpha);
 }
 
 void launch_resolve(PixelState st, int pixels, double photons_total, double iterations, float4* out, cudaStream_t s) {

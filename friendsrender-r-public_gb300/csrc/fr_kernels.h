@@ -100,6 +100,8 @@ void upload_byte_lut(cudaStream_t s);
 // Wavefront passes, launched round by round by the host: a start kernel,
 // rounds of trace / sort / shade over the live-path queue, and a tail
 // kernel.  `grid` is the block count of the persistent-style round kernels.
+void launch_next_step(uint32_t* step, cudaStream_t s);
+int pw_tail_blocks_per_sm();
 void launch_ew_start(const CameraGPU& cam, const IterParams& it, PathWave w, cudaStream_t s);
 // coherent: the queue holds rays in an order that neighbouring lanes should
 // keep (camera rays in pixel order); otherwise lanes fetch rays dynamically.
@@ -132,6 +134,8 @@ uint32_t scan_temp_words(uint32_t n, ScanTemp& t);
 void launch_gather_update(const SceneGPU& sc, const IterParams& it, HitpointBuf hp, PhotonGrid g, const GridInfo* gi,
                           PixelState st, int32_t* dbg_m, float4* dbg_phi, int resident_blocks, cudaStream_t s);
 int gather_blocks_per_sm();
+// The N/tau/R update from given per-pixel photon counts and flux sums.
+void launch_update(PixelState st, const int32_t* m, const float4* phi, int pixels, float alpha, cudaStream_t s);
 void launch_resolve(PixelState st, int pixels, double photons_total, double iterations, float4* out, cudaStream_t s);
 
 // Parity entry points.

@@ -132,7 +132,7 @@ struct SceneGPU {
 
 // Per-iteration parameters read by the kernels.
 struct IterParams {
-  uint32_t step;              // reference iteration number (starts at 1)
+  const uint32_t* step;       // device word: reference iteration number (starts at 1)
   int32_t photons;            // photon paths this iteration
   int32_t width, height;
   float alpha;                // ppm_Alpha (SPPM.cpp:20)

@@ -58,7 +58,7 @@ EXPORTS = ['fr_last_error', 'fr_create', 'fr_iterate', 'fr_synchronize', 'fr_res
            'fr_get_stats', 'fr_stream', 'fr_destroy', 'fr_trace_closest', 'fr_trace_any', 'fr_radius_query',
            'fr_read_hitpoints', 'fr_read_photon_slots', 'fr_read_gather', 'fr_read_state', 'fr_profile_enable',
            'fr_profile_read', 'fr_radius_count_noalloc', 'fr_check_exact_math',
-           'fr_read_wave_counts']
+           'fr_read_wave_counts', 'fr_save_state', 'fr_load_state', 'fr_update']
 
 STAGES = ('eye', 'photon', 'grid', 'gather', 'eye_trace', 'photon_trace')
 
@@ -98,6 +98,9 @@ def load(path=None):
     lib.fr_radius_count_noalloc.argtypes = [vp, i32, vp, i32, f32, vp, vp]
     lib.fr_check_exact_math.argtypes = [C.c_uint64, C.c_uint32, vp, vp]
     lib.fr_read_wave_counts.argtypes = [vp, vp, vp, vp, vp]
+    lib.fr_save_state.argtypes = [vp, vp, C.POINTER(C.c_size_t)]
+    lib.fr_load_state.argtypes = [vp, vp, C.c_size_t]
+    lib.fr_update.argtypes = [vp, vp, vp]
     _lib = lib
     return lib
 
@@ -268,6 +271,24 @@ class Renderer:
         pr = np.zeros(1, np.int32)
         _check(_lib.fr_read_wave_counts(self.h, _ptr(e), _ptr(p), _ptr(er), _ptr(pr)), 'fr_read_wave_counts')
         return e[:er[0] + 1].copy(), p[:pr[0] + 1].copy()
+
+    def save_state(self):
+        """Checkpoint of the iteration state (bytes)."""
+        n = C.c_size_t(0)
+        _check(_lib.fr_save_state(self.h, None, C.byref(n)), 'fr_save_state')
+        buf = np.empty(n.value, np.uint8)
+        _check(_lib.fr_save_state(self.h, _ptr(buf), C.byref(n)), 'fr_save_state')
+        return buf[:n.value].tobytes()
+
+    def load_state(self, data):
+        buf = np.frombuffer(data, np.uint8)
+        _check(_lib.fr_load_state(self.h, _ptr(buf), len(buf)), 'fr_load_state')
+
+    def update(self, m, phi):
+        """fr_update: apply per-pixel photon counts and flux sums to the state."""
+        m = np.ascontiguousarray(m, np.int32)
+        phi = np.ascontiguousarray(phi, np.float32)
+        _check(_lib.fr_update(self.h, _ptr(m), _ptr(phi)), 'fr_update')
 
     def read_gather(self):
         n = self.width * self.height

@@ -253,6 +253,23 @@ int fr_read_gather(fr_ctx* ctx, int32_t* m, float* phi4);
 /* Per-pixel progressive state: tau (3 doubles), N, R, NumGather. */
 int fr_read_state(fr_ctx* ctx, double* tau, int32_t* n, float* r, int32_t* g);
 
+/* The N/tau/R update of applyHitPointInfo (SPPM.cpp:444-449) alone: applies
+ * per-pixel photon counts m (width*height) and flux sums phi (width*height*3)
+ * to the context's state, with the arithmetic an iteration uses.  For
+ * checking the update against the reference's own M and flux sums. */
+int fr_update(fr_ctx* ctx, const int32_t* m, const float* phi);
+
+/* Checkpoint and resume between iterations (no counterpart in the reference,
+ * which renders in one call).  fr_save_state with buf == NULL stores the
+ * checkpoint size in *size; otherwise *size is buf's capacity on entry and
+ * the bytes written on return.  The checkpoint holds the iteration count, the
+ * per-pixel state and the photon slots; fr_load_state restores it into a
+ * context created with the same scene, camera and parameters (checked:
+ * resolution, photon paths, flags, alpha, initial radius, triangle count), after
+ * which iterations continue exactly as they would have in the saved context. */
+int fr_save_state(fr_ctx* ctx, void* buf, size_t* size);
+int fr_load_state(fr_ctx* ctx, const void* buf, size_t size);
+
 #ifdef __cplusplus
 }
 #endif
