@@ -236,6 +236,7 @@ struct fr_ctx {
   int32_t* dbg_m = nullptr;
   float4* dbg_phi = nullptr;
   float4* image = nullptr;
+  uint32_t* image8 = nullptr;    // exported RGBA8
   int64_t iterations = 0, photons_total = 0;
   int64_t launches = 0;  // kernels launched by fr_iterate so far
   // Stage profiler: events recorded on the stream around each stage.
@@ -712,7 +713,8 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
       (rc = c->alloc(&c->eye_wave.mq, (size_t)kShadeQueues * npix)) ||
       (rc = c->alloc(&c->gi, 1)) || (rc = c->alloc(&c->step_dev, 1)) ||
       (rc = c->alloc(&c->err, 1)) ||
-      (rc = c->alloc(&c->dbg_m, npix)) || (rc = c->alloc(&c->dbg_phi, npix)) || (rc = c->alloc(&c->image, npix)))
+      (rc = c->alloc(&c->dbg_m, npix)) || (rc = c->alloc(&c->dbg_phi, npix)) || (rc = c->alloc(&c->image, npix)) ||
+      (rc = c->alloc(&c->image8, npix)))
     return bail(rc);
   // Counters (one memset per iteration): eye rounds, photon rounds, the
   // hitpoint list, eye and photon shade queues, eye and photon trace fetches.
@@ -790,6 +792,24 @@ int fr_resolve(fr_ctx* c, float* rgba) {
   if (rc) return rc;
   FR_CUDA(cudaMemcpyAsync(rgba, c->image, sizeof(float4) * (size_t)c->W * c->H, cudaMemcpyDeviceToHost, c->stream));
   return fr_synchronize(c);
+}
+
+int fr_resolve_rgba8(fr_ctx* c, uint8_t* rgba) {
+  if (!c || !rgba) return fail(FR_ERR_INVALID, "fr_resolve_rgba8: bad arguments");
+  int rc = fr_resolve_dev(c, reinterpret_cast<float*>(c->image));
+  if (rc) return rc;
+  launch_export_rgba8(c->image, c->W, c->H, c->image8, c->stream);
+  FR_CUDA(cudaMemcpyAsync(rgba, c->image8, 4 * (size_t)c->W * c->H, cudaMemcpyDeviceToHost, c->stream));
+  return fr_synchronize(c);
+}
+
+int fr_export_png(fr_ctx* c, const char* path) {
+  if (!c || !path) return fail(FR_ERR_INVALID, "fr_export_png: bad arguments");
+  std::vector<uint8_t> px(4 * (size_t)c->W * c->H);
+  int rc = fr_resolve_rgba8(c, px.data());
+  if (rc) return rc;
+  if (fr_write_png(path, c->W, c->H, px.data()) != FR_OK) return fail(FR_ERR_INVALID, "fr_export_png: cannot write %s", path);
+  return FR_OK;
 }
 
 int fr_get_stats(fr_ctx* c, fr_stats* o) {

@@ -19,6 +19,7 @@
 #include <cuda_runtime.h>
 #include <algorithm>
 #include <cfloat>
+#include <climits>
 #include <cstdint>
 #include "fr_bsdf.cuh"
 #include "fr_grid.cuh"
@@ -1070,6 +1071,40 @@ __global__ void k_update(PixelState st, const int32_t* m, const float4* phi, int
   st.g[i] += 1;
 }
 
+// ExportPNG (TextureUtility.cpp:52-65): pixel (i, j) of the exported image is
+// the render target sampled by LinearSampler::Sample (TextureSampler.h:61-79)
+// at u = i / W, v = j / H, each channel stored as max(0, min(255,
+// int(c * 255))).  A float outside int's range converts as on the reference's
+// x86 build (to INT_MIN, so 0 after the clamp); so does NaN.
+__device__ __forceinline__ F4 image_texel(const float4* img, int idx) {
+  const float4 v = img[idx];
+  return F4{v.x, v.y, v.z, v.w};
+}
+
+__device__ __forceinline__ uint32_t quantize_255(float c) {
+  const float s = c * 255.0f;
+  const int q = (!(s == s) || fabsf(s) >= 2147483648.0f) ? INT_MIN : (int)s;
+  return (uint32_t)max(0, min(255, q));
+}
+
+__global__ void k_export_rgba8(const float4* img, int W, int H, uint32_t* out) {
+  const int idx = blockIdx.x * blockDim.x + threadIdx.x;
+  if (idx >= W * H) return;
+  const int i = idx % W, j = idx / W;
+  const float u = (float)i / (float)W, v = (float)j / (float)H;
+  const int iu = (int)((float)W * u), iv = (int)((float)H * v);
+  const int x1 = abs(iu) % W, y1 = abs(iv) % H;
+  const int x2 = min(W - 1, x1 + 1), y2 = min(H - 1, y1 + 1);
+  const F4 t00 = image_texel(img, x1 + y1 * W), t10 = image_texel(img, x2 + y1 * W);
+  const F4 t01 = image_texel(img, x1 + y2 * W), t11 = image_texel(img, x2 + y2 * W);
+  const float w = fabsf(u * (float)W) - (float)abs(iu);
+  const float h = fabsf(v * (float)H) - (float)abs(iv);
+  const F4 up = lerp4(t00, 1.0f - w, t10, w);
+  const F4 down = lerp4(t01, 1.0f - w, t11, w);
+  const F4 c = lerp4(up, 1.0f - h, down, h);
+  out[idx] = quantize_255(c.x) | quantize_255(c.y) << 8 | quantize_255(c.z) << 16 | quantize_255(c.w) << 24;
+}
+
 // ---------------------------------------------------------------- resolve
 // reconstructImageFromSharedPoints (SPPM.cpp:473-493): normalisation in FP64,
 // gamma 1/1.2 in FP32 as the reference applies it.
@@ -1265,6 +1300,10 @@ int gather_blocks_per_sm() {
 
 void launch_update(PixelState st, const int32_t* m, const float4* phi, int pixels, float alpha, cudaStream_t s) {
   k_update<<<blocks_for(pixels, 256), 256, 0, s>>>(st, m, phi, pixels, alpha);
+}
+
+void launch_export_rgba8(const float4* img, int width, int height, uint32_t* out, cudaStream_t s) {
+  k_export_rgba8<<<blocks_for((size_t)width * height, 256), 256, 0, s>>>(img, width, height, out);
 }
 
 void launch_resolve(PixelState st, int pixels, double photons_total, double iterations, float4* out, cudaStream_t s) {

@@ -134,6 +134,8 @@ uint32_t scan_temp_words(uint32_t n, ScanTemp& t);
 void launch_gather_update(const SceneGPU& sc, const IterParams& it, HitpointBuf hp, PhotonGrid g, const GridInfo* gi,
                           PixelState st, int32_t* dbg_m, float4* dbg_phi, int resident_blocks, cudaStream_t s);
 int gather_blocks_per_sm();
+// ExportPNG's resample and 8-bit quantization of a resolved image.
+void launch_export_rgba8(const float4* img, int width, int height, uint32_t* out, cudaStream_t s);
 // The N/tau/R update from given per-pixel photon counts and flux sums.
 void launch_update(PixelState st, const int32_t* m, const float4* phi, int pixels, float alpha, cudaStream_t s);
 void launch_resolve(PixelState st, int pixels, double photons_total, double iterations, float4* out, cudaStream_t s);

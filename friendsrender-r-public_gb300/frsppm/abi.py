@@ -58,7 +58,8 @@ EXPORTS = ['fr_last_error', 'fr_create', 'fr_iterate', 'fr_synchronize', 'fr_res
            'fr_get_stats', 'fr_stream', 'fr_destroy', 'fr_trace_closest', 'fr_trace_any', 'fr_radius_query',
            'fr_read_hitpoints', 'fr_read_photon_slots', 'fr_read_gather', 'fr_read_state', 'fr_profile_enable',
            'fr_profile_read', 'fr_radius_count_noalloc', 'fr_check_exact_math',
-           'fr_read_wave_counts', 'fr_save_state', 'fr_load_state', 'fr_update']
+           'fr_read_wave_counts', 'fr_save_state', 'fr_load_state', 'fr_update',
+           'fr_resolve_rgba8', 'fr_export_png', 'fr_write_png']
 
 STAGES = ('eye', 'photon', 'grid', 'gather', 'eye_trace', 'photon_trace')
 
@@ -101,6 +102,9 @@ def load(path=None):
     lib.fr_save_state.argtypes = [vp, vp, C.POINTER(C.c_size_t)]
     lib.fr_load_state.argtypes = [vp, vp, C.c_size_t]
     lib.fr_update.argtypes = [vp, vp, vp]
+    lib.fr_resolve_rgba8.argtypes = [vp, vp]
+    lib.fr_export_png.argtypes = [vp, C.c_char_p]
+    lib.fr_write_png.argtypes = [C.c_char_p, i32, i32, vp]
     _lib = lib
     return lib
 
@@ -290,6 +294,15 @@ class Renderer:
         phi = np.ascontiguousarray(phi, np.float32)
         _check(_lib.fr_update(self.h, _ptr(m), _ptr(phi)), 'fr_update')
 
+    def resolve_rgba8(self):
+        """ExportPNG's pixels: (height, width, 4) uint8."""
+        out = np.empty((self.height, self.width, 4), np.uint8)
+        _check(_lib.fr_resolve_rgba8(self.h, _ptr(out)), 'fr_resolve_rgba8')
+        return out
+
+    def export_png(self, path):
+        _check(_lib.fr_export_png(self.h, os.fsencode(path)), 'fr_export_png')
+
     def read_gather(self):
         n = self.width * self.height
         m = np.empty(n, np.int32)
@@ -318,3 +331,13 @@ def check_exact_math(samples, seed=1):
     fp = np.zeros(len(EXACT_FUNCTIONS), np.uint64)
     _check(lib.fr_check_exact_math(int(samples), int(seed), _ptr(mm), _ptr(fp)), 'fr_check_exact_math')
     return {n: (int(fp[k]), int(mm[k])) for k, n in enumerate(EXACT_FUNCTIONS)}
+
+
+def write_png(path, rgba):
+    """fr_write_png: (height, width, 4) uint8 to a PNG file (no GPU needed)."""
+    lib = load()
+    rgba = np.ascontiguousarray(rgba, np.uint8)
+    h, w = rgba.shape[:2]
+    rc = lib.fr_write_png(os.fsencode(path), w, h, _ptr(rgba))
+    if rc != FR_OK:
+        raise RuntimeError('fr_write_png failed (%d)' % rc)

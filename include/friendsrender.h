@@ -148,6 +148,20 @@ int fr_synchronize(fr_ctx* ctx);
 int fr_resolve(fr_ctx* ctx, float* rgba);
 int fr_resolve_dev(fr_ctx* ctx, float* rgba_dev);
 
+/* ExportPNG (TextureUtility.cpp:52-65): the current image resampled by the
+ * reference's bilinear sampler at u = i / W, v = j / H and quantized to
+ * max(0, min(255, int(c * 255))) per channel; width*height*4 bytes, row-major
+ * RGBA into a caller-owned host buffer. */
+int fr_resolve_rgba8(fr_ctx* ctx, uint8_t* rgba);
+
+/* fr_resolve_rgba8 written as a PNG file (8-bit RGBA; the zlib stream holds
+ * stored blocks, so the file differs from stb's but decodes to the same
+ * pixels). */
+int fr_export_png(fr_ctx* ctx, const char* path);
+
+/* Writes width*height RGBA8 pixels as a PNG file; needs no GPU. */
+int fr_write_png(const char* path, int32_t width, int32_t height, const uint8_t* rgba);
+
 int fr_get_stats(fr_ctx* ctx, fr_stats* out);
 
 /* The context's cudaStream_t (as void*), for callers that record events on it. */

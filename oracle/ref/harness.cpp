@@ -433,6 +433,8 @@ int main(int argc, char** argv) {
   std::vector<float> img;
   for (int i = 0; i < W * H; ++i) { const TColor c = rt.GetRawData()[i]; img.push_back(c[0]); img.push_back(c[1]); img.push_back(c[2]); img.push_back(c[3]); }
   npy_f32(out_dir + "/image.npy", img, {(size_t)W * H, 4});
+  // The reference's own image output (main.cpp:161).
+  TextureUtility::ExportPNG(rt, out_dir + "/image.png");
   std::vector<float> times;
   for (int s = 0; s < iters; ++s) { times.push_back(t_photon[s]); times.push_back(t_tree[s]); times.push_back(t_eye[s]); times.push_back(t_gather[s]); }
   npy_f32(out_dir + "/phase_seconds.npy", times, {(size_t)iters, 4});

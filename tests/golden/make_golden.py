@@ -13,6 +13,8 @@ Each fixture <name>.npz holds, for a scene from frsppm.scenes:
                             per-pixel state after the update
   image, meta               reconstructImageFromSharedPoints output and
                             [total photons, iterations, threads]
+  image_png                 the reference's ExportPNG of that image, decoded
+                            (height x width x RGBA8)
 with the reference's ppm_Alpha = 0.9 and FirstRadius = 0.015 (SPPM.cpp:20-21).
 """
 from __future__ import annotations
@@ -29,6 +31,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.dirname(os.path.dirname(HERE))
 sys.path.insert(0, os.path.join(REPO, 'friendsrender-r-public_gb300'))
 from frsppm import objio, scenes  # noqa: E402
+
+sys.path.insert(0, os.path.join(REPO, 'tests'))
+from pngread import decode_png  # noqa: E402
 
 FRREF = os.path.join(REPO, 'oracle', '_ref', 'frref')
 
@@ -106,7 +111,8 @@ def make(name, factory, photons, iters, out_dir=HERE):
                     rays=rays, hit_facet=np.load(os.path.join(od, 'hit_facet.npy')),
                     hit_tuv=np.load(os.path.join(od, 'hit_tuv.npy')), any_rays=arays,
                     any_hit=np.load(os.path.join(od, 'any_hit.npy')),
-                    image=np.load(os.path.join(od, 'image.npy')), meta=np.load(os.path.join(od, 'meta.npy')))
+                    image=np.load(os.path.join(od, 'image.npy')), meta=np.load(os.path.join(od, 'meta.npy')),
+                    image_png=decode_png(os.path.join(od, 'image.png')))
         for s in range(1, iters + 1):
             for k in ('hp_type', 'hp_facet', 'hp_pos', 'hp_nrm', 'hp_out', 'hp_w', 'hp_rough', 'ph', 'ph_path',
                       'ph_slot', 'gather_m', 'gather_phi', 'sp_rad', 'sp_r', 'sp_n', 'sp_g'):
