@@ -31,6 +31,7 @@ class StochasticProgressivePhotonMapping {
   // empty photon buffer; this is the fixed-iteration render it describes.)
   void RenderImage_FixStep(RenderTarget& target, const fr_scene_desc& scene, const fr_camera_desc& camera,
                            int NumPhotons, int Step) {
+    if (Step <= 0) throw std::invalid_argument("RenderImage_FixStep: Step must be positive");
     fr_ctx* ctx = create(scene, camera, NumPhotons / Step);
     check(fr_iterate(ctx, Step), ctx);
     finish(target, camera, ctx);

@@ -13,7 +13,7 @@ from conftest import GOLDEN_SCENES, REPO, load_golden
 def test_header_and_binding_agree():
     from frsppm import abi
     hdr = open(os.path.join(REPO, 'include', 'friendsrender.h')).read()
-    declared = set(re.findall(r'\b(fr_[a-z_]+)\s*\(', hdr))
+    declared = set(re.findall(r'\b(fr_[a-z0-9_]+)\s*\(', hdr))
     assert declared == set(abi.EXPORTS)
 
 
