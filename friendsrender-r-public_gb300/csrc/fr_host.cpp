@@ -993,6 +993,13 @@ int fr_radius_count_noalloc(const float* hp_dev, int32_t num_hitpoints, const fl
   return FR_OK;
 }
 
+int fr_check_tc_gemm(uint32_t seed, double* max_abs_err) {
+  if (!max_abs_err) return fail(FR_ERR_INVALID, "fr_check_tc_gemm: NULL output");
+  const char* msg = "";
+  if (check_tc_gemm(seed, max_abs_err, &msg)) return fail(FR_ERR_CUDA, "fr_check_tc_gemm: %s", msg);
+  return FR_OK;
+}
+
 int fr_check_exact_math(uint64_t samples, uint32_t seed, uint64_t* mismatches, uint64_t* fast_paths) {
   if (!mismatches || !fast_paths) return fail(FR_ERR_INVALID, "fr_check_exact_math: NULL output");
   const char* msg = "";

@@ -151,6 +151,10 @@ void launch_radius_count(const float4* hp_pos_r, int nh, PhotonGrid g, const Gri
 int radius_count_noalloc(const float* hp_dev, int32_t nh, const float* photons_dev, int32_t np, float cell,
                          int32_t* counts_dev, cudaStream_t stream, const char** msg);
 
+// Device check of the tcgen05 GEMM block (fr_tc_check.cu): max |error| of
+// three products against a host GEMM.
+int check_tc_gemm(uint32_t seed, double* max_err, const char** msg);
+
 // Device check of the float paths of fr_exact.cuh (fr_exact_check.cu).
 int check_exact_math(uint64_t samples, uint32_t seed, uint64_t* mismatches, uint64_t* fast_paths, const char** msg);
 

@@ -59,7 +59,7 @@ EXPORTS = ['fr_last_error', 'fr_create', 'fr_iterate', 'fr_synchronize', 'fr_res
            'fr_read_hitpoints', 'fr_read_photon_slots', 'fr_read_gather', 'fr_read_state', 'fr_profile_enable',
            'fr_profile_read', 'fr_radius_count_noalloc', 'fr_check_exact_math',
            'fr_read_wave_counts', 'fr_save_state', 'fr_load_state', 'fr_update',
-           'fr_resolve_rgba8', 'fr_export_png', 'fr_write_png']
+           'fr_resolve_rgba8', 'fr_export_png', 'fr_write_png', 'fr_check_tc_gemm']
 
 STAGES = ('eye', 'photon', 'grid', 'gather', 'eye_trace', 'photon_trace')
 
@@ -105,6 +105,7 @@ def load(path=None):
     lib.fr_resolve_rgba8.argtypes = [vp, vp]
     lib.fr_export_png.argtypes = [vp, C.c_char_p]
     lib.fr_write_png.argtypes = [C.c_char_p, i32, i32, vp]
+    lib.fr_check_tc_gemm.argtypes = [C.c_uint32, vp]
     _lib = lib
     return lib
 
@@ -341,3 +342,11 @@ def write_png(path, rgba):
     rc = lib.fr_write_png(os.fsencode(path), w, h, _ptr(rgba))
     if rc != FR_OK:
         raise RuntimeError('fr_write_png failed (%d)' % rc)
+
+
+def check_tc_gemm(seed=1):
+    """fr_check_tc_gemm: max |error| of the three tcgen05 products."""
+    lib = load()
+    err = np.zeros(3, np.float64)
+    _check(lib.fr_check_tc_gemm(int(seed), _ptr(err)), 'fr_check_tc_gemm')
+    return err

@@ -242,6 +242,13 @@ int fr_radius_count_noalloc(const float* hp_dev, int32_t num_hitpoints, const fl
  * refraction pdf, metal BRDF, conductor masking term, conductor tm3, conductor
  * square root. */
 #define FR_EXACT_FUNCTIONS 9
+
+/* No reference counterpart: a device self-check of the tensor-core (tcgen05)
+ * GEMM the photon guide's network uses.  Multiplies seeded random BF16
+ * matrices three ways (128x64x64, the same accumulated twice, and N = 48) and
+ * returns the largest absolute error of each against a host GEMM on the same
+ * inputs in max_abs_err[0..2]. */
+int fr_check_tc_gemm(uint32_t seed, double* max_abs_err);
 int fr_check_exact_math(uint64_t samples, uint32_t seed, uint64_t* mismatches, uint64_t* fast_paths);
 
 /* No reference counterpart: the wavefront queue lengths of the last
