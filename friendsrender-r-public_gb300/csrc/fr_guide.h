@@ -1,0 +1,63 @@
+// Photon-emission guide: network dimensions, parameter and weight-tile
+// layouts, and the device state shared by the host library and the kernels
+// (the kernels and the method are described in fr_guide.cuh).
+#pragma once
+#include <cuda_runtime.h>
+#include <cstdint>
+
+namespace fr {
+
+constexpr int kGuideIn = 5;
+constexpr int kGuideHidden = 64;
+constexpr int kGuideLobes = 8;
+constexpr int kGuideOut = 5 * kGuideLobes;  // 40
+constexpr int kGuideOutPad = 48;            // tensor-core N for the output layer
+
+// Flat FP32 parameter array; weights row-major [out][in].
+constexpr int kOffW1 = 0;                                // [64][5]
+constexpr int kOffB1 = kOffW1 + kGuideHidden * kGuideIn; // [64]
+constexpr int kOffW2 = kOffB1 + kGuideHidden;            // [64][64]
+constexpr int kOffB2 = kOffW2 + kGuideHidden * kGuideHidden;
+constexpr int kOffW3 = kOffB2 + kGuideHidden;            // [64][64]
+constexpr int kOffB3 = kOffW3 + kGuideHidden * kGuideHidden;
+constexpr int kOffW4 = kOffB3 + kGuideHidden;            // [48][64], rows 40-47 zero
+constexpr int kOffB4 = kOffW4 + kGuideOutPad * kGuideHidden;
+constexpr int kGuideParams = kOffB4 + kGuideOutPad;      // 11824
+
+// BF16 weight tiles in the tensor cores' K-major core-matrix layout
+// (fr_tc.cuh): W2, W3 (64 x 64), W4 (48 x 64) for the forward pass and their
+// transposes W2^T, W3^T (64 x 64), W4^T (64 x 48) for the backward pass.
+constexpr int kTileW2 = 0;
+constexpr int kTileW3 = kTileW2 + 64 * 64 * 2;
+constexpr int kTileW4 = kTileW3 + 64 * 64 * 2;
+constexpr int kTileW2T = kTileW4 + 48 * 64 * 2;
+constexpr int kTileW3T = kTileW2T + 64 * 64 * 2;
+constexpr int kTileW4T = kTileW3T + 64 * 64 * 2;
+constexpr int kTileBytes = kTileW4T + 64 * 48 * 2;      // 45056
+
+constexpr float kGuideKappaMin = 0.5f;
+constexpr float kGuideKappaMax = 2000.0f;
+constexpr float kGuideInvTwoPi = 0.15915494309189535f;
+
+constexpr int kErrGuide = 2;  // a tensor-core wait of the guide gave up
+
+struct GuideGPU {
+  float* params;        // kGuideParams FP32 master weights
+  float* grad;          // kGuideParams gradient sums of the current step
+  float* adam_m;        // Adam moments
+  float* adam_v;
+  uint8_t* tiles;       // kTileBytes BF16 weight tiles
+  float4* feat;         // per path: inputs x0..x3
+  float4* dir;          // per path: input x4, emission direction
+  float* importance;    // per path: flux deposited at hitpoints this iteration
+  uint32_t* batch;      // training samples (path indices)
+  uint32_t* batch_count;
+  float* weight_sum;    // sum of the batch's importance
+  uint32_t* adam_step;
+  int* err;             // device error word
+  float plain_fraction; // share of plain cosine sampling in the emission mixture
+  int batch_cap;
+  float lr;
+};
+
+}  // namespace fr

@@ -18,6 +18,7 @@
 
 #include "../../include/friendsrender.h"
 #include "fr_bvh.h"
+#include "fr_guide.h"
 #include "fr_kernels.h"
 #include "fr_layout.h"
 
@@ -229,6 +230,9 @@ struct fr_ctx {
   cudaGraphExec_t graph_exec = nullptr;
   int64_t graph_launches = 0;    // kernels per replay of the graph
   int gather_blocks = 0;         // grid of the gather (one warp per hitpoint)
+  int sms = 0;                   // streaming multiprocessors of the device
+  bool guided = false;           // learned photon-emission guide on
+  GuideGPU guide{};
   PhotonGrid grid{};
   GridInfo* gi = nullptr;
   ScanTemp scan{};
@@ -478,7 +482,10 @@ int enqueue_iteration(fr_ctx* c) {
   {
     StageMark m(c, FR_STAGE_PHOTON, s);
     const int sort_grid = (int)std::min<size_t>(((size_t)c->P + 255) / 256, 4 * (size_t)grid);
-    launch_pw_emit(c->sc, it, c->ph, c->wave, c->counts, s);
+    if (c->guided)
+      launch_pw_emit_guided(c->sc, it, c->ph, c->wave, c->counts, c->guide, s);
+    else
+      launch_pw_emit(c->sc, it, c->ph, c->wave, c->counts, s);
     for (int r = 0; r < kPhotonRounds; ++r) {
       {
         StageMark t(c, FR_STAGE_PHOTON_TRACE, s);
@@ -502,7 +509,13 @@ int enqueue_iteration(fr_ctx* c) {
     StageMark m(c, FR_STAGE_GATHER, s);
     FR_CUDA(cudaMemsetAsync(c->dbg_m, 0, sizeof(int32_t) * (size_t)c->W * c->H, s));
     FR_CUDA(cudaMemsetAsync(c->dbg_phi, 0, sizeof(float4) * (size_t)c->W * c->H, s));
-    launch_gather_update(c->sc, it, c->hp, c->grid, c->gi, c->st, c->dbg_m, c->dbg_phi, c->gather_blocks, s);
+    launch_gather_update(c->sc, it, c->hp, c->grid, c->gi, c->st, c->dbg_m, c->dbg_phi,
+                         c->guided ? c->guide.importance : nullptr, c->gather_blocks, s);
+  }
+  if (c->guided) {
+    // select, train, Adam, weight tiles, step bookkeeping
+    launch_guide_train(c->guide, c->P, c->sms, s);
+    c->launches += 5;
   }
   // iteration counter, eye and photon passes (start, rounds of
   // trace/sort/shade, tail), grid setup, count, scatter, gather
@@ -547,6 +560,7 @@ int check_device_error(fr_ctx* c) {
   FR_CUDA(cudaMemcpyAsync(&e, c->err, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
   FR_CUDA(cudaStreamSynchronize(c->stream));
   if (e & kErrStack) return fail(FR_ERR_DEVICE, "BVH traversal stack overflow (depth %d)", c->bvh_depth);
+  if (e & kErrGuide) return fail(FR_ERR_DEVICE, "photon guide: a tensor-core wait gave up");
   if (e) return fail(FR_ERR_DEVICE, "device error word %d", e);
   return FR_OK;
 }
@@ -606,6 +620,7 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
   c->photon_blocks = std::max(1, photon_pass_blocks_per_sm()) * sms;
   c->tail_blocks = std::max(1, pw_tail_blocks_per_sm()) * sms;
   c->gather_blocks = std::max(1, gather_blocks_per_sm()) * sms;
+  c->sms = sms;
 
   // ---- geometry
   const int T = scene->num_facets;
@@ -742,6 +757,33 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
     c->scan.level[l] = sw;
     sw += c->scan.level_n[l] + 1;
   }
+  // ---- photon-emission guide
+  if (params->guide) {
+    GuideGPU& g = c->guide;
+    g.plain_fraction = params->guide_plain_fraction > 0.0f ? std::min(1.0f, params->guide_plain_fraction) : 0.2f;
+    g.batch_cap = std::min(c->P, params->guide_batch > 0 ? params->guide_batch : 65536);
+    g.lr = params->guide_learning_rate > 0.0f ? params->guide_learning_rate : 0.002f;
+    if ((rc = c->alloc(&g.params, kGuideParams)) || (rc = c->alloc(&g.grad, kGuideParams)) ||
+        (rc = c->alloc(&g.adam_m, kGuideParams)) || (rc = c->alloc(&g.adam_v, kGuideParams)) ||
+        (rc = c->alloc(&g.tiles, kTileBytes)) || (rc = c->alloc(&g.feat, (size_t)c->P)) ||
+        (rc = c->alloc(&g.dir, (size_t)c->P)) || (rc = c->alloc(&g.importance, (size_t)c->P)) ||
+        (rc = c->alloc(&g.batch, (size_t)g.batch_cap)) || (rc = c->alloc(&g.batch_count, 1)) ||
+        (rc = c->alloc(&g.weight_sum, 1)) || (rc = c->alloc(&g.adam_step, 1)))
+      return bail(rc);
+    g.err = c->err;
+    if (guide_configure()) return bail(fail(FR_ERR_CUDA, "guide: shared-memory opt-in failed"));
+    const std::vector<float> p0 = guide_initial_params(params->guide_seed);
+    FR_CUDA(cudaMemcpyAsync(g.params, p0.data(), sizeof(float) * kGuideParams, cudaMemcpyHostToDevice, c->stream));
+    for (float* z : {g.grad, g.adam_m, g.adam_v})
+      FR_CUDA(cudaMemsetAsync(z, 0, sizeof(float) * kGuideParams, c->stream));
+    FR_CUDA(cudaMemsetAsync(g.batch_count, 0, 4, c->stream));
+    FR_CUDA(cudaMemsetAsync(g.weight_sum, 0, 4, c->stream));
+    FR_CUDA(cudaMemsetAsync(g.adam_step, 0, 4, c->stream));
+    FR_CUDA(cudaMemsetAsync(g.importance, 0, sizeof(float) * (size_t)c->P, c->stream));
+    launch_guide_prepare(g, c->stream);
+    c->guided = true;
+  }
+
   // Initial state: initializeSharedPoints (SPPM.cpp:356-373) and empty photon slots.
   std::vector<float> r(npix, c->r0);
   if (cudaMemcpyAsync(c->st.r, r.data(), npix * 4, cudaMemcpyHostToDevice, c->stream) != cudaSuccess)
@@ -1070,6 +1112,60 @@ int fr_update(fr_ctx* c, const int32_t* m, const float* phi) {
   return fr_synchronize(c);
 }
 
+// ------------------------------------------------------------ guide
+int fr_guide_params(fr_ctx* c, float* params) {
+  if (!c || !params || !c->guided) return fail(FR_ERR_INVALID, "fr_guide_params: no guide");
+  FR_CUDA(cudaMemcpyAsync(params, c->guide.params, sizeof(float) * kGuideParams, cudaMemcpyDeviceToHost, c->stream));
+  return fr_synchronize(c);
+}
+
+int fr_guide_set_params(fr_ctx* c, const float* params) {
+  if (!c || !params || !c->guided) return fail(FR_ERR_INVALID, "fr_guide_set_params: no guide");
+  FR_CUDA(cudaMemcpyAsync(c->guide.params, params, sizeof(float) * kGuideParams, cudaMemcpyHostToDevice, c->stream));
+  launch_guide_prepare(c->guide, c->stream);
+  return fr_synchronize(c);
+}
+
+int fr_read_guide_importance(fr_ctx* c, float* importance) {
+  if (!c || !importance || !c->guided) return fail(FR_ERR_INVALID, "fr_read_guide_importance: no guide");
+  FR_CUDA(cudaMemcpyAsync(importance, c->guide.importance, sizeof(float) * (size_t)c->P, cudaMemcpyDeviceToHost,
+                          c->stream));
+  return fr_synchronize(c);
+}
+
+int fr_guide_gradient(fr_ctx* c, int32_t n, const float* samples, float* grad, float* weight_sum) {
+  if (!c || !c->guided || n < 0 || n > c->P || n > c->guide.batch_cap || (n && !samples) || !grad || !weight_sum)
+    return fail(FR_ERR_INVALID, "fr_guide_gradient: bad arguments");
+  const GuideGPU& g = c->guide;
+  std::vector<float4> f(n), d(n);
+  std::vector<float> imp(c->P, 0.0f);
+  for (int j = 0; j < n; ++j) {
+    const float* x = samples + 9 * (size_t)j;
+    f[j] = make_float4(x[0], x[1], x[2], x[3]);
+    d[j] = make_float4(x[4], x[5], x[6], x[7]);
+    imp[j] = x[8];
+  }
+  FR_CUDA(cudaStreamSynchronize(c->stream));
+  if (n) {
+    FR_CUDA(cudaMemcpyAsync(g.feat, f.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, c->stream));
+    FR_CUDA(cudaMemcpyAsync(g.dir, d.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, c->stream));
+  }
+  FR_CUDA(cudaMemcpyAsync(g.importance, imp.data(), sizeof(float) * c->P, cudaMemcpyHostToDevice, c->stream));
+  FR_CUDA(cudaMemsetAsync(g.grad, 0, sizeof(float) * kGuideParams, c->stream));
+  FR_CUDA(cudaMemsetAsync(g.weight_sum, 0, 4, c->stream));
+  FR_CUDA(cudaMemsetAsync(g.batch_count, 0, 4, c->stream));
+  launch_guide_gradients(g, c->P, c->sms, c->stream);
+  FR_CUDA(cudaMemcpyAsync(grad, g.grad, sizeof(float) * kGuideParams, cudaMemcpyDeviceToHost, c->stream));
+  FR_CUDA(cudaMemcpyAsync(weight_sum, g.weight_sum, 4, cudaMemcpyDeviceToHost, c->stream));
+  int rc = fr_synchronize(c);
+  FR_CUDA(cudaMemsetAsync(g.grad, 0, sizeof(float) * kGuideParams, c->stream));
+  FR_CUDA(cudaMemsetAsync(g.weight_sum, 0, 4, c->stream));
+  FR_CUDA(cudaMemsetAsync(g.batch_count, 0, 4, c->stream));
+  FR_CUDA(cudaMemsetAsync(g.importance, 0, sizeof(float) * c->P, c->stream));
+  const int rc2 = fr_synchronize(c);
+  return rc ? rc : rc2;
+}
+
 // ------------------------------------------------------------ checkpoint
 // State between iterations: the iteration count and photon total (they key
 // the random streams and the resolve), the per-pixel state and the photon
@@ -1094,8 +1190,16 @@ struct StatePart {
 
 std::vector<StatePart> state_parts(fr_ctx* c) {
   const size_t np = (size_t)c->W * c->H, ns = (size_t)c->P * kPhotonSlots;
-  return {{c->st.tau, 24 * np}, {c->st.n, 4 * np},       {c->st.r, 4 * np},
-          {c->st.g, 4 * np},    {c->ph.pos, 16 * ns},    {c->ph.flux, 16 * ns}, {c->ph.dir, 16 * ns}};
+  std::vector<StatePart> parts = {{c->st.tau, 24 * np},  {c->st.n, 4 * np},     {c->st.r, 4 * np},
+                                  {c->st.g, 4 * np},     {c->ph.pos, 16 * ns},  {c->ph.flux, 16 * ns},
+                                  {c->ph.dir, 16 * ns}};
+  if (c->guided) {  // the guide's network and optimizer state
+    parts.push_back({c->guide.params, 4 * (size_t)kGuideParams});
+    parts.push_back({c->guide.adam_m, 4 * (size_t)kGuideParams});
+    parts.push_back({c->guide.adam_v, 4 * (size_t)kGuideParams});
+    parts.push_back({c->guide.adam_step, 4});
+  }
+  return parts;
 }
 
 size_t state_bytes(fr_ctx* c) {
@@ -1154,6 +1258,7 @@ int fr_load_state(fr_ctx* c, const void* buf, size_t size) {
   }
   const uint32_t step = (uint32_t)h.iterations;
   FR_CUDA(cudaMemcpyAsync(c->step_dev, &step, sizeof step, cudaMemcpyHostToDevice, c->stream));
+  if (c->guided) launch_guide_prepare(c->guide, c->stream);
   FR_CUDA(cudaStreamSynchronize(c->stream));
   c->iterations = h.iterations;
   c->photons_total = h.photons_total;

@@ -23,6 +23,7 @@
 #include <cstdint>
 #include "fr_bsdf.cuh"
 #include "fr_grid.cuh"
+#include "fr_guide.cuh"
 #include "fr_kernels.h"
 #include "fr_layout.h"
 #include "fr_math.cuh"
@@ -568,43 +569,55 @@ __device__ __forceinline__ void store_state(const PathWave& w, int i, const Phot
                        __uint_as_float((uint32_t)s.k | ((uint32_t)s.loop << 8) | ((uint32_t)s.depth << 16)));
 }
 
-// generateLightRay (SPPM.cpp:453-471) and the light-surface photon in slot 0.
-__device__ __forceinline__ void photon_start(const SceneGPU& sc, const IterParams& it, const PhotonSlots& ph, int i,
-                                             PhotonState& s) {
-  Rng rng(photon_seed(it, i));
-  const size_t base = (size_t)i * kPhotonSlots;
+// A point on a light (generateLightRay, SPPM.cpp:453-466): the light by its
+// flux alias table (LightSampler.h:86), the point (textured: the 1000-point
+// emission table, LightSampler.cpp:30-66; else uniform, Sampling.cpp:339-349),
+// its radiance and area pdf; u, v are the point's barycentrics.
+struct LightPoint {
+  V3 pos, rad, ln;
+  float pdf_area, u, v;
+};
+
+__device__ __forceinline__ void light_point(const SceneGPU& sc, Rng& rng, LightPoint& lp) {
   const uint32_t lb = (uint32_t)(((uint64_t)(uint32_t)sc.num_lights * rng.next_u24()) >> 24);
   const LightGPU& bin = sc.lights[lb];
   const int li = rng.next() < bin.alias_prob ? bin.alias_left : bin.alias_right;
   const LightGPU& L = sc.lights[li];
   const V3 P0 = v3(L.p0), P1 = v3(L.p1), P2 = v3(L.p2);
-  V3 pos, rad;
-  float pdf_area;
   if (L.textured) {
     const EmitEntry* tab = sc.emit + L.emit_offset;
     const uint32_t eb = (uint32_t)(((uint64_t)kEmitSamples * rng.next_u24()) >> 24);
     const int ei = rng.next() < tab[eb].prob ? tab[eb].left : tab[eb].right;
     const EmitEntry& e = tab[ei];
-    pos = e.uvw[0] * P0 + e.uvw[1] * P1 + (1.0f - e.uvw[0] - e.uvw[1]) * P2;
-    rad = v3(e.L);
-    pdf_area = e.pdf;
+    lp.pos = e.uvw[0] * P0 + e.uvw[1] * P1 + (1.0f - e.uvw[0] - e.uvw[1]) * P2;
+    lp.rad = v3(e.L);
+    lp.pdf_area = e.pdf;
+    lp.u = e.uvw[0];
+    lp.v = e.uvw[1];
   } else {
     float u = rng.next(), v = rng.next();
     if (v > u) { u *= 0.5f; v -= u; }
     else { v *= 0.5f; u -= v; }
-    pos = u * P0 + v * P1 + (1.0f - u - v) * P2;
-    rad = v3(L.radiance);
-    pdf_area = L.pdf_point;
+    lp.pos = u * P0 + v * P1 + (1.0f - u - v) * P2;
+    lp.rad = v3(L.radiance);
+    lp.pdf_area = L.pdf_point;
+    lp.u = u;
+    lp.v = v;
   }
-  pdf_area *= L.pdf_light;
-  const V3 ln = v3(L.normal);
-  float pdf_dir = 1.0f;
-  const V3 d = cos_sampling(rng, ln, &pdf_dir);
-  rad = rad * fminf(1.0f, fmaxf(0.0f, dot(ln, d)));
-  s.o = pos + ln * kRayOffset;
+  lp.pdf_area *= L.pdf_light;
+  lp.ln = v3(L.normal);
+}
+
+// The photon path from its light point and direction (generateLightRay,
+// SPPM.cpp:466-470) and the light-surface photon in slot 0 (SPPM.cpp:530-540).
+__device__ __forceinline__ void photon_launch(const PhotonSlots& ph, int i, const LightPoint& lp, V3 d, float pdf_dir,
+                                              const Rng& rng, PhotonState& s) {
+  const size_t base = (size_t)i * kPhotonSlots;
+  const V3 rad = lp.rad * fminf(1.0f, fmaxf(0.0f, dot(lp.ln, d)));
+  s.o = lp.pos + lp.ln * kRayOffset;
   s.d = normalized(d);
   s.flux0 = rad;
-  s.PDF = pdf_area * pdf_dir;
+  s.PDF = lp.pdf_area * pdf_dir;
   s.thr = v3(1.f, 1.f, 1.f);
   store_float4(ph.pos + base, s.o, 1.0f);
   store_float4(ph.flux + base, s.flux0 * s.thr * kPI, s.PDF);
@@ -612,6 +625,17 @@ __device__ __forceinline__ void photon_start(const SceneGPU& sc, const IterParam
   s.ix = 1.0f;
   s.k = s.loop = s.depth = 0;
   s.draw = rng.draw;
+}
+
+// generateLightRay (SPPM.cpp:453-471) with cosine-sampled direction.
+__device__ __forceinline__ void photon_start(const SceneGPU& sc, const IterParams& it, const PhotonSlots& ph, int i,
+                                             PhotonState& s) {
+  Rng rng(photon_seed(it, i));
+  LightPoint lp;
+  light_point(sc, rng, lp);
+  float pdf_dir = 1.0f;
+  const V3 d = cos_sampling(rng, lp.ln, &pdf_dir);
+  photon_launch(ph, i, lp, d, pdf_dir, rng, s);
 }
 
 // Checks at the top of each pass of the bounce loop (SPPM.cpp:549-554);
@@ -712,6 +736,116 @@ __global__ void __launch_bounds__(128) k_pw_emit(SceneGPU sc, IterParams it, Pho
     store_state(w, i, s);
     w.queue[0][i] = (uint32_t)i;
   }
+}
+
+// Guided emission: the light point as in k_pw_emit, then the direction from
+// the defensive mixture f * cosine + (1 - f) * guide, the guide's lobes coming
+// from the MLP evaluated for the CTA's 128 paths on the tensor cores; the
+// photon's pdf is the mixture's.  Also records each path's guide inputs and
+// direction (training data) and clears its importance.
+constexpr int kEmitSmW = 0;                                  // W2, W3, W4 tiles
+constexpr int kEmitSmH = kTileW2T;                           // 128 x 64 activations
+constexpr int kEmitSmP1 = kEmitSmH + 128 * 64 * 2;           // W1, b1
+constexpr int kEmitSmB = kEmitSmP1 + kOffW2 * 4;             // b2, b3, b4
+constexpr int kEmitSmMisc = kEmitSmB + (64 + 64 + 48) * 4;
+constexpr int kEmitSmem = kEmitSmMisc + 64;
+
+__global__ void __launch_bounds__(128) k_pw_emit_guided(SceneGPU sc, IterParams it, PhotonSlots ph, PathWave w,
+                                                        uint32_t* counts, GuideGPU g) {
+  extern __shared__ __align__(1024) uint8_t sm[];
+  uint8_t* W = sm + kEmitSmW;
+  uint8_t* H = sm + kEmitSmH;
+  float* p1 = reinterpret_cast<float*>(sm + kEmitSmP1);
+  float* bias = reinterpret_cast<float*>(sm + kEmitSmB);
+  uint32_t* tbase = reinterpret_cast<uint32_t*>(sm + kEmitSmMisc);
+  uint64_t* bar = reinterpret_cast<uint64_t*>(sm + kEmitSmMisc + 8);
+  const uint32_t t = threadIdx.x, warp = t >> 5;
+  const int i = (int)(blockIdx.x * blockDim.x + t);
+  const bool live = i < it.photons;
+  if (i == 0) w.qcount[0] = (uint32_t)it.photons;
+  for (uint32_t e = t; e < (uint32_t)kTileW2T / 16; e += 128)
+    reinterpret_cast<uint4*>(W)[e] = reinterpret_cast<const uint4*>(g.tiles)[e];
+  for (uint32_t e = t; e < (uint32_t)kOffW2; e += 128) p1[e] = g.params[e];
+  for (uint32_t e = t; e < 64; e += 128) {
+    bias[e] = g.params[kOffB2 + e];
+    bias[64 + e] = g.params[kOffB3 + e];
+  }
+  for (uint32_t e = t; e < 48; e += 128) bias[128 + e] = g.params[kOffB4 + e];
+  Rng rng(photon_seed(it, i));
+  LightPoint lp;
+  float x[kGuideIn] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  if (live) {
+    counts[i] = 0;
+    light_point(sc, rng, lp);
+    // Inputs: position scaled to [-1, 1] over the scene bounds, barycentrics.
+    x[0] = 2.0f * (lp.pos.x - sc.lo[0]) / fmaxf(sc.hi[0] - sc.lo[0], 1e-20f) - 1.0f;
+    x[1] = 2.0f * (lp.pos.y - sc.lo[1]) / fmaxf(sc.hi[1] - sc.lo[1], 1e-20f) - 1.0f;
+    x[2] = 2.0f * (lp.pos.z - sc.lo[2]) / fmaxf(sc.hi[2] - sc.lo[2], 1e-20f) - 1.0f;
+    x[3] = lp.u;
+    x[4] = lp.v;
+  }
+  guide_layer1(p1, x, H, t);
+  if (t == 0) tc::mbar_init(bar, 1);
+  if (warp == 0) tc::tmem_alloc(tbase, 64);
+  publish();
+  const uint32_t tm = *tbase, lane_addr = tm + ((warp * 32u) << 16);
+  const uint32_t aH = tc::smem_addr(H);
+  TcSync sy{bar, 0u, true};
+  float o[kGuideOut];
+  if (t == 0) {
+    tc::gemm_issue(tm, aH, tc::smem_addr(W + kTileW2), 64, 64, false);
+    tc::mma_commit(bar);
+  }
+  if (sy.wait()) {
+    guide_hidden_epilogue(lane_addr, bias, H, t);
+    publish();
+    if (t == 0) {
+      tc::gemm_issue(tm, aH, tc::smem_addr(W + kTileW3), 64, 64, false);
+      tc::mma_commit(bar);
+    }
+    if (sy.wait()) {
+      guide_hidden_epilogue(lane_addr, bias + 64, H, t);
+      publish();
+      if (t == 0) {
+        tc::gemm_issue(tm, aH, tc::smem_addr(W + kTileW4), kGuideOutPad, 64, false);
+        tc::mma_commit(bar);
+      }
+      if (sy.wait()) guide_output_epilogue(lane_addr, bias + 128, o);
+    }
+  }
+  if (!sy.ok && t == 0) atomicOr(g.err, kErrGuide);
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tm, 64);
+  if (!live) return;
+  V3 d;
+  float pdf_dir;
+  if (sy.ok) {
+    GuideMixture mix;
+    guide_mixture(o, mix);
+    const float f = g.plain_fraction;
+    if (rng.next() < f) {
+      d = cos_sampling(rng, lp.ln, nullptr);
+    } else {
+      const float xi = rng.next();
+      int k = 0;
+      float acc = mix.w[0];
+      while (k < kGuideLobes - 1 && xi >= acc) acc += mix.w[++k];
+      const float e1 = rng.next(), e2 = rng.next();
+      d = vmf_sample(mix.mu[k], mix.kappa[k], e1, e2);
+    }
+    pdf_dir = f * fmaxf(0.0f, dot(lp.ln, d)) / kPI + (1.0f - f) * guide_pdf(mix, d);
+  } else {
+    d = cos_sampling(rng, lp.ln, &pdf_dir);
+  }
+  PhotonState s;
+  photon_launch(ph, i, lp, d, pdf_dir, rng, s);
+  photon_top(s);  // loop 0 -> 1; true for a new path
+  store_state(w, i, s);
+  w.queue[0][i] = (uint32_t)i;
+  g.feat[i] = make_float4(x[0], x[1], x[2], x[3]);
+  g.dir[i] = make_float4(x[4], s.d.x, s.d.y, s.d.z);
+  g.importance[i] = 0.0f;
 }
 
 __global__ void __launch_bounds__(128) k_pw_shade(SceneGPU sc, IterParams it, PhotonSlots ph, PathWave w,
@@ -932,7 +1066,8 @@ __device__ __forceinline__ double tau_update(double tau, float phi, float a, flo
 constexpr int kGatherGroup = FR_GATHER_GROUP;
 
 __global__ void __launch_bounds__(256) k_gather(SceneGPU sc, IterParams it, HitpointBuf hp, PhotonGrid g,
-                                               const GridInfo* gip, PixelState st, int32_t* dbg_m, float4* dbg_phi) {
+                                               const GridInfo* gip, PixelState st, int32_t* dbg_m, float4* dbg_phi,
+                                               float* importance) {
   constexpr int G = kGatherGroup;
   const unsigned lane = threadIdx.x & 31u;
   const unsigned gl = lane & (G - 1);                        // lane within the group
@@ -1012,6 +1147,7 @@ __global__ void __launch_bounds__(256) k_gather(SceneGPU sc, IterParams it, Hitp
         const FParam p{indir, out, nn, Ii, Io, hn.w, mat.extinction, mat.reflectance};
         const float brdf = surface_brdf(type, p);
         const V3 add = v3(hw.x, hw.y, hw.z) * brdf * v3(f4.x, f4.y, f4.z) / f4.w;
+        if (importance) atomicAdd(importance + (__float_as_uint(d4.w) >> 5), add.x + add.y + add.z);
         float y, t;
         y = add.x - kx; t = sx + y; kx = (t - sx) - y; sx = t;
         y = add.y - ky; t = sy + y; ky = (t - sy) - y; sy = t;
@@ -1288,8 +1424,14 @@ int launch_scan(uint32_t* in, uint32_t* out, uint32_t n, ScanTemp& t, cudaStream
 }
 
 void launch_gather_update(const SceneGPU& sc, const IterParams& it, HitpointBuf hp, PhotonGrid g, const GridInfo* gi,
-                          PixelState st, int32_t* dbg_m, float4* dbg_phi, int resident_blocks, cudaStream_t s) {
-  k_gather<<<std::max(1, resident_blocks), 256, 0, s>>>(sc, it, hp, g, gi, st, dbg_m, dbg_phi);
+                          PixelState st, int32_t* dbg_m, float4* dbg_phi, float* importance, int resident_blocks,
+                          cudaStream_t s) {
+  k_gather<<<std::max(1, resident_blocks), 256, 0, s>>>(sc, it, hp, g, gi, st, dbg_m, dbg_phi, importance);
+}
+
+void launch_pw_emit_guided(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, PathWave w, uint32_t* counts,
+                           const GuideGPU& g, cudaStream_t s) {
+  k_pw_emit_guided<<<blocks_for(it.photons, 128), 128, kEmitSmem, s>>>(sc, it, ph, w, counts, g);
 }
 
 int gather_blocks_per_sm() {

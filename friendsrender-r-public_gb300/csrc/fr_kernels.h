@@ -2,6 +2,7 @@
 #pragma once
 #include <cuda_runtime.h>
 #include <cstdint>
+#include <vector>
 #include "fr_layout.h"
 
 namespace fr {
@@ -131,8 +132,11 @@ void launch_photon_scatter(PhotonSlots ph, const uint32_t* counts, int paths, in
 // Words of block-sum scratch launch_scan needs for n elements; fills the level sizes of t.
 uint32_t scan_temp_words(uint32_t n, ScanTemp& t);
 // One warp per listed hitpoint; resident_blocks blocks of 256 threads.
+// importance: per-path sums of the flux each path's photons bring to
+// hitpoints (the guide's training signal), or nullptr.
 void launch_gather_update(const SceneGPU& sc, const IterParams& it, HitpointBuf hp, PhotonGrid g, const GridInfo* gi,
-                          PixelState st, int32_t* dbg_m, float4* dbg_phi, int resident_blocks, cudaStream_t s);
+                          PixelState st, int32_t* dbg_m, float4* dbg_phi, float* importance, int resident_blocks,
+                          cudaStream_t s);
 int gather_blocks_per_sm();
 // ExportPNG's resample and 8-bit quantization of a resolved image.
 void launch_export_rgba8(const float4* img, int width, int height, uint32_t* out, cudaStream_t s);
@@ -150,6 +154,18 @@ void launch_radius_count(const float4* hp_pos_r, int nh, PhotonGrid g, const Gri
 // Radius count with the fixed scratch of fr_noalloc.cu (allocates nothing).
 int radius_count_noalloc(const float* hp_dev, int32_t nh, const float* photons_dev, int32_t np, float cell,
                          int32_t* counts_dev, cudaStream_t stream, const char** msg);
+
+// Photon-emission guide (fr_guide.cu).
+struct GuideGPU;
+int guide_configure();  // opts the training kernel into its shared memory
+void launch_pw_emit_guided(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, PathWave w, uint32_t* counts,
+                           const GuideGPU& g, cudaStream_t s);
+int guide_train_smem();
+void launch_guide_train(const GuideGPU& g, int paths, int sms, cudaStream_t s);
+void launch_guide_prepare(const GuideGPU& g, cudaStream_t s);
+// Sample selection and the gradient sums only (no update).
+void launch_guide_gradients(const GuideGPU& g, int paths, int sms, cudaStream_t s);
+std::vector<float> guide_initial_params(uint32_t seed);
 
 // Device check of the tcgen05 GEMM block (fr_tc_check.cu): max |error| of
 // three products against a host GEMM.

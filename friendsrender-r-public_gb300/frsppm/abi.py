@@ -44,7 +44,12 @@ class CameraDesc(C.Structure):
 
 class SPPMParams(C.Structure):
     _fields_ = [('photons_per_iteration', C.c_int32), ('alpha', C.c_float), ('initial_radius', C.c_float),
-                ('flags', C.c_uint32), ('grid_cell_scale', C.c_float)]
+                ('flags', C.c_uint32), ('grid_cell_scale', C.c_float), ('guide', C.c_int32),
+                ('guide_plain_fraction', C.c_float), ('guide_batch', C.c_int32),
+                ('guide_learning_rate', C.c_float), ('guide_seed', C.c_uint32)]
+
+
+GUIDE_PARAMS = 11824
 
 
 class Stats(C.Structure):
@@ -59,7 +64,8 @@ EXPORTS = ['fr_last_error', 'fr_create', 'fr_iterate', 'fr_synchronize', 'fr_res
            'fr_read_hitpoints', 'fr_read_photon_slots', 'fr_read_gather', 'fr_read_state', 'fr_profile_enable',
            'fr_profile_read', 'fr_radius_count_noalloc', 'fr_check_exact_math',
            'fr_read_wave_counts', 'fr_save_state', 'fr_load_state', 'fr_update',
-           'fr_resolve_rgba8', 'fr_export_png', 'fr_write_png', 'fr_check_tc_gemm']
+           'fr_resolve_rgba8', 'fr_export_png', 'fr_write_png', 'fr_check_tc_gemm', 'fr_guide_params',
+           'fr_guide_set_params', 'fr_read_guide_importance', 'fr_guide_gradient']
 
 STAGES = ('eye', 'photon', 'grid', 'gather', 'eye_trace', 'photon_trace')
 
@@ -106,6 +112,10 @@ def load(path=None):
     lib.fr_export_png.argtypes = [vp, C.c_char_p]
     lib.fr_write_png.argtypes = [C.c_char_p, i32, i32, vp]
     lib.fr_check_tc_gemm.argtypes = [C.c_uint32, vp]
+    lib.fr_guide_params.argtypes = [vp, vp]
+    lib.fr_guide_set_params.argtypes = [vp, vp]
+    lib.fr_read_guide_importance.argtypes = [vp, vp]
+    lib.fr_guide_gradient.argtypes = [vp, i32, vp, vp, vp]
     _lib = lib
     return lib
 
@@ -123,7 +133,8 @@ def _check(rc, what):
 class Renderer:
     """One fr_ctx: a scene (frsppm.scenes dict), camera and SPPM parameters."""
 
-    def __init__(self, scene, photons, alpha=0.9, radius=0.015, flags=0, cell_scale=0.0, camera=None):
+    def __init__(self, scene, photons, alpha=0.9, radius=0.015, flags=0, cell_scale=0.0, camera=None,
+                 guide=False, guide_plain_fraction=0.0, guide_batch=0, guide_lr=0.0, guide_seed=1):
         lib = load()
         self.scene = scene
         cam = camera or scene['camera']
@@ -156,7 +167,8 @@ class Renderer:
         cd.fov_degrees, cd.focal_length, cd.distance_to_lens = cam['fov'], cam['focal'], cam['dist']
         cd.aspect = cam['aspect']
         cd.lens_width = cd.lens_height = cam['lens']
-        pp = SPPMParams(int(photons), float(alpha), float(radius), int(flags), float(cell_scale))
+        pp = SPPMParams(int(photons), float(alpha), float(radius), int(flags), float(cell_scale), int(bool(guide)),
+                        float(guide_plain_fraction), int(guide_batch), float(guide_lr), int(guide_seed))
         self.width, self.height, self.photons = cam['width'], cam['height'], int(photons)
         h = C.c_void_p()
         _check(lib.fr_create(C.byref(sd), C.byref(cd), C.byref(pp), C.byref(h)), 'fr_create')
@@ -303,6 +315,30 @@ class Renderer:
 
     def export_png(self, path):
         _check(_lib.fr_export_png(self.h, os.fsencode(path)), 'fr_export_png')
+
+    def guide_params(self):
+        out = np.empty(GUIDE_PARAMS, np.float32)
+        _check(_lib.fr_guide_params(self.h, _ptr(out)), 'fr_guide_params')
+        return out
+
+    def set_guide_params(self, params):
+        p = np.ascontiguousarray(params, np.float32)
+        assert p.shape == (GUIDE_PARAMS,)
+        _check(_lib.fr_guide_set_params(self.h, _ptr(p)), 'fr_guide_set_params')
+
+    def guide_importance(self):
+        out = np.empty(self.photons, np.float32)
+        _check(_lib.fr_read_guide_importance(self.h, _ptr(out)), 'fr_read_guide_importance')
+        return out
+
+    def guide_gradient(self, samples):
+        """samples: (n, 9) float32 {5 inputs, direction, importance}; returns
+        (gradient sums (GUIDE_PARAMS,), importance sum)."""
+        smp = np.ascontiguousarray(samples, np.float32).reshape(-1, 9)
+        grad = np.empty(GUIDE_PARAMS, np.float32)
+        ws = np.zeros(1, np.float32)
+        _check(_lib.fr_guide_gradient(self.h, len(smp), _ptr(smp), _ptr(grad), _ptr(ws)), 'fr_guide_gradient')
+        return grad, float(ws[0])
 
     def read_gather(self):
         n = self.width * self.height

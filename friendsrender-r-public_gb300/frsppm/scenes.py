@@ -272,6 +272,61 @@ def mixed_materials(seed=CONFIG_SEED_BASE + 1, width=1280, height=720, n_spheres
     return scene
 
 
+def caustic_box(seed=CONFIG_SEED_BASE + 2, width=1024, height=1024, n_spheres=50, n_lat=40, n_lon=51,
+                light_tex=256, slit=0.1):
+    """Caustic scene: a 1x1 textured area light above a diffuse box whose only
+    opening is a ``slit`` x ``slit`` hole in its top, so most photons of plain
+    light sampling never enter.  Inside, ``n_spheres`` GGX-dielectric spheres
+    (IOR 1.5, roughness 0.02) stand on the diffuse floor and focus the light
+    that comes through the slit into caustics.  A pinhole camera inside the
+    box looks at the floor.  With the defaults: 198,936 triangles, 1024^2."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    textures = [noise_texture(rng, light_tex, 'emission')]
+    mats = [material('floor', DIFFUSE, (0.8, 0.8, 0.8)),
+            material('walls', DIFFUSE, (0.7, 0.65, 0.6)),
+            material('glass', GGX_DIELECTRIC, (0.98, 0.98, 0.98), roughness=0.02, index=1.5,
+                     opaque=False, sppm=False),
+            material('light', DIFFUSE, (1, 1, 1), emission=(40.0, 36.0, 32.0), tex_albedo=0)]
+    b = _Builder()
+    x0, x1, y1, h = -1.0, 1.0, 1.2, slit * 0.5
+    b.quad((x0, 0, x0), (x0, 0, x1), (x1, 0, x1), (x1, 0, x0), (0, 1, 0), 0)            # floor
+    b.quad((x0, 0, x0), (x0, y1, x0), (x0, y1, x1), (x0, 0, x1), (1, 0, 0), 1)          # walls
+    b.quad((x1, 0, x0), (x1, 0, x1), (x1, y1, x1), (x1, y1, x0), (-1, 0, 0), 1)
+    b.quad((x0, 0, x1), (x0, y1, x1), (x1, y1, x1), (x1, 0, x1), (0, 0, -1), 1)
+    b.quad((x0, 0, x0), (x1, 0, x0), (x1, y1, x0), (x0, y1, x0), (0, 0, 1), 1)
+    # Top: a slab of thickness t with the slit at its centre (inner and outer
+    # faces as four rectangles around the hole, and the hole's four sides), so
+    # photons stopped on the outside lie farther than a gather radius from the
+    # hitpoints inside.
+    t = 0.05
+    for y, ny in ((y1, -1), (y1 + t, 1)):
+        for (a0, a1, c0, c1) in ((x0, -h, x0, x1), (h, x1, x0, x1), (-h, h, x0, -h), (-h, h, h, x1)):
+            b.quad((a0, y, c0), (a1, y, c0), (a1, y, c1), (a0, y, c1), (0, ny, 0), 1)
+    b.quad((-h, y1, -h), (-h, y1 + t, -h), (-h, y1 + t, h), (-h, y1, h), (1, 0, 0), 1)
+    b.quad((h, y1, -h), (h, y1, h), (h, y1 + t, h), (h, y1 + t, -h), (-1, 0, 0), 1)
+    b.quad((-h, y1, -h), (h, y1, -h), (h, y1 + t, -h), (-h, y1 + t, -h), (0, 0, 1), 1)
+    b.quad((-h, y1, h), (-h, y1 + t, h), (h, y1 + t, h), (h, y1, h), (0, 0, -1), 1)
+    placed = []
+    while len(placed) < n_spheres:
+        r = float(rng.uniform(0.05, 0.15))
+        cx, cz = (float(v) for v in rng.uniform(-0.85, 0.85, 2))
+        if all((cx - px) ** 2 + (cz - pz) ** 2 > (r + pr + 0.01) ** 2 for px, pz, pr in placed):
+            placed.append((cx, cz, r))
+    for cx, cz, r in placed:
+        uv_sphere(b, (cx, r + 1e-3, cz), r, 2, n_lat, n_lon)
+    ly = 1.6
+    b.quad((-0.5, ly, -0.5), (0.5, ly, -0.5), (0.5, ly, 0.5), (-0.5, ly, 0.5), (0, -1, 0), 3)
+    scene = b.build()
+    scene.update(materials=mats, textures=textures,
+                 camera=_camera(PINHOLE, width, height, (0.0, 0.95, -0.95), (0.0, 0.0, 0.15), 75.0))
+    return scene
+
+
+def small_caustic(seed=CONFIG_SEED_BASE + 102, width=96, height=96):
+    """The caustic scene at a size for tests: 12 coarser spheres, 96x96."""
+    return caustic_box(seed=seed, width=width, height=height, n_spheres=12, n_lat=12, n_lon=16, light_tex=64)
+
+
 def small_mixed(seed=CONFIG_SEED_BASE + 101, width=48, height=32, tex_size=64):
     """A small scene with every feature of the mixed-materials config (four
     material types, albedo/roughness/normal textures, textured light, thin

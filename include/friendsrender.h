@@ -109,6 +109,15 @@ typedef struct fr_sppm_params {
   float initial_radius;           /* FirstRadius (SPPM.cpp:21), reference 0.015 */
   uint32_t flags;                 /* FR_FLAG_* */
   float grid_cell_scale;          /* photon grid cell = scale * mean hitpoint radius; <= 0 selects 2 */
+  /* Learned photon-emission guide (no counterpart in the reference): photon
+   * directions from a defensive mixture of cosine sampling and a network
+   * trained online, with the mixture's pdf in the photon weight.  Zero
+   * (guide = 0) is the reference's plain emission. */
+  int32_t guide;                  /* 1: guided emission */
+  float guide_plain_fraction;     /* share of cosine sampling in the mixture; <= 0 selects 0.2 */
+  int32_t guide_batch;            /* training samples per iteration; <= 0 selects 65536 */
+  float guide_learning_rate;      /* Adam step size; <= 0 selects 0.002 */
+  uint32_t guide_seed;            /* initial network weights */
 } fr_sppm_params;
 
 typedef struct fr_stats {
@@ -250,6 +259,21 @@ int fr_radius_count_noalloc(const float* hp_dev, int32_t num_hitpoints, const fl
  * inputs in max_abs_err[0..2]. */
 int fr_check_tc_gemm(uint32_t seed, double* max_abs_err);
 int fr_check_exact_math(uint64_t samples, uint32_t seed, uint64_t* mismatches, uint64_t* fast_paths);
+
+/* The photon guide's state (contexts created with guide = 1).
+ * fr_guide_params / fr_guide_set_params: the FP32 network parameters
+ * (FR_GUIDE_PARAMS floats: W1[64][5], b1, W2[64][64], b2, W3[64][64], b3,
+ * W4[48][64] (rows 40-47 zero), b4[48]).  fr_read_guide_importance: per photon
+ * path, the flux its photons brought to hitpoints in the last iteration.
+ * fr_guide_gradient: the gradient sums of the training loss
+ * sum_j -I_j log q(d_j | x_j) over n samples (n x 9 floats: 5 inputs,
+ * direction, importance I) computed by the training kernels, and sum_j I_j;
+ * the network is not updated. */
+#define FR_GUIDE_PARAMS 11824
+int fr_guide_params(fr_ctx* ctx, float* params);
+int fr_guide_set_params(fr_ctx* ctx, const float* params);
+int fr_read_guide_importance(fr_ctx* ctx, float* importance);
+int fr_guide_gradient(fr_ctx* ctx, int32_t n, const float* samples, float* grad, float* weight_sum);
 
 /* No reference counterpart: the wavefront queue lengths of the last
  * iteration.  eye_counts[r] / photon_counts[r] is the number of paths traced
