@@ -187,6 +187,103 @@ def trace_traffic_per_launch():
     return None
 
 
+# ---- guided vs plain SPPM on the caustic scene at equal wall time
+CAUSTIC_PHOTONS = 2_000_000
+CAUSTIC_ALPHA, CAUSTIC_RADIUS = 0.7, 0.01
+CAUSTIC_WORKLOAD = ('caustic box: 198,936 triangles (50 GGX-dielectric spheres, IOR 1.5, roughness 0.02, on a '
+                    'diffuse floor) in a diffuse box lit through a 0.1x0.1 slit in its top by a 1x1 textured area '
+                    'light, 1024^2 pinhole, 2M photon paths/iteration, alpha 0.7, r0 0.01')
+REL_MSE_EPS = 1e-2
+
+
+def _linear(img):
+    """fr_resolve's pixels (radiance to the power 1/1.2) back to radiance."""
+    return img[:, :3].astype('float64') ** 1.2
+
+
+def rel_mse(img, ref):
+    """Mean over pixels and channels of (x - r)^2 / (r^2 + 1e-2), radiance."""
+    a, b = _linear(img), _linear(ref)
+    return float(((a - b) ** 2 / (b * b + REL_MSE_EPS)).mean())
+
+
+def guide_eval(plain_iters=128, ref_iters=1024, photons=CAUSTIC_PHOTONS, scene=None, log=None):
+    """Plain and guided SPPM on the caustic box against a long plain run (the
+    reference image, FP64 tau), all resolved with the standard estimate
+    tau / (pi R^2 photons emitted).  The reference run's random streams start
+    past every step the two runs draw (fr_seek), so it shares no seed with
+    them.  The plain run's error after plain_iters iterations is the target;
+    the guided run's wall time to first reach it (checked at iteration marks
+    12.5% apart) and its error at the plain run's wall time are reported.
+    Wall time is fr_iterate + fr_synchronize, the guide's training included;
+    the resolves at the marks are not timed."""
+    from frsppm import abi, scenes
+    scene = scene or scenes.caustic_box()
+    kw = dict(alpha=CAUSTIC_ALPHA, radius=CAUSTIC_RADIUS, flags=abi.FLAG_STANDARD_RESOLVE)
+    max_run = 4 * plain_iters
+    first = max_run + 16
+    npix = scene['camera']['width'] * scene['camera']['height']
+    if (first + ref_iters + 1) * max(photons, npix) >= 1 << 32:
+        raise ValueError('reference run would wrap the 32-bit seeds into the compared runs')
+    t0 = time.perf_counter()
+    with abi.Renderer(scene, photons, **kw) as ref:
+        ref.seek(first)
+        done = 0
+        while done < ref_iters:
+            n = min(64, ref_iters - done)
+            ref.iterate(n)
+            done += n
+        reference = ref.resolve()
+    ref_s = time.perf_counter() - t0
+
+    marks, m = [], 1.0
+    while int(m) < plain_iters:
+        if not marks or int(m) > marks[-1]:
+            marks.append(int(m))
+        m *= 1.125
+    marks.append(plain_iters)
+
+    def run(guided, stop):
+        curve = []
+        extra = dict(guide=True) if guided else {}
+        with abi.Renderer(scene, photons, **kw, **extra) as r:
+            r.synchronize()
+            t, done, k = 0.0, 0, 0
+            while True:
+                target = marks[k] if k < len(marks) else int(done * 1.125) + 1
+                t1 = time.perf_counter()
+                r.iterate(target - done)
+                t += time.perf_counter() - t1
+                done = target
+                curve.append((done, t, rel_mse(r.resolve(), reference)))
+                if log:
+                    log('%s %d iterations %.3f s relMSE %.5f' % ('guided' if guided else 'plain', *curve[-1]))
+                k += 1
+                if stop(done, t):
+                    return curve
+
+    plain = run(False, lambda n, t: n >= plain_iters)
+    t_plain, e_plain = plain[-1][1], plain[-1][2]
+    guided = run(True, lambda n, t: t >= 1.02 * t_plain or n >= max_run)
+    reach = next(((n, t) for n, t, e in guided if e <= e_plain), None)
+    at_equal = [e for n, t, e in guided if t <= t_plain]
+    return {
+        'workload': CAUSTIC_WORKLOAD,
+        'reference': '%d plain iterations (%d photon paths), FP64 tau, standard resolve, %.1f s'
+                     % (ref_iters, ref_iters * photons, ref_s),
+        'rel_mse': 'mean of (x - ref)^2 / (ref^2 + %g) over pixels and RGB, linear radiance' % REL_MSE_EPS,
+        'plain': {'iterations': plain_iters, 'wall_s': t_plain, 'rel_mse': e_plain,
+                  'ms_per_iteration': 1e3 * t_plain / plain_iters},
+        'guided': {'iterations_to_plain_error': reach[0] if reach else None,
+                   'wall_s_to_plain_error': reach[1] if reach else None,
+                   'rel_mse_at_equal_time': at_equal[-1] if at_equal else None,
+                   'ms_per_iteration': 1e3 * guided[-1][1] / guided[-1][0]},
+        'time_to_plain_error_speedup': (t_plain / reach[1]) if reach else None,
+        'curves': {'plain': [[n, round(t, 4), round(e, 6)] for n, t, e in plain],
+                   'guided': [[n, round(t, 4), round(e, 6)] for n, t, e in guided]},
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -195,9 +292,18 @@ def main():
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
     ap.add_argument('--photons', type=int, default=PHOTONS)
+    ap.add_argument('--guide-eval', action='store_true', help='only the guided-vs-plain caustic comparison')
+    ap.add_argument('--no-guide-eval', action='store_true')
+    ap.add_argument('--guide-plain-iters', type=int, default=128)
+    ap.add_argument('--guide-ref-iters', type=int, default=1024)
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
+    if args.guide_eval:
+        out = guide_eval(args.guide_plain_iters, args.guide_ref_iters,
+                         log=lambda s: print(s, file=sys.stderr, flush=True))
+        print(json.dumps(out))
+        return 0
 
     import numpy as np
     import torch

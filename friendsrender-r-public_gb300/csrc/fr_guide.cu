@@ -275,10 +275,10 @@ __global__ void k_guide_adam(GuideGPU g) {
   }
 }
 
-__global__ void k_guide_step_done(GuideGPU g) {
+__global__ void k_guide_step_done(GuideGPU g, int last) {
   if (*g.weight_sum > 0.0f) *g.adam_step += 1;
   *g.weight_sum = 0.0f;
-  *g.batch_count = 0;
+  if (last) *g.batch_count = 0;
 }
 
 // Paths whose photons reached a hitpoint, as training samples (one atomic
@@ -301,12 +301,17 @@ __global__ void __launch_bounds__(256) k_guide_select(GuideGPU g, int paths) {
 
 int guide_train_smem() { return kTrainSmem; }
 
-void launch_guide_train(const GuideGPU& g, int paths, int sms, cudaStream_t s) {
+// One sample selection, then g.steps Adam steps on the same samples (each a
+// gradient pass with the current weights).  Returns the kernels launched.
+int launch_guide_train(const GuideGPU& g, int paths, int sms, cudaStream_t s) {
   k_guide_select<<<(paths + 255) / 256, 256, 0, s>>>(g, paths);
-  k_guide_train<<<std::max(1, sms), 128, kTrainSmem, s>>>(g);
-  k_guide_adam<<<(kGuideParams + 255) / 256, 256, 0, s>>>(g);
-  k_guide_prepare<<<16, 256, 0, s>>>(g);
-  k_guide_step_done<<<1, 1, 0, s>>>(g);
+  for (int k = 0; k < g.steps; ++k) {
+    k_guide_train<<<std::max(1, sms), 128, kTrainSmem, s>>>(g);
+    k_guide_adam<<<(kGuideParams + 255) / 256, 256, 0, s>>>(g);
+    k_guide_prepare<<<16, 256, 0, s>>>(g);
+    k_guide_step_done<<<1, 1, 0, s>>>(g, k == g.steps - 1);
+  }
+  return 1 + 4 * g.steps;
 }
 
 void launch_guide_prepare(const GuideGPU& g, cudaStream_t s) { k_guide_prepare<<<16, 256, 0, s>>>(g); }

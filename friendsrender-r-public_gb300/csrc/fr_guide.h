@@ -57,6 +57,7 @@ struct GuideGPU {
   int* err;             // device error word
   float plain_fraction; // share of plain cosine sampling in the emission mixture
   int batch_cap;
+  int steps;            // Adam steps per iteration on the iteration's samples
   float lr;
 };
 

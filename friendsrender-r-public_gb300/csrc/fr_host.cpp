@@ -226,6 +226,7 @@ struct fr_ctx {
   int photon_blocks = 0;         // grid of the wavefront round kernels
   int tail_blocks = 0;           // grid of the photon tail kernel
   uint32_t* step_dev = nullptr;  // device iteration counter (IterParams::step)
+  uint32_t step_base = 0;        // fr_seek: the counter runs at step_base + iterations
   cudaGraph_t graph = nullptr;   // one captured iteration
   cudaGraphExec_t graph_exec = nullptr;
   int64_t graph_launches = 0;    // kernels per replay of the graph
@@ -513,9 +514,8 @@ int enqueue_iteration(fr_ctx* c) {
                          c->guided ? c->guide.importance : nullptr, c->gather_blocks, s);
   }
   if (c->guided) {
-    // select, train, Adam, weight tiles, step bookkeeping
-    launch_guide_train(c->guide, c->P, c->sms, s);
-    c->launches += 5;
+    // select, then per Adam step: train, Adam, weight tiles, step bookkeeping
+    c->launches += launch_guide_train(c->guide, c->P, c->sms, s);
   }
   // iteration counter, eye and photon passes (start, rounds of
   // trace/sort/shade, tail), grid setup, count, scatter, gather
@@ -762,7 +762,8 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
     GuideGPU& g = c->guide;
     g.plain_fraction = params->guide_plain_fraction > 0.0f ? std::min(1.0f, params->guide_plain_fraction) : 0.2f;
     g.batch_cap = std::min(c->P, params->guide_batch > 0 ? params->guide_batch : 65536);
-    g.lr = params->guide_learning_rate > 0.0f ? params->guide_learning_rate : 0.002f;
+    g.lr = params->guide_learning_rate > 0.0f ? params->guide_learning_rate : 0.005f;
+    g.steps = params->guide_steps > 0 ? std::min(params->guide_steps, 64) : 4;
     if ((rc = c->alloc(&g.params, kGuideParams)) || (rc = c->alloc(&g.grad, kGuideParams)) ||
         (rc = c->alloc(&g.adam_m, kGuideParams)) || (rc = c->alloc(&g.adam_v, kGuideParams)) ||
         (rc = c->alloc(&g.tiles, kTileBytes)) || (rc = c->alloc(&g.feat, (size_t)c->P)) ||
@@ -823,7 +824,7 @@ int fr_synchronize(fr_ctx* c) {
 int fr_resolve_dev(fr_ctx* c, float* rgba_dev) {
   if (!c || !rgba_dev) return fail(FR_ERR_INVALID, "fr_resolve_dev: bad arguments");
   launch_resolve(c->st, c->W * c->H, (double)c->photons_total, (double)c->iterations,
-                 reinterpret_cast<float4*>(rgba_dev), c->stream);
+                 (c->flags & kFlagStandardResolve) != 0, reinterpret_cast<float4*>(rgba_dev), c->stream);
   FR_CUDA(cudaGetLastError());
   return FR_OK;
 }
@@ -1177,7 +1178,8 @@ struct StateHeader {
   char magic[8];  // "FRSPPMS1"
   int32_t width, height, photons, flags;
   float alpha, initial_radius;
-  int32_t triangles, reserved;
+  int32_t triangles;
+  uint32_t step_base;  // fr_seek's first step (0 without it)
   int64_t iterations, photons_total;
 };
 static_assert(sizeof(StateHeader) == 56, "checkpoint header is 56 bytes");
@@ -1226,6 +1228,7 @@ int fr_save_state(fr_ctx* c, void* buf, size_t* size) {
   h.alpha = c->alpha;
   h.initial_radius = c->r0;
   h.triangles = c->sc.num_tris;
+  h.step_base = c->step_base;
   h.iterations = c->iterations;
   h.photons_total = c->photons_total;
   std::memcpy(buf, &h, sizeof h);
@@ -1256,12 +1259,23 @@ int fr_load_state(fr_ctx* c, const void* buf, size_t size) {
     FR_CUDA(cudaMemcpyAsync(part.dev, p, part.bytes, cudaMemcpyHostToDevice, c->stream));
     p += part.bytes;
   }
-  const uint32_t step = (uint32_t)h.iterations;
+  const uint32_t step = h.step_base + (uint32_t)h.iterations;
   FR_CUDA(cudaMemcpyAsync(c->step_dev, &step, sizeof step, cudaMemcpyHostToDevice, c->stream));
   if (c->guided) launch_guide_prepare(c->guide, c->stream);
   FR_CUDA(cudaStreamSynchronize(c->stream));
+  c->step_base = h.step_base;
   c->iterations = h.iterations;
   c->photons_total = h.photons_total;
+  return FR_OK;
+}
+
+int fr_seek(fr_ctx* c, uint32_t first_step) {
+  if (!c) return fail(FR_ERR_INVALID, "fr_seek: bad arguments");
+  if (c->iterations != 0) return fail(FR_ERR_INVALID, "fr_seek: %lld iterations already run", (long long)c->iterations);
+  FR_CUDA(cudaStreamSynchronize(c->stream));
+  FR_CUDA(cudaMemcpyAsync(c->step_dev, &first_step, sizeof first_step, cudaMemcpyHostToDevice, c->stream));
+  FR_CUDA(cudaStreamSynchronize(c->stream));
+  c->step_base = first_step;
   return FR_OK;
 }
 

@@ -1244,11 +1244,16 @@ __global__ void k_export_rgba8(const float4* img, int W, int H, uint32_t* out) {
 // ---------------------------------------------------------------- resolve
 // reconstructImageFromSharedPoints (SPPM.cpp:473-493): normalisation in FP64,
 // gamma 1/1.2 in FP32 as the reference applies it.
-__global__ void k_resolve(PixelState st, int pixels, double photons_total, double iterations, float4* out) {
+// standard = 0: the reference's estimate, which scales the photons emitted by
+// the pixel's share of iterations that gathered photons (NumGather); 1: the
+// standard SPPM estimate tau / (pi R^2 * all photons emitted).
+__global__ void k_resolve(PixelState st, int pixels, double photons_total, double iterations, int standard,
+                          float4* out) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= pixels) return;
   const double R = (double)st.r[i];
-  const double denom = (photons_total * ((double)st.g[i] + 1e-4) / (1e-4 + iterations)) * (double)kPI * R * R;
+  const double share = standard ? 1.0 : ((double)st.g[i] + 1e-4) / (1e-4 + iterations);
+  const double denom = (photons_total * share) * (double)kPI * R * R;
   const double* tau = st.tau + 3 * (size_t)i;
   const float lr = (float)(tau[0] / denom), lg = (float)(tau[1] / denom), lb = (float)(tau[2] / denom);
   const float gm = 1.0f / 1.2f;
@@ -1448,8 +1453,9 @@ void launch_export_rgba8(const float4* img, int width, int height, uint32_t* out
   k_export_rgba8<<<blocks_for((size_t)width * height, 256), 256, 0, s>>>(img, width, height, out);
 }
 
-void launch_resolve(PixelState st, int pixels, double photons_total, double iterations, float4* out, cudaStream_t s) {
-  k_resolve<<<blocks_for(pixels, 256), 256, 0, s>>>(st, pixels, photons_total, iterations, out);
+void launch_resolve(PixelState st, int pixels, double photons_total, double iterations, bool standard, float4* out,
+                    cudaStream_t s) {
+  k_resolve<<<blocks_for(pixels, 256), 256, 0, s>>>(st, pixels, photons_total, iterations, standard ? 1 : 0, out);
 }
 
 void launch_trace_closest(const SceneGPU& sc, const float* rays, int n, int32_t* facet, float* tuv, int* err,

@@ -142,7 +142,8 @@ int gather_blocks_per_sm();
 void launch_export_rgba8(const float4* img, int width, int height, uint32_t* out, cudaStream_t s);
 // The N/tau/R update from given per-pixel photon counts and flux sums.
 void launch_update(PixelState st, const int32_t* m, const float4* phi, int pixels, float alpha, cudaStream_t s);
-void launch_resolve(PixelState st, int pixels, double photons_total, double iterations, float4* out, cudaStream_t s);
+void launch_resolve(PixelState st, int pixels, double photons_total, double iterations, bool standard, float4* out,
+                    cudaStream_t s);
 
 // Parity entry points.
 void launch_trace_closest(const SceneGPU& sc, const float* rays, int n, int32_t* facet, float* tuv, int* err,
@@ -161,7 +162,7 @@ int guide_configure();  // opts the training kernel into its shared memory
 void launch_pw_emit_guided(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, PathWave w, uint32_t* counts,
                            const GuideGPU& g, cudaStream_t s);
 int guide_train_smem();
-void launch_guide_train(const GuideGPU& g, int paths, int sms, cudaStream_t s);
+int launch_guide_train(const GuideGPU& g, int paths, int sms, cudaStream_t s);
 void launch_guide_prepare(const GuideGPU& g, cudaStream_t s);
 // Sample selection and the gradient sums only (no update).
 void launch_guide_gradients(const GuideGPU& g, int paths, int sms, cudaStream_t s);

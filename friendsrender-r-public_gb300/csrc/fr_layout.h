@@ -140,6 +140,7 @@ struct IterParams {
 };
 
 constexpr uint32_t kFlagFixStaleSlot = 1u;  // drop the stale photon slot quirk (SPPM.cpp:672)
+constexpr uint32_t kFlagStandardResolve = 2u;  // resolve with tau / (pi R^2 * photons emitted)
 
 // Entries of the per-thread traversal stack (a wide node pushes at most 7).
 constexpr int kTraversalStackEntries = 96;

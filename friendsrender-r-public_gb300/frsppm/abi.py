@@ -46,10 +46,13 @@ class SPPMParams(C.Structure):
     _fields_ = [('photons_per_iteration', C.c_int32), ('alpha', C.c_float), ('initial_radius', C.c_float),
                 ('flags', C.c_uint32), ('grid_cell_scale', C.c_float), ('guide', C.c_int32),
                 ('guide_plain_fraction', C.c_float), ('guide_batch', C.c_int32),
-                ('guide_learning_rate', C.c_float), ('guide_seed', C.c_uint32)]
+                ('guide_learning_rate', C.c_float), ('guide_seed', C.c_uint32),
+                ('guide_steps', C.c_int32)]
 
 
 GUIDE_PARAMS = 11824
+FLAG_FIX_STALE_PHOTON_SLOT = 1   # FR_FLAG_FIX_STALE_PHOTON_SLOT
+FLAG_STANDARD_RESOLVE = 2        # FR_FLAG_STANDARD_RESOLVE
 
 
 class Stats(C.Structure):
@@ -65,7 +68,7 @@ EXPORTS = ['fr_last_error', 'fr_create', 'fr_iterate', 'fr_synchronize', 'fr_res
            'fr_profile_read', 'fr_radius_count_noalloc', 'fr_check_exact_math',
            'fr_read_wave_counts', 'fr_save_state', 'fr_load_state', 'fr_update',
            'fr_resolve_rgba8', 'fr_export_png', 'fr_write_png', 'fr_check_tc_gemm', 'fr_guide_params',
-           'fr_guide_set_params', 'fr_read_guide_importance', 'fr_guide_gradient']
+           'fr_guide_set_params', 'fr_read_guide_importance', 'fr_guide_gradient', 'fr_seek']
 
 STAGES = ('eye', 'photon', 'grid', 'gather', 'eye_trace', 'photon_trace')
 
@@ -107,6 +110,7 @@ def load(path=None):
     lib.fr_read_wave_counts.argtypes = [vp, vp, vp, vp, vp]
     lib.fr_save_state.argtypes = [vp, vp, C.POINTER(C.c_size_t)]
     lib.fr_load_state.argtypes = [vp, vp, C.c_size_t]
+    lib.fr_seek.argtypes = [vp, C.c_uint32]
     lib.fr_update.argtypes = [vp, vp, vp]
     lib.fr_resolve_rgba8.argtypes = [vp, vp]
     lib.fr_export_png.argtypes = [vp, C.c_char_p]
@@ -134,7 +138,7 @@ class Renderer:
     """One fr_ctx: a scene (frsppm.scenes dict), camera and SPPM parameters."""
 
     def __init__(self, scene, photons, alpha=0.9, radius=0.015, flags=0, cell_scale=0.0, camera=None,
-                 guide=False, guide_plain_fraction=0.0, guide_batch=0, guide_lr=0.0, guide_seed=1):
+                 guide=False, guide_plain_fraction=0.0, guide_batch=0, guide_lr=0.0, guide_seed=1, guide_steps=0):
         lib = load()
         self.scene = scene
         cam = camera or scene['camera']
@@ -168,7 +172,8 @@ class Renderer:
         cd.aspect = cam['aspect']
         cd.lens_width = cd.lens_height = cam['lens']
         pp = SPPMParams(int(photons), float(alpha), float(radius), int(flags), float(cell_scale), int(bool(guide)),
-                        float(guide_plain_fraction), int(guide_batch), float(guide_lr), int(guide_seed))
+                        float(guide_plain_fraction), int(guide_batch), float(guide_lr), int(guide_seed),
+                        int(guide_steps))
         self.width, self.height, self.photons = cam['width'], cam['height'], int(photons)
         h = C.c_void_p()
         _check(lib.fr_create(C.byref(sd), C.byref(cd), C.byref(pp), C.byref(h)), 'fr_create')
@@ -300,6 +305,10 @@ class Renderer:
     def load_state(self, data):
         buf = np.frombuffer(data, np.uint8)
         _check(_lib.fr_load_state(self.h, _ptr(buf), len(buf)), 'fr_load_state')
+
+    def seek(self, first_step):
+        """fr_seek: iteration k of this (fresh) context draws step first_step + k."""
+        _check(_lib.fr_seek(self.h, int(first_step)), 'fr_seek')
 
     def update(self, m, phi):
         """fr_update: apply per-pixel photon counts and flux sums to the state."""

@@ -279,7 +279,9 @@ def caustic_box(seed=CONFIG_SEED_BASE + 2, width=1024, height=1024, n_spheres=50
     light sampling never enter.  Inside, ``n_spheres`` GGX-dielectric spheres
     (IOR 1.5, roughness 0.02) stand on the diffuse floor and focus the light
     that comes through the slit into caustics.  A pinhole camera inside the
-    box looks at the floor.  With the defaults: 198,936 triangles, 1024^2."""
+    box looks at the floor (its image plane, where the reference's pinhole
+    camera starts its rays, sits 0.01 behind the pinhole so that it is inside
+    the box too).  With the defaults: 198,936 triangles, 1024^2."""
     rng = np.random.Generator(np.random.PCG64(seed))
     textures = [noise_texture(rng, light_tex, 'emission')]
     mats = [material('floor', DIFFUSE, (0.8, 0.8, 0.8)),
@@ -297,10 +299,13 @@ def caustic_box(seed=CONFIG_SEED_BASE + 2, width=1024, height=1024, n_spheres=50
     # Top: a slab of thickness t with the slit at its centre (inner and outer
     # faces as four rectangles around the hole, and the hole's four sides), so
     # photons stopped on the outside lie farther than a gather radius from the
-    # hitpoints inside.
-    t = 0.05
+    # hitpoints inside.  The slab overhangs the walls (to +-1.5), so light from
+    # the 1x1 light that passes the slab's edge travels outward and never lands
+    # on the outer side of the (zero-thickness) walls, where interior
+    # hitpoints would count it.
+    t, o = 0.05, 1.5
     for y, ny in ((y1, -1), (y1 + t, 1)):
-        for (a0, a1, c0, c1) in ((x0, -h, x0, x1), (h, x1, x0, x1), (-h, h, x0, -h), (-h, h, h, x1)):
+        for (a0, a1, c0, c1) in ((-o, -h, -o, o), (h, o, -o, o), (-h, h, -o, -h), (-h, h, h, o)):
             b.quad((a0, y, c0), (a1, y, c0), (a1, y, c1), (a0, y, c1), (0, ny, 0), 1)
     b.quad((-h, y1, -h), (-h, y1 + t, -h), (-h, y1 + t, h), (-h, y1, h), (1, 0, 0), 1)
     b.quad((h, y1, -h), (h, y1, h), (h, y1 + t, h), (h, y1 + t, -h), (-1, 0, 0), 1)
@@ -318,7 +323,7 @@ def caustic_box(seed=CONFIG_SEED_BASE + 2, width=1024, height=1024, n_spheres=50
     b.quad((-0.5, ly, -0.5), (0.5, ly, -0.5), (0.5, ly, 0.5), (-0.5, ly, 0.5), (0, -1, 0), 3)
     scene = b.build()
     scene.update(materials=mats, textures=textures,
-                 camera=_camera(PINHOLE, width, height, (0.0, 0.95, -0.95), (0.0, 0.0, 0.15), 75.0))
+                 camera=_camera(PINHOLE, width, height, (0.0, 0.95, -0.95), (0.0, 0.0, 0.15), 75.0, dist=0.01))
     return scene
 
 

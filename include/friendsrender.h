@@ -100,7 +100,13 @@ typedef struct fr_camera_desc {
 enum {
   /* Drop the reference's stale photon slot (SPPM.cpp:672): off by default, so
    * the photon set of every iteration is the reference's. */
-  FR_FLAG_FIX_STALE_PHOTON_SLOT = 1u
+  FR_FLAG_FIX_STALE_PHOTON_SLOT = 1u,
+  /* Resolve with the standard SPPM estimate (tau / (pi R^2 * all emitted
+   * photons)) instead of the reference's, which divides by the emitted photons
+   * times the pixel's NumGather / iterations (SPPM.cpp:485-488) and so changes
+   * with the photon sampling.  Off by default (the reference's image); for
+   * comparing sampling strategies such as the photon guide. */
+  FR_FLAG_STANDARD_RESOLVE = 2u
 };
 
 typedef struct fr_sppm_params {
@@ -116,8 +122,9 @@ typedef struct fr_sppm_params {
   int32_t guide;                  /* 1: guided emission */
   float guide_plain_fraction;     /* share of cosine sampling in the mixture; <= 0 selects 0.2 */
   int32_t guide_batch;            /* training samples per iteration; <= 0 selects 65536 */
-  float guide_learning_rate;      /* Adam step size; <= 0 selects 0.002 */
+  float guide_learning_rate;      /* Adam step size; <= 0 selects 0.005 */
   uint32_t guide_seed;            /* initial network weights */
+  int32_t guide_steps;            /* Adam steps per iteration on its samples; <= 0 selects 4 (at most 64) */
 } fr_sppm_params;
 
 typedef struct fr_stats {
@@ -314,6 +321,15 @@ int fr_update(fr_ctx* ctx, const int32_t* m, const float* phi);
  * which iterations continue exactly as they would have in the saved context. */
 int fr_save_state(fr_ctx* ctx, void* buf, size_t* size);
 int fr_load_state(fr_ctx* ctx, const void* buf, size_t size);
+
+/* Moves the random streams of a context on which no iteration has run: its
+ * iteration k then draws the reference's seeds of step first_step + k instead
+ * of step k (eye seed pixel + pixels * step, SPPM.cpp:334; photon seed
+ * path + 135 + paths * step, SPPM.cpp:520; both 32-bit).  For independent
+ * runs of one scene whose seed ranges do not overlap (a reference image,
+ * replicas); the iteration count, the resolve and the checkpoint (which
+ * carries first_step) are unchanged.  No counterpart in the reference. */
+int fr_seek(fr_ctx* ctx, uint32_t first_step);
 
 #ifdef __cplusplus
 }

@@ -7,6 +7,7 @@
 * What the trained network gains over plain emission on the caustic scene:
   the share of photon paths that reach a visible hitpoint, and the image error
   against a long plain render after the same number of iterations.
+* fr_seek, which gives the long reference render random streams of its own.
 """
 import numpy as np
 import pytest
@@ -66,27 +67,68 @@ def test_guided_render_is_valid():
         assert np.isfinite(p).all()
 
 
+def _linear(img):
+    """Resolve's pixels (radiance to the power 1/1.2) back to radiance."""
+    return img[:, :3].astype(np.float64) ** 1.2
+
+
 def _rel_mse(img, ref):
-    a, b = img[:, :3].astype(np.float64), ref[:, :3].astype(np.float64)
+    a, b = _linear(img), _linear(ref)
     return float(np.mean((a - b) ** 2 / (b ** 2 + 1e-2)))
 
 
 def test_trained_guide_gains_over_plain():
+    """The guide against plain light sampling on the small caustic box, both
+    resolved with the standard estimate tau / (pi R^2 photons emitted)
+    (FR_FLAG_STANDARD_RESOLVE): the reference's own resolve scales each pixel
+    by its share of iterations with photons, which depends on the sampling and
+    so is not the same estimate for the two.  The reference image is a long
+    plain run whose random streams (fr_seek) share no seed with the two runs."""
     from frsppm import abi, scenes
     scene = scenes.small_caustic()
-    kw = dict(alpha=0.7, radius=0.01)
+    kw = dict(alpha=0.7, radius=0.01, flags=abi.FLAG_STANDARD_RESOLVE)
     with abi.Renderer(scene, 100000, **kw) as ref:
+        ref.seek(20000)
         ref.iterate(400)
         reference = ref.resolve()
-    iters = 40
-    with abi.Renderer(scene, 50000, **kw) as plain, abi.Renderer(scene, 50000, guide=True, **kw) as guided:
-        plain.iterate(iters)
-        guided.iterate(iters)
-        m_plain, _ = plain.read_gather()
-        m_guided, _ = guided.read_gather()
+    iters, tail = 120, 20
+    m_plain = m_guided = 0
+    with abi.Renderer(scene, 50000, **kw) as plain, \
+            abi.Renderer(scene, 50000, guide=True, guide_steps=4, guide_lr=0.005, **kw) as guided:
+        plain.iterate(iters - tail)
+        guided.iterate(iters - tail)
+        for _ in range(tail):
+            plain.iterate(1)
+            guided.iterate(1)
+            m_plain += int(plain.read_gather()[0].sum())
+            m_guided += int(guided.read_gather()[0].sum())
         useful = float((guided.guide_importance() > 0).mean())
-        e_plain, e_guided = _rel_mse(plain.resolve(), reference), _rel_mse(guided.resolve(), reference)
-    # Photons that reach the camera's hitpoints per iteration, and the error.
-    assert m_guided.sum() > 2.0 * m_plain.sum(), (m_guided.sum(), m_plain.sum())
+        img_plain, img_guided = plain.resolve(), guided.resolve()
+    e_plain, e_guided = _rel_mse(img_plain, reference), _rel_mse(img_guided, reference)
+    # Photon-hitpoint pairs per iteration once trained, paths that reached a
+    # hitpoint, the energy (the guided estimate stays unbiased) and the error.
+    assert m_guided > 4.0 * m_plain, (m_guided, m_plain)
     assert useful > 0.05, useful
-    assert e_guided < e_plain, (e_guided, e_plain)
+    e_ref = _linear(reference).mean()
+    assert abs(_linear(img_guided).mean() - e_ref) < 0.1 * e_ref, (_linear(img_guided).mean(), e_ref)
+    assert abs(_linear(img_plain).mean() - e_ref) < 0.1 * e_ref, (_linear(img_plain).mean(), e_ref)
+    assert e_guided < 0.7 * e_plain, (e_guided, e_plain)
+
+
+def test_seek_moves_random_streams():
+    """fr_seek(s) on a fresh context: its first iteration is the iteration
+    s + 1 of an unmoved context (same hitpoints), and the checkpoint keeps it."""
+    from frsppm import abi, scenes
+    scene = scenes.small_caustic(width=32, height=32)
+    with abi.Renderer(scene, 5000, radius=0.01) as a, abi.Renderer(scene, 5000, radius=0.01) as b, \
+            abi.Renderer(scene, 5000, radius=0.01) as c:
+        a.iterate(3)
+        b.seek(2)
+        b.iterate(1)
+        np.testing.assert_array_equal(a.read_hitpoints()['pos'], b.read_hitpoints()['pos'])
+        c.load_state(b.save_state())
+        a.iterate(1)
+        c.iterate(1)
+        np.testing.assert_array_equal(a.read_hitpoints()['pos'], c.read_hitpoints()['pos'])
+        with pytest.raises(RuntimeError):
+            b.seek(5)  # iterations already run
