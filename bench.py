@@ -17,6 +17,10 @@ steps (CUDA events around every stage and trace launch).
 e2e: the same metric through the C-ABI with a host result buffer: every step
 is fr_iterate + fr_resolve into pinned host memory (the image, read back each
 step); the scene is uploaded once by fr_create (reported as setup).
+guided_vs_plain: the metric's second half, on the caustic scene (198,936
+triangles, 1024^2, 2M photon paths/iteration): relMSE against a long plain
+render of plain and guided SPPM at equal wall time, and the guided run's time
+to reach the plain run's final error (guide_eval; --guide-eval runs it alone).
 --impl reference: the CPU restatement of the reference path (oracle/port,
 pinned bit-exact to the reference's own outputs) on the host cores.
 """
@@ -210,7 +214,8 @@ def rel_mse(img, ref):
 def guide_eval(plain_iters=128, ref_iters=1024, photons=CAUSTIC_PHOTONS, scene=None, log=None):
     """Plain and guided SPPM on the caustic box against a long plain run (the
     reference image, FP64 tau), all resolved with the standard estimate
-    tau / (pi R^2 photons emitted).  The reference run's random streams start
+    tau / (pi R^2 photons emitted) and with paths ended where the reference's
+    rough-dielectric BSDF turns NaN (which would leave NaN pixels).  The reference run's random streams start
     past every step the two runs draw (fr_seek), so it shares no seed with
     them.  The plain run's error after plain_iters iterations is the target;
     the guided run's wall time to first reach it (checked at iteration marks
@@ -219,7 +224,8 @@ def guide_eval(plain_iters=128, ref_iters=1024, photons=CAUSTIC_PHOTONS, scene=N
     the resolves at the marks are not timed."""
     from frsppm import abi, scenes
     scene = scene or scenes.caustic_box()
-    kw = dict(alpha=CAUSTIC_ALPHA, radius=CAUSTIC_RADIUS, flags=abi.FLAG_STANDARD_RESOLVE)
+    kw = dict(alpha=CAUSTIC_ALPHA, radius=CAUSTIC_RADIUS,
+              flags=abi.FLAG_STANDARD_RESOLVE | abi.FLAG_END_DEGENERATE_PATHS)
     max_run = 4 * plain_iters
     first = max_run + 16
     npix = scene['camera']['width'] * scene['camera']['height']
@@ -296,11 +302,12 @@ def main():
     ap.add_argument('--no-guide-eval', action='store_true')
     ap.add_argument('--guide-plain-iters', type=int, default=128)
     ap.add_argument('--guide-ref-iters', type=int, default=1024)
+    ap.add_argument('--guide-photons', type=int, default=CAUSTIC_PHOTONS)
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
     if args.guide_eval:
-        out = guide_eval(args.guide_plain_iters, args.guide_ref_iters,
+        out = guide_eval(args.guide_plain_iters, args.guide_ref_iters, args.guide_photons,
                          log=lambda s: print(s, file=sys.stderr, flush=True))
         print(json.dumps(out))
         return 0
@@ -419,6 +426,9 @@ def main():
         'clocks': clk.summary(),
         'photons_stored_last_step': stored, 'hitpoints_last_step': hits,
     }
+    if world == 1 and not args.no_guide_eval:
+        # equal-time relMSE, guided vs plain SPPM (caustic scene; not the timed workload)
+        out['guided_vs_plain'] = guide_eval(args.guide_plain_iters, args.guide_ref_iters, args.guide_photons)
     if world == 1 and not args.no_cpu_baseline:
         out['cpu_baseline'] = cpu_baseline(scene)
     print(json.dumps(out))

@@ -286,7 +286,7 @@ __global__ void k_guide_step_done(GuideGPU g, int last) {
 __global__ void __launch_bounds__(256) k_guide_select(GuideGPU g, int paths) {
   __shared__ uint32_t s_n, s_base;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool take = i < paths && g.importance[i] > 0.0f;
+  const bool take = i < paths && g.importance[i] > 0.0f && g.importance[i] < INFINITY;
   if (threadIdx.x == 0) s_n = 0;
   __syncthreads();
   uint32_t slot = 0;

@@ -125,7 +125,7 @@ __device__ __forceinline__ bool eye_top(EyeState& s, Rng& rng, float rr5, float 
 // kHitHit after writing a hitpoint, kHitNone when the path ends without one,
 // and -1 when it goes on.
 __device__ __forceinline__ int eye_shade(const SceneGPU& sc, const HitpointBuf& hp, int i, EyeState& s, Rng& rng,
-                                         const Hit& hit, float rr5, float rr6) {
+                                         const Hit& hit, float rr5, float rr6, uint32_t flags) {
   Geom g;
   calc_geometry(sc, hit, g);
   g.normal = dot(g.normal, s.d) > 0.0f ? -g.normal : g.normal;
@@ -165,6 +165,9 @@ __device__ __forceinline__ int eye_shade(const SceneGPU& sc, const HitpointBuf& 
   const float cs = fmaxf(0.0f, fminf(1.0f, dot(nd, on)));
   if (brdf < kLt1e8) return kHitNone;
   if (pdf < 0.0f) return kHitNone;
+  // The reference goes on with a NaN BSDF value or pdf, or a zero pdf, which
+  // gives the hitpoint a NaN or infinite weight; the flag ends such paths.
+  if ((flags & kFlagEndDegenerate) && !(brdf >= kLt1e8 && pdf > 0.0f)) return kHitNone;
   s.thr = s.thr * (g.albedo * cs * brdf);
   s.PDF *= pdf;
   s.o = nxt_o; s.d = nd; s.ix = nix;
@@ -476,7 +479,7 @@ __global__ void __launch_bounds__(128) k_ew_shade(SceneGPU sc, IterParams it, fl
       } else {
         Rng rng(eye_seed(it, (int)i));
         rng.seek(s.draw);
-        const int r = eye_shade(sc, hp, (int)i, s, rng, h, rr5, rr6);
+        const int r = eye_shade(sc, hp, (int)i, s, rng, h, rr5, rr6, it.flags);
         if (r < 0) {
           s.draw = rng.draw;
           store_eye(w, (int)i, s);
@@ -514,7 +517,7 @@ __global__ void __launch_bounds__(128) k_ew_tail(SceneGPU sc, IterParams it, flo
           hit_type = kHitOnlyDirect;
           break;
         }
-        const int r = eye_shade(sc, hp, i, s, rng, h, rr5, rr6);
+        const int r = eye_shade(sc, hp, i, s, rng, h, rr5, rr6, it.flags);
         if (r >= 0) {
           hit_type = r;
           break;
@@ -696,6 +699,7 @@ __device__ __forceinline__ bool photon_shade(const SceneGPU& sc, const IterParam
   const float cs = fmaxf(0.0f, fminf(1.0f, dot(nd, on)));
   if (brdf < kLt1e8) return false;
   if (pdf < 0.0f) return false;
+  if ((it.flags & kFlagEndDegenerate) && !(brdf >= kLt1e8 && pdf > 0.0f)) return false;  // as in eye_shade
   s.thr = s.thr * (g.albedo * cs * brdf);
   s.PDF *= pdf;
   s.o = nxt_o; s.d = nd; s.ix = nix;

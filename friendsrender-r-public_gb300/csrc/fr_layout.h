@@ -141,6 +141,7 @@ struct IterParams {
 
 constexpr uint32_t kFlagFixStaleSlot = 1u;  // drop the stale photon slot quirk (SPPM.cpp:672)
 constexpr uint32_t kFlagStandardResolve = 2u;  // resolve with tau / (pi R^2 * photons emitted)
+constexpr uint32_t kFlagEndDegenerate = 4u;    // end paths with a NaN BSDF value or pdf, or a zero pdf
 
 // Entries of the per-thread traversal stack (a wide node pushes at most 7).
 constexpr int kTraversalStackEntries = 96;

@@ -53,6 +53,7 @@ class SPPMParams(C.Structure):
 GUIDE_PARAMS = 11824
 FLAG_FIX_STALE_PHOTON_SLOT = 1   # FR_FLAG_FIX_STALE_PHOTON_SLOT
 FLAG_STANDARD_RESOLVE = 2        # FR_FLAG_STANDARD_RESOLVE
+FLAG_END_DEGENERATE_PATHS = 4    # FR_FLAG_END_DEGENERATE_PATHS
 
 
 class Stats(C.Structure):

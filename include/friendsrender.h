@@ -106,7 +106,15 @@ enum {
    * times the pixel's NumGather / iterations (SPPM.cpp:485-488) and so changes
    * with the photon sampling.  Off by default (the reference's image); for
    * comparing sampling strategies such as the photon guide. */
-  FR_FLAG_STANDARD_RESOLVE = 2u
+  FR_FLAG_STANDARD_RESOLVE = 2u,
+  /* End an eye or photon path where the sampled direction's BSDF value or pdf
+   * is NaN or its pdf is zero.  The reference only ends paths with a BSDF
+   * value below 1e-8 or a negative pdf (SPPM.cpp:278-281, 648-651) and goes
+   * on with the others, whose hitpoints then carry a NaN or infinite weight
+   * (its rough-dielectric BSDF returns NaN for a few rare directions), so a
+   * pixel turns NaN once a photon lands at such a hitpoint.  Off by default
+   * (the reference's hitpoints and photons). */
+  FR_FLAG_END_DEGENERATE_PATHS = 4u
 };
 
 typedef struct fr_sppm_params {

@@ -1116,6 +1116,11 @@ void port_iterate(void* h, int32_t n) {
   for (int k = 0; k < n; ++k) r->iterate();
 }
 
+// The next iteration runs step first_step + 1 (its seeds, SPPM.cpp:334,520);
+// for checking one step's eye pass without running the steps before it.  The
+// resolve then counts the skipped steps as iterations.
+void port_seek(void* h, int32_t first_step) { static_cast<Renderer*>(h)->step = first_step; }
+
 // Photon pass only (for a bounded CPU timing sample).
 void port_photon_pass(void* h, int32_t first, int32_t count) {
   Renderer* r = static_cast<Renderer*>(h);

@@ -48,6 +48,7 @@ def load():
             getattr(lib, name).argtypes = [vp]
             getattr(lib, name).restype = None
         lib.port_iterate.argtypes = [vp, C.c_int32]
+        lib.port_seek.argtypes = [vp, C.c_int32]
         lib.port_photon_pass.argtypes = [vp, C.c_int32, C.c_int32]
         lib.port_resolve.argtypes = [vp, vp]
         lib.port_trace_closest.argtypes = [vp, vp, C.c_int32, vp, vp]
@@ -146,6 +147,10 @@ class PortRenderer:
 
     def iterate(self, n=1):
         _lib.port_iterate(self.h, int(n))
+
+    def seek(self, first_step):
+        """The next iteration runs step first_step + 1."""
+        _lib.port_seek(self.h, int(first_step))
 
     def photon_pass(self, first, count):
         _lib.port_photon_pass(self.h, int(first), int(count))

@@ -16,6 +16,12 @@ Each fixture <name>.npz holds, for a scene from frsppm.scenes:
   image_png                 the reference's ExportPNG of that image, decoded
                             (height x width x RGBA8)
 with the reference's ppm_Alpha = 0.9 and FirstRadius = 0.015 (SPPM.cpp:20-21).
+
+caustic_step51_row780.npz: one row (780) of the hitpoints that the reference's
+eye pass makes at step 51 on the full caustic scene (frsppm.scenes.caustic_box,
+1024^2), where pixel 799031 gets a NaN weight from the reference's
+rough-dielectric BSDF: hp_* as above, with scene_sha, step and row.  The render
+mode dumps every step up to 51, about 3.6 GB in the working folder.
 """
 from __future__ import annotations
 
@@ -122,9 +128,39 @@ def make(name, factory, photons, iters, out_dir=HERE):
     return path
 
 
+CAUSTIC_STEP, CAUSTIC_ROW = 51, 780
+HP_KEYS = ('hp_type', 'hp_facet', 'hp_pos', 'hp_nrm', 'hp_out', 'hp_w', 'hp_rough')
+
+
+def caustic_row_fixture(scene, od, out_dir=HERE):
+    """The fixture from a finished 'render 1000 51' output folder od."""
+    W = scene['camera']['width']
+    sl = slice(CAUSTIC_ROW * W, (CAUSTIC_ROW + 1) * W)
+    data = dict(scene_sha=np.array(scene_sha(scene)), step=np.array(CAUSTIC_STEP), row=np.array(CAUSTIC_ROW))
+    for k in HP_KEYS:
+        data[k] = np.load(os.path.join(od, 'it%d_%s.npy' % (CAUSTIC_STEP, k)))[sl]
+    path = os.path.join(out_dir, 'caustic_step%d_row%d.npz' % (CAUSTIC_STEP, CAUSTIC_ROW))
+    np.savez_compressed(path, **data)
+    return path
+
+
+def make_caustic_row(out_dir=HERE, work=None):
+    scene = scenes.caustic_box()
+    with tempfile.TemporaryDirectory(dir=work) as d:
+        objio.write_scene(scene, d)
+        objio.write_materials_table(scene, os.path.join(d, 'materials.txt'))
+        objio.write_camera(scene, os.path.join(d, 'camera.txt'))
+        od = os.path.join(d, 'out')
+        os.makedirs(od)
+        run([d, 'render', '1000', str(CAUSTIC_STEP), od])
+        return caustic_row_fixture(scene, od, out_dir)
+
+
 if __name__ == '__main__':
     if not os.path.exists(FRREF):
         sys.exit('build the reference first: make -C oracle/ref')
     for name, (factory, photons, iters) in FIXTURES.items():
         p = make(name, factory, photons, iters)
         print(p, os.path.getsize(p))
+    p = make_caustic_row()
+    print(p, os.path.getsize(p))
