@@ -33,8 +33,15 @@ def check_row(hp, fx, W):
     np.testing.assert_array_equal(hp['type'][sl], fx['hp_type'])
     hit = fx['hp_type'] == 1
     np.testing.assert_array_equal(hp['facet'][sl][hit], fx['hp_facet'][hit])
-    for k, f in (('pos', 'hp_pos'), ('nrm', 'hp_nrm'), ('out', 'hp_out'), ('w', 'hp_w'), ('rough', 'hp_rough')):
-        np.testing.assert_array_equal(hp[k][sl][hit], fx[f][hit])  # NaN in the same places counts as equal
+    for k, f in (('pos', 'hp_pos'), ('nrm', 'hp_nrm'), ('out', 'hp_out'), ('rough', 'hp_rough')):
+        np.testing.assert_array_equal(hp[k][sl][hit], fx[f][hit])
+    # Weights: NaN in the same places, the rest within 1e-5 relative (the
+    # tolerance of the other reference-parity tests: the product's rounding
+    # order is not the reference's).
+    w, wr = hp['w'][sl][hit].astype(np.float64), fx['hp_w'][hit].astype(np.float64)
+    np.testing.assert_array_equal(np.isnan(w), np.isnan(wr))
+    ok = ~np.isnan(wr)
+    assert (np.abs(w[ok] - wr[ok]) <= 1e-5 * np.abs(wr[ok])).all()
 
 
 def test_oracle_caustic_step51_matches_reference():
