@@ -227,6 +227,9 @@ struct fr_ctx {
   int tail_blocks = 0;           // grid of the photon tail kernel
   uint32_t* step_dev = nullptr;  // device iteration counter (IterParams::step)
   uint32_t step_base = 0;        // fr_seek: the counter runs at step_base + iterations
+  cudaStream_t body[kPhotonRounds] = {};  // capture the bodies of the graph's nested round nodes
+  uint32_t* rounds_run = nullptr;  // gated photon rounds run so far (device)
+  bool capturing = false;        // enqueue_iteration is building the iteration graph
   cudaGraph_t graph = nullptr;   // one captured iteration
   cudaGraphExec_t graph_exec = nullptr;
   int64_t graph_launches = 0;    // kernels per replay of the graph
@@ -278,6 +281,8 @@ struct fr_ctx {
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     if (graph) cudaGraphDestroy(graph);
     if (side) cudaStreamDestroy(side);
+    for (cudaStream_t b : body)
+      if (b) cudaStreamDestroy(b);
     if (stream) cudaStreamDestroy(stream);
   }
 };
@@ -443,6 +448,46 @@ struct StageMark {
 // both passes' shade queues and trace fetch counters.
 constexpr size_t kCounters = 2 * (kWaveRounds + 2) + 1 + 2 * kWaveRounds * kShadeQueues + 2 * kWaveRounds;
 
+// Photon rounds r, r+1, ... as nested conditional (IF) nodes of the graph
+// being captured on stream s: k_round_gate sets the node's condition, and
+// the body (captured on the stream of the next nesting level) holds the
+// round's trace, sort and shade kernels and then the node of round r + 1.
+// A skipped round so ends the chain: it costs the one gate launch.
+int enqueue_gated_photon_rounds(fr_ctx* c, const IterParams& it, int r, cudaStream_t s, int grid, int sort_grid) {
+  if (r >= kPhotonRounds) return FR_OK;
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  cudaGraph_t g = nullptr;
+  FR_CUDA(cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, nullptr, nullptr, nullptr));
+  if (cs != cudaStreamCaptureStatusActive || !g) return fail(FR_ERR_CUDA, "gated round %d: stream not capturing", r);
+  cudaGraphConditionalHandle h;
+  FR_CUDA(cudaGraphConditionalHandleCreate(&h, g, 0u, cudaGraphCondAssignDefault));
+  launch_round_gate(h, c->wave, r, c->rounds_run, s);
+  c->launches += 1;  // the gate; fr_profile_read adds the rounds it lets run
+  const cudaGraphNode_t* deps = nullptr;
+  size_t ndeps = 0;
+  FR_CUDA(cudaStreamGetCaptureInfo(s, &cs, nullptr, &g, &deps, nullptr, &ndeps));
+  cudaGraphNodeParams p{};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = h;
+  p.conditional.type = cudaGraphCondTypeIf;
+  p.conditional.size = 1;
+  cudaGraphNode_t node = nullptr;
+  FR_CUDA(cudaGraphAddNode(&node, g, deps, nullptr, ndeps, &p));
+  FR_CUDA(cudaStreamUpdateCaptureDependencies(s, &node, nullptr, 1, cudaStreamSetCaptureDependencies));
+  cudaStream_t b = c->body[r - kPhotonGatedFrom];
+  FR_CUDA(cudaStreamBeginCaptureToGraph(b, p.conditional.phGraph_out[0], nullptr, nullptr, 0,
+                                        cudaStreamCaptureModeThreadLocal));
+  launch_wave_trace(c->sc, c->wave, r, grid, false, c->err, b);
+  launch_wave_sort(c->sc, c->wave, r, sort_grid, b);
+  launch_pw_shade(c->sc, it, c->ph, c->wave, c->counts, r, grid, b);
+  const int rc = enqueue_gated_photon_rounds(c, it, r + 1, b, grid, sort_grid);
+  cudaGraph_t captured = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(b, &captured);
+  if (rc) return rc;
+  if (e != cudaSuccess) return fail(FR_ERR_CUDA, "gated round %d: %s", r, cudaGetErrorString(e));
+  return FR_OK;
+}
+
 // Enqueues one iteration (the kernels read the iteration number from
 // c->step_dev, which the first kernel advances).
 int enqueue_iteration(fr_ctx* c) {
@@ -488,12 +533,18 @@ int enqueue_iteration(fr_ctx* c) {
     else
       launch_pw_emit(c->sc, it, c->ph, c->wave, c->counts, s);
     for (int r = 0; r < kPhotonRounds; ++r) {
+      if (c->capturing && r == kPhotonGatedFrom) {
+        const int rc = enqueue_gated_photon_rounds(c, it, r, s, grid, sort_grid);
+        if (rc) return rc;
+        break;
+      }
       {
         StageMark t(c, FR_STAGE_PHOTON_TRACE, s);
         launch_wave_trace(c->sc, c->wave, r, grid, false, c->err, s);
       }
       launch_wave_sort(c->sc, c->wave, r, sort_grid, s);
       launch_pw_shade(c->sc, it, c->ph, c->wave, c->counts, r, grid, s);
+      c->launches += 3;
     }
     launch_pw_tail(c->sc, it, c->ph, c->wave, c->counts, kPhotonRounds, c->tail_blocks, c->err, s);
   }
@@ -517,9 +568,9 @@ int enqueue_iteration(fr_ctx* c) {
     // select, then per Adam step: train, Adam, weight tiles, step bookkeeping
     c->launches += launch_guide_train(c->guide, c->P, c->sms, s);
   }
-  // iteration counter, eye and photon passes (start, rounds of
-  // trace/sort/shade, tail), grid setup, count, scatter, gather
-  c->launches += 5 + (2 + 3 * kEyeRounds) + (2 + 3 * kPhotonRounds);
+  // iteration counter, eye pass (start, rounds of trace/sort/shade, tail),
+  // photon emission and tail, grid setup, count, scatter, gather
+  c->launches += 5 + (2 + 3 * kEyeRounds) + 2;
   FR_CUDA(cudaGetLastError());
   return FR_OK;
 }
@@ -534,7 +585,9 @@ int run_iteration(fr_ctx* c) {
     if (!c->graph_exec) {
       const int64_t before = c->launches;
       FR_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+      c->capturing = true;
       const int rc = enqueue_iteration(c);
+      c->capturing = false;
       cudaGraph_t g = nullptr;
       const cudaError_t ec = cudaStreamEndCapture(c->stream, &g);
       if (rc) {
@@ -600,6 +653,9 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
       cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming) != cudaSuccess)
     return bail(fail(FR_ERR_CUDA, "cudaStreamCreate/cudaEventCreate failed"));
+  for (cudaStream_t& b : c->body)
+    if (cudaStreamCreateWithFlags(&b, cudaStreamNonBlocking) != cudaSuccess)
+      return bail(fail(FR_ERR_CUDA, "cudaStreamCreate failed"));
   c->W = camera->width;
   c->H = camera->height;
   c->P = params->photons_per_iteration;
@@ -726,7 +782,7 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
       (rc = c->alloc(&c->wave.qcount, kCounters)) || (rc = c->alloc(&c->hp.list, npix)) ||
       (rc = c->alloc(&c->wave.mq, (size_t)kShadeQueues * wave_n)) ||
       (rc = c->alloc(&c->eye_wave.mq, (size_t)kShadeQueues * npix)) ||
-      (rc = c->alloc(&c->gi, 1)) || (rc = c->alloc(&c->step_dev, 1)) ||
+      (rc = c->alloc(&c->gi, 1)) || (rc = c->alloc(&c->step_dev, 1)) || (rc = c->alloc(&c->rounds_run, 1)) ||
       (rc = c->alloc(&c->err, 1)) ||
       (rc = c->alloc(&c->dbg_m, npix)) || (rc = c->alloc(&c->dbg_phi, npix)) || (rc = c->alloc(&c->image, npix)) ||
       (rc = c->alloc(&c->image8, npix)))
@@ -742,6 +798,8 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
   c->wave.tfetch = c->eye_wave.tfetch + kWaveRounds;
   c->eye_wave.cap = (uint32_t)npix;
   c->wave.cap = (uint32_t)wave_n;
+  c->eye_wave.min_live = kEyeTailMin;
+  c->wave.min_live = kPhotonTailMin;
   // Photon grid: one bucket per expected photon or better (a few photons per path).
   c->grid.table = next_pow2(std::max<uint64_t>((uint64_t)c->P * 4, 1u << 16));
   const size_t cap = nslots;
@@ -797,6 +855,7 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
   cudaMemsetAsync(c->ph.flux, 0, nslots * sizeof(float4), c->stream);
   cudaMemsetAsync(c->gi, 0, sizeof(GridInfo), c->stream);
   cudaMemsetAsync(c->step_dev, 0, sizeof(uint32_t), c->stream);
+  cudaMemsetAsync(c->rounds_run, 0, sizeof(uint32_t), c->stream);
   cudaMemsetAsync(c->err, 0, sizeof(int), c->stream);
   cudaMemsetAsync(c->hp.pos, 0, npix * sizeof(float4), c->stream);
   if (cudaStreamSynchronize(c->stream) != cudaSuccess || cudaGetLastError() != cudaSuccess)
@@ -900,7 +959,11 @@ int fr_profile_read(fr_ctx* c, double* stage_ms, int64_t* stage_count, int64_t* 
     if (stage_ms) stage_ms[m.first] += ms;
     if (stage_count) stage_count[m.first] += 1;
   }
-  if (launches) *launches = c->launches;
+  if (launches) {
+    uint32_t gated = 0;  // photon rounds run inside the graph's conditional nodes: 3 kernels each
+    FR_CUDA(cudaMemcpy(&gated, c->rounds_run, sizeof gated, cudaMemcpyDeviceToHost));
+    *launches = c->launches + 3 * (int64_t)gated;
+  }
   c->ev_marks.clear();
   c->ev_used = 0;
   return FR_OK;
@@ -1061,7 +1124,18 @@ int fr_read_wave_counts(fr_ctx* c, uint32_t* eye_counts, uint32_t* photon_counts
                           cudaMemcpyDeviceToHost, c->stream));
   if (eye_rounds) *eye_rounds = kEyeRounds;
   if (photon_rounds) *photon_rounds = kPhotonRounds;
-  return fr_synchronize(c);
+  const int rc = fr_synchronize(c);
+  if (rc) return rc;
+  // Skipped rounds: their paths were run by the tail.
+  const auto fold = [](uint32_t* q, int rounds, uint32_t min_live) {
+    const int t = wave_tail_round(q, rounds, min_live);
+    if (t == rounds) return;
+    q[rounds] = q[t];
+    for (int r = t; r < rounds; ++r) q[r] = 0;
+  };
+  fold(eye_counts, kEyeRounds, kEyeTailMin);
+  fold(photon_counts, kPhotonRounds, kPhotonTailMin);
+  return FR_OK;
 }
 
 int fr_read_hitpoints(fr_ctx* c, float* pos_type, float* nrm_rough, float* out_mat, float* wgt_facet) {

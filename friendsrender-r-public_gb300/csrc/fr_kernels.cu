@@ -35,6 +35,17 @@ namespace {
 
 __device__ __forceinline__ bool near1(float s) { return fabsf(s - 1.0f) < kLt1e5; }  // SPPM.h:27-29
 
+// Round skipping (see kPhotonTailMin): the counters of a round are final
+// before its kernels start, so every kernel of the round decides alike.
+__device__ __forceinline__ bool round_skipped(const PathWave& w, int round) {
+  return round > 0 && *(volatile const uint32_t*)(w.qcount + round) < w.min_live;
+}
+__device__ __forceinline__ int tail_round(const PathWave& w, int rounds) {
+  int r = rounds > 0 ? 1 : 0;
+  while (r < rounds && *(volatile const uint32_t*)(w.qcount + r) >= w.min_live) ++r;
+  return r;
+}
+
 __device__ __forceinline__ float max3(V3 a) {
   return a.x > a.y ? (a.x > a.z ? a.x : a.z) : (a.y > a.z ? a.y : a.z);
 }
@@ -284,6 +295,7 @@ __global__ void __launch_bounds__(128) k_ew_start(CameraGPU cam, IterParams it, 
 // Closest hit of every path in queue `round`, for queues of coherent rays
 // (camera rays in pixel order): each warp takes 32 consecutive entries.
 __global__ void __launch_bounds__(128) k_wave_trace_static(SceneGPU sc, PathWave w, int round, int* err) {
+  if (round_skipped(w, round)) return;
   const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
   const uint32_t* q = w.queue[round & 1];
   for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
@@ -304,6 +316,7 @@ __global__ void __launch_bounds__(128) k_wave_trace_static(SceneGPU sc, PathWave
 // The traversal is trace_closest's (fr_trace.cuh), one node visit or leaf per
 // loop pass, so the hits are the same.
 __global__ void __launch_bounds__(128) k_wave_trace(SceneGPU sc, PathWave w, int round, int* err) {
+  if (round_skipped(w, round)) return;
   const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
   const uint32_t* q = w.queue[round & 1];
   uint32_t* fetch = w.tfetch + round;
@@ -415,6 +428,7 @@ __global__ void __launch_bounds__(128) k_wave_trace(SceneGPU sc, PathWave w, int
 // type (misses last), so that each warp of the shade kernel runs one
 // surface's code.
 __global__ void __launch_bounds__(256) k_wave_sort(SceneGPU sc, PathWave w, int round) {
+  if (round_skipped(w, round)) return;  // its shade kernel then finds no paths
   const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
   const uint32_t* q = w.queue[round & 1];
   uint32_t* mc = w.mcount + round * kShadeQueues;
@@ -497,7 +511,8 @@ __global__ void __launch_bounds__(128) k_ew_shade(SceneGPU sc, IterParams it, fl
 
 // Eye paths alive after the last wavefront round, each run to its end.
 __global__ void __launch_bounds__(128) k_ew_tail(SceneGPU sc, IterParams it, float rr5, float rr6, PathWave w,
-                                                 HitpointBuf hp, PixelState st, GridInfo* gi, int round, int* err) {
+                                                 HitpointBuf hp, PixelState st, GridInfo* gi, int rounds, int* err) {
+  const int round = tail_round(w, rounds);
   const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
   const uint32_t* q = w.queue[round & 1];
   const uint32_t stride = gridDim.x * blockDim.x;
@@ -889,7 +904,8 @@ __global__ void __launch_bounds__(128) k_pw_shade(SceneGPU sc, IterParams it, Ph
 constexpr uint32_t kTailPathsPerWarp = FR_TAIL_PATHS_PER_WARP;
 
 __global__ void __launch_bounds__(128) k_pw_tail(SceneGPU sc, IterParams it, PhotonSlots ph, PathWave w,
-                                                 uint32_t* counts, int round, int* err) {
+                                                 uint32_t* counts, int rounds, int* err) {
+  const int round = tail_round(w, rounds);
   const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
   const uint32_t* q = w.queue[round & 1];
   const uint32_t lane = threadIdx.x & 31u;
@@ -1335,6 +1351,20 @@ void launch_wave_trace(const SceneGPU& sc, PathWave w, int round, int grid, bool
     k_wave_trace_static<<<std::max(1, grid), 128, 0, s>>>(sc, w, round, err);
   else
     k_wave_trace<<<std::max(1, grid), 128, 0, s>>>(sc, w, round, err);
+}
+
+// Sets the condition of the graph IF node holding wavefront round `round`:
+// the round runs when it has at least w.min_live paths (the kernels' own
+// round_skipped rule).  Counts the rounds it lets run.
+__global__ void k_round_gate(cudaGraphConditionalHandle h, PathWave w, int round, uint32_t* rounds_run) {
+  const bool run = !round_skipped(w, round);
+  if (run) *rounds_run += 1u;
+  cudaGraphSetConditional(h, run ? 1u : 0u);
+}
+
+void launch_round_gate(cudaGraphConditionalHandle h, const PathWave& w, int round, uint32_t* rounds_run,
+                       cudaStream_t s) {
+  k_round_gate<<<1, 1, 0, s>>>(h, w, round, rounds_run);
 }
 
 void launch_wave_sort(const SceneGPU& sc, PathWave w, int round, int grid, cudaStream_t s) {

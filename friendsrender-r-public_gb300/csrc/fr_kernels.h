@@ -49,16 +49,32 @@ struct PhotonGrid {
 // sorts each round's hits into for the shade kernel.  qcount[r] counts the
 // paths of round r; every counter is zeroed once per iteration.
 // Rounds of trace/sort/shade before the tail kernel takes the paths still
-// alive.  Later rounds carry few paths and cost a launch sequence each, while
-// the tail advances a path by a bounce at the latency of one trace and shade.
+// alive.  A round with few paths is bound by the latency of its slowest path
+// and costs a launch sequence, while the tail advances each of its paths a
+// bounce at the latency of one trace and shade; so a round r >= 1 with fewer
+// than the pass's minimum of live paths is skipped (and with it every later
+// round, which then has none) and the tail starts from it.  The maximum is
+// reached only by scenes whose paths stay alive long (glass).
 #ifndef FR_EYE_ROUNDS
 #define FR_EYE_ROUNDS 8
 #endif
 #ifndef FR_PHOTON_ROUNDS
-#define FR_PHOTON_ROUNDS 5
+#define FR_PHOTON_ROUNDS 16
+#endif
+#ifndef FR_EYE_TAIL_MIN
+#define FR_EYE_TAIL_MIN 0
+#endif
+#ifndef FR_PHOTON_TAIL_MIN
+#define FR_PHOTON_TAIL_MIN 32768
 #endif
 constexpr int kEyeRounds = FR_EYE_ROUNDS;
 constexpr int kPhotonRounds = FR_PHOTON_ROUNDS;
+constexpr uint32_t kEyeTailMin = FR_EYE_TAIL_MIN;        // 0: every round runs
+constexpr uint32_t kPhotonTailMin = FR_PHOTON_TAIL_MIN;
+// In the captured iteration graph, photon rounds from this one on sit in
+// conditional (IF) nodes, so skipped rounds launch nothing; the earlier ones
+// are plain launches (skipping by themselves when they have too few paths).
+constexpr int kPhotonGatedFrom = 5;
 constexpr int kWaveRounds = kEyeRounds > kPhotonRounds ? kEyeRounds : kPhotonRounds;  // counter layout
 constexpr int kShadeQueues = 5;  // one per surface type, then misses
 struct PathWave {
@@ -70,7 +86,16 @@ struct PathWave {
   uint32_t* mcount;       // kWaveRounds * kShadeQueues counters
   uint32_t* tfetch;       // kWaveRounds counters: queue entries claimed by the trace kernel
   uint32_t cap;
+  uint32_t min_live;      // rounds r >= 1 with fewer live paths go to the tail
 };
+
+// The round the tail kernel starts from, after at most `rounds` rounds (the
+// host's copy of the rule the kernels apply to the counters).
+inline int wave_tail_round(const uint32_t* qcount, int rounds, uint32_t min_live) {
+  int r = rounds > 0 ? 1 : 0;
+  while (r < rounds && qcount[r] >= min_live) ++r;
+  return r;
+}
 
 // Per-pixel progressive state (SharedHitPoint, SPPM.h:112-126): tau in FP64.
 struct PixelState {
@@ -108,6 +133,8 @@ void launch_ew_start(const CameraGPU& cam, const IterParams& it, PathWave w, cud
 // keep (camera rays in pixel order); otherwise lanes fetch rays dynamically.
 void launch_wave_trace(const SceneGPU& sc, PathWave w, int round, int grid, bool coherent, int* err, cudaStream_t s);
 void launch_wave_sort(const SceneGPU& sc, PathWave w, int round, int grid, cudaStream_t s);
+void launch_round_gate(cudaGraphConditionalHandle h, const PathWave& w, int round, uint32_t* rounds_run,
+                       cudaStream_t s);
 void launch_ew_shade(const SceneGPU& sc, const IterParams& it, const float* rr_eye, PathWave w, HitpointBuf hp,
                      PixelState st, GridInfo* gi, int round, int grid, cudaStream_t s);
 void launch_ew_tail(const SceneGPU& sc, const IterParams& it, const float* rr_eye, PathWave w, HitpointBuf hp,

@@ -292,8 +292,9 @@ int fr_guide_gradient(fr_ctx* ctx, int32_t n, const float* samples, float* grad,
 
 /* No reference counterpart: the wavefront queue lengths of the last
  * iteration.  eye_counts[r] / photon_counts[r] is the number of paths traced
- * in round r (r < *eye_rounds / *photon_rounds) and, at r = rounds, the number
- * handed to the tail kernel; arrays of FR_MAX_WAVE_ROUNDS + 1 entries. */
+ * in round r (r < *eye_rounds / *photon_rounds; 0 for rounds skipped because
+ * too few paths were left) and, at r = rounds, the number the tail kernel
+ * finished; arrays of FR_MAX_WAVE_ROUNDS + 1 entries. */
 #define FR_MAX_WAVE_ROUNDS 16
 int fr_read_wave_counts(fr_ctx* ctx, uint32_t* eye_counts, uint32_t* photon_counts, int32_t* eye_rounds,
                         int32_t* photon_rounds);
