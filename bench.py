@@ -211,7 +211,7 @@ def rel_mse(img, ref):
     return float(((a - b) ** 2 / (b * b + REL_MSE_EPS)).mean())
 
 
-def guide_eval(plain_iters=128, ref_iters=1024, photons=CAUSTIC_PHOTONS, scene=None, log=None):
+def guide_eval(plain_iters=128, ref_iters=1024, photons=CAUSTIC_PHOTONS, scene=None, log=None, eager=False):
     """Plain and guided SPPM on the caustic box against a long plain run (the
     reference image, FP64 tau), all resolved with the standard estimate
     tau / (pi R^2 photons emitted) and with paths ended where the reference's
@@ -221,7 +221,9 @@ def guide_eval(plain_iters=128, ref_iters=1024, photons=CAUSTIC_PHOTONS, scene=N
     the guided run's wall time to first reach it (checked at iteration marks
     12.5% apart) and its error at the plain run's wall time are reported.
     Wall time is fr_iterate + fr_synchronize, the guide's training included;
-    the resolves at the marks are not timed."""
+    the resolves at the marks are not timed.  eager: iterations launched
+    directly (stage profiler on) instead of as the captured graph, whose
+    conditional nodes ncu cannot profile into; for kernel profiles only."""
     from frsppm import abi, scenes
     scene = scene or scenes.caustic_box()
     kw = dict(alpha=CAUSTIC_ALPHA, radius=CAUSTIC_RADIUS,
@@ -232,8 +234,13 @@ def guide_eval(plain_iters=128, ref_iters=1024, photons=CAUSTIC_PHOTONS, scene=N
     if (first + ref_iters + 1) * max(photons, npix) >= 1 << 32:
         raise ValueError('reference run would wrap the 32-bit seeds into the compared runs')
     t0 = time.perf_counter()
+    def direct(r, iters):
+        if eager:
+            r.profile(True, max_iterations=iters + 1)
+
     with abi.Renderer(scene, photons, **kw) as ref:
         ref.seek(first)
+        direct(ref, ref_iters)
         done = 0
         while done < ref_iters:
             n = min(64, ref_iters - done)
@@ -253,6 +260,7 @@ def guide_eval(plain_iters=128, ref_iters=1024, photons=CAUSTIC_PHOTONS, scene=N
         curve = []
         extra = dict(guide=True) if guided else {}
         with abi.Renderer(scene, photons, **kw, **extra) as r:
+            direct(r, max_run + len(marks))
             r.synchronize()
             t, done, k = 0.0, 0, 0
             while True:
@@ -303,12 +311,13 @@ def main():
     ap.add_argument('--guide-plain-iters', type=int, default=128)
     ap.add_argument('--guide-ref-iters', type=int, default=1024)
     ap.add_argument('--guide-photons', type=int, default=CAUSTIC_PHOTONS)
+    ap.add_argument('--eager', action='store_true', help='guide eval: direct launches (for ncu)')
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
     if args.guide_eval:
         out = guide_eval(args.guide_plain_iters, args.guide_ref_iters, args.guide_photons,
-                         log=lambda s: print(s, file=sys.stderr, flush=True))
+                         log=lambda s: print(s, file=sys.stderr, flush=True), eager=args.eager)
         print(json.dumps(out))
         return 0
 

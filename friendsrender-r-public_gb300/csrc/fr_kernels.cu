@@ -135,8 +135,9 @@ __device__ __forceinline__ bool eye_top(EyeState& s, Rng& rng, float rr5, float 
 // The rest of one pass after the closest hit (SPPM.cpp:123-305).  Returns
 // kHitHit after writing a hitpoint, kHitNone when the path ends without one,
 // and -1 when it goes on.
+template <bool kEndDegenerate>
 __device__ __forceinline__ int eye_shade(const SceneGPU& sc, const HitpointBuf& hp, int i, EyeState& s, Rng& rng,
-                                         const Hit& hit, float rr5, float rr6, uint32_t flags) {
+                                         const Hit& hit, float rr5, float rr6) {
   Geom g;
   calc_geometry(sc, hit, g);
   g.normal = dot(g.normal, s.d) > 0.0f ? -g.normal : g.normal;
@@ -178,7 +179,7 @@ __device__ __forceinline__ int eye_shade(const SceneGPU& sc, const HitpointBuf& 
   if (pdf < 0.0f) return kHitNone;
   // The reference goes on with a NaN BSDF value or pdf, or a zero pdf, which
   // gives the hitpoint a NaN or infinite weight; the flag ends such paths.
-  if ((flags & kFlagEndDegenerate) && !(brdf >= kLt1e8 && pdf > 0.0f)) return kHitNone;
+  if (kEndDegenerate && !(brdf >= kLt1e8 && pdf > 0.0f)) return kHitNone;
   s.thr = s.thr * (g.albedo * cs * brdf);
   s.PDF *= pdf;
   s.o = nxt_o; s.d = nd; s.ix = nix;
@@ -471,6 +472,7 @@ __device__ __forceinline__ bool wave_hit(const PathWave& w, uint32_t i, Hit& h) 
   return h.tri >= 0;
 }
 
+template <bool kEndDegenerate>
 __global__ void __launch_bounds__(128) k_ew_shade(SceneGPU sc, IterParams it, float rr5, float rr6, PathWave w,
                                                   HitpointBuf hp, PixelState st, GridInfo* gi, int round) {
   const ShadeQueues sq(w, round);
@@ -493,7 +495,7 @@ __global__ void __launch_bounds__(128) k_ew_shade(SceneGPU sc, IterParams it, fl
       } else {
         Rng rng(eye_seed(it, (int)i));
         rng.seek(s.draw);
-        const int r = eye_shade(sc, hp, (int)i, s, rng, h, rr5, rr6, it.flags);
+        const int r = eye_shade<kEndDegenerate>(sc, hp, (int)i, s, rng, h, rr5, rr6);
         if (r < 0) {
           s.draw = rng.draw;
           store_eye(w, (int)i, s);
@@ -510,6 +512,7 @@ __global__ void __launch_bounds__(128) k_ew_shade(SceneGPU sc, IterParams it, fl
 }
 
 // Eye paths alive after the last wavefront round, each run to its end.
+template <bool kEndDegenerate>
 __global__ void __launch_bounds__(128) k_ew_tail(SceneGPU sc, IterParams it, float rr5, float rr6, PathWave w,
                                                  HitpointBuf hp, PixelState st, GridInfo* gi, int rounds, int* err) {
   const int round = tail_round(w, rounds);
@@ -532,7 +535,7 @@ __global__ void __launch_bounds__(128) k_ew_tail(SceneGPU sc, IterParams it, flo
           hit_type = kHitOnlyDirect;
           break;
         }
-        const int r = eye_shade(sc, hp, i, s, rng, h, rr5, rr6, it.flags);
+        const int r = eye_shade<kEndDegenerate>(sc, hp, i, s, rng, h, rr5, rr6);
         if (r >= 0) {
           hit_type = r;
           break;
@@ -665,6 +668,7 @@ __device__ __forceinline__ bool photon_top(PhotonState& s) {
 
 // The rest of one pass after the closest hit (SPPM.cpp:556-670); false ends
 // the path.
+template <bool kEndDegenerate>
 __device__ __forceinline__ bool photon_shade(const SceneGPU& sc, const IterParams& it, const PhotonSlots& ph, int i,
                                              PhotonState& s, const Hit& hit) {
   Rng rng(photon_seed(it, i));
@@ -714,7 +718,7 @@ __device__ __forceinline__ bool photon_shade(const SceneGPU& sc, const IterParam
   const float cs = fmaxf(0.0f, fminf(1.0f, dot(nd, on)));
   if (brdf < kLt1e8) return false;
   if (pdf < 0.0f) return false;
-  if ((it.flags & kFlagEndDegenerate) && !(brdf >= kLt1e8 && pdf > 0.0f)) return false;  // as in eye_shade
+  if (kEndDegenerate && !(brdf >= kLt1e8 && pdf > 0.0f)) return false;  // as in eye_shade
   s.thr = s.thr * (g.albedo * cs * brdf);
   s.PDF *= pdf;
   s.o = nxt_o; s.d = nd; s.ix = nix;
@@ -867,6 +871,7 @@ __global__ void __launch_bounds__(128) k_pw_emit_guided(SceneGPU sc, IterParams 
   g.importance[i] = 0.0f;
 }
 
+template <bool kEndDegenerate>
 __global__ void __launch_bounds__(128) k_pw_shade(SceneGPU sc, IterParams it, PhotonSlots ph, PathWave w,
                                                   uint32_t* counts, int round) {
   const ShadeQueues sq(w, round);
@@ -882,7 +887,7 @@ __global__ void __launch_bounds__(128) k_pw_shade(SceneGPU sc, IterParams it, Ph
       PhotonState s;
       load_state(w, (int)i, s);
       Hit h;
-      const bool alive = wave_hit(w, i, h) && photon_shade(sc, it, ph, (int)i, s, h) && photon_top(s);
+      const bool alive = wave_hit(w, i, h) && photon_shade<kEndDegenerate>(sc, it, ph, (int)i, s, h) && photon_top(s);
       if (alive) {
         store_state(w, (int)i, s);
         keep = true;
@@ -903,6 +908,7 @@ __global__ void __launch_bounds__(128) k_pw_shade(SceneGPU sc, IterParams it, Ph
 #endif
 constexpr uint32_t kTailPathsPerWarp = FR_TAIL_PATHS_PER_WARP;
 
+template <bool kEndDegenerate>
 __global__ void __launch_bounds__(128) k_pw_tail(SceneGPU sc, IterParams it, PhotonSlots ph, PathWave w,
                                                  uint32_t* counts, int rounds, int* err) {
   const int round = tail_round(w, rounds);
@@ -919,7 +925,7 @@ __global__ void __launch_bounds__(128) k_pw_tail(SceneGPU sc, IterParams it, Pho
     while (true) {
       Hit h;
       if (!trace_closest(sc, s.o, s.d, kRayOffset, h, err)) break;
-      if (!photon_shade(sc, it, ph, i, s, h) || !photon_top(s)) break;
+      if (!photon_shade<kEndDegenerate>(sc, it, ph, i, s, h) || !photon_top(s)) break;
     }
     photon_finish(it, ph, counts, i, s.k);
   }
@@ -1085,6 +1091,9 @@ __device__ __forceinline__ double tau_update(double tau, float phi, float a, flo
 #endif
 constexpr int kGatherGroup = FR_GATHER_GROUP;
 
+// kImportance: also add each photon's contribution to its path's importance
+// (the guide's training signal); the plain gather keeps its registers.
+template <bool kImportance>
 __global__ void __launch_bounds__(256) k_gather(SceneGPU sc, IterParams it, HitpointBuf hp, PhotonGrid g,
                                                const GridInfo* gip, PixelState st, int32_t* dbg_m, float4* dbg_phi,
                                                float* importance) {
@@ -1167,7 +1176,7 @@ __global__ void __launch_bounds__(256) k_gather(SceneGPU sc, IterParams it, Hitp
         const FParam p{indir, out, nn, Ii, Io, hn.w, mat.extinction, mat.reflectance};
         const float brdf = surface_brdf(type, p);
         const V3 add = v3(hw.x, hw.y, hw.z) * brdf * v3(f4.x, f4.y, f4.z) / f4.w;
-        if (importance) atomicAdd(importance + (__float_as_uint(d4.w) >> 5), add.x + add.y + add.z);
+        if (kImportance) atomicAdd(importance + (__float_as_uint(d4.w) >> 5), add.x + add.y + add.z);
         float y, t;
         y = add.x - kx; t = sx + y; kx = (t - sx) - y; sx = t;
         y = add.y - ky; t = sy + y; ky = (t - sy) - y; sy = t;
@@ -1338,7 +1347,7 @@ void launch_next_step(uint32_t* step, cudaStream_t s) { k_next_step<<<1, 1, 0, s
 
 int pw_tail_blocks_per_sm() {
   int b = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pw_tail, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pw_tail<false>, 128, 0);
   return b;
 }
 
@@ -1373,12 +1382,18 @@ void launch_wave_sort(const SceneGPU& sc, PathWave w, int round, int grid, cudaS
 
 void launch_ew_shade(const SceneGPU& sc, const IterParams& it, const float* rr_eye, PathWave w, HitpointBuf hp,
                      PixelState st, GridInfo* gi, int round, int grid, cudaStream_t s) {
-  k_ew_shade<<<std::max(1, grid), 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, round);
+  if (it.flags & kFlagEndDegenerate)
+    k_ew_shade<true><<<std::max(1, grid), 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, round);
+  else
+    k_ew_shade<false><<<std::max(1, grid), 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, round);
 }
 
 void launch_ew_tail(const SceneGPU& sc, const IterParams& it, const float* rr_eye, PathWave w, HitpointBuf hp,
                     PixelState st, GridInfo* gi, int round, int grid, int* err, cudaStream_t s) {
-  k_ew_tail<<<std::max(1, grid), 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, round, err);
+  if (it.flags & kFlagEndDegenerate)
+    k_ew_tail<true><<<std::max(1, grid), 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, round, err);
+  else
+    k_ew_tail<false><<<std::max(1, grid), 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, round, err);
 }
 
 void launch_pw_emit(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, PathWave w, uint32_t* counts,
@@ -1388,12 +1403,18 @@ void launch_pw_emit(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, Pa
 
 void launch_pw_shade(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, PathWave w, uint32_t* counts,
                      int round, int grid, cudaStream_t s) {
-  k_pw_shade<<<std::max(1, grid), 128, 0, s>>>(sc, it, ph, w, counts, round);
+  if (it.flags & kFlagEndDegenerate)
+    k_pw_shade<true><<<std::max(1, grid), 128, 0, s>>>(sc, it, ph, w, counts, round);
+  else
+    k_pw_shade<false><<<std::max(1, grid), 128, 0, s>>>(sc, it, ph, w, counts, round);
 }
 
 void launch_pw_tail(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, PathWave w, uint32_t* counts,
                     int round, int grid, int* err, cudaStream_t s) {
-  k_pw_tail<<<std::max(1, grid), 128, 0, s>>>(sc, it, ph, w, counts, round, err);
+  if (it.flags & kFlagEndDegenerate)
+    k_pw_tail<true><<<std::max(1, grid), 128, 0, s>>>(sc, it, ph, w, counts, round, err);
+  else
+    k_pw_tail<false><<<std::max(1, grid), 128, 0, s>>>(sc, it, ph, w, counts, round, err);
 }
 
 int photon_pass_blocks_per_sm() {
@@ -1465,7 +1486,10 @@ int launch_scan(uint32_t* in, uint32_t* out, uint32_t n, ScanTemp& t, cudaStream
 void launch_gather_update(const SceneGPU& sc, const IterParams& it, HitpointBuf hp, PhotonGrid g, const GridInfo* gi,
                           PixelState st, int32_t* dbg_m, float4* dbg_phi, float* importance, int resident_blocks,
                           cudaStream_t s) {
-  k_gather<<<std::max(1, resident_blocks), 256, 0, s>>>(sc, it, hp, g, gi, st, dbg_m, dbg_phi, importance);
+  if (importance)
+    k_gather<true><<<std::max(1, resident_blocks), 256, 0, s>>>(sc, it, hp, g, gi, st, dbg_m, dbg_phi, importance);
+  else
+    k_gather<false><<<std::max(1, resident_blocks), 256, 0, s>>>(sc, it, hp, g, gi, st, dbg_m, dbg_phi, importance);
 }
 
 void launch_pw_emit_guided(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, PathWave w, uint32_t* counts,
@@ -1475,7 +1499,7 @@ void launch_pw_emit_guided(const SceneGPU& sc, const IterParams& it, PhotonSlots
 
 int gather_blocks_per_sm() {
   int b = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_gather, 256, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_gather<false>, 256, 0);
   return b;
 }
 
