@@ -903,10 +903,19 @@ __global__ void __launch_bounds__(128) k_pw_shade(SceneGPU sc, IterParams it, Ph
 // At most kTailPathsPerWarp paths share a warp: a tail path's bounces are a
 // chain of dependent traversals, and the fewer divergent paths a warp carries,
 // the sooner each of its paths advances.
+// Paths per warp in the photon tail: the fewest (a power of two) that give
+// every path a lane of the resident grid, at most kTailPathsPerWarp.  Fewer
+// paths per warp diverge less, and the tail's time is the latency of its
+// longest path, so idle lanes cost nothing while every path has a lane.
 #ifndef FR_TAIL_PATHS_PER_WARP
 #define FR_TAIL_PATHS_PER_WARP 16
 #endif
 constexpr uint32_t kTailPathsPerWarp = FR_TAIL_PATHS_PER_WARP;
+__device__ __forceinline__ uint32_t tail_paths_per_warp(uint32_t n, uint32_t nwarps) {
+  uint32_t ppw = 1;
+  while (ppw < kTailPathsPerWarp && (uint64_t)ppw * nwarps < n) ppw <<= 1;
+  return ppw;
+}
 
 template <bool kEndDegenerate>
 __global__ void __launch_bounds__(128) k_pw_tail(SceneGPU sc, IterParams it, PhotonSlots ph, PathWave w,
@@ -915,10 +924,11 @@ __global__ void __launch_bounds__(128) k_pw_tail(SceneGPU sc, IterParams it, Pho
   const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
   const uint32_t* q = w.queue[round & 1];
   const uint32_t lane = threadIdx.x & 31u;
-  if (lane >= kTailPathsPerWarp) return;
   const uint32_t warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const uint32_t nwarps = (gridDim.x * blockDim.x) >> 5;
-  for (uint32_t j = warp * kTailPathsPerWarp + lane; j < n; j += nwarps * kTailPathsPerWarp) {
+  const uint32_t ppw = tail_paths_per_warp(n, nwarps);
+  if (lane >= ppw) return;
+  for (uint32_t j = warp * ppw + lane; j < n; j += nwarps * ppw) {
     const int i = (int)q[j];
     PhotonState s;
     load_state(w, i, s);

@@ -65,7 +65,7 @@ struct PhotonGrid {
 #define FR_EYE_TAIL_MIN 0
 #endif
 #ifndef FR_PHOTON_TAIL_MIN
-#define FR_PHOTON_TAIL_MIN 32768
+#define FR_PHOTON_TAIL_MIN 16384
 #endif
 constexpr int kEyeRounds = FR_EYE_ROUNDS;
 constexpr int kPhotonRounds = FR_PHOTON_ROUNDS;
