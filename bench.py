@@ -298,6 +298,69 @@ def guide_eval(plain_iters=128, ref_iters=1024, photons=CAUSTIC_PHOTONS, scene=N
     }
 
 
+LARGE_PHOTONS = 8_000_000
+LARGE_WORKLOAD = ('large scene: 20,000,004 triangles (400 copies of a 50,000-triangle seeded displaced geodesic '
+                  'sphere, flattened), 16 materials of all four surface types, 4096^2 RGBA8 albedo/roughness/normal '
+                  'textures, 512^2 textured light, 3840x2160 thin lens aperture 0.02, 8M photon paths/iteration, '
+                  'learned guide on, alpha 0.7, r0 0.02')
+
+
+def run_large(args):
+    """The large-scene workload: photon paths/s of guided SPPM iterations
+    (graph replays, CUDA events on the renderer's stream; the working set is
+    far larger than L2), and the same through the C-ABI with the image read
+    back every step."""
+    import torch
+    from frsppm import abi, scenes
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    t0 = time.perf_counter()
+    scene = scenes.large_scene()
+    gen_s = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    r = abi.Renderer(scene, LARGE_PHOTONS, alpha=ALPHA, radius=RADIUS, guide=True,
+                     flags=abi.FLAG_END_DEGENERATE_PATHS)
+    setup_s = time.perf_counter() - t0
+    stats = r.stats()
+    npix = r.width * r.height
+    stream = torch.cuda.ExternalStream(r.stream())
+    W = max(3, args.warmup)
+    r.iterate(W)
+    l0 = r.profile_read()[2]
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clk:
+        a.record(stream)
+        r.iterate(args.steps, sync=False)
+        b.record(stream)
+        stream.synchronize()
+    ms = a.elapsed_time(b)
+    launches = r.profile_read()[2] - l0
+    host = torch.empty((npix, 4), dtype=torch.float32, pin_memory=True)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r.iterate(1, sync=False)
+        abi._check(abi._lib.fr_resolve(r.h, abi.C.c_void_p(host.data_ptr())), 'fr_resolve')
+    e2e_s = time.perf_counter() - t0
+    eye_q, photon_q = r.wave_counts()
+    r.close()
+    out = {'metric': METRIC, 'value': LARGE_PHOTONS * args.steps / (ms / 1000.0), 'unit': UNIT, 'n_gpus': 1,
+           'steps': args.steps, 'warmup': W, 'ms_per_step': ms / args.steps, 'higher_is_better': True,
+           'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded scene)',
+           'config': {'workload': LARGE_WORKLOAD, 'photons_per_step': LARGE_PHOTONS, 'pixels': npix,
+                      'triangles': stats['triangles'], 'bvh_nodes': stats['bvh_nodes'],
+                      'l2': 'working set far above L2 (photon slots alone 12.3 GB)'},
+           'hitpoint_updates_per_s': npix * args.steps / (ms / 1000.0),
+           'e2e': {'value': LARGE_PHOTONS * args.steps / e2e_s, 'unit': UNIT, 'h2d_bytes_per_step': 0,
+                   'd2h_bytes_per_step': npix * 16, 'scene_generation_s': gen_s, 'setup_s': setup_s,
+                   'device_bytes': int(stats['device_bytes'])},
+           'gpu_launches': launches, 'clocks': clk.summary(),
+           'tail_paths_per_step': [int(eye_q[-1]), int(photon_q[-1])]}
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -312,9 +375,13 @@ def main():
     ap.add_argument('--guide-ref-iters', type=int, default=1024)
     ap.add_argument('--guide-photons', type=int, default=CAUSTIC_PHOTONS)
     ap.add_argument('--eager', action='store_true', help='guide eval: direct launches (for ncu)')
+    ap.add_argument('--workload', default='mixed', choices=['mixed', 'large'],
+                    help='large: the 20M-triangle scene (its own JSON line)')
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
+    if args.workload == 'large':
+        return run_large(args)
     if args.guide_eval:
         out = guide_eval(args.guide_plain_iters, args.guide_ref_iters, args.guide_photons,
                          log=lambda s: print(s, file=sys.stderr, flush=True), eager=args.eager)

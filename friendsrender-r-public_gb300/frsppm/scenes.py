@@ -327,6 +327,114 @@ def caustic_box(seed=CONFIG_SEED_BASE + 2, width=1024, height=1024, n_spheres=50
     return scene
 
 
+def geodesic_sphere(freq):
+    """Unit geodesic sphere: every face of an icosahedron split into freq^2
+    triangles and projected to the sphere.  Returns unit directions (20*freq^2,
+    3, 3), counter-clockwise seen from outside."""
+    t = (1.0 + math.sqrt(5.0)) / 2.0
+    v = np.array([[-1, t, 0], [1, t, 0], [-1, -t, 0], [1, -t, 0], [0, -1, t], [0, 1, t], [0, -1, -t], [0, 1, -t],
+                  [t, 0, -1], [t, 0, 1], [-t, 0, -1], [-t, 0, 1]], np.float64)
+    v /= np.linalg.norm(v, axis=1, keepdims=True)
+    faces = [(0, 11, 5), (0, 5, 1), (0, 1, 7), (0, 7, 10), (0, 10, 11), (1, 5, 9), (5, 11, 4), (11, 10, 2),
+             (10, 7, 6), (7, 1, 8), (3, 9, 4), (3, 4, 2), (3, 2, 6), (3, 6, 8), (3, 8, 9), (4, 9, 5),
+             (2, 4, 11), (6, 2, 10), (8, 6, 7), (9, 8, 1)]
+    n = int(freq)
+    ii, jj = [], []
+    for i in range(n):
+        for j in range(n - i):
+            ii.append((i, j, i + 1, j, i, j + 1))
+            if i + j < n - 1:
+                ii.append((i + 1, j, i + 1, j + 1, i, j + 1))
+    idx = np.asarray(ii, np.float64).reshape(-1, 3, 2) / n  # (n^2, 3, [bary_b, bary_c])
+    out = []
+    for a, b, c in faces:
+        A, Bv, Cv = v[a], v[b], v[c]
+        P = A + idx[..., :1] * (Bv - A) + idx[..., 1:2] * (Cv - A)
+        out.append(P / np.linalg.norm(P, axis=-1, keepdims=True))
+    return np.concatenate(out)
+
+
+def _displaced_sphere(rng, freq, amp, waves=12):
+    """A geodesic sphere displaced radially by a seeded sum of plane waves
+    h(d) = amp * sum_k a_k cos(f_k . d + p_k): positions, analytic normals
+    and spherical UVs (each (tris, 3, k))."""
+    d = geodesic_sphere(freq)
+    f = rng.normal(size=(waves, 3)) * 3.0
+    a = rng.uniform(0.3, 1.0, waves) / waves
+    ph = rng.uniform(0.0, 2.0 * math.pi, waves)
+    arg = d @ f.T + ph
+    h = amp * (np.cos(arg) @ a)
+    g = -amp * (np.sin(arg) * a) @ f                          # gradient of h
+    gt = g - np.sum(g * d, axis=-1, keepdims=True) * d       # its tangential part
+    r = 1.0 + h
+    pos = d * r[..., None]
+    nrm = d - gt / r[..., None]
+    nrm /= np.linalg.norm(nrm, axis=-1, keepdims=True)
+    uv = np.stack([np.arctan2(d[..., 2], d[..., 0]) / (2 * math.pi) + 0.5,
+                   np.arccos(np.clip(d[..., 1], -1.0, 1.0)) / math.pi], -1)
+    return pos, nrm, uv
+
+
+def large_scene(seed=CONFIG_SEED_BASE + 4, width=3840, height=2160, instances=400, freq=50, tex_size=4096,
+                light_tex=512, aperture=0.02, extent=10.0):
+    """Large scene: ``instances`` copies of one seeded displaced geodesic sphere
+    of 20*freq^2 triangles (50,000 with the default), each scaled, turned about
+    y and placed on a textured ground quad, flattened into one triangle list
+    (the boundary takes no instances).  16 materials cycle over the copies,
+    four of each type (diffuse with the ground's textures, specular, GGX
+    conductor, GGX dielectric IOR 1.5); the ground carries ``tex_size``^2 RGBA8
+    albedo/roughness/normal textures; a ``light_tex``^2 textured area light;
+    thin-lens camera (aperture ``aperture``).  With the defaults: 20,000,004
+    triangles at 3840x2160."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    textures = [noise_texture(rng, tex_size, 'albedo'), noise_texture(rng, tex_size, 'roughness'),
+                noise_texture(rng, tex_size, 'normal'), noise_texture(rng, light_tex, 'emission')]
+    mats = [material('ground', DIFFUSE, (0.7, 0.7, 0.7), tex_albedo=0, tex_roughness=1, tex_bump=2),
+            material('light', DIFFUSE, (1, 1, 1), emission=(30.0, 28.0, 25.0), tex_albedo=3)]
+    for k in range(16):
+        mtype = k % 4
+        rough = float(rng.uniform(0.05, 0.5))
+        col = tuple(float(x) for x in rng.uniform(0.3, 0.95, 3))
+        name = 'm%02d' % k
+        if mtype == DIFFUSE:
+            mats.append(material(name, DIFFUSE, col, tex_albedo=0, tex_roughness=1, tex_bump=2))
+        elif mtype == METAL:
+            mats.append(material(name, METAL, col, sppm=False))
+        elif mtype == GGX_CONDUCTOR:
+            mats.append(material(name, GGX_CONDUCTOR, col, roughness=rough, index=1.1978, extinction=7.0488))
+        else:
+            mats.append(material(name, GGX_DIELECTRIC, (0.98, 0.98, 0.98), roughness=rough, index=1.5,
+                                 opaque=False, sppm=False))
+    base_p, base_n, base_uv = _displaced_sphere(rng, freq, 0.08)
+    ext = float(extent)
+    side = int(math.ceil(math.sqrt(instances)))
+    cell = 2.0 * ext / side
+    b = _Builder()
+    b.quad((-ext, 0, -ext), (-ext, 0, ext), (ext, 0, ext), (ext, 0, -ext), (0, 1, 0), 0,
+           uvs=((0, 0), (0, 8), (8, 8), (8, 0)))
+    for k in range(instances):
+        gx, gz = k % side, k // side
+        rad = float(rng.uniform(0.2, 0.45)) * cell
+        cx = -ext + (gx + 0.5) * cell + float(rng.uniform(-0.1, 0.1)) * cell
+        cz = -ext + (gz + 0.5) * cell + float(rng.uniform(-0.1, 0.1)) * cell
+        R = _rot_y(float(rng.uniform(0.0, 360.0)))
+        pos = (base_p @ R.T) * rad + np.array([cx, 1.1 * rad + 1e-3, cz])
+        b.tris(pos, base_n @ R.T, base_uv, 2 + k % 16)
+    lh, ly = 0.3 * ext, 1.2 * ext
+    b.quad((-lh, ly, -lh), (lh, ly, -lh), (lh, ly, lh), (-lh, ly, lh), (0, -1, 0), 1)
+    scene = b.build()
+    scene.update(materials=mats, textures=textures,
+                 camera=_camera(THINLENS, width, height, (0.0, 0.55 * ext, -1.55 * ext), (0.0, 0.0, 0.1 * ext),
+                                40.0, focal=0.9, dist=1.0, lens=aperture))
+    return scene
+
+
+def small_large_scene(seed=CONFIG_SEED_BASE + 104):
+    """The large scene's construction at a size for tests: 16 copies of a
+    2,000-triangle sphere, 64x36 pixels, 64^2 textures."""
+    return large_scene(seed=seed, width=64, height=36, instances=16, freq=10, tex_size=64, light_tex=32)
+
+
 def small_caustic(seed=CONFIG_SEED_BASE + 102, width=96, height=96):
     """The caustic scene at a size for tests: 12 coarser spheres, 96x96."""
     return caustic_box(seed=seed, width=width, height=height, n_spheres=12, n_lat=12, n_lon=16, light_tex=64)

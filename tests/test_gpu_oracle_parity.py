@@ -15,6 +15,10 @@ CASES = {
     'mixed128x72': (lambda s: s.mixed_materials(width=128, height=72, n_spheres=24, field_n=48, tex_size=128,
                                                 light_tex=64, n_lat=12, n_lon=16, extent=0.8, aperture=0.05),
                     20000, 3, 0.7, 0.02),
+    # The caustic box (glass spheres, slit) and the large scene's construction
+    # (displaced geodesic spheres, instanced and flattened), small.
+    'caustic96': (lambda s: s.small_caustic(), 20000, 3, 0.7, 0.01),
+    'large64x36': (lambda s: s.small_large_scene(), 20000, 3, 0.7, 0.02),
 }
 
 
