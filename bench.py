@@ -361,6 +361,77 @@ def run_large(args):
     return 0
 
 
+BATCH_WORKLOAD = ('batched uneven SPPM: 64 seeded scenes of the mixed-materials construction, triangles '
+                  'log-uniform over 10k-2M (30.5M in all), resolutions uniform over 128^2/256^2/512^2/1024^2, '
+                  '50k-1M photon paths/iteration each (33.8M in all), 256^2 textures, alpha 0.7, r0 0.02; '
+                  'all contexts advanced together by fr_iterate_batch, each autotuned by fr_autotune')
+
+
+def run_batch(args):
+    """The batched workload: one step is one iteration of every scene
+    (fr_iterate_batch).  value = photon paths of all scenes / wall time of the
+    batch steps; the same scenes iterated one after another (each context's
+    graph-replay time, CUDA events) are reported beside it."""
+    # More hardware queues for the contexts' streams (read at context creation).
+    os.environ.setdefault('CUDA_DEVICE_MAX_CONNECTIONS', '32')
+    import multiprocessing
+    from concurrent.futures import ProcessPoolExecutor
+    from frsppm import scenes
+    specs = scenes.batch_specs()
+    t0 = time.perf_counter()
+    with ProcessPoolExecutor(max_workers=min(16, os.cpu_count() or 1),
+                             mp_context=multiprocessing.get_context('spawn')) as ex:
+        scene_list = list(ex.map(scenes.batch_scene, specs))
+    gen_s = time.perf_counter() - t0
+    import torch
+    from frsppm import abi
+    torch.cuda.set_device(dist_env()[2])
+    t0 = time.perf_counter()
+    rs = [abi.Renderer(sc, sp['photons'], alpha=ALPHA, radius=RADIUS) for sc, sp in zip(scene_list, specs)]
+    setup_s = time.perf_counter() - t0
+    tuned = [r.autotune(1) if not args.no_autotune else None for r in rs]
+    # One after another: each context's graph replays alone.
+    seq_ms = 0.0
+    for r in rs:
+        s = torch.cuda.ExternalStream(r.stream())
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        r.iterate(1)
+        a.record(s)
+        r.iterate(2, sync=False)
+        b.record(s)
+        r.synchronize()
+        seq_ms += a.elapsed_time(b) / 2
+    W = max(3, args.warmup)
+    abi.iterate_batch(rs, W)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    abi.iterate_batch(rs, args.steps)
+    dt = time.perf_counter() - t0
+    photons = sum(sp['photons'] for sp in specs)
+    pixels = sum(r.width * r.height for r in rs)
+    dev = sum(r.stats()['device_bytes'] for r in rs)
+    tris = sum(len(sc['pos']) for sc in scene_list)
+    for r in rs:
+        r.close()
+    hist = {}
+    for t in tuned:
+        hist[str(t)] = hist.get(str(t), 0) + 1
+    out = {'metric': METRIC, 'value': photons * args.steps / dt, 'unit': UNIT, 'n_gpus': 1, 'steps': args.steps,
+           'warmup': W, 'ms_per_step': 1e3 * dt / args.steps, 'higher_is_better': True, 'scaling': 'weak',
+           'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded scenes)',
+           'config': {'workload': BATCH_WORKLOAD, 'scenes': len(rs), 'triangles': tris,
+                      'photons_per_step': photons, 'pixels': pixels,
+                      'l2': 'working set far above L2 (64 contexts, %.1f GB)' % (dev / 1e9)},
+           'hitpoint_updates_per_s': pixels * args.steps / dt,
+           'sequential': {'ms_per_step': seq_ms, 'value': photons / (seq_ms / 1e3),
+                          'note': 'sum over the scenes of one graph replay alone (CUDA events)'},
+           'batch_speedup': seq_ms / (1e3 * dt / args.steps),
+           'autotune': {'photon_tail_min_chosen': hist},
+           'setup': {'scene_generation_s': gen_s, 'contexts_s': setup_s, 'device_bytes': int(dev)}}
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -375,13 +446,16 @@ def main():
     ap.add_argument('--guide-ref-iters', type=int, default=1024)
     ap.add_argument('--guide-photons', type=int, default=CAUSTIC_PHOTONS)
     ap.add_argument('--eager', action='store_true', help='guide eval: direct launches (for ncu)')
-    ap.add_argument('--workload', default='mixed', choices=['mixed', 'large'],
-                    help='large: the 20M-triangle scene (its own JSON line)')
+    ap.add_argument('--workload', default='mixed', choices=['mixed', 'large', 'batch'],
+                    help='large: the 20M-triangle scene; batch: 64 uneven scenes (each its own JSON line)')
+    ap.add_argument('--no-autotune', action='store_true')
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
     if args.workload == 'large':
         return run_large(args)
+    if args.workload == 'batch':
+        return run_batch(args)
     if args.guide_eval:
         out = guide_eval(args.guide_plain_iters, args.guide_ref_iters, args.guide_photons,
                          log=lambda s: print(s, file=sys.stderr, flush=True), eager=args.eager)

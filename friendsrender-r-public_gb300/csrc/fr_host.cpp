@@ -873,6 +873,71 @@ int fr_iterate(fr_ctx* c, int n) {
   return FR_OK;
 }
 
+int fr_iterate_batch(fr_ctx* const* ctxs, int count, int n) {
+  if (!ctxs || count < 0 || n < 0) return fail(FR_ERR_INVALID, "fr_iterate_batch: bad arguments");
+  for (int j = 0; j < count; ++j)
+    if (!ctxs[j]) return fail(FR_ERR_INVALID, "fr_iterate_batch: context %d is NULL", j);
+  // Iteration k of every context before iteration k + 1 of any: each context
+  // replays its graph on its own streams, so the scenes' kernels share the
+  // GPU and the small ones fill what the large ones leave idle.
+  for (int k = 0; k < n; ++k)
+    for (int j = 0; j < count; ++j) {
+      const int rc = run_iteration(ctxs[j]);
+      if (rc) return rc;
+    }
+  return FR_OK;
+}
+
+namespace {
+// Graph replay time of `iterations` iterations (ms); the graph is captured
+// (and one iteration run) first.
+int timed_iterations(fr_ctx* c, int iterations, float* ms) {
+  int rc = run_iteration(c);
+  if (rc) return rc;
+  cudaEvent_t a = nullptr, b = nullptr;
+  FR_CUDA(cudaEventCreate(&a));
+  FR_CUDA(cudaEventCreate(&b));
+  FR_CUDA(cudaEventRecord(a, c->stream));
+  for (int k = 0; k < iterations && !rc; ++k) rc = run_iteration(c);
+  FR_CUDA(cudaEventRecord(b, c->stream));
+  FR_CUDA(cudaEventSynchronize(b));
+  FR_CUDA(cudaEventElapsedTime(ms, a, b));
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  return rc ? rc : check_device_error(c);
+}
+
+void drop_graph(fr_ctx* c) {
+  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
+  if (c->graph) cudaGraphDestroy(c->graph);
+  c->graph_exec = nullptr;
+  c->graph = nullptr;
+}
+}  // namespace
+
+int fr_autotune(fr_ctx* c, int iterations, uint32_t* photon_tail_min) {
+  if (!c || iterations < 1) return fail(FR_ERR_INVALID, "fr_autotune: bad arguments");
+  if (c->profiling) return fail(FR_ERR_INVALID, "fr_autotune: stage profiler on");
+  static const uint32_t kCandidates[] = {4096u, 8192u, 16384u, 32768u, 65536u};
+  uint32_t best = c->wave.min_live;
+  float best_ms = 3.0e38f;
+  for (uint32_t cand : kCandidates) {
+    c->wave.min_live = cand;
+    drop_graph(c);
+    float ms = 0.0f;
+    const int rc = timed_iterations(c, iterations, &ms);
+    if (rc) return rc;
+    if (ms < best_ms) {
+      best_ms = ms;
+      best = cand;
+    }
+  }
+  c->wave.min_live = best;
+  drop_graph(c);
+  if (photon_tail_min) *photon_tail_min = best;
+  return FR_OK;
+}
+
 int fr_synchronize(fr_ctx* c) {
   if (!c) return fail(FR_ERR_INVALID, "fr_synchronize: NULL context");
   FR_CUDA(cudaStreamSynchronize(c->stream));
@@ -1134,7 +1199,7 @@ int fr_read_wave_counts(fr_ctx* c, uint32_t* eye_counts, uint32_t* photon_counts
     for (int r = t; r < rounds; ++r) q[r] = 0;
   };
   fold(eye_counts, kEyeRounds, kEyeTailMin);
-  fold(photon_counts, kPhotonRounds, kPhotonTailMin);
+  fold(photon_counts, kPhotonRounds, c->wave.min_live);
   return FR_OK;
 }
 

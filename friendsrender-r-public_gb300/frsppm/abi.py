@@ -69,7 +69,8 @@ EXPORTS = ['fr_last_error', 'fr_create', 'fr_iterate', 'fr_synchronize', 'fr_res
            'fr_profile_read', 'fr_radius_count_noalloc', 'fr_check_exact_math',
            'fr_read_wave_counts', 'fr_save_state', 'fr_load_state', 'fr_update',
            'fr_resolve_rgba8', 'fr_export_png', 'fr_write_png', 'fr_check_tc_gemm', 'fr_guide_params',
-           'fr_guide_set_params', 'fr_read_guide_importance', 'fr_guide_gradient', 'fr_seek']
+           'fr_guide_set_params', 'fr_read_guide_importance', 'fr_guide_gradient', 'fr_seek', 'fr_iterate_batch',
+           'fr_autotune']
 
 STAGES = ('eye', 'photon', 'grid', 'gather', 'eye_trace', 'photon_trace')
 
@@ -112,6 +113,8 @@ def load(path=None):
     lib.fr_save_state.argtypes = [vp, vp, C.POINTER(C.c_size_t)]
     lib.fr_load_state.argtypes = [vp, vp, C.c_size_t]
     lib.fr_seek.argtypes = [vp, C.c_uint32]
+    lib.fr_iterate_batch.argtypes = [C.POINTER(vp), C.c_int, C.c_int]
+    lib.fr_autotune.argtypes = [vp, C.c_int, C.POINTER(C.c_uint32)]
     lib.fr_update.argtypes = [vp, vp, vp]
     lib.fr_resolve_rgba8.argtypes = [vp, vp]
     lib.fr_export_png.argtypes = [vp, C.c_char_p]
@@ -307,6 +310,12 @@ class Renderer:
         buf = np.frombuffer(data, np.uint8)
         _check(_lib.fr_load_state(self.h, _ptr(buf), len(buf)), 'fr_load_state')
 
+    def autotune(self, iterations=2):
+        """fr_autotune: runs 5 * (iterations + 1) iterations; returns the chosen threshold."""
+        out = C.c_uint32(0)
+        _check(_lib.fr_autotune(self.h, int(iterations), C.byref(out)), 'fr_autotune')
+        return int(out.value)
+
     def seek(self, first_step):
         """fr_seek: iteration k of this (fresh) context draws step first_step + k."""
         _check(_lib.fr_seek(self.h, int(first_step)), 'fr_seek')
@@ -396,3 +405,13 @@ def check_tc_gemm(seed=1):
     err = np.zeros(3, np.float64)
     _check(lib.fr_check_tc_gemm(int(seed), _ptr(err)), 'fr_check_tc_gemm')
     return err
+
+
+def iterate_batch(renderers, n=1, sync=True):
+    """fr_iterate_batch over Renderer objects (n iterations of each)."""
+    arr = (C.c_void_p * len(renderers))(*[r.h.value if isinstance(r.h, C.c_void_p) else r.h for r in renderers])
+    _check(_lib.fr_iterate_batch(arr, len(renderers), int(n)), 'fr_iterate_batch')
+    if sync:
+        for r in renderers:
+            r.synchronize()
+

@@ -435,6 +435,42 @@ def small_large_scene(seed=CONFIG_SEED_BASE + 104):
     return large_scene(seed=seed, width=64, height=36, instances=16, freq=10, tex_size=64, light_tex=32)
 
 
+BATCH_RESOLUTIONS = (128, 256, 512, 1024)
+
+
+def batch_specs(seed=CONFIG_SEED_BASE + 3, count=64, tri_lo=10_000, tri_hi=2_000_000, photons_lo=50_000,
+                photons_hi=1_000_000):
+    """The batched workload's draw: per scene a triangle budget log-uniform
+    over [tri_lo, tri_hi], a square resolution from BATCH_RESOLUTIONS and a
+    photon count uniform over [photons_lo, photons_hi], plus a scene seed."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for k in range(count):
+        tris = int(round(math.exp(rng.uniform(math.log(tri_lo), math.log(tri_hi)))))
+        res = int(BATCH_RESOLUTIONS[int(rng.integers(0, len(BATCH_RESOLUTIONS)))])
+        photons = int(rng.integers(photons_lo, photons_hi + 1))
+        out.append(dict(triangles=tris, resolution=res, photons=photons, seed=int(rng.integers(0, 2 ** 62))))
+    return out
+
+
+def batch_scene(spec, tex_size=256, light_tex=64):
+    """One scene of the batch: the mixed-materials construction (height field,
+    spheres of the four surface types, textured field and light, thin lens)
+    sized to the spec's triangle budget, half in the field and half in the
+    spheres.  Textures are ``tex_size``^2 (the mixed-materials config's are
+    1024^2) to keep the generation of 64 scenes short."""
+    t = spec['triangles']
+    field_n = max(8, int(math.sqrt(t / 4.0)) + 1)
+    sphere_tris = max(0, t - 2 * (field_n - 1) ** 2)
+    n_spheres = int(min(400, max(8, sphere_tris // 2376)))
+    per = max(64, sphere_tris // n_spheres)
+    n_lon = max(6, int(math.sqrt(per / 2.0)))
+    n_lat = max(4, per // (2 * n_lon) + 1)
+    res = spec['resolution']
+    return mixed_materials(seed=spec['seed'], width=res, height=res, n_spheres=n_spheres, field_n=field_n,
+                           tex_size=tex_size, light_tex=light_tex, n_lat=n_lat, n_lon=n_lon)
+
+
 def small_caustic(seed=CONFIG_SEED_BASE + 102, width=96, height=96):
     """The caustic scene at a size for tests: 12 coarser spheres, 96x96."""
     return caustic_box(seed=seed, width=width, height=height, n_spheres=12, n_lat=12, n_lon=16, light_tex=64)

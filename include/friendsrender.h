@@ -166,6 +166,24 @@ int fr_iterate(fr_ctx* ctx, int n);
 /* Waits for the context's stream and reports kernel errors. */
 int fr_synchronize(fr_ctx* ctx);
 
+/* Batched rendering of uneven scenes (no counterpart in the reference, which
+ * renders one scene per call): n iterations of each of `count` contexts,
+ * iteration k of every context enqueued before iteration k + 1 of any.  Each
+ * context replays its own iteration graph on its own streams, so the scenes'
+ * kernels run concurrently and small scenes fill the SMs that large ones
+ * leave idle.  Every context's results are those of fr_iterate.
+ * Asynchronous; fr_synchronize each context. */
+int fr_iterate_batch(fr_ctx* const* ctxs, int count, int n);
+
+/* Autotuner (no counterpart in the reference): picks the context's photon
+ * wavefront threshold (a round with fewer live paths hands them to the tail
+ * kernel) from 4096, 8192, 16384, 32768 and 65536 by timing `iterations`
+ * replays of the iteration graph with each (plus one untimed).  These are
+ * real iterations of the render, 5 * (iterations + 1) in all; the threshold
+ * changes the speed only, never a result.  *photon_tail_min (may be NULL)
+ * receives the choice. */
+int fr_autotune(fr_ctx* ctx, int iterations, uint32_t* photon_tail_min);
+
 /* Writes the image (reconstructImageFromSharedPoints, SPPM.cpp:473-493):
  * width*height RGBA floats, pixel x + y*width.  rgba is a host pointer;
  * fr_resolve_dev takes a device pointer and does not synchronize. */
