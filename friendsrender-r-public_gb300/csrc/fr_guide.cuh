@@ -25,6 +25,14 @@ namespace fr {
 __device__ __forceinline__ void st_bf16(uint8_t* tile, uint32_t r, uint32_t k, uint32_t K, float v) {
   *reinterpret_cast<__nv_bfloat16*>(tile + tc::tile_offset(r, k, K)) = __float2bfloat16_rn(v);
 }
+// Eight values of row r, columns k0..k0+7 (k0 a multiple of 8): one 16-byte
+// store, the eight being contiguous in the core-matrix layout.
+__device__ __forceinline__ void st_bf16x8(uint8_t* tile, uint32_t r, uint32_t k0, uint32_t K, const float v[8]) {
+  __nv_bfloat162 h[4];
+#pragma unroll
+  for (int j = 0; j < 4; ++j) h[j] = __floats2bfloat162_rn(v[2 * j], v[2 * j + 1]);
+  *reinterpret_cast<uint4*>(tile + tc::tile_offset(r, k0, K)) = *reinterpret_cast<const uint4*>(h);
+}
 __device__ __forceinline__ float ld_bf16(const uint8_t* tile, uint32_t r, uint32_t k, uint32_t K) {
   return __bfloat162float(*reinterpret_cast<const __nv_bfloat16*>(tile + tc::tile_offset(r, k, K)));
 }
@@ -55,11 +63,16 @@ struct TcSync {
 // Layer 1 (FP32) of this thread's sample into tile h1 (row t).  p1 holds W1
 // and b1 at their parameter offsets.
 __device__ __forceinline__ void guide_layer1(const float* p1, const float x[kGuideIn], uint8_t* h1, uint32_t t) {
-  for (int j = 0; j < kGuideHidden; ++j) {
-    float z = p1[kOffB1 + j];
+  for (int j0 = 0; j0 < kGuideHidden; j0 += 8) {
+    float h[8];
 #pragma unroll
-    for (int k = 0; k < kGuideIn; ++k) z += p1[kOffW1 + j * kGuideIn + k] * x[k];
-    st_bf16(h1, t, j, 64, fmaxf(z, 0.0f));
+    for (int j = 0; j < 8; ++j) {
+      float z = p1[kOffB1 + j0 + j];
+#pragma unroll
+      for (int k = 0; k < kGuideIn; ++k) z += p1[kOffW1 + (j0 + j) * kGuideIn + k] * x[k];
+      h[j] = fmaxf(z, 0.0f);
+    }
+    st_bf16x8(h1, t, j0, 64, h);
   }
 }
 
@@ -70,7 +83,9 @@ __device__ __forceinline__ void guide_hidden_epilogue(uint32_t taddr, const floa
     float v[16];
     tc::tmem_ld16(taddr + c0, v);
 #pragma unroll
-    for (int k = 0; k < 16; ++k) st_bf16(h, t, c0 + k, 64, fmaxf(v[k] + bias[c0 + k], 0.0f));
+    for (int k = 0; k < 16; ++k) v[k] = fmaxf(v[k] + bias[c0 + k], 0.0f);
+    st_bf16x8(h, t, c0, 64, v);
+    st_bf16x8(h, t, c0 + 8, 64, v + 8);
   }
 }
 
@@ -91,6 +106,7 @@ __device__ __forceinline__ void guide_output_epilogue(uint32_t taddr, const floa
 struct GuideMixture {
   V3 mu[kGuideLobes];
   float kappa[kGuideLobes], w[kGuideLobes];
+  float lnorm[kGuideLobes];  // log of the vMF normalization kappa / (2 pi (1 - e^{-2 kappa}))
   float norm[kGuideLobes];  // |raw mean| (for the gradient)
   float kraw[kGuideLobes];  // raw concentration (for the gradient)
 };
@@ -110,6 +126,7 @@ __device__ __forceinline__ void guide_mixture(const float o[kGuideOut], GuideMix
     g.mu[k] = m * (1.0f / n);
     g.kraw[k] = o[5 * k + 3];
     g.kappa[k] = fminf(kGuideKappaMin + softplus(o[5 * k + 3]), kGuideKappaMax);
+    g.lnorm[k] = logf(g.kappa[k] * kGuideInvTwoPi) - log1pf(-expf(-2.0f * g.kappa[k]));
     g.w[k] = expf(o[5 * k + 4] - amax);
     wsum += g.w[k];
   }
@@ -125,7 +142,7 @@ __device__ __forceinline__ float vmf_log_pdf(float kappa, float cosang) {
 __device__ __forceinline__ float guide_pdf(const GuideMixture& g, V3 d) {
   float p = 0.0f;
 #pragma unroll
-  for (int k = 0; k < kGuideLobes; ++k) p += g.w[k] * expf(vmf_log_pdf(g.kappa[k], dot(g.mu[k], d)));
+  for (int k = 0; k < kGuideLobes; ++k) p += g.w[k] * expf(g.lnorm[k] + g.kappa[k] * (dot(g.mu[k], d) - 1.0f));
   return p;
 }
 
@@ -146,7 +163,7 @@ __device__ __forceinline__ void guide_loss_grad(const GuideMixture& g, V3 d, flo
   float lf[kGuideLobes], lmax = -3.0e38f;
 #pragma unroll
   for (int k = 0; k < kGuideLobes; ++k) {
-    lf[k] = logf(g.w[k]) + vmf_log_pdf(g.kappa[k], dot(g.mu[k], d));
+    lf[k] = logf(g.w[k]) + (g.lnorm[k] + g.kappa[k] * (dot(g.mu[k], d) - 1.0f));  // + vmf_log_pdf
     lmax = fmaxf(lmax, lf[k]);
   }
   float s = 0.0f;
