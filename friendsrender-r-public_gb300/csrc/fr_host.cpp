@@ -1252,6 +1252,14 @@ int fr_update(fr_ctx* c, const int32_t* m, const float* phi) {
   return fr_synchronize(c);
 }
 
+int fr_update_dev(fr_ctx* c, const int32_t* m_dev, const float* phi4_dev) {
+  if (!c || !m_dev || !phi4_dev) return fail(FR_ERR_INVALID, "fr_update_dev: bad arguments");
+  if ((reinterpret_cast<uintptr_t>(phi4_dev) & 15u) != 0) return fail(FR_ERR_INVALID, "fr_update_dev: phi4 not 16-byte aligned");
+  launch_update(c->st, m_dev, reinterpret_cast<const float4*>(phi4_dev), c->W * c->H, c->alpha, c->stream);
+  FR_CUDA(cudaGetLastError());
+  return FR_OK;
+}
+
 // ------------------------------------------------------------ guide
 int fr_guide_params(fr_ctx* c, float* params) {
   if (!c || !params || !c->guided) return fail(FR_ERR_INVALID, "fr_guide_params: no guide");

@@ -70,7 +70,7 @@ EXPORTS = ['fr_last_error', 'fr_create', 'fr_iterate', 'fr_synchronize', 'fr_res
            'fr_read_wave_counts', 'fr_save_state', 'fr_load_state', 'fr_update',
            'fr_resolve_rgba8', 'fr_export_png', 'fr_write_png', 'fr_check_tc_gemm', 'fr_guide_params',
            'fr_guide_set_params', 'fr_read_guide_importance', 'fr_guide_gradient', 'fr_seek', 'fr_iterate_batch',
-           'fr_autotune']
+           'fr_autotune', 'fr_update_dev']
 
 STAGES = ('eye', 'photon', 'grid', 'gather', 'eye_trace', 'photon_trace')
 
@@ -116,6 +116,7 @@ def load(path=None):
     lib.fr_iterate_batch.argtypes = [C.POINTER(vp), C.c_int, C.c_int]
     lib.fr_autotune.argtypes = [vp, C.c_int, C.POINTER(C.c_uint32)]
     lib.fr_update.argtypes = [vp, vp, vp]
+    lib.fr_update_dev.argtypes = [vp, vp, vp]
     lib.fr_resolve_rgba8.argtypes = [vp, vp]
     lib.fr_export_png.argtypes = [vp, C.c_char_p]
     lib.fr_write_png.argtypes = [C.c_char_p, i32, i32, vp]
@@ -319,6 +320,12 @@ class Renderer:
     def seek(self, first_step):
         """fr_seek: iteration k of this (fresh) context draws step first_step + k."""
         _check(_lib.fr_seek(self.h, int(first_step)), 'fr_seek')
+
+    def update_dev(self, m_ptr, phi4_ptr, sync=True):
+        """fr_update_dev: device pointers to width*height int32 M and float4 flux sums."""
+        _check(_lib.fr_update_dev(self.h, C.c_void_p(m_ptr), C.c_void_p(phi4_ptr)), 'fr_update_dev')
+        if sync:
+            self.synchronize()
 
     def update(self, m, phi):
         """fr_update: apply per-pixel photon counts and flux sums to the state."""

@@ -338,6 +338,14 @@ int fr_read_state(fr_ctx* ctx, double* tau, int32_t* n, float* r, int32_t* g);
  * checking the update against the reference's own M and flux sums. */
 int fr_update(fr_ctx* ctx, const int32_t* m, const float* phi);
 
+/* fr_update with device-resident inputs: m_dev (width*height int32) and
+ * phi4_dev (width*height x 4 floats, RGB and an unused fourth, 16-byte
+ * aligned), applied on the context's stream without a host round trip.  For
+ * a sharded render, where each GPU gathers its own photons and an all-reduce
+ * of the per-pixel counts and flux sums precedes the update.  Asynchronous
+ * (fr_synchronize). */
+int fr_update_dev(fr_ctx* ctx, const int32_t* m_dev, const float* phi4_dev);
+
 /* Checkpoint and resume between iterations (no counterpart in the reference,
  * which renders in one call).  fr_save_state with buf == NULL stores the
  * checkpoint size in *size; otherwise *size is buf's capacity on entry and

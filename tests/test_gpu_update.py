@@ -43,3 +43,26 @@ def test_update_leaves_pixels_without_photons():
         assert after['g'][5] == 1 and after['n'][5] == int(np.float32(3) * np.float32(0.7))
         np.testing.assert_allclose(after['tau'][5], np.array([1.0, 2.0, 3.0]) * (2.1 / 3.0), rtol=1e-6)
         assert after['r'][5] == np.float32(0.02) * np.sqrt(np.float32(2.1) / np.float32(3.0), dtype=np.float32)
+
+
+@pytest.mark.parametrize('name', sorted(GOLDEN_SCENES))
+def test_update_dev_matches_update(name):
+    """fr_update_dev (device inputs) reaches the state fr_update reaches."""
+    import torch
+    from frsppm import abi
+    gold = load_golden(name)
+    mk = lambda: abi.Renderer(GOLDEN_SCENES[name](), int(gold['photons']), alpha=0.9, radius=0.015)
+    with mk() as a, mk() as b:
+        for s in range(1, int(gold['iters']) + 1):
+            m = gold['it%d_gather_m' % s]
+            phi = gold['it%d_gather_phi' % s]
+            a.update(m, phi)
+            md = torch.from_numpy(np.ascontiguousarray(m, np.int32)).cuda()
+            p4 = np.zeros((len(m), 4), np.float32)
+            p4[:, :3] = phi.reshape(-1, 3)
+            pd = torch.from_numpy(p4).cuda()
+            torch.cuda.synchronize()
+            b.update_dev(md.data_ptr(), pd.data_ptr())
+            sa, sb = a.read_state(), b.read_state()
+            for k in ('n', 'r', 'g', 'tau'):
+                np.testing.assert_array_equal(sa[k], sb[k])
