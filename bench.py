@@ -432,6 +432,56 @@ def run_batch(args):
     return 0
 
 
+# Bytes one N/tau/R update (k_update) must move: read M 4, the flux sums as
+# float4 16 (fr_update_dev's layout), N 4, tau 24 (FP64 x 3), R 4, NumGather 4;
+# write tau 24, R 4, N 4, NumGather 4.
+UPDATE_BYTES_PER_PIXEL = 92
+
+
+def run_update(args):
+    """The N/tau/R update alone (fr_update_dev) over a 3840x2160 pixel state,
+    every pixel with photons: hitpoint updates/s and the kernel's achieved
+    HBM bandwidth (the working set, 8.3M x 92 B, is far above L2)."""
+    import torch
+    from frsppm import abi, scenes
+    torch.cuda.set_device(dist_env()[2])
+    r = abi.Renderer(scenes.cornell_box(width=3840, height=2160), 1000, alpha=ALPHA, radius=RADIUS)
+    npix = r.width * r.height
+    gen = torch.Generator(device='cuda')
+    gen.manual_seed(1)
+    m = torch.randint(1, 8, (npix,), dtype=torch.int32, device='cuda', generator=gen)
+    phi = torch.rand((npix, 4), device='cuda', generator=gen)
+    torch.cuda.synchronize()
+    W = max(3, args.warmup)
+    for _ in range(W):
+        r.update_dev(m.data_ptr(), phi.data_ptr(), sync=False)
+    stream = torch.cuda.ExternalStream(r.stream())
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    r.synchronize()
+    with ClockSampler(dist_env()[2]) as clk:
+        for a, b in evs:
+            a.record(stream)
+            r.update_dev(m.data_ptr(), phi.data_ptr(), sync=False)
+            b.record(stream)
+        r.synchronize()
+    ms = sum(a.elapsed_time(b) for a, b in evs) / args.steps
+    r.close()
+    peak, kind = measured_peaks()
+    achieved = UPDATE_BYTES_PER_PIXEL * npix / (ms / 1e3) / 1e9
+    out = {'metric': 'hitpoint updates/s (N/tau/R update alone)', 'value': npix / (ms / 1e3),
+           'unit': 'hitpoint updates/s', 'n_gpus': 1, 'steps': args.steps, 'warmup': W, 'ms_per_step': ms,
+           'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f64',
+           'data': 'synthetic (random per-pixel counts 1-7 and flux sums)',
+           'config': {'workload': 'fr_update_dev over 3840x2160 = 8,294,400 pixels, every pixel updated',
+                      'l2': 'inputs larger than L2 (763 MB per step)'},
+           'roofline': {'bound': 'hbm', 'kernel': 'k_update', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
+                        'frac': achieved / peak, 'traffic': None, 'peak_source': kind,
+                        'algorithmic_bytes_per_launch': UPDATE_BYTES_PER_PIXEL * npix},
+           'gpu_launches': args.steps, 'clocks': clk.summary()}
+    print(json.dumps(out))
+    return 0
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -446,8 +496,9 @@ def main():
     ap.add_argument('--guide-ref-iters', type=int, default=1024)
     ap.add_argument('--guide-photons', type=int, default=CAUSTIC_PHOTONS)
     ap.add_argument('--eager', action='store_true', help='guide eval: direct launches (for ncu)')
-    ap.add_argument('--workload', default='mixed', choices=['mixed', 'large', 'batch'],
-                    help='large: the 20M-triangle scene; batch: 64 uneven scenes (each its own JSON line)')
+    ap.add_argument('--workload', default='mixed', choices=['mixed', 'large', 'batch', 'update'],
+                    help='large: the 20M-triangle scene; batch: 64 uneven scenes; update: the N/tau/R update '
+                         'alone (each its own JSON line)')
     ap.add_argument('--no-autotune', action='store_true')
     args = ap.parse_args()
     if args.impl == 'reference':
@@ -456,6 +507,8 @@ def main():
         return run_large(args)
     if args.workload == 'batch':
         return run_batch(args)
+    if args.workload == 'update':
+        return run_update(args)
     if args.guide_eval:
         out = guide_eval(args.guide_plain_iters, args.guide_ref_iters, args.guide_photons,
                          log=lambda s: print(s, file=sys.stderr, flush=True), eager=args.eager)
