@@ -819,9 +819,9 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
   if (params->guide) {
     GuideGPU& g = c->guide;
     g.plain_fraction = params->guide_plain_fraction > 0.0f ? std::min(1.0f, params->guide_plain_fraction) : 0.2f;
-    g.batch_cap = std::min(c->P, params->guide_batch > 0 ? params->guide_batch : 65536);
+    g.batch_cap = std::min(c->P, params->guide_batch > 0 ? params->guide_batch : 16384);
     g.lr = params->guide_learning_rate > 0.0f ? params->guide_learning_rate : 0.005f;
-    g.steps = params->guide_steps > 0 ? std::min(params->guide_steps, 64) : 4;
+    g.steps = params->guide_steps > 0 ? std::min(params->guide_steps, 64) : 16;
     if ((rc = c->alloc(&g.params, kGuideParams)) || (rc = c->alloc(&g.grad, kGuideParams)) ||
         (rc = c->alloc(&g.adam_m, kGuideParams)) || (rc = c->alloc(&g.adam_v, kGuideParams)) ||
         (rc = c->alloc(&g.tiles, kTileBytes)) || (rc = c->alloc(&g.feat, (size_t)c->P)) ||

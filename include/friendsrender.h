@@ -129,10 +129,10 @@ typedef struct fr_sppm_params {
    * (guide = 0) is the reference's plain emission. */
   int32_t guide;                  /* 1: guided emission */
   float guide_plain_fraction;     /* share of cosine sampling in the mixture; <= 0 selects 0.2 */
-  int32_t guide_batch;            /* training samples per iteration; <= 0 selects 65536 */
+  int32_t guide_batch;            /* training samples per iteration; <= 0 selects 16384 */
   float guide_learning_rate;      /* Adam step size; <= 0 selects 0.005 */
   uint32_t guide_seed;            /* initial network weights */
-  int32_t guide_steps;            /* Adam steps per iteration on its samples; <= 0 selects 4 (at most 64) */
+  int32_t guide_steps;            /* Adam steps per iteration on its samples; <= 0 selects 16 (at most 64) */
 } fr_sppm_params;
 
 typedef struct fr_stats {
