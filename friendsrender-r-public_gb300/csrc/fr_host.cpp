@@ -513,6 +513,7 @@ int enqueue_iteration(fr_ctx* c) {
     cudaStream_t e = c->side;
     StageMark m(c, FR_STAGE_EYE, e);
     const int sort_grid = (int)std::min<size_t>(((size_t)c->W * c->H + 255) / 256, 4 * (size_t)grid);
+    if (c->sc.env) FR_CUDA(cudaMemsetAsync(c->hp.dl, 0, sizeof(float4) * (size_t)c->W * c->H, e));
     launch_ew_start(c->cam, it, c->eye_wave, e);
     for (int r = 0; r < kEyeRounds; ++r) {
       {
@@ -759,9 +760,30 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
   }
   TextureGPU* d_texs;
   if ((rc = c->upload(&d_texs, texs.data(), texs.size()))) return bail(rc);
+  // Environment map: texels c = byte / 255.0f (TextureUtility.cpp:28)
+  // converted as LightSampler.cpp:24 does, 0.4 * (c^2, c^2, c^2, 0) (the
+  // double literal meets Vec4's operator*(float, Vec4)).
+  float4* d_env = nullptr;
+  int32_t env_w = 0, env_h = 0;
+  if (const fr_texture_desc* e = scene->environment) {
+    if (e->width <= 0 || e->height <= 0 || !e->texels) return bail(fail(FR_ERR_INVALID, "scene: bad environment map"));
+    env_w = e->width;
+    env_h = e->height;
+    std::vector<float4> env((size_t)env_w * env_h);
+    const uint8_t* px = static_cast<const uint8_t*>(e->texels);
+    for (size_t k = 0; k < env.size(); ++k) {
+      float v[4];
+      for (int ch = 0; ch < 4; ++ch) {
+        const float cv = ch < 3 ? px[4 * k + ch] / 255.0f : 0.0f;
+        v[ch] = 0.4f * (cv * cv);
+      }
+      env[k] = make_float4(v[0], v[1], v[2], v[3]);
+    }
+    if ((rc = c->upload(&d_env, env.data(), env.size()))) return bail(rc);
+  }
   c->sc = SceneGPU{d_nodes, d_tris, d_shade, d_mats, d_texs, d_lights, d_emit,
                    (int32_t)bvh.nodes.size(), T, T, (int32_t)lights.size(),
-                   {lo[0], lo[1], lo[2]}, {hi[0], hi[1], hi[2]}};
+                   {lo[0], lo[1], lo[2]}, {hi[0], hi[1], hi[2]}, reinterpret_cast<const float*>(d_env), env_w, env_h};
 
   // ---- per-iteration buffers (all allocated here; iterations allocate nothing)
   const size_t npix = (size_t)c->W * c->H;
@@ -769,7 +791,8 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
   const size_t wave_n = (size_t)c->P;
   if ((rc = c->alloc(&c->hp.pos, npix)) || (rc = c->alloc(&c->hp.nrm, npix)) || (rc = c->alloc(&c->hp.out, npix)) ||
       (rc = c->alloc(&c->hp.wgt, npix)) || (rc = c->alloc(&c->st.tau, 3 * npix)) || (rc = c->alloc(&c->st.n, npix)) ||
-      (rc = c->alloc(&c->st.r, npix)) || (rc = c->alloc(&c->st.g, npix)) || (rc = c->alloc(&c->ph.pos, nslots)) ||
+      (rc = c->alloc(&c->st.r, npix)) || (rc = c->alloc(&c->st.g, npix)) || (rc = c->alloc(&c->st.dl, npix)) ||
+      (rc = c->alloc(&c->hp.dl, npix)) || (rc = c->alloc(&c->ph.pos, nslots)) ||
       (rc = c->alloc(&c->ph.flux, nslots)) || (rc = c->alloc(&c->ph.dir, nslots)) ||
       (rc = c->alloc(&c->counts, (size_t)c->P)) || (rc = c->alloc(&c->wave.a, wave_n)) ||
       (rc = c->alloc(&c->wave.b, wave_n)) || (rc = c->alloc(&c->wave.c, wave_n)) ||
@@ -850,6 +873,8 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
   cudaMemsetAsync(c->st.tau, 0, 3 * npix * sizeof(double), c->stream);
   cudaMemsetAsync(c->st.n, 0, npix * 4, c->stream);
   cudaMemsetAsync(c->st.g, 0, npix * 4, c->stream);
+  cudaMemsetAsync(c->st.dl, 0, npix * sizeof(float4), c->stream);
+  cudaMemsetAsync(c->hp.dl, 0, npix * sizeof(float4), c->stream);
   cudaMemsetAsync(c->ph.dir, 0, nslots * sizeof(float4), c->stream);
   cudaMemsetAsync(c->ph.pos, 0, nslots * sizeof(float4), c->stream);
   cudaMemsetAsync(c->ph.flux, 0, nslots * sizeof(float4), c->stream);
@@ -1203,6 +1228,22 @@ int fr_read_wave_counts(fr_ctx* c, uint32_t* eye_counts, uint32_t* photon_counts
   return FR_OK;
 }
 
+int fr_read_direct(fr_ctx* c, float* last3, float* sum3, int32_t* count) {
+  if (!c) return fail(FR_ERR_INVALID, "fr_read_direct: NULL context");
+  const size_t np = (size_t)c->W * c->H;
+  std::vector<float4> a(last3 ? np : 0), b((sum3 || count) ? np : 0);
+  if (last3) FR_CUDA(cudaMemcpyAsync(a.data(), c->hp.dl, 16 * np, cudaMemcpyDeviceToHost, c->stream));
+  if (sum3 || count) FR_CUDA(cudaMemcpyAsync(b.data(), c->st.dl, 16 * np, cudaMemcpyDeviceToHost, c->stream));
+  const int rc = fr_synchronize(c);
+  if (rc) return rc;
+  for (size_t i = 0; i < np; ++i) {
+    if (last3) { last3[3 * i] = a[i].x; last3[3 * i + 1] = a[i].y; last3[3 * i + 2] = a[i].z; }
+    if (sum3) { sum3[3 * i] = b[i].x; sum3[3 * i + 1] = b[i].y; sum3[3 * i + 2] = b[i].z; }
+    if (count) { int32_t k; std::memcpy(&k, &b[i].w, 4); count[i] = k; }
+  }
+  return FR_OK;
+}
+
 int fr_read_hitpoints(fr_ctx* c, float* pos_type, float* nrm_rough, float* out_mat, float* wgt_facet) {
   if (!c) return fail(FR_ERR_INVALID, "fr_read_hitpoints: NULL context");
   const size_t bytes = sizeof(float4) * (size_t)c->W * c->H;
@@ -1340,7 +1381,8 @@ struct StatePart {
 std::vector<StatePart> state_parts(fr_ctx* c) {
   const size_t np = (size_t)c->W * c->H, ns = (size_t)c->P * kPhotonSlots;
   std::vector<StatePart> parts = {{c->st.tau, 24 * np},  {c->st.n, 4 * np},     {c->st.r, 4 * np},
-                                  {c->st.g, 4 * np},     {c->ph.pos, 16 * ns},  {c->ph.flux, 16 * ns},
+                                  {c->st.g, 4 * np},     {c->st.dl, 16 * np},   {c->ph.pos, 16 * ns},
+                                  {c->ph.flux, 16 * ns},
                                   {c->ph.dir, 16 * ns}};
   if (c->guided) {  // the guide's network and optimizer state
     parts.push_back({c->guide.params, 4 * (size_t)kGuideParams});

@@ -86,18 +86,20 @@ __global__ void k_next_step(uint32_t* step) { *step += 1u; }
 // ------------------------------------------------------------------ eye pass
 // createHitpoints + getHitpointInfo (SPPM.cpp:98-353) as a wavefront: k_ew_start
 // makes every camera ray, rounds of k_wave_trace and k_ew_shade advance the
-// live paths, k_ew_tail finishes the rest.  A path ends at its first SPPM
-// surface (makeHitPoint, SPPM.cpp:79-96): with no IBL nothing after the first
-// hitpoint reaches the image.
+// live paths, k_ew_tail finishes the rest.  Without an environment map a
+// path ends at its first SPPM surface (makeHitPoint, SPPM.cpp:79-96): nothing
+// after the first hitpoint reaches the image.  With one it goes on, as the
+// reference's does (SPPM.cpp:170-173), until it ends or misses the scene.
 //
 // Path state between kernels (one entry per pixel):
 //   a: origin.xyz, ray index of refraction   b: direction.xyz, PDF
-//   c: throughput.xyz, camera PDF            d: draw counter, depth
+//   c: throughput.xyz, camera PDF            d: draw counter, depth, hitpoint stored
 struct EyeState {
   V3 o, d, thr;
   float ix, PDF, cam_pdf;
   uint32_t draw;
   int depth;
+  int stored;  // isStoredPhoton (SPPM.cpp:170-173)
 };
 
 __device__ __forceinline__ uint32_t eye_seed(const IterParams& it, int i) {
@@ -111,13 +113,14 @@ __device__ __forceinline__ void load_eye(const PathWave& w, int i, EyeState& s) 
   s.thr = v3(c.x, c.y, c.z); s.cam_pdf = c.w;
   s.draw = __float_as_uint(d.x);
   s.depth = __float_as_int(d.y);
+  s.stored = __float_as_int(d.z);
 }
 
 __device__ __forceinline__ void store_eye(const PathWave& w, int i, const EyeState& s) {
   w.a[i] = make_float4(s.o.x, s.o.y, s.o.z, s.ix);
   w.b[i] = make_float4(s.d.x, s.d.y, s.d.z, s.PDF);
   w.c[i] = make_float4(s.thr.x, s.thr.y, s.thr.z, s.cam_pdf);
-  w.d[i] = make_float4(__uint_as_float(s.draw), __int_as_float(s.depth), 0.f, 0.f);
+  w.d[i] = make_float4(__uint_as_float(s.draw), __int_as_float(s.depth), __int_as_float(s.stored), 0.f);
 }
 
 // Top of the bounce loop (SPPM.cpp:99-122): depth cap and Russian roulette
@@ -130,6 +133,52 @@ __device__ __forceinline__ bool eye_top(EyeState& s, Rng& rng, float rr5, float 
     s.PDF *= rus;
   }
   return true;
+}
+
+// IBL::GetIBLColorFromDirection (IBL.h:122-129) with the SPHERE mapping
+// (GetUVFromDirection, IBL.h:96-104; acos of a float there is the double
+// ::acos) and LinearSampler::Sample (TextureSampler.h:61-79) on the converted
+// texels.
+__device__ __forceinline__ V3 env_color(const SceneGPU& sc, V3 dir) {
+  float u = 0.0f, v = 0.0f;
+  if (!(fabsf(dir.x) < kLt1e6 && fabsf(dir.z) < kLt1e6)) {
+    const V3 xz = normalized(v3(dir.x, 0.0f, dir.z));
+    const double ax = acos((double)xz.x);
+    const double two_pi = (double)(2.0f * kPI);
+    u = (float)((xz.z >= 0.0f ? ax : two_pi - ax) / two_pi);
+    v = (float)(acos((double)dir.y) / (double)kPI);
+  }
+  const int W = sc.env_w, H = sc.env_h;
+  const int iu = (int)((float)W * u), iv = (int)((float)H * v);
+  const int x1 = abs(iu) % W, y1 = abs(iv) % H;
+  const int x2 = min(W - 1, x1 + 1), y2 = min(H - 1, y1 + 1);
+  const float4* env = reinterpret_cast<const float4*>(sc.env);
+  const float4 t00 = env[x1 + y1 * W], t10 = env[x2 + y1 * W];
+  const float4 t01 = env[x1 + y2 * W], t11 = env[x2 + y2 * W];
+  const float w = fabsf(u * (float)W) - (float)abs(iu);
+  const float h = fabsf(v * (float)H) - (float)abs(iv);
+  const F4 up = lerp4(F4{t00.x, t00.y, t00.z, t00.w}, 1.0f - w, F4{t10.x, t10.y, t10.z, t10.w}, w);
+  const F4 down = lerp4(F4{t01.x, t01.y, t01.z, t01.w}, 1.0f - w, F4{t11.x, t11.y, t11.z, t11.w}, w);
+  const F4 c = lerp4(up, 1.0f - h, down, h);
+  return v3(c.x, c.y, c.z);
+}
+
+// An eye path that leaves the scene (SPPM.cpp:290-300): with an environment
+// map, its colour times the throughput over the path pdf and (createHitpoints,
+// SPPM.cpp:345) the camera pdf is the pixel's direct light, added to the
+// pixel's sum when its squared norm exceeds 1e-8 (applyHitPointInfo,
+// SPPM.cpp:411-414).  Returns the hitpoint type the path ends with.
+__device__ __forceinline__ int eye_miss(const SceneGPU& sc, const HitpointBuf& hp, const PixelState& st, int i,
+                                        const EyeState& s) {
+  if (sc.env) {
+    const V3 dl = ((env_color(sc, s.d) * s.thr) / s.PDF) / s.cam_pdf;
+    hp.dl[i] = make_float4(dl.x, dl.y, dl.z, 0.0f);
+    if (norm2(dl) > kGt1e8) {
+      const float4 a = st.dl[i];
+      st.dl[i] = make_float4(a.x + dl.x, a.y + dl.y, a.z + dl.z, __int_as_float(__float_as_int(a.w) + 1));
+    }
+  }
+  return s.stored ? kHitHit : kHitOnlyDirect;
 }
 
 // The rest of one pass after the closest hit (SPPM.cpp:123-305).  Returns
@@ -145,26 +194,29 @@ __device__ __forceinline__ int eye_shade(const SceneGPU& sc, const HitpointBuf& 
   if (g.translucency > 0.5f) {
     s.thr = s.thr * v3(g.translucency, g.translucency, g.translucency);
     s.o = g.pos + s.d * kRayOffset;
-    return eye_top(s, rng, rr5, rr6) ? -1 : kHitNone;
+    return eye_top(s, rng, rr5, rr6) ? -1 : (s.stored ? kHitHit : kHitNone);
   }
-  if (g.flags & kMatSPPM) {
+  if ((g.flags & kMatSPPM) && !s.stored) {
     const V3 wgt = (s.thr / s.PDF) / s.cam_pdf;
     store_float4(hp.pos + i, g.pos, __int_as_float(kHitHit));
     store_float4(hp.nrm + i, g.normal, g.rough);
     store_float4(hp.out + i, -s.d, __int_as_float(g.mat));
     store_float4(hp.wgt + i, wgt, __int_as_float(hit.facet));
-    return kHitHit;
+    s.stored = 1;
+    if (!sc.env) return kHitHit;
   }
+  // How the path ends from here: with its hitpoint if it made one.
+  const int end = s.stored ? kHitHit : kHitNone;
   float Ii, Io;
   if (near1(s.ix)) { Ii = 1.0f; Io = g.index; }
   else { Ii = s.ix; Io = 1.0f; }
   FParam p{s.d, s.d, g.normal, Ii, Io, g.rough, g.extinction, g.reflectance};
   float pdf = 1.0f;
   const V3 nd = surface_sample(g.type, rng, p, &pdf);
-  if (!is_valid_direction(nd)) return kHitNone;
+  if (!is_valid_direction(nd)) return end;
   float nix = s.ix;
   if (g.flags & kMatOpaque) {
-    if (dot(nd, g.normal) < kLt1e6) return kHitNone;
+    if (dot(nd, g.normal) < kLt1e6) return end;
   } else {
     const bool reflect = !(dot(nd, g.normal) < 0.0f);
     nix = reflect ? s.ix : Io;
@@ -175,16 +227,16 @@ __device__ __forceinline__ int eye_shade(const SceneGPU& sc, const HitpointBuf& 
   nxt_o = nxt_o + on * kRayOffset;
   const float brdf = surface_brdf(g.type, p);
   const float cs = fmaxf(0.0f, fminf(1.0f, dot(nd, on)));
-  if (brdf < kLt1e8) return kHitNone;
-  if (pdf < 0.0f) return kHitNone;
+  if (brdf < kLt1e8) return end;
+  if (pdf < 0.0f) return end;
   // The reference goes on with a NaN BSDF value or pdf, or a zero pdf, which
   // gives the hitpoint a NaN or infinite weight; the flag ends such paths.
-  if (kEndDegenerate && !(brdf >= kLt1e8 && pdf > 0.0f)) return kHitNone;
+  if (kEndDegenerate && !(brdf >= kLt1e8 && pdf > 0.0f)) return end;
   s.thr = s.thr * (g.albedo * cs * brdf);
   s.PDF *= pdf;
   s.o = nxt_o; s.d = nd; s.ix = nix;
   ++s.depth;
-  return eye_top(s, rng, rr5, rr6) ? -1 : kHitNone;
+  return eye_top(s, rng, rr5, rr6) ? -1 : end;
 }
 
 // Appends i to queue t of T (queue t starts at q + t * cap, its length is
@@ -288,6 +340,7 @@ __global__ void __launch_bounds__(128) k_ew_start(CameraGPU cam, IterParams it, 
     s.PDF = 1.0f;
     s.thr = v3(1.f, 1.f, 1.f);
     s.depth = 0;
+    s.stored = 0;
     s.draw = rng.draw;
     store_eye(w, i, s);
   }
@@ -490,7 +543,7 @@ __global__ void __launch_bounds__(128) k_ew_shade(SceneGPU sc, IterParams it, fl
       load_eye(w, (int)i, s);
       Hit h;
       if (!wave_hit(w, i, h)) {
-        hit_type = kHitOnlyDirect;  // miss: ONLY_DIRECTLIGHT with no IBL (SPPM.cpp:290-300)
+        hit_type = eye_miss(sc, hp, st, (int)i, s);  // SPPM.cpp:290-300
         ended = true;
       } else {
         Rng rng(eye_seed(it, (int)i));
@@ -532,7 +585,7 @@ __global__ void __launch_bounds__(128) k_ew_tail(SceneGPU sc, IterParams it, flo
       while (true) {
         Hit h;
         if (!trace_closest(sc, s.o, s.d, kRayOffset, h, err)) {
-          hit_type = kHitOnlyDirect;
+          hit_type = eye_miss(sc, hp, st, i, s);
           break;
         }
         const int r = eye_shade<kEndDegenerate>(sc, hp, i, s, rng, h, rr5, rr6);
@@ -1294,7 +1347,11 @@ __global__ void k_resolve(PixelState st, int pixels, double photons_total, doubl
   const double share = standard ? 1.0 : ((double)st.g[i] + 1e-4) / (1e-4 + iterations);
   const double denom = (photons_total * share) * (double)kPI * R * R;
   const double* tau = st.tau + 3 * (size_t)i;
-  const float lr = (float)(tau[0] / denom), lg = (float)(tau[1] / denom), lb = (float)(tau[2] / denom);
+  // Direct (environment) light over its count (SPPM.cpp:485), zero without one.
+  const float4 dl = st.dl[i];
+  const float dn = (float)__float_as_int(dl.w) + 0.0001f;
+  const float lr = dl.x / dn + (float)(tau[0] / denom), lg = dl.y / dn + (float)(tau[1] / denom),
+              lb = dl.z / dn + (float)(tau[2] / denom);
   const float gm = 1.0f / 1.2f;
   out[i] = make_float4(powf(lr, gm), powf(lg, gm), powf(lb, gm), 1.0f);
 }

@@ -17,6 +17,7 @@ struct HitpointBuf {
   float4* nrm;
   float4* out;
   float4* wgt;
+  float4* dl;            // this iteration's direct light per pixel (with an environment map)
   uint32_t* list;        // pixels holding a hitpoint this iteration, in no set order
   uint32_t* list_count;  // zeroed before the eye pass
 };
@@ -103,6 +104,7 @@ struct PixelState {
   int32_t* n;     // NumPhoton (int, truncating update, SPPM.cpp:447)
   float* r;       // Radius
   int32_t* g;     // NumGather
+  float4* dl;     // DirectLight (xyz) and NumDirectLight (w, int bits)
 };
 
 // Scratch shared by the kernels of one iteration.

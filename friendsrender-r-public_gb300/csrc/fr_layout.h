@@ -128,6 +128,8 @@ struct SceneGPU {
   const EmitEntry* emit;
   int32_t num_nodes, num_tris, num_facets, num_lights;
   float lo[3], hi[3];   // scene bounds
+  const float* env;     // environment map: 4 floats per converted texel, 16-byte aligned; or null
+  int32_t env_w, env_h;
 };
 
 // Per-iteration parameters read by the kernels.

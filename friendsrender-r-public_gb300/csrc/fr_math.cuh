@@ -48,6 +48,7 @@ constexpr float kLt1e5 = 0x1.4f8b5ap-17f;      // (double)g < 1e-5
 constexpr float kGt1e6 = 0x1.0c6f7ap-20f;      // (double)g > 1e-6
 constexpr float kLt1e6 = 0x1.0c6f7cp-20f;      // (double)g < 1e-6
 constexpr float kLt1e8 = 0x1.5798f0p-27f;      // (double)g < 1e-8
+constexpr float kGt1e8 = 0x1.5798eep-27f;      // (double)g > 1e-8
 constexpr float kGt0_999999 = 0x1.ffffdep-1f;  // (double)g > 0.999999
 constexpr float kGt0_9 = 0x1.ccccccp-1f;       // (double)g > 0.9
 

@@ -32,7 +32,7 @@ class SceneDesc(C.Structure):
     _fields_ = [('num_facets', C.c_int32), ('positions', C.c_void_p), ('normals', C.c_void_p),
                 ('uvs', C.c_void_p), ('material_ids', C.c_void_p), ('num_materials', C.c_int32),
                 ('materials', C.POINTER(MaterialDesc)), ('num_textures', C.c_int32),
-                ('textures', C.POINTER(TextureDesc))]
+                ('textures', C.POINTER(TextureDesc)), ('environment', C.POINTER(TextureDesc))]
 
 
 class CameraDesc(C.Structure):
@@ -70,7 +70,7 @@ EXPORTS = ['fr_last_error', 'fr_create', 'fr_iterate', 'fr_synchronize', 'fr_res
            'fr_read_wave_counts', 'fr_save_state', 'fr_load_state', 'fr_update',
            'fr_resolve_rgba8', 'fr_export_png', 'fr_write_png', 'fr_check_tc_gemm', 'fr_guide_params',
            'fr_guide_set_params', 'fr_read_guide_importance', 'fr_guide_gradient', 'fr_seek', 'fr_iterate_batch',
-           'fr_autotune', 'fr_update_dev']
+           'fr_autotune', 'fr_update_dev', 'fr_read_direct']
 
 STAGES = ('eye', 'photon', 'grid', 'gather', 'eye_trace', 'photon_trace')
 
@@ -117,6 +117,7 @@ def load(path=None):
     lib.fr_autotune.argtypes = [vp, C.c_int, C.POINTER(C.c_uint32)]
     lib.fr_update.argtypes = [vp, vp, vp]
     lib.fr_update_dev.argtypes = [vp, vp, vp]
+    lib.fr_read_direct.argtypes = [vp, vp, vp, vp]
     lib.fr_resolve_rgba8.argtypes = [vp, vp]
     lib.fr_export_png.argtypes = [vp, C.c_char_p]
     lib.fr_write_png.argtypes = [C.c_char_p, i32, i32, vp]
@@ -169,6 +170,11 @@ class Renderer:
         self._keep += [mats, tds]
         sd = SceneDesc(len(pos), pos.ctypes.data, nrm.ctypes.data, uv.ctypes.data, mat.ctypes.data,
                        len(scene['materials']), mats, len(texs), tds)
+        if scene.get('ibl') is not None:  # environment map
+            env = np.ascontiguousarray(scene['ibl'], np.uint8)
+            ed = TextureDesc(env.shape[1], env.shape[0], env.ctypes.data)
+            self._keep += [env, ed]
+            sd.environment = C.pointer(ed)
         cd = CameraDesc()
         cd.type, cd.width, cd.height = cam['type'], cam['width'], cam['height']
         cd.position = _f3(*cam['pos'])
@@ -320,6 +326,14 @@ class Renderer:
     def seek(self, first_step):
         """fr_seek: iteration k of this (fresh) context draws step first_step + k."""
         _check(_lib.fr_seek(self.h, int(first_step)), 'fr_seek')
+
+    def read_direct(self):
+        """fr_read_direct: (last iteration's per-pixel direct light, per-pixel sums, counts)."""
+        n = self.width * self.height
+        last, tot = np.empty((n, 3), np.float32), np.empty((n, 3), np.float32)
+        cnt = np.empty(n, np.int32)
+        _check(_lib.fr_read_direct(self.h, _ptr(last), _ptr(tot), _ptr(cnt)), 'fr_read_direct')
+        return last, tot, cnt
 
     def update_dev(self, m_ptr, phi4_ptr, sync=True):
         """fr_update_dev: device pointers to width*height int32 M and float4 flux sums."""

@@ -45,6 +45,8 @@ def write_scene(scene, directory, name='scene'):
     os.makedirs(md, exist_ok=True)
     for i, tex in enumerate(scene['textures']):
         write_png_rgba(os.path.join(md, 'tex%d.png' % i), tex)
+    if scene.get('ibl') is not None:  # environment map (the reference's IBL texture)
+        write_png_rgba(os.path.join(md, 'ibl.png'), scene['ibl'])
     with open(os.path.join(md, name + '.mtl'), 'w') as f:
         for m in scene['materials']:
             f.write('newmtl %s\n' % m['name'])

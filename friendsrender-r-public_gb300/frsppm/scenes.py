@@ -141,6 +141,26 @@ def noise_texture(rng, size, kind):
     return out
 
 
+def sky_texture(rng, width=128, height=64):
+    """RGBA8 equirectangular environment map for the reference's IBL (SPHERE
+    mapping: u around y, v = acos(y) / pi from the top): a seeded sky, bright
+    near the top, with value noise."""
+    v = (np.arange(height) + 0.5)[:, None] / height
+    n = value_noise(rng, max(width, height), 8, 3)[:height, :width]
+    base = np.clip(1.0 - v, 0.0, 1.0)[..., None] * np.array([0.55, 0.7, 1.0]) + 0.15
+    rgb = np.clip(base * (0.75 + 0.5 * n), 0.0, 1.0)
+    out = np.empty((height, width, 4), np.uint8)
+    out[..., :3] = np.round(rgb * 255.0).astype(np.uint8)
+    out[..., 3] = 255
+    return out
+
+
+def with_sky(scene, seed):
+    """The scene lit also by a seeded environment map (sky_texture)."""
+    scene['ibl'] = sky_texture(np.random.Generator(np.random.PCG64(seed)))
+    return scene
+
+
 def cornell_box(seed=CONFIG_SEED_BASE + 0, width=256, height=256, light_rgb=(17.0, 12.0, 4.0)):
     """Procedural Cornell box: unit cube with 5 diffuse walls, a diffuse box and
     a GGX-conductor box (roughness 0.2) rotated by U(0,30) degrees, and a
@@ -476,13 +496,17 @@ def small_caustic(seed=CONFIG_SEED_BASE + 102, width=96, height=96):
     return caustic_box(seed=seed, width=width, height=height, n_spheres=12, n_lat=12, n_lon=16, light_tex=64)
 
 
-def small_mixed(seed=CONFIG_SEED_BASE + 101, width=48, height=32, tex_size=64):
+def small_mixed(seed=CONFIG_SEED_BASE + 101, width=48, height=32, tex_size=64, ibl=False):
     """A small scene with every feature of the mixed-materials config (four
     material types, albedo/roughness/normal textures, textured light, thin
-    lens) at a size the reference and the oracle finish in seconds."""
-    return mixed_materials(seed=seed, width=width, height=height, n_spheres=12, field_n=24,
-                           tex_size=tex_size, light_tex=32, n_lat=10, n_lon=12, aperture=0.05,
-                           extent=0.6)
+    lens) at a size the reference and the oracle finish in seconds.  ibl: an
+    environment map (sky_texture) lights the paths that leave the scene."""
+    scene = mixed_materials(seed=seed, width=width, height=height, n_spheres=12, field_n=24,
+                            tex_size=tex_size, light_tex=32, n_lat=10, n_lon=12, aperture=0.05,
+                            extent=0.6)
+    if ibl:
+        scene['ibl'] = sky_texture(np.random.Generator(np.random.PCG64(seed + 7)))
+    return scene
 
 
 def scene_stats(scene):

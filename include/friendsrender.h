@@ -79,6 +79,14 @@ typedef struct fr_scene_desc {
   const fr_material_desc* materials;
   int32_t num_textures;
   const fr_texture_desc* textures;
+  /* Environment map lighting the eye paths that leave the scene (the
+   * reference's IBL texture, LightSampler.cpp:22-26: texels converted to
+   * 0.4 * c^2, SPHERE mapping IBL.h:96-104); NULL for none.  With one, an
+   * eye path goes on after its hitpoint (SPPM.cpp:170-173) and a path that
+   * misses adds the map's colour times its throughput to the pixel's direct
+   * light (SPPM.cpp:290-300, 409-414), which the resolve adds
+   * (SPPM.cpp:485). */
+  const fr_texture_desc* environment;
 } fr_scene_desc;
 
 /* Replaces iCamera (Camera.h:11-54) with PinholeCamera / ThinLensCamera.
@@ -328,6 +336,12 @@ int fr_read_photon_slots(fr_ctx* ctx, float* pos, float* flux, float* dir, uint3
 
 /* Per-pixel photon count M and flux sum of the last iteration's gather. */
 int fr_read_gather(fr_ctx* ctx, int32_t* m, float* phi4);
+
+/* Direct (environment) light: the last iteration's per-pixel value
+ * (HitPoint::DirectLight after the camera-pdf division, SPPM.cpp:345; 3
+ * floats, zero where the path did not miss) and the per-pixel sums and counts
+ * (SharedHitPoint::DirectLight / NumDirectLight).  Any pointer may be NULL. */
+int fr_read_direct(fr_ctx* ctx, float* last3, float* sum3, int32_t* count);
 
 /* Per-pixel progressive state: tau (3 doubles), N, R, NumGather. */
 int fr_read_state(fr_ctx* ctx, double* tau, int32_t* n, float* r, int32_t* g);

@@ -595,12 +595,13 @@ struct Geometry {  // SPPM.h:56-68
 struct HitPoint {  // SPPM.h:83-110
   int type = 0;    // 0 NONE, 1 HIT, 2 ONLY_DIRECTLIGHT
   V pos, normal, out, weight;
+  V dl;            // DirectLight: environment light at the path's end
   float rough = 0;
   int facet = -1;
   const Material* m = nullptr;
 };
 struct Photon { V pos, flux, dir; float index, pdf; bool valid = false; };  // SPPM.h:128-143
-struct Shared { V rad; int n = 0; float r = 0; int g = 0; };                 // SPPM.h:112-126
+struct Shared { V rad; int n = 0; float r = 0; int g = 0; V dl; int ndl = 0; };  // SPPM.h:112-126
 
 struct KdNode { int photon, axis, left, right; };
 
@@ -612,6 +613,8 @@ struct Renderer {
   Table light_table;
   Camera cam;
   BVH bvh;
+  Texture ibl;            // environment map, converted as LightSampler.cpp:24 does
+  bool has_ibl = false;
   int P = 0;
   float alpha = 0.9f, r0 = 0.015f;
   bool fix_stale = false;
@@ -704,6 +707,21 @@ struct Renderer {
 
   static bool near1(float s) { return std::abs(s - 1.0f) < 0.00001; }  // SPPM.h:27-29
 
+  // IBL::GetIBLColorFromDirection (IBL.h:122-129) with the SPHERE mapping of
+  // GetUVFromDirection (IBL.h:96-104): acos of a float is the double ::acos.
+  V ibl_color(V dir) const {
+    float u = 0.0f, v = 0.0f;
+    if (!(std::abs(dir.x) < 1e-6 && std::abs(dir.z) < 1e-6)) {
+      const V xz = normalized(V(dir.x, 0.0f, dir.z));
+      const double ax = ::acos((double)xz.x);
+      u = (float)((xz.z >= 0 ? ax : (double)(2.0f * PI) - ax) / (double)(2.0f * PI));
+      v = (float)(::acos((double)dir.y) / (double)PI);
+    }
+    float c[4];
+    tex_sample(ibl, u, v, c);
+    return V(c[0], c[1], c[2]);
+  }
+
   // getHitpointInfo (SPPM.cpp:98-306); stops at the first hitpoint (nothing
   // after it reaches the image without an environment light).
   HitPoint eye(int i) const {
@@ -717,6 +735,7 @@ struct Renderer {
     V thr(1, 1, 1);
     int depth = 0;
     HitPoint hp;
+    bool stored = false;  // isStoredPhoton
     while (true) {
       if (depth > 6) break;
       if (depth > 4) {
@@ -726,7 +745,9 @@ struct Renderer {
       }
       Hit hit;
       if (!closest(bvh, F, cur, hit)) {
-        hp.type = 2;
+        // Sample IBL (SPPM.cpp:290-300)
+        if (has_ibl) hp.dl = hp.dl + ibl_color(cur.d) * thr / PDF;
+        if (hp.type == 0) hp.type = 2;
         break;
       }
       Geometry g;
@@ -738,7 +759,7 @@ struct Renderer {
         cur.o = g.pos + cur.d * RAY_OFFSET;
         continue;
       }
-      if (g.m->sppm) {  // makeHitPoint (SPPM.cpp:79-96)
+      if (g.m->sppm && !stored) {  // makeHitPoint (SPPM.cpp:79-96), once per path (SPPM.cpp:170-173)
         hp.type = 1;
         hp.pos = g.pos;
         hp.normal = g.normal;
@@ -747,7 +768,11 @@ struct Renderer {
         hp.rough = g.rough;
         hp.facet = hit.facet;
         hp.m = g.m;
-        return hp;
+        hp.dl = V(0, 0, 0);
+        stored = true;
+        // The path goes on only for the environment light: without one,
+        // nothing after the hitpoint reaches the image.
+        if (!has_ibl) return hp;
       }
       float Ii, Io;
       if (near1(cur.index)) { Ii = 1.0f; Io = g.m->index; }
@@ -774,6 +799,7 @@ struct Renderer {
       cur = nxt;
       ++depth;
     }
+    hp.dl = hp.dl / cam_pdf;  // createHitpoints (SPPM.cpp:345)
     return hp;
   }
 
@@ -933,8 +959,13 @@ struct Renderer {
       const HitPoint& h = hp[v];
       gather_m[v] = 0;
       gather_phi[v] = V(0, 0, 0);
-      if (h.type != 1) continue;
+      if (h.type == 0) continue;
       Shared& s = sp[v];
+      if (norm2(h.dl) > 1e-8) {  // SPPM.cpp:411-414
+        s.dl = s.dl + h.dl;
+        s.ndl++;
+      }
+      if (h.type != 1) continue;
       const V bmin = h.pos - s.r * V(1, 1, 1), bmax = h.pos + s.r * V(1, 1, 1);
       V add(0, 0, 0);
       int m = 0;
@@ -966,7 +997,7 @@ struct Renderer {
     for (int i = 0; i < npix; ++i) {
       const Shared& s = sp[i];
       const float d = ((float)total_photons * (s.g + 0.0001f) / (0.0001f + (float)step)) * PI * s.r * s.r;
-      const V L = s.rad / d;
+      const V L = s.dl / (float)(s.ndl + 0.0001f) + s.rad / d;
       out[4 * i] = std::pow(L.x, 1.0f / 1.2f);
       out[4 * i + 1] = std::pow(L.y, 1.0f / 1.2f);
       out[4 * i + 2] = std::pow(L.z, 1.0f / 1.2f);
@@ -1193,6 +1224,34 @@ void port_read_gather(void* h, int32_t* m, float* phi) {
   for (size_t i = 0; i < r->gather_m.size(); ++i) {
     m[i] = r->gather_m[i];
     phi[3 * i] = r->gather_phi[i].x; phi[3 * i + 1] = r->gather_phi[i].y; phi[3 * i + 2] = r->gather_phi[i].z;
+  }
+}
+
+// Environment map (RGBA8, w x h) as the IBL texture: each texel value / 255.0f
+// (TextureUtility.cpp:28), converted by 0.4 * (c^2, c^2, c^2, 0)
+// (LightSampler.cpp:24: the literal 0.4 meets operator*(float, Vec4)).
+void port_set_ibl(void* h, int32_t w, int32_t hh, const uint8_t* texels) {
+  Renderer* r = static_cast<Renderer*>(h);
+  r->ibl.w = w;
+  r->ibl.h = hh;
+  r->ibl.c.resize((size_t)w * hh * 4);
+  for (size_t i = 0; i < (size_t)w * hh; ++i)
+    for (int k = 0; k < 4; ++k) {
+      const float c = k < 3 ? texels[4 * i + k] / 255.0f : 0.0f;
+      r->ibl.c[4 * i + k] = 0.4f * (c * c);
+    }
+  r->has_ibl = true;
+}
+
+// Per-hitpoint direct light of the last iteration and per-pixel sums and counts.
+void port_read_direct(void* h, float* hp_dl, float* sp_dl, int32_t* sp_ndl) {
+  Renderer* r = static_cast<Renderer*>(h);
+  for (size_t i = 0; i < r->sp.size(); ++i) {
+    const HitPoint& p = r->hp[i];
+    const Shared& s = r->sp[i];
+    hp_dl[3 * i] = p.dl.x; hp_dl[3 * i + 1] = p.dl.y; hp_dl[3 * i + 2] = p.dl.z;
+    sp_dl[3 * i] = s.dl.x; sp_dl[3 * i + 1] = s.dl.y; sp_dl[3 * i + 2] = s.dl.z;
+    sp_ndl[i] = s.ndl;
   }
 }
 

@@ -48,6 +48,8 @@ def load():
             getattr(lib, name).argtypes = [vp]
             getattr(lib, name).restype = None
         lib.port_iterate.argtypes = [vp, C.c_int32]
+        lib.port_set_ibl.argtypes = [vp, C.c_int32, C.c_int32, vp]
+        lib.port_read_direct.argtypes = [vp, vp, vp, vp]
         lib.port_seek.argtypes = [vp, C.c_int32]
         lib.port_photon_pass.argtypes = [vp, C.c_int32, C.c_int32]
         lib.port_resolve.argtypes = [vp, vp]
@@ -126,6 +128,9 @@ class PortRenderer:
                                  int(fix_stale))
         if not self.h:
             raise RuntimeError('port_create failed (no emissive facets?)')
+        if scene.get('ibl') is not None:
+            ibl = np.ascontiguousarray(scene['ibl'], np.uint8)
+            lib.port_set_ibl(self.h, ibl.shape[1], ibl.shape[0], _p(ibl))
         self.width, self.height, self.photons = c['width'], c['height'], int(photons)
 
     def close(self):
@@ -180,6 +185,15 @@ class PortRenderer:
         rough = np.empty(n, np.float32)
         _lib.port_read_hitpoints(self.h, _p(t), _p(f), *[_p(x) for x in a], _p(rough))
         return dict(type=t, facet=f, pos=a[0], nrm=a[1], out=a[2], w=a[3], rough=rough)
+
+    def read_direct(self):
+        """Direct (environment) light: per hitpoint of the last iteration, and
+        per pixel the sum and count (SharedHitPoint::DirectLight, NumDirectLight)."""
+        n = self.width * self.height
+        hp, sp = np.empty((n, 3), np.float32), np.empty((n, 3), np.float32)
+        cnt = np.empty(n, np.int32)
+        _lib.port_read_direct(self.h, _p(hp), _p(sp), _p(cnt))
+        return hp, sp, cnt
 
     def compacted_photons(self):
         n = int(_lib.port_num_photons(self.h))

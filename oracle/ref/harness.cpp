@@ -176,8 +176,13 @@ int main(int argc, char** argv) {
   std::FILE* devnull = std::freopen("/dev/null", "w", stdout);
   (void)devnull;
 
+  // An environment map, when the scene has one (meshData/ibl.png), goes to
+  // CreateScene as the IBL texture (main.cpp:132-143).
+  Texture2D ibl;
+  const bool has_ibl = access("meshData/ibl.png", R_OK) == 0;
+  if (has_ibl && !TextureUtility::LoadTextureFromFile(ibl, "meshData//ibl.png")) { std::fprintf(stderr, "IBL load failed\n"); return 2; }
   Scene scene;
-  if (!scene.CreateScene("meshData//scene.obj", &mats, nullptr)) { std::fprintf(stderr, "CreateScene failed\n"); return 2; }
+  if (!scene.CreateScene("meshData//scene.obj", &mats, has_ibl ? &ibl : nullptr)) { std::fprintf(stderr, "CreateScene failed\n"); return 2; }
 
   // Rebuild the scene BVH with the reference's single-threaded Build2
   // (bvh8.h:44-76): Build3, which CreateScene uses (Scene.cpp:210-211), calls
@@ -395,12 +400,13 @@ int main(int argc, char** argv) {
     const std::string pre = out_dir + "/it" + std::to_string(s) + "_";
     const size_t HW = (size_t)W * H;
     std::vector<int32_t> hp_type(HW), hp_facet(HW);
-    std::vector<float> hp_pos, hp_nrm, hp_out, hp_w, hp_rough;
+    std::vector<float> hp_pos, hp_nrm, hp_out, hp_w, hp_rough, hp_dl;
     for (size_t v = 0; v < HW; ++v) {
       const auto& h = hitPoints[v];
       hp_type[v] = h.Type;
       hp_facet[v] = h.Type == SPPMR::HitPoint::HIT ? h.Facet._FacetID : -1;
       push3(hp_pos, h.Position); push3(hp_nrm, h.Gmt.Normal); push3(hp_out, h.OutDir); push3(hp_w, h.PixelWeight);
+      push3(hp_dl, h.DirectLight);
       hp_rough.push_back(h.Gmt.param.Roughness);
     }
     npy_i32(pre + "hp_type.npy", hp_type, {HW});
@@ -409,6 +415,7 @@ int main(int argc, char** argv) {
     npy_f32(pre + "hp_nrm.npy", hp_nrm, {HW, 3});
     npy_f32(pre + "hp_out.npy", hp_out, {HW, 3});
     npy_f32(pre + "hp_w.npy", hp_w, {HW, 3});
+    npy_f32(pre + "hp_dl.npy", hp_dl, {HW, 3});
     npy_f32(pre + "hp_rough.npy", hp_rough, {HW});
     std::vector<float> ph;
     for (const auto& p : photon) {
@@ -419,8 +426,13 @@ int main(int argc, char** argv) {
     npy_i32(pre + "ph_slot.npy", ph_slot, {photon.size()});
     npy_i32(pre + "gather_m.npy", gM, {HW});
     npy_f32(pre + "gather_phi.npy", gPhi, {HW, 3});
-    std::vector<float> sp_rad, sp_r; std::vector<int32_t> sp_n, sp_g;
-    for (const auto& sp : sharedPoints) { push3(sp_rad, sp.Radiance); sp_r.push_back(sp.Radius); sp_n.push_back(sp.NumPhoton); sp_g.push_back(sp.NumGather); }
+    std::vector<float> sp_rad, sp_r, sp_dl; std::vector<int32_t> sp_n, sp_g, sp_ndl;
+    for (const auto& sp : sharedPoints) {
+      push3(sp_rad, sp.Radiance); sp_r.push_back(sp.Radius); sp_n.push_back(sp.NumPhoton); sp_g.push_back(sp.NumGather);
+      push3(sp_dl, sp.DirectLight); sp_ndl.push_back(sp.NumDirectLight);
+    }
+    npy_f32(pre + "sp_dl.npy", sp_dl, {HW, 3});
+    npy_i32(pre + "sp_ndl.npy", sp_ndl, {HW});
     npy_f32(pre + "sp_rad.npy", sp_rad, {HW, 3});
     npy_f32(pre + "sp_r.npy", sp_r, {HW});
     npy_i32(pre + "sp_n.npy", sp_n, {HW});

@@ -47,6 +47,7 @@ FIXTURES = {
     # name: (scene factory, photons per iteration, iterations)
     'cornell32': (lambda: scenes.cornell_box(width=32, height=32), 2000, 3),
     'mixed48x32': (lambda: scenes.small_mixed(), 2000, 3),
+    'mixed48x32_ibl': (lambda: scenes.small_mixed(ibl=True), 2000, 3),
 }
 
 
@@ -56,6 +57,8 @@ def scene_sha(scene):
         h.update(np.ascontiguousarray(scene[k]).tobytes())
     for t in scene['textures']:
         h.update(np.ascontiguousarray(t).tobytes())
+    if scene.get('ibl') is not None:
+        h.update(b'ibl' + np.ascontiguousarray(scene['ibl']).tobytes())
     h.update(repr([sorted(m.items()) for m in scene['materials']]).encode())
     h.update(repr(sorted(scene['camera'].items())).encode())
     return h.hexdigest()
@@ -120,8 +123,8 @@ def make(name, factory, photons, iters, out_dir=HERE):
                     image=np.load(os.path.join(od, 'image.npy')), meta=np.load(os.path.join(od, 'meta.npy')),
                     image_png=decode_png(os.path.join(od, 'image.png')))
         for s in range(1, iters + 1):
-            for k in ('hp_type', 'hp_facet', 'hp_pos', 'hp_nrm', 'hp_out', 'hp_w', 'hp_rough', 'ph', 'ph_path',
-                      'ph_slot', 'gather_m', 'gather_phi', 'sp_rad', 'sp_r', 'sp_n', 'sp_g'):
+            for k in ('hp_type', 'hp_facet', 'hp_pos', 'hp_nrm', 'hp_out', 'hp_w', 'hp_rough', 'hp_dl', 'ph', 'ph_path',
+                      'ph_slot', 'gather_m', 'gather_phi', 'sp_rad', 'sp_r', 'sp_n', 'sp_g', 'sp_dl', 'sp_ndl'):
                 data['it%d_%s' % (s, k)] = np.load(os.path.join(od, 'it%d_%s.npy' % (s, k)))
     path = os.path.join(out_dir, name + '.npz')
     np.savez_compressed(path, **data)
@@ -159,8 +162,12 @@ def make_caustic_row(out_dir=HERE, work=None):
 if __name__ == '__main__':
     if not os.path.exists(FRREF):
         sys.exit('build the reference first: make -C oracle/ref')
+    only = sys.argv[1:]
     for name, (factory, photons, iters) in FIXTURES.items():
+        if only and name not in only:
+            continue
         p = make(name, factory, photons, iters)
         print(p, os.path.getsize(p))
-    p = make_caustic_row()
-    print(p, os.path.getsize(p))
+    if not only or 'caustic' in only:
+        p = make_caustic_row()
+        print(p, os.path.getsize(p))

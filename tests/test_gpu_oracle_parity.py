@@ -19,6 +19,11 @@ CASES = {
     # (displaced geodesic spheres, instanced and flattened), small.
     'caustic96': (lambda s: s.small_caustic(), 20000, 3, 0.7, 0.01),
     'large64x36': (lambda s: s.small_large_scene(), 20000, 3, 0.7, 0.02),
+    # With an environment map: eye paths go on after their hitpoints.
+    'mixed128x72_ibl': (lambda s: s.with_sky(s.mixed_materials(width=128, height=72, n_spheres=24, field_n=48,
+                                                               tex_size=128, light_tex=64, n_lat=12, n_lon=16,
+                                                               extent=0.8, aperture=0.05), 77),
+                        20000, 3, 0.7, 0.02),
 }
 
 
@@ -55,6 +60,13 @@ def test_gpu_matches_oracle(name):
             sg, sc = g.read_state(), c.read_state()
             np.testing.assert_array_equal(sg['n'], sc['n'])
             np.testing.assert_array_equal(sg['r'], sc['r'])
+            if scene.get('ibl') is not None:
+                np.testing.assert_array_equal(hg['type'], hc['type'])
+                lg, tg, ng = g.read_direct()
+                lc, tc, nc = c.read_direct()
+                np.testing.assert_array_equal(ng, nc)
+                for a, b in ((lg, lc), (tg, tc)):
+                    assert np.abs(a - b).max() <= 1e-4 * np.abs(b).max() + 1e-30
             assert np.abs(sg['tau'] - sc['tau']).max() <= 1e-4 * np.abs(sc['tau']).max()
         ig, ic = g.resolve(), c.resolve()
     assert np.abs(ig - ic).max() <= 1e-4 * np.abs(ic).max()

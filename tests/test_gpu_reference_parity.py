@@ -87,6 +87,13 @@ def test_iterations_match_reference(name):
             np.testing.assert_array_equal(st['r'], gold['it%d_sp_r' % s])
             ref_tau = gold['it%d_sp_rad' % s]
             assert np.abs(st['tau'] - ref_tau).max() <= 1e-4 * np.abs(ref_tau).max() + 1e-30
+            if 'it%d_hp_dl' % s in gold:  # environment light (IBL)
+                # HIT / ONLY_DIRECTLIGHT / NONE as the reference's.
+                np.testing.assert_array_equal(hp['type'], t_ref)
+                last, tot, cnt = r.read_direct()
+                np.testing.assert_array_equal(cnt, gold['it%d_sp_ndl' % s])
+                for got, ref in ((last, gold['it%d_hp_dl' % s]), (tot, gold['it%d_sp_dl' % s])):
+                    assert np.abs(got - ref).max() <= 1e-4 * np.abs(ref).max() + 1e-30
         img = r.resolve()
     ref = gold['image']
     assert np.isfinite(img).all()

@@ -63,6 +63,12 @@ def test_oracle_iterations_match_reference(port, name):
             np.testing.assert_array_equal(st['r'], gold['it%d_sp_r' % s])
             np.testing.assert_array_equal(st['g'], gold['it%d_sp_g' % s])
             assert np.abs(st['tau'] - gold['it%d_sp_rad' % s]).max() <= 1e-5 * np.abs(gold['it%d_sp_rad' % s]).max()
+            if 'it%d_hp_dl' % s in gold:  # environment light: types, direct light, sums, counts
+                np.testing.assert_array_equal(hp['type'], t)
+                last, tot, cnt = r.read_direct()
+                np.testing.assert_array_equal(last, gold['it%d_hp_dl' % s])
+                np.testing.assert_array_equal(tot, gold['it%d_sp_dl' % s])
+                np.testing.assert_array_equal(cnt, gold['it%d_sp_ndl' % s])
         img = r.resolve()
     assert np.abs(img - gold['image']).max() <= 1e-5 * np.abs(gold['image']).max()
 
