@@ -1360,7 +1360,8 @@ int fr_guide_gradient(fr_ctx* c, int32_t n, const float* samples, float* grad, f
 // the random streams and the resolve), the per-pixel state and the photon
 // slots (a slot stored in an earlier iteration can join a later iteration's
 // photon set, SPPM.cpp:672).  Layout: a fixed header, then tau, N, R,
-// NumGather, slot positions, fluxes and directions, each as on the device.
+// NumGather, direct light with its count, slot positions, fluxes and
+// directions, each as on the device.
 namespace {
 struct StateHeader {
   char magic[8];  // "FRSPPMS1"

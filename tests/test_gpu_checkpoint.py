@@ -64,7 +64,7 @@ def test_checkpoint_size_and_refusals():
         a.iterate(1)
         ckpt = a.save_state()
         npix, slots = 96 * 64, 15000 * 32
-        assert len(ckpt) == 56 + npix * (24 + 4 + 4 + 4) + slots * 48
+        assert len(ckpt) == 56 + npix * (24 + 4 + 4 + 4 + 16) + slots * 48
         a.load_state(ckpt)                 # same context: accepted
         with pytest.raises(RuntimeError):
             a.load_state(ckpt[:-1])        # truncated
