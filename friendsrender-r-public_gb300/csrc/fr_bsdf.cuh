@@ -297,39 +297,181 @@ __device__ __forceinline__ float ggxglass_brdf(const FParam& p) {
   return (wi_wm * wo_wm) / (wi_n * wo_n) * (Io * Io) * (1.0f - F) * G * D * pow_m2(Ii * wo_wm + Io * wi_wm);
 }
 
-// Virtual Surface dispatch (material.h:137-146) for the four surfaces.
+// ------------------------------------------- the demo's further surfaces
+// BiMetalSurface, GlassSurface, GlossTransmitSurface, DiffuseTransmitSurface
+// (material.h:427-531, 637-766).  Where the reference promotes to double (a
+// double literal), the restatement computes in double: these surfaces are
+// rare enough that FP64 costs nothing measurable, and IEEE double gives the
+// reference's bits.
+
+// The surface normal facing the incoming ray's side (material.h:429, 485, 698).
+__device__ __forceinline__ V3 facing(V3 n, V3 in) { return dot(n, in) < 0.0f ? n : -n; }
+
+// Sampling::Refract_Sampling (Sampling.cpp:329-337)
+__device__ __forceinline__ V3 refract_sampling(V3 n, V3 in, float ii, float io) {
+  const float eta = ii / io;
+  const V3 NN = dot(in, n) > 0.0f ? -n : n;
+  const float LN = -dot(in, NN);
+  const float sq = fmaxf(0.00000001f, 1.0f - eta * eta * (1.0f - LN * LN));
+  return normalized(-NN * sqrtf(sq) - eta * (-in - LN * NN));
+}
+
+// GlassSurface::Refract (material.h:470-477): as Refract_Sampling.
+__device__ __forceinline__ V3 glass_refract(float from, float to, V3 in, V3 n) { return refract_sampling(n, in, from, to); }
+
+// GlossTransmitSurface::ReflectByN (material.h:683-686)
+__device__ __forceinline__ V3 reflect_by_n(V3 r, V3 n) { return r - 2.0f * dot(n, r) * n; }
+
+// BiMetalSurface (material.h:427-463)
+__device__ __forceinline__ float bimetal_brdf(const FParam& p) {
+  const V3 N = facing(p.n, p.in);
+  if (!opaque_reflect(p)) return 0.0f;
+  const V3 ref = reflect_sampling(N, p.in);
+  if (dot(ref, p.out) > 1.0f - 1.0f / kDeltaPDF) return metal_brdf(dot(p.out, N), kDeltaPDF);
+  return 0.0f;
+}
+__device__ __forceinline__ float bimetal_pdf(const FParam& p) {
+  const V3 ref = reflect_sampling(facing(p.n, p.in), p.in);
+  return dot(ref, p.out) > 1.0f - 1.0f / kDeltaPDF ? kDeltaPDF : kSMin;
+}
+
+// GlassSurface (material.h:465-531)
+__device__ __forceinline__ V3 glass_sampling(Rng& rng, const FParam& p, float* pdf) {
+  const V3 NN = facing(p.n, p.in);
+  const float reflectance = fresnel_reflectance(NN, p.in, p.from, p.to);
+  if (reflectance > rng.next()) {
+    *pdf = reflectance;
+    return reflect_sampling(NN, p.in);
+  }
+  *pdf = 1.0f - reflectance;
+  const float eta = p.from / p.to;
+  const float LN = -dot(p.in, NN);
+  const float sq = (float)(1.0f - (double)(eta * eta) * (1.0 - (double)(LN * LN)));
+  if (sq < kLt1e6) return reflect_sampling(p.n, p.in);
+  return glass_refract(p.from, p.to, p.in, p.n);
+}
+__device__ __forceinline__ float glass_brdf(const FParam& p) {
+  const V3 NN = facing(p.n, p.in);
+  const float reflectance = fresnel_reflectance(NN, p.in, p.from, p.to);
+  const float w = is_reflect(p.in, p.out, p.n) ? kDeltaPDF * reflectance : kDeltaPDF * (1.0f - reflectance);
+  return (float)((double)w / ((double)fabsf(dot(p.out, NN)) + 0.0001));
+}
+__device__ __forceinline__ float glass_pdf_delta(const FParam& p) {
+  const V3 NN = facing(p.n, p.in);
+  const float reflectance = fresnel_reflectance(NN, p.in, p.from, p.to);
+  if (is_reflect(p.in, p.out, p.n)) {
+    const V3 ref = reflect_sampling(NN, p.in);
+    return fabsf(dot(ref, p.out)) > kGt0_99 ? kDeltaPDF * reflectance : kSMin;
+  }
+  const V3 rac = refract_sampling(NN, p.in, p.from, p.to);
+  return fabsf(dot(rac, p.out)) > kGt0_99 ? kDeltaPDF * (1.0f - reflectance) : kSMin;
+}
+
+// DiffuseTransmitSurface (material.h:637-675)
+__device__ __forceinline__ V3 diffuse_transmit_sampling(Rng& rng, const FParam& p, float* pdf) {
+  const V3 n = dot(p.n, p.in) > 0.0f ? p.n : -p.n;
+  if (p.refl > rng.next()) {
+    const V3 rs = cos_sampling(rng, -n, pdf);
+    *pdf *= p.refl;
+    return rs;
+  }
+  const V3 rs = cos_sampling(rng, n, pdf);
+  *pdf *= (1.0f - p.refl);
+  return rs;
+}
+__device__ __forceinline__ float diffuse_transmit_brdf(const FParam& p) {
+  return is_reflect(p.in, p.out, p.n) ? p.refl / kPI : (1.0f - p.refl) / kPI;
+}
+__device__ __forceinline__ float diffuse_transmit_pdf(const FParam& p) {
+  const float c = (float)fabs((double)dot(p.out, p.n) + 0.00001);
+  return is_reflect(p.in, p.out, p.n) ? p.refl * c / kPI : (1.0f - p.refl) * c / kPI;
+}
+
+// GlossTransmitSurface (material.h:677-766)
+__device__ __forceinline__ V3 gloss_transmit_sampling(Rng& rng, const FParam& p, float* pdf) {
+  const V3 n = facing(p.n, p.in);
+  if (p.refl > rng.next()) {
+    const V3 rs = ggx_sampling(rng, n, p.in, p.rough, pdf);
+    *pdf *= p.refl;
+    return rs;
+  }
+  const V3 rs = reflect_by_n(ggx_sampling(rng, n, p.in, p.rough, pdf), n);
+  *pdf *= (1.0f - p.refl);
+  return rs;
+}
+__device__ __forceinline__ float gloss_transmit_brdf(const FParam& p) {
+  constexpr float kSmall = 1e-10f;
+  const float power = is_reflect(p.in, p.out, p.n) ? p.refl : 1.0f - p.refl;
+  const V3 in = p.in;
+  const V3 N = facing(p.n, in);
+  V3 out = p.out;
+  if (dot(out, N) < 0.0f) out = reflect_by_n(out, N);
+  if (dot(in, N) > -kSmall || dot(out, N) < kSmall) return 0.0f;
+  const float alpha = p.rough;
+  const V3 h = normalized(-in + out);
+  const float ccs = dot(h, N);
+  if (ccs < kSmall || dot(h, in) > -kSmall || dot(h, out) < kSmall) return 0.0f;
+  const float dd = 1.0001f - (1.0f - alpha * alpha) * ccs * ccs;
+  const float D = fmaxf(kSMin, (alpha * alpha) / (kPI * (dd * dd)));
+  const float lc = fmaxf(0.0f, fminf(0.9999f, dot(in, -N)));
+  const float lv = fmaxf(0.0f, fminf(0.9999f, dot(out, N)));
+  if (lc < kSMin || lv < kSMin) return 0.0f;
+  const float L_l = conductor_lambda(alpha * alpha, 1.0f / (lc * lc));
+  const float L_v = conductor_lambda(alpha * alpha, 1.0f / (lv * lv));
+  const float G = 1.0f / ((1.0f + L_l) * (1.0f + L_v));
+  const float fx = (4.0f * dot(in, -N) * dot(out, N));
+  return power * (G * D) / fx;
+}
+__device__ __forceinline__ float gloss_transmit_pdf(const FParam& p) {
+  if (is_reflect(p.in, p.out, p.n)) return p.refl * ggx_sampling_pdf(p.out, p.n, p.in, p.rough);
+  return (1.0f - p.refl) * ggx_sampling_pdf(reflect_by_n(p.out, p.n), p.n, p.in, p.rough);
+}
+
+// Virtual Surface dispatch (material.h:137-146) for the eight surfaces.
 __device__ __forceinline__ V3 surface_sample(int type, Rng& rng, const FParam& p, float* pdf) {
   switch (type) {
-    case 0: return cos_sampling(rng, p.n, pdf);                                        // DiffuseSurface
-    case 1: *pdf = kDeltaPDF; return reflect_sampling(p.n, p.in);                      // MetalSurface
-    case 2: return ggx_sampling(rng, p.n, p.in, p.rough, pdf);                         // Roughconductor
-    default: return ggxglass_sampling(rng, p.n, p.in, p.rough, p.from, p.to, pdf);    // GGXGlass
+    case kSurfDiffuse: return cos_sampling(rng, p.n, pdf);                                 // DiffuseSurface
+    case kSurfMetal: *pdf = kDeltaPDF; return reflect_sampling(p.n, p.in);                 // MetalSurface
+    case kSurfConductor: return ggx_sampling(rng, p.n, p.in, p.rough, pdf);                // Roughconductor
+    case kSurfGGXGlass: return ggxglass_sampling(rng, p.n, p.in, p.rough, p.from, p.to, pdf);  // GGXGlass
+    case kSurfBiMetal: *pdf = kDeltaPDF; return reflect_sampling(facing(p.n, p.in), p.in);
+    case kSurfGlass: return glass_sampling(rng, p, pdf);
+    case kSurfGlossTransmit: return gloss_transmit_sampling(rng, p, pdf);
+    default: return diffuse_transmit_sampling(rng, p, pdf);                               // DiffuseTransmit
   }
 }
 
 __device__ __forceinline__ float surface_brdf(int type, const FParam& p) {
   switch (type) {
-    case 0: return opaque_reflect(p) ? 1.0f / kPI : 0.0f;
-    case 1: {
+    case kSurfDiffuse: return opaque_reflect(p) ? 1.0f / kPI : 0.0f;
+    case kSurfMetal: {
       if (!opaque_reflect(p)) return 0.0f;
       const V3 ref = reflect_sampling(p.n, p.in);
       if (dot(ref, p.out) > 1.0f - 1.0f / kDeltaPDF) return metal_brdf(dot(p.out, p.n), kDeltaPDF);
       return 0.0f;
     }
-    case 2: return roughconductor_brdf(p);
-    default: return ggxglass_brdf(p);
+    case kSurfConductor: return roughconductor_brdf(p);
+    case kSurfGGXGlass: return ggxglass_brdf(p);
+    case kSurfBiMetal: return bimetal_brdf(p);
+    case kSurfGlass: return glass_brdf(p);
+    case kSurfGlossTransmit: return gloss_transmit_brdf(p);
+    default: return diffuse_transmit_brdf(p);
   }
 }
 
 __device__ __forceinline__ float surface_pdf(int type, const FParam& p) {
   switch (type) {
-    case 0: return fmaxf(kSMin, dot(p.out, p.n) / kPI);
-    case 1: {
+    case kSurfDiffuse: return fmaxf(kSMin, dot(p.out, p.n) / kPI);
+    case kSurfMetal: {
       const V3 ref = reflect_sampling(p.n, p.in);
       return dot(ref, p.out) > 1.0f - 1.0f / kDeltaPDF ? kDeltaPDF : kSMin;
     }
-    case 2: return ggx_sampling_pdf(p.out, p.n, p.in, p.rough);
-    default: return ggxglass_sampling_pdf(p.out, p.n, p.in, p.rough, p.from, p.to);
+    case kSurfConductor: return ggx_sampling_pdf(p.out, p.n, p.in, p.rough);
+    case kSurfGGXGlass: return ggxglass_sampling_pdf(p.out, p.n, p.in, p.rough, p.from, p.to);
+    case kSurfBiMetal: return bimetal_pdf(p);
+    case kSurfGlass: return glass_pdf_delta(p);
+    case kSurfGlossTransmit: return gloss_transmit_pdf(p);
+    default: return diffuse_transmit_pdf(p);
   }
 }
 

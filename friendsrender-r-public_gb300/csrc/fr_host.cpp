@@ -299,7 +299,7 @@ int check_scene(const fr_scene_desc* s) {
       return fail(FR_ERR_INVALID, "scene: texture %d is empty", t);
   for (int m = 0; m < s->num_materials; ++m) {
     const fr_material_desc& d = s->materials[m];
-    if (d.type < 0 || d.type > 3) return fail(FR_ERR_INVALID, "material %d: type %d", m, d.type);
+    if (d.type < 0 || d.type > 7) return fail(FR_ERR_INVALID, "material %d: type %d", m, d.type);
     const int tex[3] = {d.tex_albedo, d.tex_roughness, d.tex_bump};
     for (int k = 0; k < 3; ++k)
       if (tex[k] < -1 || tex[k] >= s->num_textures) return fail(FR_ERR_INVALID, "material %d: texture index", m);

@@ -494,7 +494,8 @@ __global__ void __launch_bounds__(256) k_wave_sort(SceneGPU sc, PathWave w, int 
     if (j < n) {
       i = q[j];
       const int facet = __float_as_int(w.hit[i].w);
-      type = facet >= 0 ? sc.mats[sc.shade[facet].attr].type : kShadeQueues - 1;
+      // The demo's further surfaces (types 4-7) share the four queues (type mod 4).
+      type = facet >= 0 ? (sc.mats[sc.shade[facet].attr].type & 3) : kShadeQueues - 1;
     }
     block_append<kShadeQueues>(w.mq, w.cap, mc, type, i);
   }

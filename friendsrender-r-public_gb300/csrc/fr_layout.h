@@ -15,6 +15,9 @@ constexpr uint32_t kPhiloxKeyHi = 0x5350504Du;  // second Philox key word of eve
 
 // Hitpoint types (SPPM.h:85-89).
 constexpr int kHitNone = 0, kHitHit = 1, kHitOnlyDirect = 2;
+// Surface types (FR_MAT_*).
+constexpr int kSurfDiffuse = 0, kSurfMetal = 1, kSurfConductor = 2, kSurfGGXGlass = 3, kSurfBiMetal = 4,
+              kSurfGlass = 5, kSurfGlossTransmit = 6, kSurfDiffuseTransmit = 7;
 
 // Material flags.
 constexpr int kMatSPPM = 1;    // SURFACE_PARAM::isSPPMSurface
@@ -22,7 +25,7 @@ constexpr int kMatOpaque = 2;  // SURFACE_PARAM::IfOpeque
 
 // One attribute (Normal_Facet.h:67-113): the Surface subclass and its SURFACE_PARAM.
 struct MaterialGPU {
-  int32_t type;        // 0 Diffuse, 1 Metal, 2 GGX conductor, 3 GGX dielectric
+  int32_t type;        // kSurf*
   int32_t flags;       // kMatSPPM | kMatOpaque
   int32_t tex_albedo;  // texture index or -1 (map_Kd)
   int32_t tex_rough;   // (map_d)

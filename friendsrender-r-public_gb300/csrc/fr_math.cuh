@@ -51,6 +51,7 @@ constexpr float kLt1e8 = 0x1.5798f0p-27f;      // (double)g < 1e-8
 constexpr float kGt1e8 = 0x1.5798eep-27f;      // (double)g > 1e-8
 constexpr float kGt0_999999 = 0x1.ffffdep-1f;  // (double)g > 0.999999
 constexpr float kGt0_9 = 0x1.ccccccp-1f;       // (double)g > 0.9
+constexpr float kGt0_99 = 0x1.fae146p-1f;      // (double)g > 0.99
 
 // ---------------------------------------------------------------- Philox
 // Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11).  A stream is keyed by the

@@ -25,6 +25,8 @@ import math
 import numpy as np
 
 DIFFUSE, METAL, GGX_CONDUCTOR, GGX_DIELECTRIC = 0, 1, 2, 3
+# The demo's further surfaces (material.h:427-766, used by main.cpp:14-114).
+BIMETAL, GLASS, GLOSS_TRANSMIT, DIFFUSE_TRANSMIT = 4, 5, 6, 7
 PINHOLE, THINLENS = 0, 1
 
 CONFIG_SEED_BASE = 0x5EED0000
@@ -489,6 +491,59 @@ def batch_scene(spec, tex_size=256, light_tex=64):
     res = spec['resolution']
     return mixed_materials(seed=spec['seed'], width=res, height=res, n_spheres=n_spheres, field_n=field_n,
                            tex_size=tex_size, light_tex=light_tex, n_lat=n_lat, n_lon=n_lon)
+
+
+def demo_surface(k, name, rng):
+    """Material k % 8 of the eight surface types, with the reference demo's
+    parameters for the further four (main.cpp:14-114)."""
+    t = k % 8
+    col = tuple(float(x) for x in rng.uniform(0.3, 0.95, 3))
+    rough = float(rng.uniform(0.05, 0.5))
+    if t == DIFFUSE:
+        return material(name, DIFFUSE, col)
+    if t == METAL:
+        return material(name, METAL, col, sppm=False)
+    if t == GGX_CONDUCTOR:
+        return material(name, GGX_CONDUCTOR, col, roughness=rough, index=1.1978, extinction=7.0488)
+    if t == GGX_DIELECTRIC:
+        return material(name, GGX_DIELECTRIC, (0.98, 0.98, 0.98), roughness=rough, index=1.5, opaque=False,
+                        sppm=False)
+    if t == BIMETAL:
+        return material(name, BIMETAL, col, sppm=False)
+    if t == GLASS:
+        return material(name, GLASS, (0.98, 0.98, 0.98), index=1.5, opaque=False, sppm=False)
+    if t == GLOSS_TRANSMIT:
+        return material(name, GLOSS_TRANSMIT, (0.97, 0.98, 0.98), roughness=0.25, reflectance=0.1,
+                        opaque=False, sppm=True)
+    return material(name, DIFFUSE_TRANSMIT, col, reflectance=0.7, opaque=False, sppm=True)
+
+
+def demo_materials(seed=CONFIG_SEED_BASE + 105, width=48, height=32, n_spheres=16, field_n=24, tex_size=64,
+                   light_tex=32, n_lat=10, n_lon=12, aperture=0.05, extent=0.6):
+    """The mixed-materials construction with spheres of all eight surface
+    types in turn: the four of the mixed-materials config and the demo's
+    BiMetal, Glass, GlossTransmit and DiffuseTransmit surfaces."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    textures = [noise_texture(rng, tex_size, 'albedo'), noise_texture(rng, tex_size, 'roughness'),
+                noise_texture(rng, tex_size, 'normal'), noise_texture(rng, light_tex, 'emission')]
+    mats = [material('field', DIFFUSE, (0.7, 0.7, 0.7), tex_albedo=0, tex_roughness=1, tex_bump=2),
+            material('light', DIFFUSE, (1, 1, 1), emission=(10.0, 9.0, 8.0), tex_albedo=3)]
+    b = _Builder()
+    ext = float(extent)
+    k_s = ext / 4.0
+    height_field(b, rng, field_n, -ext, ext, -ext, ext, 0.25 * k_s, 0)
+    for k in range(n_spheres):
+        mats.append(demo_surface(k, 'd%03d' % k, rng))
+        r = float(rng.uniform(0.05, 0.3)) * k_s
+        cx, cz = rng.uniform(-ext * 0.85, ext * 0.85, 2)
+        uv_sphere(b, (cx, 0.25 * k_s + r, cz), r, len(mats) - 1, n_lat, n_lon)
+    ly, lh = 3.0 * k_s, 1.0 * k_s
+    b.quad((-lh, ly, -lh), (lh, ly, -lh), (lh, ly, lh), (-lh, ly, lh), (0, -1, 0), 1)
+    scene = b.build()
+    scene.update(materials=mats, textures=textures,
+                 camera=_camera(THINLENS, width, height, (0.0, 2.6 * k_s, -7.5 * k_s), (0.0, 0.2 * k_s, 0.0),
+                                30.0, focal=0.9, dist=1.0, lens=aperture))
+    return scene
 
 
 def small_caustic(seed=CONFIG_SEED_BASE + 102, width=96, height=96):

@@ -34,7 +34,12 @@ enum {
   FR_MAT_DIFFUSE = 0,          /* DiffuseSurface  (material.h:163-177) */
   FR_MAT_METAL = 1,            /* MetalSurface    (material.h:396-425) */
   FR_MAT_GGX_CONDUCTOR = 2,    /* Roughconductor  (material.h:222-278) */
-  FR_MAT_GGX_DIELECTRIC = 3    /* GGXGlass        (material.h:280-394) */
+  FR_MAT_GGX_DIELECTRIC = 3,   /* GGXGlass        (material.h:280-394) */
+  /* The demo's further surfaces (main.cpp:14-114). */
+  FR_MAT_BIMETAL = 4,          /* BiMetalSurface          (material.h:427-463) */
+  FR_MAT_GLASS = 5,            /* GlassSurface            (material.h:465-531) */
+  FR_MAT_GLOSS_TRANSMIT = 6,   /* GlossTransmitSurface    (material.h:677-766) */
+  FR_MAT_DIFFUSE_TRANSMIT = 7  /* DiffuseTransmitSurface  (material.h:637-675) */
 };
 
 enum { FR_CAMERA_PINHOLE = 0, FR_CAMERA_THINLENS = 1 };

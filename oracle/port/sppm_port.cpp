@@ -553,13 +553,129 @@ float glass_brdf(const FP& p) {
   return (wi_wm * wo_wm) / (wi_n * wo_n) * (Io * Io) * (1.0f - F) * G * D * powm2(Ii * wo_wm + Io * wi_wm);
 }
 
-// Surface virtual interface (material.h:137-146) over the four surfaces.
+// ------------------------------------------- the demo's further surfaces
+inline V facing(V n, V in) { return dot(n, in) < 0 ? n : -n; }
+// Sampling::Refract_Sampling (Sampling.cpp:329-337)
+V refract_sampling(V n, V in, float ii, float io) {
+  const float eta = ii / io;
+  const V NN = (dot(in, n) > 0) ? -n : n;
+  const float LN = -dot(in, NN);
+  const float sq = std::max(0.00000001f, 1.0f - eta * eta * (1.0f - LN * LN));
+  return normalized(-NN * std::sqrt(sq) - eta * (-in - LN * NN));
+}
+inline bool if_reflect(V n, V in, V out) { return dot(n, in) * dot(n, out) < 0.0f; }
+inline V reflect_by_n(V r, V n) { return r - 2.0f * dot(n, r) * n; }  // material.h:683-686
+
+// BiMetalSurface (material.h:427-463)
+float bimetal_brdf(const FP& p) {
+  const V N = facing(p.n, p.in);
+  if (!opaque_reflect(p)) return 0.0f;
+  const V r = reflect(N, p.in);
+  if (dot(r, p.out) > 1.0f - 1.0f / 1.0f) return 1.0f / (dot(p.out, N) + 0.00001);
+  return 0.0f;
+}
+// GlassSurface (material.h:465-531); its Reflect is Reflect_Sampling's
+// expression, its Refract Refract_Sampling's.
+V glasssurf_sample(Rng& mt, const FP& p, float* pdf) {
+  const V NN = facing(p.n, p.in);
+  const float reflectance = fresnel(NN, p.in, p.from, p.to);
+  if (reflectance > mt.real()) {
+    *pdf = reflectance;
+    return reflect(NN, p.in);
+  }
+  *pdf = 1.0f - reflectance;
+  const float eta = p.from / p.to;
+  const float LN = -dot(p.in, NN);
+  const float sq = 1.0f - eta * eta * (1.0 - LN * LN);
+  if (sq < 0.000001) return reflect(p.n, p.in);
+  return refract_sampling(p.n, p.in, p.from, p.to);
+}
+float glasssurf_brdf(const FP& p) {
+  const V NN = facing(p.n, p.in);
+  const float reflectance = fresnel(NN, p.in, p.from, p.to);
+  if (if_reflect(p.n, p.in, p.out)) return 1.0f * reflectance / (std::abs(dot(p.out, NN)) + 0.0001);
+  return 1.0f * (1.0f - reflectance) / (std::abs(dot(p.out, NN)) + 0.0001);
+}
+float glasssurf_pdf(const FP& p) {
+  const V NN = facing(p.n, p.in);
+  const float reflectance = fresnel(NN, p.in, p.from, p.to);
+  if (if_reflect(p.n, p.in, p.out)) {
+    const V r = reflect(NN, p.in);
+    return std::abs(dot(r, p.out)) > 0.99 ? 1.0f * reflectance : sMin;
+  }
+  const V rac = refract_sampling(NN, p.in, p.from, p.to);
+  return std::abs(dot(rac, p.out)) > 0.99 ? 1.0f * (1.0f - reflectance) : sMin;
+}
+// DiffuseTransmitSurface (material.h:637-675)
+V difftrans_sample(Rng& mt, const FP& p, float* pdf) {
+  const V n = dot(p.n, p.in) > 0 ? p.n : -p.n;
+  V rs;
+  if (p.refl > mt.real()) {
+    rs = cos_sampling(mt, -n, pdf);
+    *pdf *= p.refl;
+  } else {
+    rs = cos_sampling(mt, n, pdf);
+    *pdf *= (1.0f - p.refl);
+  }
+  return rs;
+}
+float difftrans_brdf(const FP& p) { return if_reflect(p.n, p.in, p.out) ? p.refl / PI : (1.0f - p.refl) / PI; }
+float difftrans_pdf(const FP& p) {
+  const float c = std::abs(dot(p.out, p.n) + 0.00001);
+  return if_reflect(p.n, p.in, p.out) ? p.refl * c / PI : (1.0f - p.refl) * c / PI;
+}
+// GlossTransmitSurface (material.h:677-766)
+V glosstrans_sample(Rng& mt, const FP& p, float* pdf) {
+  const V n = facing(p.n, p.in);
+  V rs;
+  if (p.refl > mt.real()) {
+    rs = ggx_sampling(mt, n, p.in, p.rough, pdf);
+    *pdf *= p.refl;
+  } else {
+    rs = reflect_by_n(ggx_sampling(mt, n, p.in, p.rough, pdf), n);
+    *pdf *= (1.0f - p.refl);
+  }
+  return rs;
+}
+float glosstrans_brdf(const FP& p) {
+  const float power = if_reflect(p.n, p.in, p.out) ? p.refl : 1.0f - p.refl;
+  const V in = p.in;
+  const V N = facing(p.n, in);
+  V out = p.out;
+  if (dot(out, N) < 0) out = reflect_by_n(out, N);
+  constexpr float small = 1e-10;
+  if (dot(in, N) > -small || dot(out, N) < small) return 0.0f;
+  const float alpha = p.rough;
+  const V h = normalized(-in + out);
+  const float ccs = dot(h, N);
+  if (ccs < small || dot(h, in) > -small || dot(h, out) < small) return 0.0f;
+  const float dd = 1.0001f - (1.0f - alpha * alpha) * ccs * ccs;
+  const float D = std::max(sMin, (alpha * alpha) / (PI * (dd * dd)));  // pow(x, 2.0f): folded to x * x
+  const float lc = std::max(0.0f, std::min(0.9999f, dot(in, -N)));
+  const float lv = std::max(0.0f, std::min(0.9999f, dot(out, N)));
+  if (lc < sMin || lv < sMin) return 0.0f;
+  const float L_l = (-1.0f + std::sqrt(1.0f + alpha * alpha * (1.0f / (lc * lc) - 1.0))) * 0.5;
+  const float L_v = (-1.0f + std::sqrt(1.0f + alpha * alpha * (1.0f / (lv * lv) - 1.0))) * 0.5;
+  const float G = 1.0f / ((1.0f + L_l) * (1.0f + L_v));
+  const float fx = (4.0f * dot(in, -N) * dot(out, N));
+  return power * (G * D) / fx;
+}
+float glosstrans_pdf(const FP& p) {
+  if (if_reflect(p.n, p.in, p.out)) return p.refl * ggx_pdf(p.out, p.n, p.in, p.rough);
+  return (1.0f - p.refl) * ggx_pdf(reflect_by_n(p.out, p.n), p.n, p.in, p.rough);
+}
+
+// Surface virtual interface (material.h:137-146) over the eight surfaces.
 V surf_sample(int type, Rng& mt, const FP& p, float* pdf) {
   switch (type) {
     case 0: return cos_sampling(mt, p.n, pdf);                          // DiffuseSurface (material.h:165-167)
     case 1: *pdf = 1.0f; return reflect(p.n, p.in);                     // MetalSurface (material.h:398-403)
     case 2: return ggx_sampling(mt, p.n, p.in, p.rough, pdf);           // Roughconductor (material.h:224-226)
-    default: return glass_sampling(mt, p.n, p.in, p.rough, p.from, p.to, pdf);  // GGXGlass (material.h:311-313)
+    case 3: return glass_sampling(mt, p.n, p.in, p.rough, p.from, p.to, pdf);  // GGXGlass (material.h:311-313)
+    case 4: *pdf = 1.0f; return reflect(facing(p.n, p.in), p.in);       // BiMetalSurface (material.h:429-436)
+    case 5: return glasssurf_sample(mt, p, pdf);
+    case 6: return glosstrans_sample(mt, p, pdf);
+    default: return difftrans_sample(mt, p, pdf);
   }
 }
 float surf_brdf(int type, const FP& p) {
@@ -572,7 +688,11 @@ float surf_brdf(int type, const FP& p) {
       return 0.0f;
     }
     case 2: return conductor_brdf(p);
-    default: return glass_brdf(p);
+    case 3: return glass_brdf(p);
+    case 4: return bimetal_brdf(p);
+    case 5: return glasssurf_brdf(p);
+    case 6: return glosstrans_brdf(p);
+    default: return difftrans_brdf(p);
   }
 }
 float surf_pdf(int type, const FP& p) {
@@ -580,7 +700,11 @@ float surf_pdf(int type, const FP& p) {
     case 0: return std::max(sMin, dot(p.out, p.n) / PI);  // material.h:174-176
     case 1: return dot(reflect(p.n, p.in), p.out) > 1.0f - 1.0f / 1.0f ? 1.0f : sMin;  // material.h:416-424
     case 2: return ggx_pdf(p.out, p.n, p.in, p.rough);
-    default: return glass_pdf(p.out, p.n, p.in, p.rough, p.from, p.to);
+    case 3: return glass_pdf(p.out, p.n, p.in, p.rough, p.from, p.to);
+    case 4: return dot(reflect(facing(p.n, p.in), p.in), p.out) > 1.0f - 1.0f / 1.0f ? 1.0f : sMin;  // material.h:452-462
+    case 5: return glasssurf_pdf(p);
+    case 6: return glosstrans_pdf(p);
+    default: return difftrans_pdf(p);
   }
 }
 

@@ -118,6 +118,11 @@ class TableMaterials : public SceneMaterialManager {
       case 1: s = new Material::MetalSurface(); at->m_SurfaceParam.IfDeltaSurface = true; break;
       case 2: s = new Material::Roughconductor(); break;
       case 3: s = new Material::GGXGlass(); break;
+      // The demo's further surfaces (main.cpp:14-114).
+      case 4: s = new Material::BiMetalSurface(); at->m_SurfaceParam.IfDeltaSurface = true; break;
+      case 5: s = new Material::GlassSurface(); break;
+      case 6: s = new Material::GlossTransmitSurface(); break;
+      case 7: s = new Material::DiffuseTransmitSurface(); break;
       default: std::fprintf(stderr, "bad material type\n"); std::exit(2);
     }
     at->m_Surface = s;

@@ -25,6 +25,7 @@ GOLDEN_SCENES = {
     'cornell32': lambda: __import__('frsppm.scenes', fromlist=['x']).cornell_box(width=32, height=32),
     'mixed48x32': lambda: __import__('frsppm.scenes', fromlist=['x']).small_mixed(),
     'mixed48x32_ibl': lambda: __import__('frsppm.scenes', fromlist=['x']).small_mixed(ibl=True),
+    'demo48x32': lambda: __import__('frsppm.scenes', fromlist=['x']).demo_materials(),
 }
 
 

@@ -48,6 +48,7 @@ FIXTURES = {
     'cornell32': (lambda: scenes.cornell_box(width=32, height=32), 2000, 3),
     'mixed48x32': (lambda: scenes.small_mixed(), 2000, 3),
     'mixed48x32_ibl': (lambda: scenes.small_mixed(ibl=True), 2000, 3),
+    'demo48x32': (lambda: scenes.demo_materials(), 3000, 3),
 }
 
 

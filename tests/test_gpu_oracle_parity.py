@@ -19,6 +19,10 @@ CASES = {
     # (displaced geodesic spheres, instanced and flattened), small.
     'caustic96': (lambda s: s.small_caustic(), 20000, 3, 0.7, 0.01),
     'large64x36': (lambda s: s.small_large_scene(), 20000, 3, 0.7, 0.02),
+    # All eight surface types (the demo's BiMetal, Glass, GlossTransmit and
+    # DiffuseTransmit beside the four of the configs).
+    'demo128x72': (lambda s: s.demo_materials(width=128, height=72, n_spheres=32, field_n=48, tex_size=128,
+                                              light_tex=64, extent=0.8), 20000, 3, 0.7, 0.02),
     # With an environment map: eye paths go on after their hitpoints.
     'mixed128x72_ibl': (lambda s: s.with_sky(s.mixed_materials(width=128, height=72, n_spheres=24, field_n=48,
                                                                tex_size=128, light_tex=64, n_lat=12, n_lon=16,
