@@ -156,6 +156,27 @@ BVHResult build_bvh8(const float* positions, int num_tris, float pad_abs) {
   b.nodes.reserve(2 * (size_t)num_tris);
   const int root = b.build(0, num_tris, 0);
 
+  std::vector<BinNode> bn(b.nodes.size());
+  for (size_t i = 0; i < b.nodes.size(); ++i) {
+    const BNode& n = b.nodes[i];
+    for (int a = 0; a < 3; ++a) { bn[i].lo[a] = n.box.lo[a]; bn[i].hi[a] = n.box.hi[a]; }
+    bn[i].left = n.left;
+    bn[i].right = n.right;
+    bn[i].first = n.first;
+    bn[i].count = n.count;
+  }
+  return collapse_bvh8(bn, root, b.perm, pad_abs);
+}
+
+namespace {
+float bin_area(const BinNode& n) {
+  const float dx = n.hi[0] - n.lo[0], dy = n.hi[1] - n.lo[1], dz = n.hi[2] - n.lo[2];
+  if (dx < 0 || dy < 0 || dz < 0) return 0.0f;
+  return 2.0f * (dx * dy + dy * dz + dz * dx);
+}
+}  // namespace
+
+BVHResult collapse_bvh8(const std::vector<BinNode>& bnodes, int root, const std::vector<int>& perm, float pad_abs) {
   BVHResult out;
   // Collapse breadth first: each wide node takes up to 8 binary descendants,
   // opening the largest-area inner child first; its internal children get
@@ -174,7 +195,7 @@ BVHResult build_bvh8(const float* positions, int num_tris, float pad_abs) {
     const Job j = jobs[head++];
     maxd = std::max(maxd, j.depth);
     std::vector<int> kids;
-    const BNode& bn = b.nodes[j.bnode];
+    const BinNode& bn = bnodes[j.bnode];
     if (bn.left < 0) {
       kids.push_back(j.bnode);  // a root that is a leaf
     } else {
@@ -184,11 +205,11 @@ BVHResult build_bvh8(const float* positions, int num_tris, float pad_abs) {
         int pick = -1;
         float pa = -1.0f;
         for (int k = 0; k < (int)kids.size(); ++k) {
-          const BNode& c = b.nodes[kids[k]];
-          if (c.left >= 0 && c.box.area() > pa) { pa = c.box.area(); pick = k; }
+          const BinNode& c = bnodes[kids[k]];
+          if (c.left >= 0 && bin_area(c) > pa) { pa = bin_area(c); pick = k; }
         }
         if (pick < 0) break;
-        const BNode& c = b.nodes[kids[pick]];
+        const BinNode& c = bnodes[kids[pick]];
         const int l = c.left, r = c.right;
         kids[pick] = l;
         kids.push_back(r);
@@ -202,24 +223,24 @@ BVHResult build_bvh8(const float* positions, int num_tris, float pad_abs) {
     }
     int ninternal = 0;
     for (int c = 0; c < (int)kids.size(); ++c)
-      if (b.nodes[kids[c]].left >= 0) ++ninternal;
+      if (bnodes[kids[c]].left >= 0) ++ninternal;
     node.child_base = (uint32_t)out.nodes.size();
     node.tri_base = (uint32_t)out.tri_order.size();
     for (int i = 0; i < ninternal; ++i) out.nodes.emplace_back();
     int next_internal = 0;
     uint32_t tri_off = 0;
     for (int c = 0; c < (int)kids.size(); ++c) {
-      const BNode& k = b.nodes[kids[c]];
-      node.lox[c] = pad(k.box.lo[0], false); node.hix[c] = pad(k.box.hi[0], true);
-      node.loy[c] = pad(k.box.lo[1], false); node.hiy[c] = pad(k.box.hi[1], true);
-      node.loz[c] = pad(k.box.lo[2], false); node.hiz[c] = pad(k.box.hi[2], true);
+      const BinNode& k = bnodes[kids[c]];
+      node.lox[c] = pad(k.lo[0], false); node.hix[c] = pad(k.hi[0], true);
+      node.loy[c] = pad(k.lo[1], false); node.hiy[c] = pad(k.hi[1], true);
+      node.loz[c] = pad(k.lo[2], false); node.hiz[c] = pad(k.hi[2], true);
       if (k.left >= 0) {
         node.imask |= 1u << c;
         node.meta[c] = 0x80;
         jobs.push_back({kids[c], (int)node.child_base + next_internal++, j.depth + 1});
       } else {
         node.meta[c] = (uint8_t)(0x80u | ((uint32_t)(k.count - 1) << 5) | tri_off);
-        for (int t = 0; t < k.count; ++t) out.tri_order.push_back(b.perm[k.first + t]);
+        for (int t = 0; t < k.count; ++t) out.tri_order.push_back(perm[k.first + t]);
         tri_off += (uint32_t)k.count;
       }
     }

@@ -689,7 +689,16 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
     }
   const float diag = std::sqrt((hi[0] - lo[0]) * (hi[0] - lo[0]) + (hi[1] - lo[1]) * (hi[1] - lo[1]) +
                                (hi[2] - lo[2]) * (hi[2] - lo[2]));
-  BVHResult bvh = build_bvh8(scene->positions, T, 1e-5f * diag + 1e-7f);
+  BVHResult bvh;
+  if (params->bvh_builder == FR_BVH_DEVICE_LBVH) {
+    const char* msg = "";
+    if (build_bvh8_lbvh(scene->positions, T, lo, hi, 1e-5f * diag + 1e-7f, bvh, &msg))
+      return bail(fail(FR_ERR_CUDA, "device BVH build: %s", msg));
+  } else if (params->bvh_builder == FR_BVH_HOST_SAH) {
+    bvh = build_bvh8(scene->positions, T, 1e-5f * diag + 1e-7f);
+  } else {
+    return bail(fail(FR_ERR_INVALID, "params: bvh_builder %d", params->bvh_builder));
+  }
   c->bvh_depth = bvh.depth;
   if (bvh.depth * 7 + 1 > kTraversalStackEntries) return bail(fail(FR_ERR_INVALID, "BVH depth %d exceeds the traversal stack", bvh.depth));
   std::vector<TriGPU> tris(T);

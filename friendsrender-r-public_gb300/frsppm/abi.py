@@ -47,13 +47,14 @@ class SPPMParams(C.Structure):
                 ('flags', C.c_uint32), ('grid_cell_scale', C.c_float), ('guide', C.c_int32),
                 ('guide_plain_fraction', C.c_float), ('guide_batch', C.c_int32),
                 ('guide_learning_rate', C.c_float), ('guide_seed', C.c_uint32),
-                ('guide_steps', C.c_int32)]
+                ('guide_steps', C.c_int32), ('bvh_builder', C.c_int32)]
 
 
 GUIDE_PARAMS = 11824
 FLAG_FIX_STALE_PHOTON_SLOT = 1   # FR_FLAG_FIX_STALE_PHOTON_SLOT
 FLAG_STANDARD_RESOLVE = 2        # FR_FLAG_STANDARD_RESOLVE
 FLAG_END_DEGENERATE_PATHS = 4    # FR_FLAG_END_DEGENERATE_PATHS
+BVH_HOST_SAH, BVH_DEVICE_LBVH = 0, 1  # FR_BVH_*
 
 
 class Stats(C.Structure):
@@ -144,7 +145,8 @@ class Renderer:
     """One fr_ctx: a scene (frsppm.scenes dict), camera and SPPM parameters."""
 
     def __init__(self, scene, photons, alpha=0.9, radius=0.015, flags=0, cell_scale=0.0, camera=None,
-                 guide=False, guide_plain_fraction=0.0, guide_batch=0, guide_lr=0.0, guide_seed=1, guide_steps=0):
+                 guide=False, guide_plain_fraction=0.0, guide_batch=0, guide_lr=0.0, guide_seed=1, guide_steps=0,
+                 bvh_builder=0):
         lib = load()
         self.scene = scene
         cam = camera or scene['camera']
@@ -184,7 +186,7 @@ class Renderer:
         cd.lens_width = cd.lens_height = cam['lens']
         pp = SPPMParams(int(photons), float(alpha), float(radius), int(flags), float(cell_scale), int(bool(guide)),
                         float(guide_plain_fraction), int(guide_batch), float(guide_lr), int(guide_seed),
-                        int(guide_steps))
+                        int(guide_steps), int(bvh_builder))
         self.width, self.height, self.photons = cam['width'], cam['height'], int(photons)
         h = C.c_void_p()
         _check(lib.fr_create(C.byref(sd), C.byref(cd), C.byref(pp), C.byref(h)), 'fr_create')

@@ -146,7 +146,14 @@ typedef struct fr_sppm_params {
   float guide_learning_rate;      /* Adam step size; <= 0 selects 0.005 */
   uint32_t guide_seed;            /* initial network weights */
   int32_t guide_steps;            /* Adam steps per iteration on its samples; <= 0 selects 16 (at most 64) */
+  /* Scene BVH builder (no counterpart in the reference, which builds on the
+   * host, bvh8.h:135-189): FR_BVH_HOST_SAH (0, binned SAH on the host) or
+   * FR_BVH_DEVICE_LBVH (1, Morton-code radix tree built on the GPU).  Both
+   * give the same hits; the SAH tree traces faster, the LBVH builds faster. */
+  int32_t bvh_builder;
 } fr_sppm_params;
+
+enum { FR_BVH_HOST_SAH = 0, FR_BVH_DEVICE_LBVH = 1 };
 
 typedef struct fr_stats {
   int64_t iterations;         /* iterations run so far */
