@@ -305,6 +305,11 @@ LARGE_WORKLOAD = ('large scene: 20,000,004 triangles (400 copies of a 50,000-tri
                   'learned guide on, alpha 0.7, r0 0.02')
 
 
+def bvh_builder(args):
+    from frsppm import abi
+    return abi.BVH_DEVICE_LBVH if args.bvh == 'lbvh' else abi.BVH_HOST_SAH
+
+
 def run_large(args):
     """The large-scene workload: photon paths/s of guided SPPM iterations
     (graph replays, CUDA events on the renderer's stream; the working set is
@@ -319,7 +324,7 @@ def run_large(args):
     gen_s = time.perf_counter() - t0
     t0 = time.perf_counter()
     r = abi.Renderer(scene, LARGE_PHOTONS, alpha=ALPHA, radius=RADIUS, guide=True,
-                     flags=abi.FLAG_END_DEGENERATE_PATHS)
+                     flags=abi.FLAG_END_DEGENERATE_PATHS, bvh_builder=bvh_builder(args))
     setup_s = time.perf_counter() - t0
     stats = r.stats()
     npix = r.width * r.height
@@ -348,7 +353,7 @@ def run_large(args):
     out = {'metric': METRIC, 'value': LARGE_PHOTONS * args.steps / (ms / 1000.0), 'unit': UNIT, 'n_gpus': 1,
            'steps': args.steps, 'warmup': W, 'ms_per_step': ms / args.steps, 'higher_is_better': True,
            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded scene)',
-           'config': {'workload': LARGE_WORKLOAD, 'photons_per_step': LARGE_PHOTONS, 'pixels': npix,
+           'config': {'workload': LARGE_WORKLOAD, 'photons_per_step': LARGE_PHOTONS, 'pixels': npix, 'bvh': args.bvh,
                       'triangles': stats['triangles'], 'bvh_nodes': stats['bvh_nodes'],
                       'l2': 'working set far above L2 (photon slots alone 12.3 GB)'},
            'hitpoint_updates_per_s': npix * args.steps / (ms / 1000.0),
@@ -387,7 +392,8 @@ def run_batch(args):
     from frsppm import abi
     torch.cuda.set_device(dist_env()[2])
     t0 = time.perf_counter()
-    rs = [abi.Renderer(sc, sp['photons'], alpha=ALPHA, radius=RADIUS) for sc, sp in zip(scene_list, specs)]
+    rs = [abi.Renderer(sc, sp['photons'], alpha=ALPHA, radius=RADIUS, bvh_builder=bvh_builder(args))
+          for sc, sp in zip(scene_list, specs)]
     setup_s = time.perf_counter() - t0
     tuned = [r.autotune(1) if not args.no_autotune else None for r in rs]
     # One after another: each context's graph replays alone.
@@ -419,7 +425,7 @@ def run_batch(args):
     out = {'metric': METRIC, 'value': photons * args.steps / dt, 'unit': UNIT, 'n_gpus': 1, 'steps': args.steps,
            'warmup': W, 'ms_per_step': 1e3 * dt / args.steps, 'higher_is_better': True, 'scaling': 'weak',
            'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded scenes)',
-           'config': {'workload': BATCH_WORKLOAD, 'scenes': len(rs), 'triangles': tris,
+           'config': {'workload': BATCH_WORKLOAD, 'scenes': len(rs), 'triangles': tris, 'bvh': args.bvh,
                       'photons_per_step': photons, 'pixels': pixels,
                       'l2': 'working set far above L2 (64 contexts, %.1f GB)' % (dev / 1e9)},
            'hitpoint_updates_per_s': pixels * args.steps / dt,
@@ -500,6 +506,8 @@ def main():
                     help='large: the 20M-triangle scene; batch: 64 uneven scenes; update: the N/tau/R update '
                          'alone (each its own JSON line)')
     ap.add_argument('--no-autotune', action='store_true')
+    ap.add_argument('--bvh', default='sah', choices=['sah', 'lbvh'],
+                    help='scene BVH: host binned SAH (default) or the device LBVH build')
     args = ap.parse_args()
     if args.impl == 'reference':
         return run_reference(args)
@@ -527,7 +535,7 @@ def main():
     W = max(3, args.warmup)
     scene = scenes.mixed_materials()
     t0 = time.perf_counter()
-    r = abi.Renderer(scene, args.photons, alpha=ALPHA, radius=RADIUS)
+    r = abi.Renderer(scene, args.photons, alpha=ALPHA, radius=RADIUS, bvh_builder=bvh_builder(args))
     setup_s = time.perf_counter() - t0
     stats = r.stats()
     npix = r.width * r.height
@@ -610,7 +618,7 @@ def main():
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps, 'warmup': W,
         'ms_per_step': total_ms / args.steps, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
         'dtype': 'f32', 'data': 'synthetic (seeded scene, random-init textures)',
-        'config': {'workload': WORKLOAD, 'photons_per_step': args.photons, 'pixels': npix,
+        'config': {'workload': WORKLOAD, 'photons_per_step': args.photons, 'pixels': npix, 'bvh': args.bvh,
                    'triangles': stats['triangles'], 'bvh_nodes': stats['bvh_nodes'],
                    'l2': 'flushed (256 MB write) before every timed step',
                    'parallelism': 'replicas' if world > 1 else 'single GPU'},
