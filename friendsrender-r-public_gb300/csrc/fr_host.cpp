@@ -19,6 +19,7 @@
 #include "../../include/friendsrender.h"
 #include "fr_bvh.h"
 #include "fr_guide.h"
+#include "fr_ingest.h"
 #include "fr_kernels.h"
 #include "fr_layout.h"
 
@@ -620,6 +621,11 @@ int check_device_error(fr_ctx* c) {
 }
 
 }  // namespace
+
+int fr::set_last_error(int code, const std::string& message) {
+  g_error = message;
+  return code;
+}
 
 extern "C" {
 

@@ -50,6 +50,10 @@ class SPPMParams(C.Structure):
                 ('guide_steps', C.c_int32), ('bvh_builder', C.c_int32)]
 
 
+# fr_material_fn: int (*)(void* user, const char* name, fr_material_desc* material)
+MATERIAL_FN = C.CFUNCTYPE(C.c_int, C.c_void_p, C.c_char_p, C.POINTER(MaterialDesc))
+FR_ERR_IO = 5
+
 GUIDE_PARAMS = 11824
 FLAG_FIX_STALE_PHOTON_SLOT = 1   # FR_FLAG_FIX_STALE_PHOTON_SLOT
 FLAG_STANDARD_RESOLVE = 2        # FR_FLAG_STANDARD_RESOLVE
@@ -71,7 +75,8 @@ EXPORTS = ['fr_last_error', 'fr_create', 'fr_iterate', 'fr_synchronize', 'fr_res
            'fr_read_wave_counts', 'fr_save_state', 'fr_load_state', 'fr_update',
            'fr_resolve_rgba8', 'fr_export_png', 'fr_write_png', 'fr_check_tc_gemm', 'fr_guide_params',
            'fr_guide_set_params', 'fr_read_guide_importance', 'fr_guide_gradient', 'fr_seek', 'fr_iterate_batch',
-           'fr_autotune', 'fr_update_dev', 'fr_read_direct']
+           'fr_autotune', 'fr_update_dev', 'fr_read_direct', 'fr_scene_load_obj', 'fr_scene_get_desc',
+           'fr_scene_material_name', 'fr_scene_free', 'fr_texture_load']
 
 STAGES = ('eye', 'photon', 'grid', 'gather', 'eye_trace', 'photon_trace')
 
@@ -127,6 +132,14 @@ def load(path=None):
     lib.fr_guide_set_params.argtypes = [vp, vp]
     lib.fr_read_guide_importance.argtypes = [vp, vp]
     lib.fr_guide_gradient.argtypes = [vp, i32, vp, vp, vp]
+    lib.fr_scene_load_obj.argtypes = [C.c_char_p, C.c_char_p, C.c_char_p, MATERIAL_FN, vp, C.POINTER(vp)]
+    lib.fr_scene_get_desc.argtypes = [vp]
+    lib.fr_scene_get_desc.restype = C.POINTER(SceneDesc)
+    lib.fr_scene_material_name.argtypes = [vp, i32]
+    lib.fr_scene_material_name.restype = C.c_char_p
+    lib.fr_scene_free.argtypes = [vp]
+    lib.fr_scene_free.restype = None
+    lib.fr_texture_load.argtypes = [C.c_char_p, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), vp]
     _lib = lib
     return lib
 
@@ -438,3 +451,91 @@ def iterate_batch(renderers, n=1, sync=True):
         for r in renderers:
             r.synchronize()
 
+
+
+# ------------------------------------------------------------------ scene ingest
+
+_MATERIAL_FIELDS = ('type', 'sppm', 'opaque', 'index', 'roughness', 'extinction', 'reflectance')
+
+
+def load_texture(path):
+    """fr_texture_load: (H x W x 4 uint8 RGBA8, channel count stbi_load reports)."""
+    lib = load()
+    w, h, c = C.c_int32(), C.c_int32(), C.c_int32()
+    _check(lib.fr_texture_load(os.fsencode(path), C.byref(w), C.byref(h), C.byref(c), None), 'fr_texture_load')
+    out = np.empty((h.value, w.value, 4), np.uint8)
+    _check(lib.fr_texture_load(os.fsencode(path), None, None, None, _ptr(out)), 'fr_texture_load')
+    return out, c.value
+
+
+def load_obj_scene(obj_file, asset_dir=None, environment=None, materials=None):
+    """fr_scene_load_obj: Scene::CreateScene on an OBJ file, as a scene dict
+    (the layout frsppm.scenes makes, without a camera).
+
+    ``materials`` is the material plug-in (SceneMaterialManager): None keeps
+    the loader's defaults, a dict maps material names to dicts of any of
+    type, sppm, opaque, index, roughness, extinction, reflectance (names not
+    in it keep the defaults), and a callable f(name, fields) may change the
+    ``fields`` dict (the same keys plus albedo and emission) in place."""
+    lib = load()
+    errors = []
+
+    def plugin(_user, name, desc):
+        try:
+            d = desc.contents
+            name = name.decode()
+            fields = dict(type=d.type, sppm=d.sppm_surface, opaque=d.opaque, index=d.index,
+                          roughness=d.roughness, extinction=d.extinction, reflectance=d.reflectance,
+                          albedo=tuple(d.albedo), emission=tuple(d.emission))
+            if callable(materials):
+                materials(name, fields)
+            elif name in materials:
+                fields.update(materials[name])
+            d.type, d.sppm_surface, d.opaque = int(fields['type']), int(fields['sppm']), int(fields['opaque'])
+            d.index, d.roughness = float(fields['index']), float(fields['roughness'])
+            d.extinction, d.reflectance = float(fields['extinction']), float(fields['reflectance'])
+            d.albedo = _f3(*fields['albedo'])
+            d.emission = _f3(*fields['emission'])
+            return 0
+        except Exception as e:  # reported after the call; the loader sees a failure
+            errors.append(e)
+            return 1
+
+    cb = MATERIAL_FN(plugin) if materials is not None else MATERIAL_FN()
+    h = C.c_void_p()
+    rc = lib.fr_scene_load_obj(os.fsencode(obj_file), None if asset_dir is None else os.fsencode(asset_dir),
+                               None if environment is None else os.fsencode(environment), cb, None, C.byref(h))
+    if errors:
+        raise errors[0]
+    _check(rc, 'fr_scene_load_obj')
+    try:
+        d = lib.fr_scene_get_desc(h).contents
+        t = d.num_facets
+
+        def arr(ptr, ctype, shape):
+            n = int(np.prod(shape))
+            if n == 0:
+                return np.zeros(shape, np.dtype(ctype))
+            return np.ctypeslib.as_array(C.cast(ptr, C.POINTER(ctype)), (n,)).reshape(shape).copy()
+
+        scene = dict(pos=arr(d.positions, C.c_float, (t, 3, 3)), nrm=arr(d.normals, C.c_float, (t, 3, 3)),
+                     uv=arr(d.uvs, C.c_float, (t, 3, 2)), mat=arr(d.material_ids, C.c_int32, (t,)))
+        mats = []
+        for m in range(d.num_materials):
+            md = d.materials[m]
+            mats.append(dict(name=lib.fr_scene_material_name(h, m).decode(), type=md.type, sppm=bool(md.sppm_surface),
+                             opaque=bool(md.opaque), tex_albedo=md.tex_albedo, tex_roughness=md.tex_roughness,
+                             tex_bump=md.tex_bump, albedo=tuple(md.albedo), emission=tuple(md.emission),
+                             index=md.index, roughness=md.roughness, extinction=md.extinction,
+                             reflectance=md.reflectance))
+        scene['materials'] = mats
+        scene['textures'] = [arr(d.textures[k].texels, C.c_uint8, (d.textures[k].height, d.textures[k].width, 4))
+                             for k in range(d.num_textures)]
+        if d.environment:
+            e = d.environment.contents
+            scene['ibl'] = arr(e.texels, C.c_uint8, (e.height, e.width, 4))
+        else:
+            scene['ibl'] = None
+        return scene
+    finally:
+        lib.fr_scene_free(h)

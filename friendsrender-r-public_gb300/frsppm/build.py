@@ -27,7 +27,7 @@ CXX_FLAGS = ['-O2', '-std=c++17', '-fPIC', '-ffp-contract=off', '-fno-fast-math'
              '-I' + os.path.join(CUDA_HOME, 'include')]
 
 CU_SOURCES = ['fr_kernels.cu', 'fr_noalloc.cu', 'fr_exact_check.cu', 'fr_tc_check.cu', 'fr_guide.cu', 'fr_bvh_gpu.cu']
-CXX_SOURCES = ['fr_host.cpp', 'fr_bvh.cpp', 'fr_png.cpp']
+CXX_SOURCES = ['fr_host.cpp', 'fr_bvh.cpp', 'fr_png.cpp', 'fr_image_read.cpp', 'fr_ingest.cpp']
 
 
 def _newer(target, deps):

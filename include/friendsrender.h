@@ -26,7 +26,8 @@ enum {
   FR_ERR_INVALID = 1,   /* bad argument or descriptor */
   FR_ERR_CUDA = 2,      /* CUDA runtime error */
   FR_ERR_OOM = 3,       /* device allocation failed */
-  FR_ERR_DEVICE = 4     /* a kernel reported an error (traversal stack) */
+  FR_ERR_DEVICE = 4,    /* a kernel reported an error (traversal stack) */
+  FR_ERR_IO = 5         /* a scene or image file could not be read or decoded */
 };
 
 /* Surface types: the reference's Surface subclasses (SPPM/SPPM/material.h). */
@@ -176,6 +177,61 @@ const char* fr_last_error(void);
  * RenderImage_FixRenderTime (SPPM.cpp:682-766). */
 int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr_sppm_params* params,
               fr_ctx** out);
+
+/* ---------------------------------------------------------------- scene ingest
+ * Scene::CreateScene (Scene.cpp:13-218) on the host, no GPU needed: reads an
+ * OBJ file and its MTL libraries the way tinyobjloader 0.9.22 (vendored by the
+ * reference as tiny_obj_loader.cpp) does with its default flags (polygons
+ * fanned into triangles, vertices shared within a face group), decodes the
+ * textures the MTL names, and returns an fr_scene_desc whose arrays the
+ * fr_scene owns.
+ *
+ * asset_dir is the prefix put before MTL and texture names (the reference
+ * hard-codes "meshData//", Scene.cpp:20-21; NULL means that).  MTL keys:
+ * Kd albedo, Ke emission, map_Kd albedo texture, map_d roughness texture,
+ * map_bump (or bump) normal map (Scene.cpp:60-77); a texture name of two
+ * characters or fewer, or a file that does not decode, leaves that texture
+ * unset, as in the reference.  A face whose usemtl names no material gets
+ * material -1, which fr_create rejects (the reference's attribute lookup
+ * throws on it).  environment_file, when not NULL, is decoded as the
+ * environment map (the IBL texture main.cpp:132-143 hands to CreateScene).
+ *
+ * Images: PNG (all colour types, bit depths 1-16, Adam7) decoded to what
+ * stb_image 2.12 returns with req_comp 0 (16-bit samples keep their high
+ * byte; grey below 8 bits is scaled to 0..255; tRNS adds an alpha channel),
+ * then widened to RGBA8 the way LoadTextureFromFile (TextureUtility.cpp:12-35)
+ * fills a colour: C channels per pixel, C being the count stbi_load reports,
+ * missing ones 0 and alpha 255 (so grey+alpha lands in red and green, and a
+ * grey or RGB image with tRNS, whose reported C leaves out the added alpha,
+ * is read with the reference's short stride).  Other formats return
+ * FR_ERR_IO. */
+typedef struct fr_scene fr_scene;
+
+/* The material extension point, SceneMaterialManager::SetParamtoAttribute_p
+ * (SceneMaterial.h:13-16): called once per MTL material, in file order, with
+ * its name and a descriptor holding the Attribute's values before the call
+ * (Scene.cpp:62-65): albedo = Kd, emission = Ke, index 1, roughness,
+ * extinction and reflectance 1, opaque 1, sppm_surface 0, type
+ * FR_MAT_DIFFUSE (SURFACE_PARAM(), material.h:76-89).  It may change any
+ * field; the tex_* fields are set after it returns (Scene.cpp:72-76).  A
+ * non-zero return fails the load with FR_ERR_INVALID.  A NULL callback keeps
+ * the defaults, like the reference's default SceneMaterialManager (a diffuse
+ * surface that is not an SPPM surface, so such a scene stores no hitpoints). */
+typedef int (*fr_material_fn)(void* user, const char* material_name, fr_material_desc* material);
+
+int fr_scene_load_obj(const char* obj_file, const char* asset_dir, const char* environment_file,
+                      fr_material_fn material_fn, void* user, fr_scene** out);
+/* The loaded scene, valid until fr_scene_free. */
+const fr_scene_desc* fr_scene_get_desc(const fr_scene* scene);
+/* Name of material m (newmtl), or NULL when m is out of range. */
+const char* fr_scene_material_name(const fr_scene* scene, int32_t m);
+void fr_scene_free(fr_scene* scene);
+
+/* TextureUtility::LoadTextureFromFile (TextureUtility.cpp:12-35) for one
+ * image file: writes its size and the channel count stb would report; when
+ * rgba is not NULL, also width*height*4 bytes of RGBA8 (row j at
+ * rgba + 4*width*j, the file's row order). */
+int fr_texture_load(const char* file, int32_t* width, int32_t* height, int32_t* channels, uint8_t* rgba);
 
 /* Enqueues n SPPM iterations on the context's stream (the loop body of
  * RenderImage_FixRenderTime, SPPM.cpp:768-848, with a fixed photon count).

@@ -7,6 +7,7 @@
 //   frref <scene_dir> trace  <rays.bin> <out_dir>
 //   frref <scene_dir> any    <rays.bin> <out_dir>
 //   frref <scene_dir> render <photons_per_iter> <iterations> <out_dir>
+//   frref <dir> texture <image_file> <out_dir>
 //
 // <scene_dir> holds meshData/scene.obj (+ .mtl, textures), materials.txt and
 // camera.txt as written by frsppm.objio.
@@ -53,6 +54,7 @@
 #include "SPPM.h"
 #include "Scene.h"
 #include "TextureUtility.h"
+#include "stb_image.hpp"
 #undef private
 
 using namespace PTUtility;
@@ -110,7 +112,12 @@ class TableMaterials : public SceneMaterialManager {
   std::map<std::string, MatRow> rows;
   Material::Surface* SetParamtoAttribute_p(Attribute* at, const std::string& name) const override {
     auto it = rows.find(name);
-    if (it == rows.end()) { std::fprintf(stderr, "unknown material %s\n", name.c_str()); std::exit(2); }
+    if (it == rows.end()) {
+      // Not in the table: what the reference's default manager does
+      // (SceneMaterial.h:13-16).
+      at->m_Surface = new Material::DiffuseSurface();
+      return at->m_Surface;
+    }
     const MatRow& r = it->second;
     Material::Surface* s = nullptr;
     switch (r.type) {
@@ -169,6 +176,24 @@ int main(int argc, char** argv) {
   std::string out_dir;
   if (chdir(argv[1]) != 0) { std::perror("chdir"); return 2; }
 
+  if (mode == "texture") {
+    // TextureUtility::LoadTextureFromFile (TextureUtility.cpp:12-35) on one
+    // image, and the channel count stbi_load reports for it.
+    if (argc < 5) return 2;
+    Texture2D tex;
+    if (!TextureUtility::LoadTextureFromFile(tex, argv[3])) { std::fprintf(stderr, "load failed\n"); return 3; }
+    int X = 0, Y = 0, C = 0;
+    unsigned char* raw = stbi_load(argv[3], &X, &Y, &C, 0);
+    if (raw) stbi_image_free(raw);
+    const size_t W = tex.GetWidth(), H = tex.GetHeight();
+    std::vector<float> texels(W * H * 4);
+    for (size_t i = 0; i < W * H; ++i)
+      for (int c = 0; c < 4; ++c) texels[i * 4 + c] = tex.GetRawData()[i][c];
+    npy_f32(std::string(argv[4]) + "/texels.npy", texels, {H, W, 4});
+    npy_i32(std::string(argv[4]) + "/channels.npy", std::vector<int32_t>{C}, {1});
+    return 0;
+  }
+
   TableMaterials mats;
   {
     std::ifstream f("materials.txt");
@@ -225,6 +250,27 @@ int main(int argc, char** argv) {
     npy_f32(out_dir + "/facet_nrm.npy", nrm, {T, 3, 3});
     npy_f32(out_dir + "/facet_uv.npy", uv, {T, 3, 2});
     npy_i32(out_dir + "/facet_attr.npy", attr, {T});
+    // Attributes as CreateScene left them (Scene.cpp:60-77): Kd, Ke, the
+    // surface parameters (index, roughness, extinction, reflectance, SPPM
+    // surface, opaque) and the texture file names bound to albedo, roughness
+    // and normal map.
+    {
+      std::vector<float> kd, ke, par;
+      std::ofstream names(out_dir + "/attr_textures.txt");
+      for (const auto& kv : scene.m_Attributes.m_AttributeTable) {
+        const Attribute* at = kv.second.get();
+        const auto& sp = at->m_SurfaceParam;
+        push3(kd, sp.Albedo);
+        push3(ke, sp.Radiance);
+        for (float x : {sp.Index, sp.Roughness, sp.Extinction, sp.Reflectance, (float)sp.isSPPMSurface, (float)sp.IfOpeque})
+          par.push_back(x);
+        names << kv.first << '\t' << at->m_AlbedoTextureFileName << '\t' << at->m_RoughnessTextureFileName << '\t'
+              << at->m_BumpMapTextureFileName << '\n';
+      }
+      npy_f32(out_dir + "/attr_albedo.npy", kd, {kd.size() / 3, 3});
+      npy_f32(out_dir + "/attr_radiance.npy", ke, {ke.size() / 3, 3});
+      npy_f32(out_dir + "/attr_params.npy", par, {par.size() / 6, 6});
+    }
     // Area lights and their alias tables (LightSampler.cpp:6-66, TableSampler.h:44-120).
     const LightSampler* ls = scene.GetLightManager();
     const int NL = ls->GetNumAreaLights();

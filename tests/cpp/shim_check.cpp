@@ -2,10 +2,19 @@
 // with a diffuse floor, a GGX-conductor back wall and a ceiling area light,
 // seen by a pinhole camera.  RenderImage_FixStep must give the image the
 // C-ABI calls give for the same iterations, and bad arguments must throw.
+// The scene is also written as OBJ/MTL into <dir> and read back with
+// fr::Scene::CreateScene and a SceneMaterialManager: the facets must be the
+// hand-built ones and render the same image.
+//
+//   shim_check <dir>          everything (needs a GPU)
+//   shim_check <dir> ingest   the OBJ round trip only (host code)
+//
 // Exit status 0 on success; prints the failing check otherwise.
 #include <cmath>
 #include <cstdio>
+#include <cstring>
 #include <stdexcept>
+#include <string>
 #include <vector>
 
 #include "friendsrender.hpp"
@@ -34,9 +43,86 @@ int fail(const char* what) {
   return 1;
 }
 
+const char* kNames[3] = {"floor", "wall", "light"};
+
+// Writes the box as <dir>/box.obj and <dir>/box.mtl, one v/vt/vn per corner.
+bool write_obj(const Box& b, const fr_material_desc* mats, const std::string& dir) {
+  std::FILE* m = std::fopen((dir + "/box.mtl").c_str(), "w");
+  std::FILE* o = std::fopen((dir + "/box.obj").c_str(), "w");
+  if (!m || !o) return false;
+  for (int k = 0; k < 3; ++k)
+    std::fprintf(m, "newmtl %s\nKd %.9g %.9g %.9g\nKe %.9g %.9g %.9g\n\n", kNames[k], mats[k].albedo[0],
+                 mats[k].albedo[1], mats[k].albedo[2], mats[k].emission[0], mats[k].emission[1], mats[k].emission[2]);
+  std::fprintf(o, "mtllib box.mtl\n");
+  for (size_t t = 0; t < b.mat.size(); ++t) {
+    for (int c = 0; c < 3; ++c) {
+      const float* p = &b.pos[(t * 3 + c) * 3];
+      const float* n = &b.nrm[(t * 3 + c) * 3];
+      const float* u = &b.uv[(t * 3 + c) * 2];
+      std::fprintf(o, "v %.9g %.9g %.9g\nvt %.9g %.9g\nvn %.9g %.9g %.9g\n", p[0], p[1], p[2], u[0], u[1], n[0], n[1],
+                   n[2]);
+    }
+    const int v = (int)t * 3 + 1;
+    std::fprintf(o, "usemtl %s\nf %d/%d/%d %d/%d/%d %d/%d/%d\n", kNames[b.mat[t]], v, v, v, v + 1, v + 1, v + 1, v + 2,
+                 v + 2, v + 2);
+  }
+  std::fclose(m);
+  std::fclose(o);
+  return true;
+}
+
+// The reference's way of giving materials their surfaces (main.cpp:14-114).
+class BoxMaterials : public fr::SceneMaterialManager {
+ public:
+  explicit BoxMaterials(const fr_material_desc* mats) : mats_(mats) {}
+  void SetParamtoAttribute(fr_material_desc& m, const std::string& name) const override {
+    for (int k = 0; k < 3; ++k) {
+      if (name != kNames[k]) continue;
+      m.type = mats_[k].type;
+      m.sppm_surface = mats_[k].sppm_surface;
+      m.opaque = mats_[k].opaque;
+      m.index = mats_[k].index;
+      m.roughness = mats_[k].roughness;
+      m.extinction = mats_[k].extinction;
+      m.reflectance = mats_[k].reflectance;
+      return;
+    }
+    throw std::runtime_error("unknown material " + name);
+  }
+
+ private:
+  const fr_material_desc* mats_;
+};
+
+// Reads the box back and compares it with the hand-built arrays.
+int check_ingest(const Box& b, const fr_material_desc* mats, const std::string& dir, fr::Scene& loaded) {
+  if (!write_obj(b, mats, dir)) return fail("cannot write the OBJ files");
+  BoxMaterials plugin(mats);
+  const std::string asset_dir = dir + "/";
+  if (!loaded.CreateScene((dir + "/box.obj").c_str(), &plugin, nullptr, asset_dir.c_str()))
+    return fail("CreateScene failed");
+  const fr_scene_desc& d = loaded.desc();
+  if (d.num_facets != (int32_t)b.mat.size() || d.num_materials != 3 || d.num_textures != 0) return fail("counts");
+  if (std::memcmp(d.positions, b.pos.data(), b.pos.size() * 4) || std::memcmp(d.normals, b.nrm.data(), b.nrm.size() * 4) ||
+      std::memcmp(d.uvs, b.uv.data(), b.uv.size() * 4) || std::memcmp(d.material_ids, b.mat.data(), b.mat.size() * 4))
+    return fail("loaded facets differ from the written ones");
+  for (int k = 0; k < 3; ++k) {
+    const fr_material_desc& m = d.materials[k];
+    if (loaded.material_name(k) != kNames[k] || m.type != mats[k].type || m.sppm_surface != mats[k].sppm_surface ||
+        m.roughness != mats[k].roughness || m.emission[0] != mats[k].emission[0] || m.tex_albedo != -1)
+      return fail("loaded material differs");
+  }
+  fr::Scene missing;
+  if (missing.CreateScene((dir + "/no_such.obj").c_str())) return fail("missing OBJ accepted");
+  return 0;
+}
+
 }  // namespace
 
-int main() {
+int main(int argc, char** argv) {
+  if (argc < 2) return fail("usage: shim_check <dir> [ingest]");
+  const std::string dir = argv[1];
+  const bool ingest_only = argc > 2 && std::strcmp(argv[2], "ingest") == 0;
   Box b;
   const float f0[3] = {-1, 0, -1}, f1[3] = {1, 0, -1}, f2[3] = {1, 0, 1}, f3[3] = {-1, 0, 1}, up[3] = {0, 1, 0};
   const float w0[3] = {-1, 0, -1}, w1[3] = {-1, 2, -1}, w2[3] = {1, 2, -1}, w3[3] = {1, 0, -1}, fw[3] = {0, 0, 1};
@@ -66,6 +152,12 @@ int main() {
   }
   fr_scene_desc scene{(int32_t)b.mat.size(), b.pos.data(), b.nrm.data(), b.uv.data(), b.mat.data(), 3, mats, 0,
                       nullptr};
+  fr::Scene loaded;
+  if (const int rc = check_ingest(b, mats, dir, loaded)) return rc;
+  if (ingest_only) {
+    std::printf("ok\n");
+    return 0;
+  }
   fr_camera_desc cam{};
   cam.type = FR_CAMERA_PINHOLE;
   cam.width = 64;
@@ -111,6 +203,15 @@ int main() {
   }
   if (lit < 64 * 48) return fail("image mostly black");
   if (diff > 1e-5 * peak) return fail("FixStep image differs from the C-ABI render");
+
+  fr::RenderTarget from_obj;
+  try {
+    render.RenderImage_FixStep(from_obj, loaded, cam, photons * steps, steps);
+  } catch (const std::exception& e) {
+    std::printf("FAIL: RenderImage_FixStep on the loaded scene threw: %s\n", e.what());
+    return 1;
+  }
+  if (from_obj.rgba != target.rgba) return fail("the scene read from OBJ renders differently");
 
   bool threw = false;
   try {
