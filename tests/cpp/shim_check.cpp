@@ -107,10 +107,15 @@ int check_ingest(const Box& b, const fr_material_desc* mats, const std::string& 
       std::memcmp(d.uvs, b.uv.data(), b.uv.size() * 4) || std::memcmp(d.material_ids, b.mat.data(), b.mat.size() * 4))
     return fail("loaded facets differ from the written ones");
   for (int k = 0; k < 3; ++k) {
-    const fr_material_desc& m = d.materials[k];
-    if (loaded.material_name(k) != kNames[k] || m.type != mats[k].type || m.sppm_surface != mats[k].sppm_surface ||
-        m.roughness != mats[k].roughness || m.emission[0] != mats[k].emission[0] || m.tex_albedo != -1)
+    if (loaded.material_name(k) != kNames[k]) return fail("loaded material name differs");
+    if (std::memcmp(&d.materials[k], &mats[k], sizeof(fr_material_desc)) != 0) {
+      const fr_material_desc& m = d.materials[k];
+      std::printf("material %d: type %d/%d sppm %d/%d opaque %d/%d tex %d %d %d idx %g/%g rough %g/%g ext %g/%g refl %g/%g\n", k,
+                  m.type, mats[k].type, m.sppm_surface, mats[k].sppm_surface, m.opaque, mats[k].opaque, m.tex_albedo,
+                  m.tex_roughness, m.tex_bump, m.index, mats[k].index, m.roughness, mats[k].roughness, m.extinction,
+                  mats[k].extinction, m.reflectance, mats[k].reflectance);
       return fail("loaded material differs");
+    }
   }
   fr::Scene missing;
   if (missing.CreateScene((dir + "/no_such.obj").c_str())) return fail("missing OBJ accepted");
@@ -211,7 +216,12 @@ int main(int argc, char** argv) {
     std::printf("FAIL: RenderImage_FixStep on the loaded scene threw: %s\n", e.what());
     return 1;
   }
-  if (from_obj.rgba != target.rgba) return fail("the scene read from OBJ renders differently");
+  // A grid cell's photons are summed in the order its atomic counter gave
+  // them slots, so renders agree to float rounding, not bit for bit (as above).
+  if (from_obj.rgba.size() != target.rgba.size()) return fail("OBJ render size");
+  double odiff = 0;
+  for (size_t i = 0; i < target.rgba.size(); ++i) odiff = std::fmax(odiff, std::fabs((double)from_obj.rgba[i] - target.rgba[i]));
+  if (odiff > 1e-5 * peak) return fail("the scene read from OBJ renders differently");
 
   bool threw = false;
   try {

@@ -2,7 +2,8 @@
 GPU what the reference renders from the same files: the golden fixtures were
 made by the reference's CreateScene + render on exactly the files
 frsppm.objio writes.  Per-pixel photon counts N exact, the image within
-1e-4 relative, and bit-identical to the render of the generator's arrays."""
+1e-4 relative of the reference's and within float rounding (1e-5) of the
+render of the generator's arrays."""
 import os
 
 import numpy as np
@@ -38,4 +39,6 @@ def test_render_from_obj_matches_reference(tmp_path, name):
     ref = gold['image']
     err = np.abs(images[0] - ref).max() / np.abs(ref).max()
     assert err < 1e-4, err
-    np.testing.assert_array_equal(images[0], images[1])
+    # A grid cell's photons are summed in the order its atomic counter gave
+    # them slots, so two renders agree to float rounding.
+    assert np.abs(images[0] - images[1]).max() <= 1e-5 * np.abs(images[1]).max()
