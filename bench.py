@@ -491,7 +491,9 @@ def run_update(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
-    ap.add_argument('--steps', type=int, default=10)
+    ap.add_argument('--steps', type=int, default=None,
+                    help='timed steps (default: 200 for the mixed-materials and update workloads, whose steps '
+                         'take milliseconds, so that the clock sampler sees the timed region; 10 otherwise)')
     ap.add_argument('--warmup', type=int, default=3)
     ap.add_argument('--impl', default='ours', choices=['ours', 'reference'])
     ap.add_argument('--no-cpu-baseline', action='store_true')
@@ -509,6 +511,8 @@ def main():
     ap.add_argument('--bvh', default='sah', choices=['sah', 'lbvh'],
                     help='scene BVH: host binned SAH (default) or the device LBVH build')
     args = ap.parse_args()
+    if args.steps is None:
+        args.steps = 200 if args.impl == 'ours' and args.workload in ('mixed', 'update') else 10
     if args.impl == 'reference':
         return run_reference(args)
     if args.workload == 'large':
