@@ -47,6 +47,38 @@ WORKLOAD = ('mixed materials: 997,444 triangles (200 UV spheres + 512^2 height f
             'aperture 0.02, 1M photon paths/iteration, alpha 0.7, r0 0.02')
 
 
+# Traversal work per closest-hit ray of this workload on the reference's own
+# BVH (N_BVH8::findClosestElement, bvh8.h:568-641): 168 V + 40 X FP32
+# operations, V internal nodes and X leaf triangle tests per ray, counted by
+# the reference's harness on a 10% sample of the rays of one iteration
+# (tests/golden/make_traversal_work.py -> tests/golden/traversal_work_mixed.json).
+TRAVERSAL_FP32_OPS_PER_RAY = {'eye': 2336.0085393334575, 'photon': 2640.158385979652}
+
+
+def fp32_peak_tflops(sm_mhz):
+    """Nominal FP32 rate: SMs x 128 FP32 lanes x 2 (FMA) x SM clock."""
+    import torch
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    return sms * 128 * 2 * sm_mhz * 1e6 / 1e12
+
+
+def traversal_block(rays, eye_rays, photon_rays, trace_s, eye_q, photon_q, clocks):
+    """Trace-kernel throughput: rays per second of trace-kernel time, and the
+    reference's traversal work on those rays (TRAVERSAL_FP32_OPS_PER_RAY) as a
+    fraction of the nominal FP32 rate at the SM clock seen while timing."""
+    ops = eye_rays * TRAVERSAL_FP32_OPS_PER_RAY['eye'] + photon_rays * TRAVERSAL_FP32_OPS_PER_RAY['photon']
+    mhz = clocks.get('sm_mhz') or clocks.get('sm_max_mhz') or 2070.0
+    peak = fp32_peak_tflops(mhz)
+    achieved = ops / trace_s / 1e12
+    return {'kernel': 'k_wave_trace', 'rays_per_step': rays, 'rays_per_s': rays / trace_s,
+            'tail_paths_per_step': int(eye_q[-1]) + int(photon_q[-1]),
+            'reference_work': {'fp32_ops_per_ray': TRAVERSAL_FP32_OPS_PER_RAY, 'achieved_tflops': achieved,
+                               'peak_tflops': peak, 'frac': achieved / peak,
+                               'peak_source': 'nominal: SMs x 128 FP32 lanes x 2 x %.0f MHz' % mhz,
+                               'work': '168 V + 40 X per ray on the reference BVH (bvh8.h:568-641), '
+                                       'tests/golden/traversal_work_mixed.json'}}
+
+
 def dist_env():
     return int(os.environ.get('RANK', 0)), int(os.environ.get('WORLD_SIZE', 1)), int(os.environ.get('LOCAL_RANK', 0))
 
@@ -588,7 +620,8 @@ def main():
 
     # ---- rays traced and photons stored in the last timed iteration
     eye_q, photon_q = r.wave_counts()
-    rays = int(eye_q[:-1].sum()) + int(photon_q[:-1].sum())
+    eye_rays, photon_rays = int(eye_q[:-1].sum()), int(photon_q[:-1].sum())
+    rays = eye_rays + photon_rays
     counts = np.empty(r.photons, np.uint32)
     abi._check(abi._lib.fr_read_photon_slots(r.h, None, None, None, abi._ptr(counts)), 'fr_read_photon_slots')
     stored = int(counts.sum())
@@ -618,6 +651,7 @@ def main():
     trace_s = (stage_ms['eye_trace'] + stage_ms['photon_trace']) / 1000.0 / args.steps
     bytes_per_launch = rays * TRACE_BYTES_PER_RAY / trace_launches
     achieved = bytes_per_launch / (trace_s / trace_launches) / 1e9
+    clocks = clk.summary()
     out = {
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps, 'warmup': W,
         'ms_per_step': total_ms / args.steps, 'higher_is_better': True, 'scaling': 'weak', 'vs_baseline': None,
@@ -632,13 +666,12 @@ def main():
                      'frac': achieved / peak, 'traffic': trace_traffic_per_launch(), 'peak_source': peak_kind,
                      'algorithmic_bytes_per_launch': bytes_per_launch, 'launches_per_step': trace_launches,
                      'note': 'latency-bound BVH traversal; eye and photon launches overlap in time'},
-        'traversal': {'kernel': 'k_wave_trace', 'rays_per_step': rays, 'rays_per_s': rays / trace_s,
-                      'tail_paths_per_step': int(eye_q[-1]) + int(photon_q[-1])},
+        'traversal': traversal_block(rays, eye_rays, photon_rays, trace_s, eye_q, photon_q, clocks),
         'e2e': {'value': world * args.photons * args.steps / e2e_s, 'unit': UNIT, 'h2d_bytes_per_step': 0,
                 'd2h_bytes_per_step': npix * 16, 'setup_s': setup_s,
                 'device_bytes': int(stats['device_bytes'])},
         'gpu_launches': launches,
-        'clocks': clk.summary(),
+        'clocks': clocks,
         'photons_stored_last_step': stored, 'hitpoints_last_step': hits,
     }
     if world == 1 and not args.no_guide_eval:

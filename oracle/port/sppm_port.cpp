@@ -19,11 +19,13 @@
 #include <omp.h>
 
 #include <algorithm>
+#include <atomic>
 #include <cfloat>
 #include <cmath>
 #include <cstdint>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <vector>
 
 namespace port {
@@ -752,6 +754,23 @@ struct Renderer {
   std::vector<KdNode> kd;
   std::vector<int> gather_m;
   std::vector<V> gather_phi;
+  // Closest-hit rays kept for measurement: every ray_stride-th traced ray (in
+  // the order the threads reach the counter), up to ray_cap; 8 floats each:
+  // origin, direction, index, pass (0 eye, 1 photon).
+  mutable std::atomic<long long> ray_count{0};
+  long long ray_stride = 0;
+  size_t ray_cap = 0;
+  mutable std::mutex ray_mu;
+  mutable std::vector<float> ray_sample;
+
+  bool trace(const Ray& r, Hit& h, int pass) const {
+    if (ray_stride > 0 && ray_count.fetch_add(1) % ray_stride == 0) {
+      std::lock_guard<std::mutex> lock(ray_mu);
+      if (ray_sample.size() < ray_cap * 8)
+        ray_sample.insert(ray_sample.end(), {r.o.x, r.o.y, r.o.z, r.d.x, r.d.y, r.d.z, r.index, (float)pass});
+    }
+    return closest(bvh, F, r, h);
+  }
 
   // calculateGeometry (SPPM.cpp:36-77)
   void geometry(const Hit& h, Geometry& g) const {
@@ -868,7 +887,7 @@ struct Renderer {
         PDF *= rus;
       }
       Hit hit;
-      if (!closest(bvh, F, cur, hit)) {
+      if (!trace(cur, hit, 0)) {
         // Sample IBL (SPPM.cpp:290-300)
         if (has_ibl) hp.dl = hp.dl + ibl_color(cur.d) * thr / PDF;
         if (hp.type == 0) hp.type = 2;
@@ -965,7 +984,7 @@ struct Renderer {
       if (loop++ > 32 || k >= 32 - 1) break;
       if (thr.x < 1e-8 || thr.y < 1e-8 || thr.z < 1e-8) break;
       Hit hit;
-      if (!closest(bvh, F, cur, hit)) break;
+      if (!trace(cur, hit, 1)) break;
       Geometry g;
       geometry(hit, g);
       g.normal = dot(g.normal, cur.d) > 0 ? -g.normal : g.normal;
@@ -1274,6 +1293,22 @@ void port_iterate(void* h, int32_t n) {
 // The next iteration runs step first_step + 1 (its seeds, SPPM.cpp:334,520);
 // for checking one step's eye pass without running the steps before it.  The
 // resolve then counts the skipped steps as iterations.
+// Starts (stride > 0) or stops keeping every stride-th closest-hit ray, up
+// to cap rays; clears the kept ones.
+void port_sample_rays(void* h, int64_t stride, int64_t cap) {
+  Renderer* r = static_cast<Renderer*>(h);
+  r->ray_stride = stride;
+  r->ray_cap = (size_t)std::max<int64_t>(0, cap);
+  r->ray_count = 0;
+  r->ray_sample.clear();
+}
+// Copies the kept rays (8 floats each) to out when out is not NULL; returns their count.
+int64_t port_read_ray_sample(void* h, float* out) {
+  Renderer* r = static_cast<Renderer*>(h);
+  if (out) std::memcpy(out, r->ray_sample.data(), r->ray_sample.size() * sizeof(float));
+  return (int64_t)(r->ray_sample.size() / 8);
+}
+
 void port_seek(void* h, int32_t first_step) { static_cast<Renderer*>(h)->step = first_step; }
 
 // Photon pass only (for a bounded CPU timing sample).

@@ -51,6 +51,9 @@ def load():
         lib.port_set_ibl.argtypes = [vp, C.c_int32, C.c_int32, vp]
         lib.port_read_direct.argtypes = [vp, vp, vp, vp]
         lib.port_seek.argtypes = [vp, C.c_int32]
+        lib.port_sample_rays.argtypes = [vp, C.c_int64, C.c_int64]
+        lib.port_read_ray_sample.argtypes = [vp, vp]
+        lib.port_read_ray_sample.restype = C.c_int64
         lib.port_photon_pass.argtypes = [vp, C.c_int32, C.c_int32]
         lib.port_resolve.argtypes = [vp, vp]
         lib.port_trace_closest.argtypes = [vp, vp, C.c_int32, vp, vp]
@@ -156,6 +159,17 @@ class PortRenderer:
     def seek(self, first_step):
         """The next iteration runs step first_step + 1."""
         _lib.port_seek(self.h, int(first_step))
+
+    def sample_rays(self, stride, cap):
+        """Keep every stride-th closest-hit ray the next iterations trace (up to cap)."""
+        _lib.port_sample_rays(self.h, int(stride), int(cap))
+
+    def ray_sample(self):
+        """The kept rays: (N x 7 float32 {origin, direction, index}, N pass tags 0 eye / 1 photon)."""
+        n = int(_lib.port_read_ray_sample(self.h, None))
+        out = np.empty((n, 8), np.float32)
+        _lib.port_read_ray_sample(self.h, _p(out))
+        return np.ascontiguousarray(out[:, :7]), out[:, 7].astype(np.int32)
 
     def photon_pass(self, first, count):
         _lib.port_photon_pass(self.h, int(first), int(count))

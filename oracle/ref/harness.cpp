@@ -8,6 +8,7 @@
 //   frref <scene_dir> any    <rays.bin> <out_dir>
 //   frref <scene_dir> render <photons_per_iter> <iterations> <out_dir>
 //   frref <dir> texture <image_file> <out_dir>
+//   frref <scene_dir> count <rays.bin> <out_dir>
 //
 // <scene_dir> holds meshData/scene.obj (+ .mtl, textures), materials.txt and
 // camera.txt as written by frsppm.objio.
@@ -41,6 +42,7 @@
 #include <sstream>
 #include <string>
 #include <thread>
+#include <type_traits>
 #include <utility>
 #include <vector>
 #include <unistd.h>
@@ -159,6 +161,55 @@ class PixelStreamSampler : public iCameraSsmpler {
 };
 
 struct CamSpec { int type, W, H; float pos[3], tgt[3], fov, focal, dist, aspect, lens; };
+
+// The reference's closest-hit traversal, N_BVH8::findClosestElement
+// (bvh8.h:568-641), with its loop kept step for step and two counters
+// added: V, the internal nodes whose eight child boxes are tested
+// (Intersect_AABB8_RAY), and X, the leaves whose triangle is tested.  The
+// traversal work of a ray on the reference's tree is 168 V + 40 X FP32
+// operations (21 per slab test of one child, about 40 per Moller-Trumbore
+// test, Intersect.cpp:67-89, 515-553).
+template <class B>
+float count_closest(const B& b, const Primitive::Ray& ray, int32_t& V, int32_t& X) {
+  using NodeT = typename std::decay<decltype(b.m_NodeArray[0])>::type;
+  std::deque<unsigned int> stack;
+  stack.push_back(0u);
+  float best = ray.m_MaxT;
+  int num_box = 0;
+  V = X = 0;
+  while (stack.size() > 0 && num_box < (int)b.m_NumNodes) {
+    const unsigned int id = *(stack.end() - 1);
+    const NodeT& node = b.m_NodeArray[id];
+    stack.pop_back();
+    num_box++;
+    if (node.isLeaf()) {
+      if (node.m_children[0] != NodeT::InvalidID) {
+        ++X;
+        Isc::IntersectInfo info;
+        if (Isc::Intersect(b.m_ElementArray[node.m_children[0]].second, ray, info))
+          if (best >= info.t && info.t > ray.m_MinT) best = info.t;
+      }
+      continue;
+    }
+    ++V;
+    std::array<float, 8> hd;
+    if (!Isc::Intersect_AABB8_RAY(node.m_childAABBs, ray, hd)) continue;
+    std::array<std::pair<unsigned int, float>, 8> res;
+    const bool of = ray.m_Dir[node.getAxis(0)] > 0, of0 = ray.m_Dir[node.getAxis(1)] > 0;
+    const bool of00 = ray.m_Dir[node.getAxis(3)] > 0;
+    res[of * 4 + of0 * 2 + of00] = {0u, hd[0]};
+    res[of * 4 + of0 * 2 + !of00] = {1u, hd[1]};
+    res[of * 4 + !of0 * 2 + of00] = {2u, hd[2]};
+    res[of * 4 + !of0 * 2 + !of00] = {3u, hd[3]};
+    res[!of * 4 + of0 * 2 + of00] = {4u, hd[4]};
+    res[!of * 4 + of0 * 2 + !of00] = {5u, hd[5]};
+    res[!of * 4 + !of0 * 2 + of00] = {6u, hd[6]};
+    res[!of * 4 + !of0 * 2 + !of00] = {7u, hd[7]};
+    for (int i = 0; i < 8; ++i)
+      if (res[i].second < best) stack.push_back(node.m_children[res[i].first]);
+  }
+  return best;
+}
 
 CamSpec read_camera(const std::string& path) {
   CamSpec c{};
@@ -317,6 +368,31 @@ int main(int argc, char** argv) {
     cam.push_back(camera->_Fov); cam.push_back(camera->_PlaneWidth); cam.push_back(camera->_PlaneHeight);
     cam.push_back(camera->_LensWidth); cam.push_back(camera->_LensHeight); cam.push_back(camera->_F); cam.push_back(camera->_DistanceToLens);
     npy_f32(out_dir + "/camera.npy", cam, {cam.size()});
+    return 0;
+  }
+
+  if (mode == "count") {
+    // rays.bin as for "trace"; out: visits.npy, N x 2 int32 (V, X), and
+    // best_t.npy, the closest t (FLT_MAX for a miss) as a check on the loop.
+    const std::string rays_path = argv[3];
+    out_dir = argv[4];
+    std::ifstream f(rays_path, std::ios::binary | std::ios::ate);
+    const size_t bytes = (size_t)f.tellg();
+    f.seekg(0);
+    std::vector<float> rays(bytes / 4);
+    f.read(reinterpret_cast<char*>(rays.data()), bytes);
+    const size_t N = rays.size() / 7;
+    std::vector<int32_t> vx(N * 2);
+    std::vector<float> best_t(N);
+    const auto& bvh = *scene.m_Aobject;
+#pragma omp parallel for schedule(dynamic, 64)
+    for (long i = 0; i < (long)N; ++i) {
+      const float* r = &rays[i * 7];
+      Primitive::Ray ray(Vec3(r[0], r[1], r[2]), Vec3(r[3], r[4], r[5]), r[6], Primitive::Ray::RAY_OFFSET, FLT_MAX);
+      best_t[i] = count_closest(bvh, ray, vx[i * 2], vx[i * 2 + 1]);
+    }
+    npy_i32(out_dir + "/visits.npy", vx, {N, 2});
+    npy_f32(out_dir + "/best_t.npy", best_t, {N});
     return 0;
   }
 
