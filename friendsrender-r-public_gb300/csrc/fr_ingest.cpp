@@ -59,26 +59,25 @@ bool is_blank(char c) { return c == ' ' || c == '\t'; }
 bool is_line_end(char c) { return c == '\r' || c == '\n' || c == '\0'; }
 bool is_digit(char c) { return (unsigned)(c - '0') < 10u; }
 
-// Splits text into lines ending at "\n", "\r\n" or "\r" (a last line without
-// an ending counts when it is not empty).
-std::vector<std::string> split_lines(const std::string& text) {
-  std::vector<std::string> lines;
+// Calls fn(line) for each line of text, lines ending at "\n", "\r\n" or
+// "\r" (a last line without an ending counts when it is not empty).
+template <class Fn>
+void for_each_line(const std::string& text, Fn fn) {
   std::string cur;
-  for (size_t i = 0; i < text.size(); ++i) {
-    const char c = text[i];
-    if (c == '\n') {
-      lines.push_back(cur);
-      cur.clear();
-    } else if (c == '\r') {
-      if (i + 1 < text.size() && text[i + 1] == '\n') ++i;
-      lines.push_back(cur);
-      cur.clear();
-    } else {
-      cur += c;
+  size_t i = 0;
+  const size_t n = text.size();
+  while (i < n) {
+    size_t j = i;
+    while (j < n && text[j] != '\n' && text[j] != '\r') ++j;
+    cur.assign(text, i, j - i);
+    if (j < n) {
+      if (text[j] == '\r' && j + 1 < n && text[j + 1] == '\n') ++j;
+      fn(cur);
+    } else if (!cur.empty()) {
+      fn(cur);
     }
+    i = j + 1;
   }
-  if (!cur.empty()) lines.push_back(cur);
-  return lines;
 }
 
 bool read_file(const std::string& path, std::string* text) {
@@ -258,43 +257,43 @@ void load_mtl(const std::string& path, ObjData* obj) {
     obj->materials.push_back(mat);
   };
   if (ok) {
-    for (const std::string& line : split_lines(text)) {
+    for_each_line(text, [&](const std::string& line) {
       const char* t = line.c_str();
       t += std::strspn(t, " \t");
-      if (t[0] == '\0' || t[0] == '#') continue;
+      if (t[0] == '\0' || t[0] == '#') return;
       if (!std::strncmp(t, "newmtl", 6) && is_blank(t[6])) {
         if (!m.name.empty()) flush(m);
         m = MtlMaterial();
         m.name = first_word(t + 7);
-        continue;
+        return;
       }
       if (t[0] == 'K' && t[1] == 'd' && is_blank(t[2])) {
         t += 2;
         for (float& x : m.kd) x = parse_float(t);
-        continue;
+        return;
       }
       if (t[0] == 'K' && t[1] == 'e' && is_blank(t[2])) {
         t += 2;
         for (float& x : m.ke) x = parse_float(t);
-        continue;
+        return;
       }
       if (!std::strncmp(t, "map_Kd", 6) && is_blank(t[6])) {
         m.map_kd = t + 7;
-        continue;
+        return;
       }
       if (!std::strncmp(t, "map_bump", 8) && is_blank(t[8])) {
         m.map_bump = t + 9;
-        continue;
+        return;
       }
       if (!std::strncmp(t, "map_d", 5) && is_blank(t[5])) {
         m.map_d = t + 6;
-        continue;
+        return;
       }
       if (!std::strncmp(t, "bump", 4) && is_blank(t[4])) {
         m.map_bump = t + 5;
-        continue;
+        return;
       }
-    }
+    });
   }
   flush(m);  // the last material, or a default one named "" (also for a file that cannot be read)
 }
@@ -350,10 +349,11 @@ std::string load_obj(const std::string& path, const std::string& base, ObjData* 
   Shape shape;
   int material = -1;
   std::string error;
-  for (const std::string& line : split_lines(text)) {
+  for_each_line(text, [&](const std::string& line) {
+    if (!error.empty()) return;
     const char* t = line.c_str();
     t += std::strspn(t, " \t");
-    if (t[0] == '\0' || t[0] == '#') continue;
+    if (t[0] == '\0' || t[0] == '#') return;
     if (t[0] == 'v' && is_blank(t[1])) {
       t += 2;
       for (int k = 0; k < 3; ++k) obj->v.push_back(parse_float(t));
@@ -387,8 +387,8 @@ std::string load_obj(const std::string& path, const std::string& base, ObjData* 
       shape = Shape();
       group.clear();
     }
-    if (!error.empty()) return path + ": " + error;
-  }
+  });
+  if (!error.empty()) return path + ": " + error;
   if (flush_group(*obj, group, material, &shape, &error)) obj->shapes.push_back(std::move(shape));
   if (!error.empty()) return path + ": " + error;
   return "";
