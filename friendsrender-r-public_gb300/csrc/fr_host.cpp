@@ -246,6 +246,12 @@ struct fr_ctx {
   float4* dbg_phi = nullptr;
   float4* image = nullptr;
   uint32_t* image8 = nullptr;    // exported RGBA8
+  // fr_resolve_async: images {image, image_b} in turn, copied to the host on
+  // copy_stream; ready[b] marks resolve b written, copied[b] its copy landed.
+  float4* image_b = nullptr;
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ready[2] = {}, copied[2] = {};
+  uint64_t async_seq = 0;
   int64_t iterations = 0, photons_total = 0;
   int64_t launches = 0;  // kernels launched by fr_iterate so far
   // Stage profiler: events recorded on the stream around each stage.
@@ -277,8 +283,14 @@ struct fr_ctx {
     if (side) cudaStreamSynchronize(side);
     for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
     for (auto& b : bufs) cudaFree(b.p);
+    if (copy_stream) cudaStreamSynchronize(copy_stream);
     if (fork_ev) cudaEventDestroy(fork_ev);
     if (join_ev) cudaEventDestroy(join_ev);
+    for (int k = 0; k < 2; ++k) {
+      if (ready[k]) cudaEventDestroy(ready[k]);
+      if (copied[k]) cudaEventDestroy(copied[k]);
+    }
+    if (copy_stream) cudaStreamDestroy(copy_stream);
     if (graph_exec) cudaGraphExecDestroy(graph_exec);
     if (graph) cudaGraphDestroy(graph);
     if (side) cudaStreamDestroy(side);
@@ -663,6 +675,12 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
   for (cudaStream_t& b : c->body)
     if (cudaStreamCreateWithFlags(&b, cudaStreamNonBlocking) != cudaSuccess)
       return bail(fail(FR_ERR_CUDA, "cudaStreamCreate failed"));
+  if (cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking) != cudaSuccess)
+    return bail(fail(FR_ERR_CUDA, "cudaStreamCreate failed"));
+  for (int k = 0; k < 2; ++k)
+    if (cudaEventCreateWithFlags(&c->ready[k], cudaEventDisableTiming) != cudaSuccess ||
+        cudaEventCreateWithFlags(&c->copied[k], cudaEventDisableTiming) != cudaSuccess)
+      return bail(fail(FR_ERR_CUDA, "cudaEventCreate failed"));
   c->W = camera->width;
   c->H = camera->height;
   c->P = params->photons_per_iteration;
@@ -823,7 +841,7 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
       (rc = c->alloc(&c->gi, 1)) || (rc = c->alloc(&c->step_dev, 1)) || (rc = c->alloc(&c->rounds_run, 1)) ||
       (rc = c->alloc(&c->err, 1)) ||
       (rc = c->alloc(&c->dbg_m, npix)) || (rc = c->alloc(&c->dbg_phi, npix)) || (rc = c->alloc(&c->image, npix)) ||
-      (rc = c->alloc(&c->image8, npix)))
+      (rc = c->alloc(&c->image_b, npix)) || (rc = c->alloc(&c->image8, npix)))
     return bail(rc);
   // Counters (one memset per iteration): eye rounds, photon rounds, the
   // hitpoint list, eye and photon shade queues, eye and photon trace fetches.
@@ -993,8 +1011,37 @@ int fr_resolve_dev(fr_ctx* c, float* rgba_dev) {
   return FR_OK;
 }
 
+int fr_resolve_async(fr_ctx* c, float* rgba, uint64_t* ticket) {
+  if (!c || !rgba) return fail(FR_ERR_INVALID, "fr_resolve_async: bad arguments");
+  const int b = (int)(c->async_seq & 1u);
+  float4* img = b ? c->image_b : c->image;
+  // The copy that last read this image (two calls ago) must have landed
+  // before the resolve overwrites it; a never-recorded event is no wait.
+  FR_CUDA(cudaStreamWaitEvent(c->stream, c->copied[b], 0));
+  int rc = fr_resolve_dev(c, reinterpret_cast<float*>(img));
+  if (rc) return rc;
+  FR_CUDA(cudaEventRecord(c->ready[b], c->stream));
+  FR_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ready[b], 0));
+  FR_CUDA(cudaMemcpyAsync(rgba, img, sizeof(float4) * (size_t)c->W * c->H, cudaMemcpyDeviceToHost, c->copy_stream));
+  FR_CUDA(cudaEventRecord(c->copied[b], c->copy_stream));
+  if (ticket) *ticket = c->async_seq;
+  ++c->async_seq;
+  return FR_OK;
+}
+
+int fr_resolve_wait(fr_ctx* c, uint64_t ticket) {
+  if (!c || ticket >= c->async_seq) return fail(FR_ERR_INVALID, "fr_resolve_wait: bad arguments");
+  // The event of this ticket's buffer was recorded for this copy or a later
+  // one on the same copy stream; either way, once it completes this copy has.
+  // The device error word is left to fr_synchronize / fr_resolve: reading it
+  // here would wait for the iteration now running.
+  FR_CUDA(cudaEventSynchronize(c->copied[ticket & 1u]));
+  return FR_OK;
+}
+
 int fr_resolve(fr_ctx* c, float* rgba) {
   if (!c || !rgba) return fail(FR_ERR_INVALID, "fr_resolve: bad arguments");
+  FR_CUDA(cudaStreamWaitEvent(c->stream, c->copied[0], 0));  // an asynchronous copy of `image` in flight
   int rc = fr_resolve_dev(c, reinterpret_cast<float*>(c->image));
   if (rc) return rc;
   FR_CUDA(cudaMemcpyAsync(rgba, c->image, sizeof(float4) * (size_t)c->W * c->H, cudaMemcpyDeviceToHost, c->stream));
@@ -1003,6 +1050,7 @@ int fr_resolve(fr_ctx* c, float* rgba) {
 
 int fr_resolve_rgba8(fr_ctx* c, uint8_t* rgba) {
   if (!c || !rgba) return fail(FR_ERR_INVALID, "fr_resolve_rgba8: bad arguments");
+  FR_CUDA(cudaStreamWaitEvent(c->stream, c->copied[0], 0));
   int rc = fr_resolve_dev(c, reinterpret_cast<float*>(c->image));
   if (rc) return rc;
   launch_export_rgba8(c->image, c->W, c->H, c->image8, c->stream);

@@ -76,7 +76,7 @@ EXPORTS = ['fr_last_error', 'fr_create', 'fr_iterate', 'fr_synchronize', 'fr_res
            'fr_resolve_rgba8', 'fr_export_png', 'fr_write_png', 'fr_check_tc_gemm', 'fr_guide_params',
            'fr_guide_set_params', 'fr_read_guide_importance', 'fr_guide_gradient', 'fr_seek', 'fr_iterate_batch',
            'fr_autotune', 'fr_update_dev', 'fr_read_direct', 'fr_scene_load_obj', 'fr_scene_get_desc',
-           'fr_scene_material_name', 'fr_scene_free', 'fr_texture_load']
+           'fr_scene_material_name', 'fr_scene_free', 'fr_texture_load', 'fr_resolve_async', 'fr_resolve_wait']
 
 STAGES = ('eye', 'photon', 'grid', 'gather', 'eye_trace', 'photon_trace')
 
@@ -99,6 +99,8 @@ def load(path=None):
     lib.fr_synchronize.argtypes = [vp]
     lib.fr_resolve.argtypes = [vp, vp]
     lib.fr_resolve_dev.argtypes = [vp, vp]
+    lib.fr_resolve_async.argtypes = [vp, vp, C.POINTER(C.c_uint64)]
+    lib.fr_resolve_wait.argtypes = [vp, C.c_uint64]
     lib.fr_get_stats.argtypes = [vp, C.POINTER(Stats)]
     lib.fr_stream.argtypes = [vp]
     lib.fr_stream.restype = vp
@@ -250,6 +252,16 @@ class Renderer:
 
     def resolve_dev(self, dev_ptr):
         _check(_lib.fr_resolve_dev(self.h, C.c_void_p(dev_ptr)), 'fr_resolve_dev')
+
+    def resolve_async(self, host_ptr):
+        """fr_resolve_async into the host buffer at host_ptr (width*height*4
+        floats, best pinned); returns the ticket for resolve_wait."""
+        t = C.c_uint64()
+        _check(_lib.fr_resolve_async(self.h, C.c_void_p(host_ptr), C.byref(t)), 'fr_resolve_async')
+        return t.value
+
+    def resolve_wait(self, ticket):
+        _check(_lib.fr_resolve_wait(self.h, C.c_uint64(ticket)), 'fr_resolve_wait')
 
     def stats(self):
         s = Stats()

@@ -266,6 +266,17 @@ int fr_autotune(fr_ctx* ctx, int iterations, uint32_t* photon_tail_min);
 int fr_resolve(fr_ctx* ctx, float* rgba);
 int fr_resolve_dev(fr_ctx* ctx, float* rgba_dev);
 
+/* fr_resolve without the wait, so that the read-back overlaps the next
+ * fr_iterate: queues the image of the current state and its copy into the
+ * host buffer rgba (pinned memory lets the copy run alongside the next
+ * iteration) on a copy stream of the context, and returns a ticket.
+ * fr_resolve_wait(ticket) returns once that copy has landed; rgba must stay
+ * valid until then.  The context holds two device images, used in turn, so
+ * a third call's resolve waits on the device for the first call's copy.
+ * Kernel errors are reported by the next fr_synchronize or fr_resolve. */
+int fr_resolve_async(fr_ctx* ctx, float* rgba, uint64_t* ticket);
+int fr_resolve_wait(fr_ctx* ctx, uint64_t ticket);
+
 /* ExportPNG (TextureUtility.cpp:52-65): the current image resampled by the
  * reference's bilinear sampler at u = i / W, v = j / H and quantized to
  * max(0, min(255, int(c * 255))) per channel; width*height*4 bytes, row-major
