@@ -64,6 +64,27 @@ def fp32_peak_tflops(sm_mhz):
     return sms * 128 * 2 * sm_mhz * 1e6 / 1e12
 
 
+def pipelined_e2e(r, npix, steps):
+    """Seconds for `steps` iterations through the C-ABI, each one's image
+    copied into pinned host memory by fr_resolve_async (two buffers in turn)
+    and waited for while the next iteration runs; the last wait and the
+    device error check (fr_synchronize) are inside the timed region."""
+    import torch
+    hosts = [torch.empty((npix, 4), dtype=torch.float32, pin_memory=True) for _ in range(2)]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    prev = None
+    for k in range(steps):
+        r.iterate(1, sync=False)
+        ticket = r.resolve_async(hosts[k % 2].data_ptr())
+        if prev is not None:
+            r.resolve_wait(prev)  # step k-1's image is on the host
+        prev = ticket
+    r.resolve_wait(prev)
+    r.synchronize()
+    return time.perf_counter() - t0
+
+
 def traversal_block(rays, eye_rays, photon_rays, trace_s, eye_q, photon_q, clocks):
     """Trace-kernel throughput: rays per second of trace-kernel time, and the
     reference's traversal work on those rays (TRAVERSAL_FP32_OPS_PER_RAY) as a
@@ -375,13 +396,7 @@ def run_large(args):
         stream.synchronize()
     ms = a.elapsed_time(b)
     launches = r.profile_read()[2] - l0
-    host = torch.empty((npix, 4), dtype=torch.float32, pin_memory=True)
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        r.iterate(1, sync=False)
-        abi._check(abi._lib.fr_resolve(r.h, abi.C.c_void_p(host.data_ptr())), 'fr_resolve')
-    e2e_s = time.perf_counter() - t0
+    e2e_s = pipelined_e2e(r, npix, args.steps)
     eye_q, photon_q = r.wave_counts()
     r.close()
     out = {'metric': METRIC, 'value': LARGE_PHOTONS * args.steps / (ms / 1000.0), 'unit': UNIT, 'n_gpus': 1,
@@ -633,20 +648,8 @@ def main():
     # step's image is copied to the host (fr_resolve_async, two buffers in
     # turn) and waited for while the next step runs; the last one and the
     # device error check close the timed region.
-    hosts = [torch.empty((npix, 4), dtype=torch.float32, pin_memory=True) for _ in range(2)]
     barrier()
-    torch.cuda.synchronize()
-    t0 = time.perf_counter()
-    prev = None
-    for k in range(args.steps):
-        r.iterate(1, sync=False)
-        ticket = r.resolve_async(hosts[k % 2].data_ptr())
-        if prev is not None:
-            r.resolve_wait(prev)  # step k-1's image is on the host
-        prev = ticket
-    r.resolve_wait(prev)
-    r.synchronize()
-    e2e_s = time.perf_counter() - t0
+    e2e_s = pipelined_e2e(r, npix, args.steps)
     if world > 1:
         t = torch.tensor([e2e_s], device='cuda')
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
