@@ -459,9 +459,31 @@ def run_batch(args):
     W = max(3, args.warmup)
     abi.iterate_batch(rs, W)
     torch.cuda.synchronize()
+    l0 = sum(r.profile_read()[2] for r in rs)
+    with ClockSampler(0) as clk:
+        t0 = time.perf_counter()
+        abi.iterate_batch(rs, args.steps)
+        dt = time.perf_counter() - t0
+    launches = sum(r.profile_read()[2] for r in rs) - l0
+    # End to end: every step, every scene's image copied into pinned host
+    # memory (fr_resolve_async, two buffers per scene in turn) and waited for
+    # while the next step runs.
+    hosts = [[torch.empty((r.width * r.height, 4), dtype=torch.float32, pin_memory=True) for _ in range(2)]
+             for r in rs]
+    torch.cuda.synchronize()
     t0 = time.perf_counter()
-    abi.iterate_batch(rs, args.steps)
-    dt = time.perf_counter() - t0
+    prev = None
+    for k in range(args.steps):
+        abi.iterate_batch(rs, 1)
+        tickets = [r.resolve_async(h[k % 2].data_ptr()) for r, h in zip(rs, hosts)]
+        if prev is not None:
+            for r, t in zip(rs, prev):
+                r.resolve_wait(t)
+        prev = tickets
+    for r, t in zip(rs, prev):
+        r.resolve_wait(t)
+        r.synchronize()
+    e2e_dt = time.perf_counter() - t0
     photons = sum(sp['photons'] for sp in specs)
     pixels = sum(r.width * r.height for r in rs)
     dev = sum(r.stats()['device_bytes'] for r in rs)
@@ -482,7 +504,10 @@ def run_batch(args):
                           'note': 'sum over the scenes of one graph replay alone (CUDA events)'},
            'batch_speedup': seq_ms / (1e3 * dt / args.steps),
            'autotune': {'photon_tail_min_chosen': hist},
-           'setup': {'scene_generation_s': gen_s, 'contexts_s': setup_s, 'device_bytes': int(dev)}}
+           'setup': {'scene_generation_s': gen_s, 'contexts_s': setup_s, 'device_bytes': int(dev)},
+           'e2e': {'value': photons * args.steps / e2e_dt, 'unit': UNIT, 'h2d_bytes_per_step': 0,
+                   'd2h_bytes_per_step': pixels * 16},
+           'gpu_launches': launches, 'clocks': clk.summary()}
     print(json.dumps(out))
     return 0
 
