@@ -53,7 +53,7 @@ __global__ void __launch_bounds__(128) k_guide_train(GuideGPU g) {
   float* bias = reinterpret_cast<float*>(sm + kSmB);  // b2 [0,64), b3 [64,128), b4 [128,176)
   uint32_t* tbase = reinterpret_cast<uint32_t*>(sm + kSmMisc);
   uint64_t* bar = reinterpret_cast<uint64_t*>(sm + kSmMisc + 8);
-  float* wsum = reinterpret_cast<float*>(sm + kSmMisc + 16);
+  float* wsum = reinterpret_cast<float*>(sm + kSmMisc + 16);  // one per warp
   const uint32_t t = threadIdx.x, warp = t >> 5;
 
   const uint32_t n_all = min(*g.batch_count, (uint32_t)g.batch_cap);
@@ -70,10 +70,7 @@ __global__ void __launch_bounds__(128) k_guide_train(GuideGPU g) {
   }
   for (uint32_t e = t; e < 48; e += 128) bias[128 + e] = g.params[kOffB4 + e];
   for (uint32_t e = t; e < (128 * 128 * 2 + 80 * 128 * 2) / 16; e += 128) reinterpret_cast<uint4*>(AT)[e] = uint4{0, 0, 0, 0};
-  if (t == 0) {
-    tc::mbar_init(bar, 1);
-    *wsum = 0.0f;
-  }
+  if (t == 0) tc::mbar_init(bar, 1);
   if (warp == 0) tc::tmem_alloc(tbase, kTmCols);
   publish();
   const uint32_t tm = *tbase;
@@ -97,7 +94,7 @@ __global__ void __launch_bounds__(128) k_guide_train(GuideGPU g) {
       const float4 f = g.feat[i], dd = g.dir[i];
       x[0] = f.x; x[1] = f.y; x[2] = f.z; x[3] = f.w; x[4] = dd.x;
       d = v3(dd.y, dd.z, dd.w);
-      I = g.importance[i];
+      I = g.batch_w[j0];
     }
     my_wsum += I;
     // ---- forward
@@ -203,42 +200,49 @@ __global__ void __launch_bounds__(128) k_guide_train(GuideGPU g) {
     // rows 64-127 and BT rows 65-79 stay zero.
     first = false;
   }
-  // ---- gradient sums of this CTA to global memory (thread t: unit t)
+  // ---- gradient sums of this CTA to its own row of grad_part (thread t:
+  // unit t); k_guide_reduce adds the rows in CTA order, so the step's
+  // gradient does not depend on which CTA finishes first.
+  float* gp = g.grad_part + (size_t)blockIdx.x * kGuideParams;
   if (!first && sy.ok) {
     float v[16];
     for (int c0 = 0; c0 < 80; c0 += 16) {
       tc::tmem_ld16(lane_addr + kTmG4 + c0, v);
       for (int k = 0; k < 16; ++k) {
         const int c = c0 + k;
-        if (t < (uint32_t)kGuideOut && c < 64) atomicAdd(g.grad + kOffW4 + t * 64 + c, v[k]);
-        if (t < (uint32_t)kGuideOut && c == 64) atomicAdd(g.grad + kOffB4 + t, v[k]);
+        if (t < (uint32_t)kGuideOut && c < 64) gp[kOffW4 + t * 64 + c] = v[k];
+        if (t < (uint32_t)kGuideOut && c == 64) gp[kOffB4 + t] = v[k];
       }
       tc::tmem_ld16(lane_addr + kTmG3 + c0, v);
       for (int k = 0; k < 16; ++k) {
         const int c = c0 + k;
-        if (t < 64 && c < 64) atomicAdd(g.grad + kOffW3 + t * 64 + c, v[k]);
-        if (t < 64 && c == 64) atomicAdd(g.grad + kOffB3 + t, v[k]);
+        if (t < 64 && c < 64) gp[kOffW3 + t * 64 + c] = v[k];
+        if (t < 64 && c == 64) gp[kOffB3 + t] = v[k];
       }
       tc::tmem_ld16(lane_addr + kTmG2 + c0, v);
       for (int k = 0; k < 16; ++k) {
         const int c = c0 + k;
-        if (t < 64 && c < 64) atomicAdd(g.grad + kOffW2 + t * 64 + c, v[k]);
-        if (t < 64 && c == 64) atomicAdd(g.grad + kOffB2 + t, v[k]);
+        if (t < 64 && c < 64) gp[kOffW2 + t * 64 + c] = v[k];
+        if (t < 64 && c == 64) gp[kOffB2 + t] = v[k];
       }
     }
     tc::tmem_ld16(lane_addr + kTmG1, v);
     if (t < 64) {
-      for (int k = 0; k < kGuideIn; ++k) atomicAdd(g.grad + kOffW1 + t * kGuideIn + k, v[k]);
-      atomicAdd(g.grad + kOffB1 + t, v[kGuideIn]);
+      for (int k = 0; k < kGuideIn; ++k) gp[kOffW1 + t * kGuideIn + k] = v[k];
+      gp[kOffB1 + t] = v[kGuideIn];
     }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) my_wsum += __shfl_down_sync(0xffffffffu, my_wsum, o);
-    if ((t & 31) == 0) atomicAdd(wsum, my_wsum);
+    if ((t & 31) == 0) wsum[warp] = my_wsum;
+  } else {
+    // A wait gave up: this CTA's row adds nothing.
+    for (uint32_t e = t; e < (uint32_t)kGuideParams; e += 128) gp[e] = 0.0f;
+    if ((t & 31) == 0) wsum[warp] = 0.0f;
   }
   if (!sy.ok && t == 0) atomicOr(g.err, kErrGuide);
   tc::fence_before_sync();
   __syncthreads();
-  if (t == 0 && !first && sy.ok) atomicAdd(g.weight_sum, *wsum);
+  if (t == 0) g.wsum_part[blockIdx.x] = ((wsum[0] + wsum[1]) + wsum[2]) + wsum[3];
   if (warp == 0) tc::tmem_dealloc(tm, kTmCols);
 }
 
@@ -281,20 +285,101 @@ __global__ void k_guide_step_done(GuideGPU g, int last) {
   if (last) *g.batch_count = 0;
 }
 
-// Paths whose photons reached a hitpoint, as training samples (one atomic
-// per block).
-__global__ void __launch_bounds__(256) k_guide_select(GuideGPU g, int paths) {
-  __shared__ uint32_t s_n, s_base;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const bool take = i < paths && g.importance[i] > 0.0f && g.importance[i] < INFINITY;
-  if (threadIdx.x == 0) s_n = 0;
+// Paths whose photons reached a hitpoint, as training samples, in path
+// order (so the batch, and with it the training, is the same run to run):
+// per-block counts, one exclusive scan of them, then each block writes its
+// paths at its offset.  The first batch_cap such paths are taken; a path's
+// index says nothing about its photons, so they are an unbiased subset.
+constexpr int kSelectBlock = 256;
+constexpr int kSelectScanThreads = 1024;
+
+__device__ __forceinline__ bool guide_takes(const GuideGPU& g, int i, int paths) {
+  return i < paths && (g.importance[2 * (size_t)i] | g.importance[2 * (size_t)i + 1]) != 0ull;
+}
+
+// Number of paths a block takes, and each thread's rank among them.
+__device__ __forceinline__ uint32_t select_block_rank(bool take, uint32_t* rank) {
+  __shared__ uint32_t s_warp[kSelectBlock / 32];
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t bal = __ballot_sync(0xffffffffu, take);
+  if (lane == 0) s_warp[warp] = __popc(bal);
   __syncthreads();
-  uint32_t slot = 0;
-  if (take) slot = atomicAdd(&s_n, 1u);
+  uint32_t before = 0, total = 0;
+  for (uint32_t w = 0; w < kSelectBlock / 32; ++w) {
+    if (w < warp) before += s_warp[w];
+    total += s_warp[w];
+  }
+  *rank = before + __popc(bal & ((1u << lane) - 1u));
+  return total;
+}
+
+__global__ void __launch_bounds__(kSelectBlock) k_guide_select_count(GuideGPU g, int paths) {
+  uint32_t rank;
+  const uint32_t n = select_block_rank(guide_takes(g, blockIdx.x * kSelectBlock + threadIdx.x, paths), &rank);
+  if (threadIdx.x == 0) g.select_part[blockIdx.x] = n;
+}
+
+// One block: select_part[0..blocks) becomes exclusive offsets; batch_count
+// the number of paths taken (before the cap).
+__global__ void __launch_bounds__(kSelectScanThreads) k_guide_select_scan(GuideGPU g, int blocks) {
+  __shared__ uint32_t s_sum[kSelectScanThreads];
+  const uint32_t t = threadIdx.x;
+  const uint32_t per = (blocks + kSelectScanThreads - 1) / kSelectScanThreads;
+  const uint32_t b0 = t * per, b1 = min(b0 + per, (uint32_t)blocks);
+  uint32_t mine = 0;
+  for (uint32_t b = b0; b < b1; ++b) mine += g.select_part[b];
+  s_sum[t] = mine;
   __syncthreads();
-  if (threadIdx.x == 0) s_base = s_n ? atomicAdd(g.batch_count, s_n) : 0u;
-  __syncthreads();
-  if (take && s_base + slot < (uint32_t)g.batch_cap) g.batch[s_base + slot] = (uint32_t)i;
+  for (uint32_t o = 1; o < kSelectScanThreads; o <<= 1) {  // inclusive Hillis-Steele scan
+    const uint32_t v = t >= o ? s_sum[t - o] : 0u;
+    __syncthreads();
+    s_sum[t] += v;
+    __syncthreads();
+  }
+  uint32_t run = s_sum[t] - mine;
+  for (uint32_t b = b0; b < b1; ++b) {
+    const uint32_t c = g.select_part[b];
+    g.select_part[b] = run;
+    run += c;
+  }
+  if (t == kSelectScanThreads - 1) *g.batch_count = s_sum[t];
+}
+
+__global__ void __launch_bounds__(kSelectBlock) k_guide_select_write(GuideGPU g, int paths) {
+  const int i = blockIdx.x * kSelectBlock + threadIdx.x;
+  const bool take = guide_takes(g, i, paths);
+  uint32_t rank;
+  select_block_rank(take, &rank);
+  const uint32_t slot = g.select_part[blockIdx.x] + rank;
+  if (take && slot < (uint32_t)g.batch_cap) {
+    g.batch[slot] = (uint32_t)i;
+    g.batch_w[slot] = importance_value(g.importance[2 * (size_t)i], g.importance[2 * (size_t)i + 1]);
+  }
+}
+
+// The step's gradient and importance sums: the training CTAs' rows added in
+// CTA order.  Rows of CTAs that had no tile are not read.
+__global__ void k_guide_reduce(GuideGPU g) {
+  const uint32_t n_all = min(*g.batch_count, (uint32_t)g.batch_cap);
+  const uint32_t rows = min((n_all + 127) / 128, (uint32_t)g.train_ctas);
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < kGuideParams; p += gridDim.x * blockDim.x) {
+    float sum = 0.0f;
+    for (uint32_t r = 0; r < rows; ++r) sum += g.grad_part[(size_t)r * kGuideParams + p];
+    const bool pad = (p >= kOffW4 + kGuideOut * 64 && p < kOffB4) || p >= kOffB4 + kGuideOut;
+    g.grad[p] = pad ? 0.0f : sum;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    float ws = 0.0f;
+    for (uint32_t r = 0; r < rows; ++r) ws += g.wsum_part[r];
+    *g.weight_sum = ws;
+  }
+}
+
+inline void launch_guide_select(const GuideGPU& g, int paths, cudaStream_t s) {
+  const int blocks = (paths + kSelectBlock - 1) / kSelectBlock;
+  k_guide_select_count<<<blocks, kSelectBlock, 0, s>>>(g, paths);
+  k_guide_select_scan<<<1, kSelectScanThreads, 0, s>>>(g, blocks);
+  k_guide_select_write<<<blocks, kSelectBlock, 0, s>>>(g, paths);
 }
 
 }  // namespace
@@ -303,23 +388,27 @@ int guide_train_smem() { return kTrainSmem; }
 
 // One sample selection, then g.steps Adam steps on the same samples (each a
 // gradient pass with the current weights).  Returns the kernels launched.
-int launch_guide_train(const GuideGPU& g, int paths, int sms, cudaStream_t s) {
-  k_guide_select<<<(paths + 255) / 256, 256, 0, s>>>(g, paths);
+int launch_guide_train(const GuideGPU& g, int paths, cudaStream_t s) {
+  launch_guide_select(g, paths, s);
   for (int k = 0; k < g.steps; ++k) {
-    k_guide_train<<<std::max(1, sms), 128, kTrainSmem, s>>>(g);
+    k_guide_train<<<g.train_ctas, 128, kTrainSmem, s>>>(g);
+    k_guide_reduce<<<(kGuideParams + 255) / 256, 256, 0, s>>>(g);
     k_guide_adam<<<(kGuideParams + 255) / 256, 256, 0, s>>>(g);
     k_guide_prepare<<<16, 256, 0, s>>>(g);
     k_guide_step_done<<<1, 1, 0, s>>>(g, k == g.steps - 1);
   }
-  return 1 + 4 * g.steps;
+  return 3 + 5 * g.steps;
 }
 
 void launch_guide_prepare(const GuideGPU& g, cudaStream_t s) { k_guide_prepare<<<16, 256, 0, s>>>(g); }
 
-void launch_guide_gradients(const GuideGPU& g, int paths, int sms, cudaStream_t s) {
-  k_guide_select<<<(paths + 255) / 256, 256, 0, s>>>(g, paths);
-  k_guide_train<<<std::max(1, sms), 128, kTrainSmem, s>>>(g);
+void launch_guide_gradients(const GuideGPU& g, int paths, cudaStream_t s) {
+  launch_guide_select(g, paths, s);
+  k_guide_train<<<g.train_ctas, 128, kTrainSmem, s>>>(g);
+  k_guide_reduce<<<(kGuideParams + 255) / 256, 256, 0, s>>>(g);
 }
+
+int guide_select_blocks(int paths) { return (paths + kSelectBlock - 1) / kSelectBlock; }
 
 int guide_configure() {
   return cudaFuncSetAttribute(k_guide_train, cudaFuncAttributeMaxDynamicSharedMemorySize, kTrainSmem) == cudaSuccess

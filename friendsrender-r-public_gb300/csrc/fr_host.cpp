@@ -580,7 +580,7 @@ int enqueue_iteration(fr_ctx* c) {
   }
   if (c->guided) {
     // select, then per Adam step: train, Adam, weight tiles, step bookkeeping
-    c->launches += launch_guide_train(c->guide, c->P, c->sms, s);
+    c->launches += launch_guide_train(c->guide, c->P, s);
   }
   // iteration counter, eye pass (start, rounds of trace/sort/shade, tail),
   // photon emission and tail, grid setup, count, scatter, gather
@@ -628,6 +628,8 @@ int check_device_error(fr_ctx* c) {
   FR_CUDA(cudaStreamSynchronize(c->stream));
   if (e & kErrStack) return fail(FR_ERR_DEVICE, "BVH traversal stack overflow (depth %d)", c->bvh_depth);
   if (e & kErrGuide) return fail(FR_ERR_DEVICE, "photon guide: a tensor-core wait gave up");
+  if (e & kErrQuery) return fail(FR_ERR_INVALID, "radius query: a ball was refused (radius not finite, or more "
+                                                 "than %d cells along an axis)", kMaxQuerySpan);
   if (e) return fail(FR_ERR_DEVICE, "device error word %d", e);
   return FR_OK;
 }
@@ -878,12 +880,16 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
     g.batch_cap = std::min(c->P, params->guide_batch > 0 ? params->guide_batch : 16384);
     g.lr = params->guide_learning_rate > 0.0f ? params->guide_learning_rate : 0.005f;
     g.steps = params->guide_steps > 0 ? std::min(params->guide_steps, 64) : 16;
+    g.train_ctas = std::max(1, c->sms);
     if ((rc = c->alloc(&g.params, kGuideParams)) || (rc = c->alloc(&g.grad, kGuideParams)) ||
         (rc = c->alloc(&g.adam_m, kGuideParams)) || (rc = c->alloc(&g.adam_v, kGuideParams)) ||
         (rc = c->alloc(&g.tiles, kTileBytes)) || (rc = c->alloc(&g.feat, (size_t)c->P)) ||
-        (rc = c->alloc(&g.dir, (size_t)c->P)) || (rc = c->alloc(&g.importance, (size_t)c->P)) ||
-        (rc = c->alloc(&g.batch, (size_t)g.batch_cap)) || (rc = c->alloc(&g.batch_count, 1)) ||
-        (rc = c->alloc(&g.weight_sum, 1)) || (rc = c->alloc(&g.adam_step, 1)))
+        (rc = c->alloc(&g.dir, (size_t)c->P)) || (rc = c->alloc(&g.importance, 2 * (size_t)c->P)) ||
+        (rc = c->alloc(&g.batch, (size_t)g.batch_cap)) || (rc = c->alloc(&g.batch_w, (size_t)g.batch_cap)) ||
+        (rc = c->alloc(&g.batch_count, 1)) || (rc = c->alloc(&g.select_part, (size_t)guide_select_blocks(c->P))) ||
+        (rc = c->alloc(&g.grad_part, (size_t)g.train_ctas * kGuideParams)) ||
+        (rc = c->alloc(&g.wsum_part, (size_t)g.train_ctas)) || (rc = c->alloc(&g.weight_sum, 1)) ||
+        (rc = c->alloc(&g.adam_step, 1)))
       return bail(rc);
     g.err = c->err;
     if (guide_configure()) return bail(fail(FR_ERR_CUDA, "guide: shared-memory opt-in failed"));
@@ -894,7 +900,7 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
     FR_CUDA(cudaMemsetAsync(g.batch_count, 0, 4, c->stream));
     FR_CUDA(cudaMemsetAsync(g.weight_sum, 0, 4, c->stream));
     FR_CUDA(cudaMemsetAsync(g.adam_step, 0, 4, c->stream));
-    FR_CUDA(cudaMemsetAsync(g.importance, 0, sizeof(float) * (size_t)c->P, c->stream));
+    FR_CUDA(cudaMemsetAsync(g.importance, 0, 2 * sizeof(unsigned long long) * (size_t)c->P, c->stream));
     launch_guide_prepare(g, c->stream);
     c->guided = true;
   }
@@ -1157,7 +1163,7 @@ int fr_trace_any(fr_ctx* c, const float* rays, int32_t n, int32_t* hit) {
 int fr_radius_query(fr_ctx* c, const float* hp, int32_t nh, const float* photons_xyz, int32_t np, float cell,
                     int32_t* counts, uint32_t* pairs, uint32_t pair_capacity, uint32_t* pair_count) {
   if (!c || nh < 0 || np < 0 || (nh && (!hp || !counts)) || (np && !photons_xyz) || !(cell > 0.0f) ||
-      (pairs && !pair_count))
+      !(cell <= 3.0e38f) || (pairs && !pair_count))
     return fail(FR_ERR_INVALID, "fr_radius_query: bad arguments");
   if (!nh) return FR_OK;
   if (!np) {
@@ -1182,6 +1188,14 @@ int fr_radius_query(fr_ctx* c, const float* hp, int32_t nh, const float* photons
   gi.cell = cell;
   gi.inv_cell = 1.0f / cell;
   for (int a = 0; a < 3; ++a) gi.origin[a] = lo[a] - cell;
+  // The kernel refuses the same balls (count -1); refusing them here keeps
+  // the device error word clear.
+  for (int i = 0; i < nh; ++i)
+    if (!query_ball_ok(hp[4 * i], hp[4 * i + 1], hp[4 * i + 2], hp[4 * i + 3], gi.origin, gi.inv_cell))
+      return fail(FR_ERR_INVALID,
+                  "fr_radius_query: hitpoint %d: radius %g is not finite or spans more than %d cells of %g along "
+                  "an axis",
+                  i, (double)hp[4 * i + 3], kMaxQuerySpan, (double)cell);
   ScanTemp st{};
   const uint32_t words = scan_temp_words(g.table + 1, st);
   std::vector<void*> tmp;
@@ -1227,7 +1241,7 @@ int fr_radius_query(fr_ctx* c, const float* hp, int32_t nh, const float* photons
     launch_photon_count(ph, d_ones, np, 1, g, d_gi, s);
     launch_scan(g.cell_count, g.cell_start, g.table + 1, st, s);
     launch_photon_scatter(ph, d_ones, np, 1, g, s);
-    launch_radius_count(d_hp, nh, g, d_gi, d_m, d_pairs, pair_capacity, d_pc, s);
+    launch_radius_count(d_hp, nh, g, d_gi, d_m, d_pairs, pair_capacity, d_pc, c->err, s);
     cudaMemcpyAsync(counts, d_m, 4 * (size_t)nh, cudaMemcpyDeviceToHost, s);
     if (pairs) {
       uint32_t total = 0;
@@ -1380,9 +1394,13 @@ int fr_guide_set_params(fr_ctx* c, const float* params) {
 
 int fr_read_guide_importance(fr_ctx* c, float* importance) {
   if (!c || !importance || !c->guided) return fail(FR_ERR_INVALID, "fr_read_guide_importance: no guide");
-  FR_CUDA(cudaMemcpyAsync(importance, c->guide.importance, sizeof(float) * (size_t)c->P, cudaMemcpyDeviceToHost,
-                          c->stream));
-  return fr_synchronize(c);
+  std::vector<unsigned long long> fx(2 * (size_t)c->P);
+  FR_CUDA(cudaMemcpyAsync(fx.data(), c->guide.importance, sizeof(unsigned long long) * fx.size(),
+                          cudaMemcpyDeviceToHost, c->stream));
+  const int rc = fr_synchronize(c);
+  if (rc) return rc;
+  for (size_t i = 0; i < (size_t)c->P; ++i) importance[i] = importance_value(fx[2 * i], fx[2 * i + 1]);
+  return FR_OK;
 }
 
 int fr_guide_gradient(fr_ctx* c, int32_t n, const float* samples, float* grad, float* weight_sum) {
@@ -1390,30 +1408,31 @@ int fr_guide_gradient(fr_ctx* c, int32_t n, const float* samples, float* grad, f
     return fail(FR_ERR_INVALID, "fr_guide_gradient: bad arguments");
   const GuideGPU& g = c->guide;
   std::vector<float4> f(n), d(n);
-  std::vector<float> imp(c->P, 0.0f);
+  std::vector<unsigned long long> imp(2 * (size_t)c->P, 0ull);
   for (int j = 0; j < n; ++j) {
     const float* x = samples + 9 * (size_t)j;
     f[j] = make_float4(x[0], x[1], x[2], x[3]);
     d[j] = make_float4(x[4], x[5], x[6], x[7]);
-    imp[j] = x[8];
+    importance_split(x[8], &imp[2 * (size_t)j], &imp[2 * (size_t)j + 1]);
   }
   FR_CUDA(cudaStreamSynchronize(c->stream));
   if (n) {
     FR_CUDA(cudaMemcpyAsync(g.feat, f.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, c->stream));
     FR_CUDA(cudaMemcpyAsync(g.dir, d.data(), sizeof(float4) * n, cudaMemcpyHostToDevice, c->stream));
   }
-  FR_CUDA(cudaMemcpyAsync(g.importance, imp.data(), sizeof(float) * c->P, cudaMemcpyHostToDevice, c->stream));
+  FR_CUDA(cudaMemcpyAsync(g.importance, imp.data(), sizeof(unsigned long long) * imp.size(), cudaMemcpyHostToDevice,
+                          c->stream));
   FR_CUDA(cudaMemsetAsync(g.grad, 0, sizeof(float) * kGuideParams, c->stream));
   FR_CUDA(cudaMemsetAsync(g.weight_sum, 0, 4, c->stream));
   FR_CUDA(cudaMemsetAsync(g.batch_count, 0, 4, c->stream));
-  launch_guide_gradients(g, c->P, c->sms, c->stream);
+  launch_guide_gradients(g, c->P, c->stream);
   FR_CUDA(cudaMemcpyAsync(grad, g.grad, sizeof(float) * kGuideParams, cudaMemcpyDeviceToHost, c->stream));
   FR_CUDA(cudaMemcpyAsync(weight_sum, g.weight_sum, 4, cudaMemcpyDeviceToHost, c->stream));
   int rc = fr_synchronize(c);
   FR_CUDA(cudaMemsetAsync(g.grad, 0, sizeof(float) * kGuideParams, c->stream));
   FR_CUDA(cudaMemsetAsync(g.weight_sum, 0, 4, c->stream));
   FR_CUDA(cudaMemsetAsync(g.batch_count, 0, 4, c->stream));
-  FR_CUDA(cudaMemsetAsync(g.importance, 0, sizeof(float) * c->P, c->stream));
+  FR_CUDA(cudaMemsetAsync(g.importance, 0, 2 * sizeof(unsigned long long) * c->P, c->stream));
   const int rc2 = fr_synchronize(c);
   return rc ? rc : rc2;
 }

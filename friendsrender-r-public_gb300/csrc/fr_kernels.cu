@@ -922,7 +922,7 @@ __global__ void __launch_bounds__(128) k_pw_emit_guided(SceneGPU sc, IterParams 
   w.queue[0][i] = (uint32_t)i;
   g.feat[i] = make_float4(x[0], x[1], x[2], x[3]);
   g.dir[i] = make_float4(x[4], s.d.x, s.d.y, s.d.z);
-  g.importance[i] = 0.0f;
+  reinterpret_cast<ulonglong2*>(g.importance)[i] = make_ulonglong2(0ull, 0ull);
 }
 
 template <bool kEndDegenerate>
@@ -1160,7 +1160,7 @@ constexpr int kGatherGroup = FR_GATHER_GROUP;
 template <bool kImportance>
 __global__ void __launch_bounds__(256) k_gather(SceneGPU sc, IterParams it, HitpointBuf hp, PhotonGrid g,
                                                const GridInfo* gip, PixelState st, int32_t* dbg_m, float4* dbg_phi,
-                                               float* importance) {
+                                               unsigned long long* importance) {
   constexpr int G = kGatherGroup;
   const unsigned lane = threadIdx.x & 31u;
   const unsigned gl = lane & (G - 1);                        // lane within the group
@@ -1240,7 +1240,13 @@ __global__ void __launch_bounds__(256) k_gather(SceneGPU sc, IterParams it, Hitp
         const FParam p{indir, out, nn, Ii, Io, hn.w, mat.extinction, mat.reflectance};
         const float brdf = surface_brdf(type, p);
         const V3 add = v3(hw.x, hw.y, hw.z) * brdf * v3(f4.x, f4.y, f4.z) / f4.w;
-        if (kImportance) atomicAdd(importance + (__float_as_uint(d4.w) >> 5), add.x + add.y + add.z);
+        if (kImportance) {  // fixed point: the sum is the same in any order
+          unsigned long long hi, lo;
+          importance_split(add.x + add.y + add.z, &hi, &lo);
+          unsigned long long* ip = importance + 2 * (size_t)(__float_as_uint(d4.w) >> 5);
+          if (hi) atomicAdd(ip, hi);
+          if (lo) atomicAdd(ip + 1, lo);
+        }
         float y, t;
         y = add.x - kx; t = sx + y; kx = (t - sx) - y; sx = t;
         y = add.y - ky; t = sy + y; ky = (t - sy) - y; sy = t;
@@ -1380,13 +1386,19 @@ __global__ void k_trace_any(SceneGPU sc, const float* rays, int n, int32_t* hit,
   hit[i] = trace_any(sc, v3(r[0], r[1], r[2]), v3(r[3], r[4], r[5]), r[6], r[7], err) ? 1 : 0;
 }
 
-// hp: xyz position, w radius
+// hp: xyz position, w radius.  A ball query_ball_ok refuses gets the count
+// -1 and sets kErrQuery in *err (when err is given).
 __global__ void k_radius_count(const float4* hp, int nh, PhotonGrid g, const GridInfo* gip, int32_t* m,
-                               uint32_t* pairs, uint32_t cap, uint32_t* pair_count) {
+                               uint32_t* pairs, uint32_t cap, uint32_t* pair_count, int* err) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= nh) return;
   const GridInfo gi = *gip;
   const float4 h = hp[i];
+  if (!query_ball_ok(h.x, h.y, h.z, h.w, gi.origin, gi.inv_cell)) {
+    m[i] = -1;
+    if (err) atomicOr(err, kErrQuery);
+    return;
+  }
   int M = 0;
   for_each_photon_in_ball(g, gi, v3(h.x, h.y, h.z), h.w, [&](uint32_t j, float4) {
     ++M;
@@ -1552,7 +1564,8 @@ int launch_scan(uint32_t* in, uint32_t* out, uint32_t n, ScanTemp& t, cudaStream
 }
 
 void launch_gather_update(const SceneGPU& sc, const IterParams& it, HitpointBuf hp, PhotonGrid g, const GridInfo* gi,
-                          PixelState st, int32_t* dbg_m, float4* dbg_phi, float* importance, int resident_blocks,
+                          PixelState st, int32_t* dbg_m, float4* dbg_phi, unsigned long long* importance,
+                          int resident_blocks,
                           cudaStream_t s) {
   if (importance)
     k_gather<true><<<std::max(1, resident_blocks), 256, 0, s>>>(sc, it, hp, g, gi, st, dbg_m, dbg_phi, importance);
@@ -1594,8 +1607,8 @@ void launch_trace_any(const SceneGPU& sc, const float* rays, int n, int32_t* hit
 }
 
 void launch_radius_count(const float4* hp, int nh, PhotonGrid g, const GridInfo* gi, int32_t* m, uint32_t* pairs,
-                         uint32_t cap, uint32_t* pair_count, cudaStream_t s) {
-  k_radius_count<<<blocks_for(nh, 128), 128, 0, s>>>(hp, nh, g, gi, m, pairs, cap, pair_count);
+                         uint32_t cap, uint32_t* pair_count, int* err, cudaStream_t s) {
+  k_radius_count<<<blocks_for(nh, 128), 128, 0, s>>>(hp, nh, g, gi, m, pairs, cap, pair_count, err);
 }
 
 }  // namespace fr

@@ -162,10 +162,11 @@ void launch_photon_scatter(PhotonSlots ph, const uint32_t* counts, int paths, in
 uint32_t scan_temp_words(uint32_t n, ScanTemp& t);
 // One warp per listed hitpoint; resident_blocks blocks of 256 threads.
 // importance: per-path sums of the flux each path's photons bring to
-// hitpoints (the guide's training signal), or nullptr.
+// hitpoints (the guide's training signal, fixed point: importance_split in
+// fr_guide.h), or nullptr.
 void launch_gather_update(const SceneGPU& sc, const IterParams& it, HitpointBuf hp, PhotonGrid g, const GridInfo* gi,
-                          PixelState st, int32_t* dbg_m, float4* dbg_phi, float* importance, int resident_blocks,
-                          cudaStream_t s);
+                          PixelState st, int32_t* dbg_m, float4* dbg_phi, unsigned long long* importance,
+                          int resident_blocks, cudaStream_t s);
 int gather_blocks_per_sm();
 // ExportPNG's resample and 8-bit quantization of a resolved image.
 void launch_export_rgba8(const float4* img, int width, int height, uint32_t* out, cudaStream_t s);
@@ -178,8 +179,10 @@ void launch_resolve(PixelState st, int pixels, double photons_total, double iter
 void launch_trace_closest(const SceneGPU& sc, const float* rays, int n, int32_t* facet, float* tuv, int* err,
                           cudaStream_t s);
 void launch_trace_any(const SceneGPU& sc, const float* rays, int n, int32_t* hit, int* err, cudaStream_t s);
+// A ball that query_ball_ok refuses gets the count -1 and sets kErrQuery in
+// *err when err is not NULL.
 void launch_radius_count(const float4* hp_pos_r, int nh, PhotonGrid g, const GridInfo* gi, int32_t* m,
-                         uint32_t* pairs, uint32_t pair_cap, uint32_t* pair_count, cudaStream_t s);
+                         uint32_t* pairs, uint32_t pair_cap, uint32_t* pair_count, int* err, cudaStream_t s);
 
 // Radius count with the fixed scratch of fr_noalloc.cu (allocates nothing).
 int radius_count_noalloc(const float* hp_dev, int32_t nh, const float* photons_dev, int32_t np, float cell,
@@ -191,10 +194,11 @@ int guide_configure();  // opts the training kernel into its shared memory
 void launch_pw_emit_guided(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, PathWave w, uint32_t* counts,
                            const GuideGPU& g, cudaStream_t s);
 int guide_train_smem();
-int launch_guide_train(const GuideGPU& g, int paths, int sms, cudaStream_t s);
+int launch_guide_train(const GuideGPU& g, int paths, cudaStream_t s);
 void launch_guide_prepare(const GuideGPU& g, cudaStream_t s);
 // Sample selection and the gradient sums only (no update).
-void launch_guide_gradients(const GuideGPU& g, int paths, int sms, cudaStream_t s);
+void launch_guide_gradients(const GuideGPU& g, int paths, cudaStream_t s);
+int guide_select_blocks(int paths);  // blocks of the sample selection (select_part words)
 std::vector<float> guide_initial_params(uint32_t seed);
 
 // Device check of the tcgen05 GEMM block (fr_tc_check.cu): max |error| of

@@ -153,6 +153,34 @@ constexpr int kTraversalStackEntries = 96;
 
 // Device error word bits.
 constexpr int kErrStack = 1;        // traversal stack overflow
-constexpr int kErrTableFull = 2;    // photon cell table overflow
+constexpr int kErrQuery = 64;       // a radius query ball refused by query_ball_ok
+
+// A radius query visits every grid cell its box (x - R, x + R) overlaps.  A
+// ball that is not finite, or that spans more than kMaxQuerySpan cells along
+// an axis, is refused: its loop over cells would take minutes, or never end
+// once a cell index saturates.  Cell coordinates are bounded by
+// kMaxQueryCellCoord so that the float-to-int conversion is exact.
+constexpr int kMaxQuerySpan = 128;
+constexpr float kMaxQueryCellCoord = 1.0e9f;
+
+#if defined(__CUDACC__)
+#define FR_HOST_DEVICE __host__ __device__
+#else
+#define FR_HOST_DEVICE
+#endif
+
+// The same float operations as the grid's cell_of on the box's corners
+// ((x - R - origin) * inv_cell on each axis, no contraction).
+FR_HOST_DEVICE inline bool query_ball_ok(float x, float y, float z, float R, const float origin[3], float inv_cell) {
+  if (!(R >= 0.0f) || !(R <= 3.0e38f)) return false;  // NaN, negative or infinite radius
+  const float c[3] = {x, y, z};
+  for (int a = 0; a < 3; ++a) {
+    const float f0 = (c[a] - R - origin[a]) * inv_cell;
+    const float f1 = (c[a] + R - origin[a]) * inv_cell;
+    if (!(f0 >= -kMaxQueryCellCoord) || !(f1 <= kMaxQueryCellCoord) || !(f1 - f0 <= (float)kMaxQuerySpan))
+      return false;
+  }
+  return true;
+}
 
 }  // namespace fr

@@ -15,6 +15,7 @@
 // threads) race on the arrays and return wrong counts.
 #include <cuda_runtime.h>
 
+#include <cstdint>
 #include <cstdio>
 #include <mutex>
 
@@ -84,10 +85,20 @@ int na_fail(int code, const char* what, cudaError_t e) {
   return code;
 }
 
-int scratch_for_current_device(Scratch** out) {
-  int dev = 0;
+// The scratch of the current device, which must be the stream's device: the
+// arrays' addresses differ between devices.
+int scratch_for_stream(cudaStream_t stream, Scratch** out) {
+  int dev = 0, stream_dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return na_fail(FR_ERR_CUDA, "cudaGetDevice", e);
+  if ((e = cudaStreamGetDevice(stream, &stream_dev)) != cudaSuccess)
+    return na_fail(FR_ERR_CUDA, "cudaStreamGetDevice", e);
+  if (stream_dev != dev) {
+    std::snprintf(g_na_msg, sizeof(g_na_msg),
+                  "fr_radius_count_noalloc: the stream belongs to device %d but device %d is current", stream_dev,
+                  dev);
+    return FR_ERR_INVALID;
+  }
   if (dev < 0 || dev >= kMaxDevices) {
     std::snprintf(g_na_msg, sizeof(g_na_msg), "fr_radius_count_noalloc: device %d beyond the %d supported",
                   dev, kMaxDevices);
@@ -114,8 +125,13 @@ int radius_count_noalloc(const float* hp_dev, int32_t nh, const float* photons_d
                          int32_t* counts_dev, cudaStream_t stream, const char** msg) {
   g_na_msg[0] = 0;
   *msg = g_na_msg;
-  if (nh < 0 || np < 0 || !(cell > 0.0f) || (nh && (!hp_dev || !counts_dev)) || (np && !photons_dev)) {
+  if (nh < 0 || np < 0 || !(cell > 0.0f) || !(cell <= 3.0e38f) || (nh && (!hp_dev || !counts_dev)) ||
+      (np && !photons_dev)) {
     std::snprintf(g_na_msg, sizeof(g_na_msg), "fr_radius_count_noalloc: bad arguments");
+    return FR_ERR_INVALID;
+  }
+  if (reinterpret_cast<uintptr_t>(hp_dev) % 16 != 0) {  // read as float4
+    std::snprintf(g_na_msg, sizeof(g_na_msg), "fr_radius_count_noalloc: hp_dev is not 16-byte aligned");
     return FR_ERR_INVALID;
   }
   if (np > kNoAllocMaxPhotons) {
@@ -132,7 +148,7 @@ int radius_count_noalloc(const float* hp_dev, int32_t nh, const float* photons_d
     return FR_OK;
   }
   Scratch* s = nullptr;
-  int rc = scratch_for_current_device(&s);
+  int rc = scratch_for_stream(stream, &s);
   if (rc) return rc;
   ScanTemp st{};
   if (scan_temp_words(kNoAllocTable + 1, st) > (uint32_t)kNoAllocScanWords) {
@@ -157,7 +173,7 @@ int radius_count_noalloc(const float* hp_dev, int32_t nh, const float* photons_d
   g.cell_start = s->start;
   g.table = kNoAllocTable;
   launch_radius_count(reinterpret_cast<const float4*>(hp_dev), nh, g, s->grid, counts_dev, nullptr, 0, nullptr,
-                      stream);
+                      nullptr, stream);
   if ((e = cudaGetLastError()) != cudaSuccess) return na_fail(FR_ERR_CUDA, "kernel launch", e);
   return FR_OK;
 }

@@ -336,7 +336,9 @@ int fr_trace_any(fr_ctx* ctx, const float* rays, int32_t n, int32_t* hit);
  * hp[4h..4h+2], radius hp[4h+3]) counts photons p with
  * isIncludePoint(p, x - R, x + R) && |p - x|^2 < R^2 (kdtree.h:78-88,
  * SPPM.cpp:424-432).  If pairs is not NULL it receives up to pair_capacity
- * (hitpoint, photon) index pairs in any order and *pair_count the total. */
+ * (hitpoint, photon) index pairs in any order and *pair_count the total.
+ * A hitpoint whose radius is not finite or negative, or whose ball spans
+ * more than 128 cells of `cell` along an axis, returns FR_ERR_INVALID. */
 int fr_radius_query(fr_ctx* ctx, const float* hp, int32_t num_hitpoints, const float* photons_xyz,
                     int32_t num_photons, float cell, int32_t* counts, uint32_t* pairs, uint32_t pair_capacity,
                     uint32_t* pair_count);
@@ -351,6 +353,11 @@ int fr_radius_query(fr_ctx* ctx, const float* hp, int32_t num_hitpoints, const f
  * num_hitpoints x {x, y, z, R} floats, photons_dev num_photons x {x, y, z}
  * floats, counts_dev receives num_hitpoints counts; the work is enqueued on
  * `stream` (a cudaStream_t, NULL for the default stream) and not waited for.
+ * hp_dev must be 16-byte aligned (FR_ERR_INVALID otherwise), and the current
+ * device must be the stream's device.  The grid's origin is 0: a hitpoint
+ * whose radius is not finite, or whose ball spans more than 128 cells along
+ * an axis or lies beyond 1e9 cells from the origin, gets the count -1 (the
+ * host cannot check device inputs without waiting for them).
  * All intermediate buffers are fixed device arrays inside the library, sized
  * for FR_NOALLOC_MAX_PHOTONS photons (about 10.5 MB, held by every GPU that
  * loads the library until exit); more photons return FR_ERR_INVALID.  The

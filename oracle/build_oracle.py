@@ -3,8 +3,8 @@
 * oracle/_build/libfrport.so — the CPU restatement in oracle/port/ (g++,
   OpenMP, no fast-math, no FMA contraction), built on every machine.
 * oracle/_ref/frref — the reference's own SPPM path compiled from its sources
-  by oracle/ref/Makefile; only where those sources exist and on x86-64 (the
-  reference uses AVX intrinsics).
+  by oracle/ref/Makefile; only when FR_REFERENCE_SRC names the reference's
+  SPPM/SPPM directory and on x86-64 (the reference uses AVX intrinsics).
 """
 from __future__ import annotations
 
@@ -16,7 +16,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, '_build')
 PORT_LIB = os.path.join(BUILD, 'libfrport.so')
 PORT_SRC = os.path.join(HERE, 'port', 'sppm_port.cpp')
-REF_SRC = os.environ.get('FR_REFERENCE_SRC', '/root/reference/SPPM/SPPM')
+# The reference's SPPM/SPPM source directory; the reference is built only
+# when this names one.
+REF_SRC = os.environ.get('FR_REFERENCE_SRC', '')
 REF_BIN = os.path.join(HERE, '_ref', 'frref')
 
 
@@ -33,7 +35,7 @@ def build_port(force=False):
 
 
 def build_reference():
-    if not os.path.isdir(REF_SRC) or platform.machine() not in ('x86_64', 'AMD64'):
+    if not REF_SRC or not os.path.isdir(REF_SRC) or platform.machine() not in ('x86_64', 'AMD64'):
         return None
     r = subprocess.run(['make', '-s', '-j8', 'REF=' + REF_SRC], cwd=os.path.join(HERE, 'ref'),
                        capture_output=True, text=True)

@@ -64,3 +64,19 @@ def test_radius_query_empty_inputs():
         assert (counts == 0).all()
         counts, _ = r.radius_query(np.zeros((0, 3)), np.zeros(0), np.zeros((3, 3)), 0.1)
         assert counts.shape == (0,)
+
+
+def test_radius_query_refuses_unbounded_balls():
+    """A radius that is not finite or negative, or a ball more than 128 cells
+    wide, is refused with FR_ERR_INVALID before any kernel runs; the context
+    stays usable."""
+    from frsppm import abi
+    ph = np.random.Generator(np.random.PCG64(5)).uniform(0, 1, (1000, 3)).astype(np.float32)
+    hp = np.full((3, 3), 0.5, np.float32)
+    with abi.Renderer(GOLDEN_SCENES['cornell32'](), 64) as r:
+        for bad in (np.nan, np.inf, -0.01, 3.0):
+            R = np.array([0.05, bad, 0.05], np.float32)
+            with pytest.raises(RuntimeError, match='radius'):
+                r.radius_query(hp, R, ph, 0.02)
+        counts, _ = r.radius_query(hp, np.full(3, 0.05, np.float32), ph, 0.02)
+        assert (counts == [len(j) for j in brute_pairs(hp, np.full(3, 0.05, np.float32), ph)]).all()

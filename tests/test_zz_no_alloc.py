@@ -60,3 +60,37 @@ def test_noalloc_rejects_more_photons_than_its_scratch():
                                      limit + 1, ctypes.c_float(0.1), ctypes.c_void_p(out.data_ptr()), None)
     assert rc == 1  # FR_ERR_INVALID
     assert b'exceed' in lib.fr_last_error()
+
+
+def test_noalloc_marks_unbounded_balls_and_checks_alignment():
+    """Device inputs cannot be checked on the host without waiting for them:
+    a hitpoint whose radius is not finite, or whose ball is more than 128
+    cells wide, gets the count -1 and the others their counts.  A hitpoint
+    pointer that is not 16-byte aligned is refused."""
+    import torch
+    from frsppm import abi
+    lib = abi.load()
+    hp, R, ph = _inputs(23, 1000, 20_000)
+    R[[3, 10, 500]] = [np.nan, np.inf, 10.0]
+    cell = 0.04
+    with abi.Renderer(GOLDEN_SCENES['cornell32'](), 16) as r:
+        ok = np.ones(len(R), bool)
+        ok[[3, 10, 500]] = False
+        want, _ = r.radius_query(hp[ok], R[ok], ph, cell)
+    hp_dev = torch.from_numpy(np.concatenate([hp, R[:, None]], 1)).cuda()
+    ph_dev = torch.from_numpy(ph).cuda()
+    out = torch.zeros(len(R), dtype=torch.int32, device='cuda')
+    stream = torch.cuda.current_stream().cuda_stream
+    rc = lib.fr_radius_count_noalloc(ctypes.c_void_p(hp_dev.data_ptr()), len(R), ctypes.c_void_p(ph_dev.data_ptr()),
+                                     len(ph), ctypes.c_float(cell), ctypes.c_void_p(out.data_ptr()),
+                                     ctypes.c_void_p(stream))
+    assert rc == 0, lib.fr_last_error()
+    torch.cuda.synchronize()
+    got = out.cpu().numpy()
+    assert (got[~ok] == -1).all()
+    np.testing.assert_array_equal(got[ok], want)
+    flat = torch.zeros(4 * 8 + 1, dtype=torch.float32, device='cuda')
+    rc = lib.fr_radius_count_noalloc(ctypes.c_void_p(flat.data_ptr() + 4), 8, ctypes.c_void_p(ph_dev.data_ptr()),
+                                     len(ph), ctypes.c_float(cell), ctypes.c_void_p(out.data_ptr()),
+                                     ctypes.c_void_p(stream))
+    assert rc == 1 and b'aligned' in lib.fr_last_error()
