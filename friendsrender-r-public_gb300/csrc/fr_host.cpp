@@ -816,9 +816,22 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
     }
     if ((rc = c->upload(&d_env, env.data(), env.size()))) return bail(rc);
   }
+  // Watertight mode: the exact v1, v2 of every triangle in leaf order (the
+  // test must see the vertices a neighbouring triangle shares, not v0 + e1).
+  float4* d_v12 = nullptr;
+  if (params->flags & kFlagWatertight) {
+    std::vector<float4> v12(2 * (size_t)T);
+    for (int k = 0; k < T; ++k) {
+      const float* P = scene->positions + 9 * (size_t)bvh.tri_order[k];
+      v12[2 * (size_t)k] = make_float4(P[3], P[4], P[5], 0.0f);
+      v12[2 * (size_t)k + 1] = make_float4(P[6], P[7], P[8], 0.0f);
+    }
+    if ((rc = c->upload(&d_v12, v12.data(), v12.size()))) return bail(rc);
+  }
   c->sc = SceneGPU{d_nodes, d_tris, d_shade, d_mats, d_texs, d_lights, d_emit,
                    (int32_t)bvh.nodes.size(), T, T, (int32_t)lights.size(),
-                   {lo[0], lo[1], lo[2]}, {hi[0], hi[1], hi[2]}, reinterpret_cast<const float*>(d_env), env_w, env_h};
+                   {lo[0], lo[1], lo[2]}, {hi[0], hi[1], hi[2]}, reinterpret_cast<const float*>(d_env), env_w, env_h,
+                   reinterpret_cast<const float*>(d_v12), d_v12 ? 1 : 0, 0};
 
   // ---- per-iteration buffers (all allocated here; iterations allocate nothing)
   const size_t npix = (size_t)c->W * c->H;

@@ -348,6 +348,7 @@ __global__ void __launch_bounds__(128) k_ew_start(CameraGPU cam, IterParams it, 
 
 // Closest hit of every path in queue `round`, for queues of coherent rays
 // (camera rays in pixel order): each warp takes 32 consecutive entries.
+template <bool kWT>
 __global__ void __launch_bounds__(128) k_wave_trace_static(SceneGPU sc, PathWave w, int round, int* err) {
   if (round_skipped(w, round)) return;
   const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
@@ -356,7 +357,7 @@ __global__ void __launch_bounds__(128) k_wave_trace_static(SceneGPU sc, PathWave
     const uint32_t i = q[j];
     const float4 a = w.a[i], b = w.b[i];
     Hit h;
-    if (trace_closest(sc, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), kRayOffset, h, err))
+    if (trace_closest<kWT>(sc, v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), kRayOffset, h, err))
       w.hit[i] = make_float4(h.u, h.v, __int_as_float(h.tri), __int_as_float(h.facet));
     else
       w.hit[i] = make_float4(0.f, 0.f, __int_as_float(-1), __int_as_float(-1));
@@ -369,6 +370,7 @@ __global__ void __launch_bounds__(128) k_wave_trace_static(SceneGPU sc, PathWave
 // queue entries 32 at a time with one atomic and hands them to its idle lanes.
 // The traversal is trace_closest's (fr_trace.cuh), one node visit or leaf per
 // loop pass, so the hits are the same.
+template <bool kWT>
 __global__ void __launch_bounds__(128) k_wave_trace(SceneGPU sc, PathWave w, int round, int* err) {
   if (round_skipped(w, round)) return;
   const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
@@ -455,7 +457,7 @@ __global__ void __launch_bounds__(128) k_wave_trace(SceneGPU sc, PathWave w, int
         for (int k = 0; k < count; ++k) {
           const TriGPU tr = load_tri(sc.tris, first + k);
           float t, u, v;
-          if (intersect_triangle(org, dir, tr, t, u, v) && t > kRayOffset) {
+          if (tri_test<kWT>(sc, org, dir, tr, first + k, t, u, v) && t > kRayOffset) {
             const int32_t facet = __float_as_int(tr.v0[3]);
             if (t < tbest || (t == tbest && facet > best_facet)) {
               tbest = t; bu = u; bv = v; best_tri = first + k; best_facet = facet;
@@ -566,7 +568,7 @@ __global__ void __launch_bounds__(128) k_ew_shade(SceneGPU sc, IterParams it, fl
 }
 
 // Eye paths alive after the last wavefront round, each run to its end.
-template <bool kEndDegenerate>
+template <bool kEndDegenerate, bool kWT>
 __global__ void __launch_bounds__(128) k_ew_tail(SceneGPU sc, IterParams it, float rr5, float rr6, PathWave w,
                                                  HitpointBuf hp, PixelState st, GridInfo* gi, int rounds, int* err) {
   const int round = tail_round(w, rounds);
@@ -585,7 +587,7 @@ __global__ void __launch_bounds__(128) k_ew_tail(SceneGPU sc, IterParams it, flo
       rng.seek(s.draw);
       while (true) {
         Hit h;
-        if (!trace_closest(sc, s.o, s.d, kRayOffset, h, err)) {
+        if (!trace_closest<kWT>(sc, s.o, s.d, kRayOffset, h, err)) {
           hit_type = eye_miss(sc, hp, st, i, s);
           break;
         }
@@ -775,6 +777,14 @@ __device__ __forceinline__ bool photon_shade(const SceneGPU& sc, const IterParam
   if (kEndDegenerate && !(brdf >= kLt1e8 && pdf > 0.0f)) return false;  // as in eye_shade
   s.thr = s.thr * (g.albedo * cs * brdf);
   s.PDF *= pdf;
+  // The path's weight is kept as two running products (flux and PDF) that
+  // grow together bounce by bounce: sharp glass lobes multiply both by ~1e3,
+  // so a long path inside a cluster of rough dielectrics overflows both to
+  // infinity and its photons then carry inf / inf.  Such a path ends here.
+  if (kEndDegenerate) {
+    const V3 f = s.flux0 * s.thr;
+    if (!(isfinite(s.PDF) && isfinite(f.x) && isfinite(f.y) && isfinite(f.z))) return false;
+  }
   s.o = nxt_o; s.d = nd; s.ix = nix;
   ++s.depth;
   return true;
@@ -971,7 +981,7 @@ __device__ __forceinline__ uint32_t tail_paths_per_warp(uint32_t n, uint32_t nwa
   return ppw;
 }
 
-template <bool kEndDegenerate>
+template <bool kEndDegenerate, bool kWT>
 __global__ void __launch_bounds__(128) k_pw_tail(SceneGPU sc, IterParams it, PhotonSlots ph, PathWave w,
                                                  uint32_t* counts, int rounds, int* err) {
   const int round = tail_round(w, rounds);
@@ -988,7 +998,7 @@ __global__ void __launch_bounds__(128) k_pw_tail(SceneGPU sc, IterParams it, Pho
     load_state(w, i, s);
     while (true) {
       Hit h;
-      if (!trace_closest(sc, s.o, s.d, kRayOffset, h, err)) break;
+      if (!trace_closest<kWT>(sc, s.o, s.d, kRayOffset, h, err)) break;
       if (!photon_shade<kEndDegenerate>(sc, it, ph, i, s, h) || !photon_top(s)) break;
     }
     photon_finish(it, ph, counts, i, s.k);
@@ -1364,12 +1374,13 @@ __global__ void k_resolve(PixelState st, int pixels, double photons_total, doubl
 }
 
 // ------------------------------------------------------------ parity kernels
+template <bool kWT>
 __global__ void k_trace_closest(SceneGPU sc, const float* rays, int n, int32_t* facet, float* tuv, int* err) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float* r = rays + 7 * (size_t)i;
   Hit h;
-  if (trace_closest(sc, v3(r[0], r[1], r[2]), v3(r[3], r[4], r[5]), kRayOffset, h, err)) {
+  if (trace_closest<kWT>(sc, v3(r[0], r[1], r[2]), v3(r[3], r[4], r[5]), kRayOffset, h, err)) {
     facet[i] = h.facet;
     tuv[3 * i] = h.t; tuv[3 * i + 1] = h.u; tuv[3 * i + 2] = h.v;
   } else {
@@ -1379,11 +1390,12 @@ __global__ void k_trace_closest(SceneGPU sc, const float* rays, int n, int32_t* 
 }
 
 // rays: N x 8 {org, dir, minT, maxT}
+template <bool kWT>
 __global__ void k_trace_any(SceneGPU sc, const float* rays, int n, int32_t* hit, int* err) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float* r = rays + 8 * (size_t)i;
-  hit[i] = trace_any(sc, v3(r[0], r[1], r[2]), v3(r[3], r[4], r[5]), r[6], r[7], err) ? 1 : 0;
+  hit[i] = trace_any<kWT>(sc, v3(r[0], r[1], r[2]), v3(r[3], r[4], r[5]), r[6], r[7], err) ? 1 : 0;
 }
 
 // hp: xyz position, w radius.  A ball query_ball_ok refuses gets the count
@@ -1427,7 +1439,7 @@ void launch_next_step(uint32_t* step, cudaStream_t s) { k_next_step<<<1, 1, 0, s
 
 int pw_tail_blocks_per_sm() {
   int b = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pw_tail<false>, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_pw_tail<false, false>, 128, 0);
   return b;
 }
 
@@ -1436,10 +1448,14 @@ void launch_ew_start(const CameraGPU& cam, const IterParams& it, PathWave w, cud
 }
 
 void launch_wave_trace(const SceneGPU& sc, PathWave w, int round, int grid, bool coherent, int* err, cudaStream_t s) {
-  if (coherent)
-    k_wave_trace_static<<<std::max(1, grid), 128, 0, s>>>(sc, w, round, err);
-  else
-    k_wave_trace<<<std::max(1, grid), 128, 0, s>>>(sc, w, round, err);
+  const unsigned g = (unsigned)std::max(1, grid);
+  if (coherent) {
+    if (sc.watertight) k_wave_trace_static<true><<<g, 128, 0, s>>>(sc, w, round, err);
+    else k_wave_trace_static<false><<<g, 128, 0, s>>>(sc, w, round, err);
+  } else {
+    if (sc.watertight) k_wave_trace<true><<<g, 128, 0, s>>>(sc, w, round, err);
+    else k_wave_trace<false><<<g, 128, 0, s>>>(sc, w, round, err);
+  }
 }
 
 // Sets the condition of the graph IF node holding wavefront round `round`:
@@ -1470,10 +1486,15 @@ void launch_ew_shade(const SceneGPU& sc, const IterParams& it, const float* rr_e
 
 void launch_ew_tail(const SceneGPU& sc, const IterParams& it, const float* rr_eye, PathWave w, HitpointBuf hp,
                     PixelState st, GridInfo* gi, int round, int grid, int* err, cudaStream_t s) {
-  if (it.flags & kFlagEndDegenerate)
-    k_ew_tail<true><<<std::max(1, grid), 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, round, err);
-  else
-    k_ew_tail<false><<<std::max(1, grid), 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, round, err);
+  const unsigned g = (unsigned)std::max(1, grid);
+  const bool end = (it.flags & kFlagEndDegenerate) != 0;
+  if (sc.watertight) {
+    if (end) k_ew_tail<true, true><<<g, 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, round, err);
+    else k_ew_tail<false, true><<<g, 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, round, err);
+  } else {
+    if (end) k_ew_tail<true, false><<<g, 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, round, err);
+    else k_ew_tail<false, false><<<g, 128, 0, s>>>(sc, it, rr_eye[0], rr_eye[1], w, hp, st, gi, round, err);
+  }
 }
 
 void launch_pw_emit(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, PathWave w, uint32_t* counts,
@@ -1491,15 +1512,20 @@ void launch_pw_shade(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, P
 
 void launch_pw_tail(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, PathWave w, uint32_t* counts,
                     int round, int grid, int* err, cudaStream_t s) {
-  if (it.flags & kFlagEndDegenerate)
-    k_pw_tail<true><<<std::max(1, grid), 128, 0, s>>>(sc, it, ph, w, counts, round, err);
-  else
-    k_pw_tail<false><<<std::max(1, grid), 128, 0, s>>>(sc, it, ph, w, counts, round, err);
+  const unsigned g = (unsigned)std::max(1, grid);
+  const bool end = (it.flags & kFlagEndDegenerate) != 0;
+  if (sc.watertight) {
+    if (end) k_pw_tail<true, true><<<g, 128, 0, s>>>(sc, it, ph, w, counts, round, err);
+    else k_pw_tail<false, true><<<g, 128, 0, s>>>(sc, it, ph, w, counts, round, err);
+  } else {
+    if (end) k_pw_tail<true, false><<<g, 128, 0, s>>>(sc, it, ph, w, counts, round, err);
+    else k_pw_tail<false, false><<<g, 128, 0, s>>>(sc, it, ph, w, counts, round, err);
+  }
 }
 
 int photon_pass_blocks_per_sm() {
   int b = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wave_trace, 128, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, k_wave_trace<false>, 128, 0);
   return b;
 }
 
@@ -1599,11 +1625,13 @@ void launch_resolve(PixelState st, int pixels, double photons_total, double iter
 
 void launch_trace_closest(const SceneGPU& sc, const float* rays, int n, int32_t* facet, float* tuv, int* err,
                           cudaStream_t s) {
-  k_trace_closest<<<blocks_for(n, 128), 128, 0, s>>>(sc, rays, n, facet, tuv, err);
+  if (sc.watertight) k_trace_closest<true><<<blocks_for(n, 128), 128, 0, s>>>(sc, rays, n, facet, tuv, err);
+  else k_trace_closest<false><<<blocks_for(n, 128), 128, 0, s>>>(sc, rays, n, facet, tuv, err);
 }
 
 void launch_trace_any(const SceneGPU& sc, const float* rays, int n, int32_t* hit, int* err, cudaStream_t s) {
-  k_trace_any<<<blocks_for(n, 128), 128, 0, s>>>(sc, rays, n, hit, err);
+  if (sc.watertight) k_trace_any<true><<<blocks_for(n, 128), 128, 0, s>>>(sc, rays, n, hit, err);
+  else k_trace_any<false><<<blocks_for(n, 128), 128, 0, s>>>(sc, rays, n, hit, err);
 }
 
 void launch_radius_count(const float4* hp, int nh, PhotonGrid g, const GridInfo* gi, int32_t* m, uint32_t* pairs,

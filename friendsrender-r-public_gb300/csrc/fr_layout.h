@@ -133,6 +133,12 @@ struct SceneGPU {
   float lo[3], hi[3];   // scene bounds
   const float* env;     // environment map: 4 floats per converted texel, 16-byte aligned; or null
   int32_t env_w, env_h;
+  // Watertight mode: per triangle in leaf order 8 floats, the exact vertices
+  // v1 and v2 (xyz, w unused; 16-byte aligned); v0 is TriGPU::v0.  Null in
+  // the reference's mode.
+  const float* tri_v12;
+  int32_t watertight;
+  int32_t pad0;
 };
 
 // Per-iteration parameters read by the kernels.
@@ -147,6 +153,7 @@ struct IterParams {
 constexpr uint32_t kFlagFixStaleSlot = 1u;  // drop the stale photon slot quirk (SPPM.cpp:672)
 constexpr uint32_t kFlagStandardResolve = 2u;  // resolve with tau / (pi R^2 * photons emitted)
 constexpr uint32_t kFlagEndDegenerate = 4u;    // end paths with a NaN BSDF value or pdf, or a zero pdf
+constexpr uint32_t kFlagWatertight = 8u;       // watertight triangle test instead of Moller-Trumbore
 
 // Entries of the per-thread traversal stack (a wide node pushes at most 7).
 constexpr int kTraversalStackEntries = 96;

@@ -40,6 +40,51 @@ __device__ __forceinline__ bool intersect_triangle(const V3 org, const V3 dir, c
   return true;
 }
 
+// Watertight ray-triangle test (Woop, Benthin and Wald, JCGT 2(1), 2013):
+// the vertices are moved into a ray-aligned frame (kz the direction's
+// largest axis, the frame sheared so the ray is its z axis) and the three
+// 2-D edge functions decide; an edge function that is exactly zero in float
+// is evaluated again in double, so an edge shared by two triangles is never
+// missed by both.  No backface culling.  u, v are the weights of p1 and p2
+// (as Moller-Trumbore's), t the distance along dir.  The CPU oracle runs the
+// same float and double operations in the same order.
+__device__ __forceinline__ float axis_of(V3 a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
+
+__device__ __forceinline__ bool intersect_watertight(const V3 org, const V3 dir, const V3 p0, const V3 p1,
+                                                     const V3 p2, float& t, float& u, float& v) {
+  const float adx = fabsf(dir.x), ady = fabsf(dir.y), adz = fabsf(dir.z);
+  const int kz = adx > ady ? (adx > adz ? 0 : 2) : (ady > adz ? 1 : 2);
+  int kx = kz == 2 ? 0 : kz + 1;
+  int ky = kx == 2 ? 0 : kx + 1;
+  const float dz = axis_of(dir, kz);
+  if (dz < 0.0f) {  // keep the winding
+    const int k = kx;
+    kx = ky;
+    ky = k;
+  }
+  const float Sx = axis_of(dir, kx) / dz, Sy = axis_of(dir, ky) / dz, Sz = 1.0f / dz;
+  const V3 A = p0 - org, B = p1 - org, C = p2 - org;
+  const float Az0 = axis_of(A, kz), Bz0 = axis_of(B, kz), Cz0 = axis_of(C, kz);
+  const float Ax = axis_of(A, kx) - Sx * Az0, Ay = axis_of(A, ky) - Sy * Az0;
+  const float Bx = axis_of(B, kx) - Sx * Bz0, By = axis_of(B, ky) - Sy * Bz0;
+  const float Cx = axis_of(C, kx) - Sx * Cz0, Cy = axis_of(C, ky) - Sy * Cz0;
+  float U = Cx * By - Cy * Bx, V = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
+  if (U == 0.0f || V == 0.0f || W == 0.0f) {
+    U = (float)((double)Cx * (double)By - (double)Cy * (double)Bx);
+    V = (float)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+    W = (float)((double)Bx * (double)Ay - (double)By * (double)Ax);
+  }
+  if ((U < 0.0f || V < 0.0f || W < 0.0f) && (U > 0.0f || V > 0.0f || W > 0.0f)) return false;
+  const float det = U + V + W;
+  if (det == 0.0f) return false;
+  const float T = U * (Sz * Az0) + V * (Sz * Bz0) + W * (Sz * Cz0);
+  const float rcp = 1.0f / det;
+  t = T * rcp;
+  u = V * rcp;
+  v = W * rcp;
+  return true;
+}
+
 __device__ __forceinline__ TriGPU load_tri(const TriGPU* tris, int i) {
   const float4* p = reinterpret_cast<const float4*>(tris + i);
   const float4 a = __ldg(p), b = __ldg(p + 1), c = __ldg(p + 2);
@@ -48,6 +93,22 @@ __device__ __forceinline__ TriGPU load_tri(const TriGPU* tris, int i) {
   t.e1[0] = b.x; t.e1[1] = b.y; t.e1[2] = b.z; t.e1[3] = b.w;
   t.e2[0] = c.x; t.e2[1] = c.y; t.e2[2] = c.z; t.e2[3] = c.w;
   return t;
+}
+
+// The scene's triangle test for triangle slot i (already loaded as tr): the
+// reference's Moller-Trumbore, or (kWT, a scene with FR_FLAG_WATERTIGHT) the
+// watertight test on the exact vertices.  The traversal kernels are
+// instantiated for both, so the reference's mode keeps its registers.
+template <bool kWT>
+__device__ __forceinline__ bool tri_test(const SceneGPU& sc, const V3 org, const V3 dir, const TriGPU& tr, int i,
+                                         float& t, float& u, float& v) {
+  if constexpr (!kWT) {
+    return intersect_triangle(org, dir, tr, t, u, v);
+  } else {
+    const float4* q = reinterpret_cast<const float4*>(sc.tri_v12) + 2 * (size_t)i;
+    const float4 a = __ldg(q), b = __ldg(q + 1);
+    return intersect_watertight(org, dir, v3(tr.v0), v3(a.x, a.y, a.z), v3(b.x, b.y, b.z), t, u, v);
+  }
 }
 
 struct RayPre {
@@ -134,6 +195,7 @@ __device__ __forceinline__ RayPre ray_pre(V3 org, V3 dir) {
 }
 
 // Closest hit on (tmin, +inf).  Returns false on a miss; sets *err on stack overflow.
+template <bool kWT>
 __device__ bool trace_closest(const SceneGPU& sc, V3 org, V3 dir, float tmin, Hit& hit, int* err) {
   const RayPre r = ray_pre(org, dir);
   float tbest = FLT_MAX;
@@ -171,7 +233,7 @@ __device__ bool trace_closest(const SceneGPU& sc, V3 org, V3 dir, float tmin, Hi
         for (int k = 0; k < count; ++k) {
           const TriGPU tr = load_tri(sc.tris, first + k);
           float t, u, v;
-          if (intersect_triangle(org, dir, tr, t, u, v) && t > tmin) {
+          if (tri_test<kWT>(sc, org, dir, tr, first + k, t, u, v) && t > tmin) {
             const int32_t facet = __float_as_int(tr.v0[3]);
             if (t < tbest || (t == tbest && facet > best_facet)) {
               tbest = t; bu = u; bv = v; best_tri = first + k; best_facet = facet;
@@ -191,6 +253,7 @@ __device__ bool trace_closest(const SceneGPU& sc, V3 org, V3 dir, float tmin, Hi
 }
 
 // Any hit with t in (tmin, tmax] (findAnyElement, bvh8.h:643-707).
+template <bool kWT>
 __device__ bool trace_any(const SceneGPU& sc, V3 org, V3 dir, float tmin, float tmax, int* err) {
   const RayPre r = ray_pre(org, dir);
   uint32_t stack[kTraversalStack];
@@ -216,7 +279,7 @@ __device__ bool trace_any(const SceneGPU& sc, V3 org, V3 dir, float tmin, float 
       for (int k = 0; k < count; ++k) {
         const TriGPU tr = load_tri(sc.tris, first + k);
         float t, u, v;
-        if (intersect_triangle(org, dir, tr, t, u, v) && tmax >= t && t > tmin) return true;
+        if (tri_test<kWT>(sc, org, dir, tr, first + k, t, u, v) && tmax >= t && t > tmin) return true;
       }
     }
     if (sp == 0) return false;

@@ -126,9 +126,20 @@ enum {
    * value below 1e-8 or a negative pdf (SPPM.cpp:278-281, 648-651) and goes
    * on with the others, whose hitpoints then carry a NaN or infinite weight
    * (its rough-dielectric BSDF returns NaN for a few rare directions), so a
-   * pixel turns NaN once a photon lands at such a hitpoint.  Off by default
-   * (the reference's hitpoints and photons). */
-  FR_FLAG_END_DEGENERATE_PATHS = 4u
+   * pixel turns NaN once a photon lands at such a hitpoint.  Also ends a
+   * photon path whose flux or PDF product is no longer finite (both grow
+   * bounce by bounce; long paths among sharp rough dielectrics overflow both,
+   * and their photons then carry inf / inf).  Off by default (the reference's
+   * hitpoints and photons). */
+  FR_FLAG_END_DEGENERATE_PATHS = 4u,
+  /* Watertight ray-triangle test (Woop, Benthin and Wald, "Watertight
+   * Ray/Triangle Intersection", JCGT 2(1), 2013) in place of the reference's
+   * Moller-Trumbore (Intersect.cpp:67-89): a ray that crosses an edge or a
+   * vertex shared by triangles of a closed mesh meets at least one of them,
+   * where Moller-Trumbore's rounding can let it pass between them.  Same
+   * acceptance rule (t > 1e-4, nearest t, equal t to the larger facet index)
+   * and the same (u, v) meaning.  Off by default (the reference's test). */
+  FR_FLAG_WATERTIGHT = 8u
 };
 
 typedef struct fr_sppm_params {

@@ -1,7 +1,9 @@
 """ORACLE build recipe (test infrastructure only).
 
 * oracle/_build/libfrport.so — the CPU restatement in oracle/port/ (g++,
-  OpenMP, no fast-math, no FMA contraction), built on every machine.
+  OpenMP, no fast-math, no FMA contraction), built on every machine; beside
+  it libfrport64.so (the FP64 oracle) and libfrport_timing.so (the CPU
+  baseline's build).
 * oracle/_ref/frref — the reference's own SPPM path compiled from its sources
   by oracle/ref/Makefile; only when FR_REFERENCE_SRC names the reference's
   SPPM/SPPM directory and on x86-64 (the reference uses AVX intrinsics).
@@ -22,16 +24,30 @@ REF_SRC = os.environ.get('FR_REFERENCE_SRC', '')
 REF_BIN = os.path.join(HERE, '_ref', 'frref')
 
 
-def build_port(force=False):
+# Builds of the restatement: the parity build (the reference's float
+# arithmetic exactly: no fast-math, no FMA contraction), the FP64 oracle (the
+# same source with FR_PORT_REAL=double) and the timing build for the CPU
+# baseline, with the reference's own optimisation flags (SPPM/SPPM/makefile:
+# -O2 -ffast-math -Ofast -fopenmp; its -mavx is x86-only and left out, so
+# the same build runs on the Arm host).
+PORT_BUILDS = {
+    'f32': (PORT_LIB, ['-O2', '-fno-fast-math', '-ffp-contract=off']),
+    'f64': (os.path.join(BUILD, 'libfrport64.so'), ['-O2', '-fno-fast-math', '-ffp-contract=off',
+                                                     '-DFR_PORT_REAL=double']),
+    'timing': (os.path.join(BUILD, 'libfrport_timing.so'), ['-O2', '-ffast-math', '-Ofast']),
+}
+
+
+def build_port(kind='f32', force=False):
     os.makedirs(BUILD, exist_ok=True)
-    if not force and os.path.exists(PORT_LIB) and os.path.getmtime(PORT_LIB) >= os.path.getmtime(PORT_SRC):
-        return PORT_LIB
-    cmd = ['g++', '-O2', '-std=c++17', '-fopenmp', '-fPIC', '-shared', '-fno-fast-math', '-ffp-contract=off',
-           PORT_SRC, '-o', PORT_LIB]
+    lib, flags = PORT_BUILDS[kind]
+    if not force and os.path.exists(lib) and os.path.getmtime(lib) >= os.path.getmtime(PORT_SRC):
+        return lib
+    cmd = ['g++', '-std=c++17', '-fopenmp', '-fPIC', '-shared'] + flags + [PORT_SRC, '-o', lib]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError('oracle port build failed:\n' + r.stdout + r.stderr)
-    return PORT_LIB
+    return lib
 
 
 def build_reference():
@@ -45,7 +61,9 @@ def build_reference():
 
 
 def build_all():
-    build_port()
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(len(PORT_BUILDS)) as ex:
+        list(ex.map(build_port, PORT_BUILDS))
     build_reference()
 
 

@@ -30,18 +30,27 @@
 
 namespace port {
 
-constexpr float PI = 3.14159f;           // Vec.h:10
-constexpr float RAY_OFFSET = 1e-4f;      // Primitive.h:31
-constexpr float sMin = 1e-16f;           // Sampling.h:8
+// The arithmetic type of the restatement.  float (the default) is the
+// reference's arithmetic, bit for bit; FR_PORT_REAL=double builds the FP64
+// oracle: the same estimator with every float evaluated in double (the
+// random draws, the reference's constants and the scene data are the same).
+#ifndef FR_PORT_REAL
+#define FR_PORT_REAL float
+#endif
+using Real = FR_PORT_REAL;
+
+constexpr Real PI = 3.14159f;           // Vec.h:10
+constexpr Real RAY_OFFSET = 1e-4f;      // Primitive.h:31
+constexpr Real sMin = 1e-16f;           // Sampling.h:8
 constexpr int NUM_SAMPLE = 1000;         // LightSampler.h:17
 constexpr int SLOTS = 32;                // SPPM.cpp:753
 
 // ------------------------------------------------------------------ Vec3
 struct V {
-  float x = 0, y = 0, z = 0;
+  Real x = 0, y = 0, z = 0;
   V() = default;
-  V(float a, float b, float c) : x(a), y(b), z(c) {}
-  float operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
+  V(Real a, Real b, Real c) : x(a), y(b), z(c) {}
+  Real operator[](int i) const { return i == 0 ? x : (i == 1 ? y : z); }
 };
 // Vec.h:179-243, 303-323
 inline V operator+(V a, V b) { return V(a.x + b.x, a.y + b.y, a.z + b.z); }
@@ -49,24 +58,27 @@ inline V operator-(V a, V b) { return V(a.x - b.x, a.y - b.y, a.z - b.z); }
 inline V operator*(V a, V b) { return V(a.x * b.x, a.y * b.y, a.z * b.z); }
 inline V operator/(V a, V b) { return V(a.x / b.x, a.y / b.y, a.z / b.z); }
 inline V operator-(V a) { return V(-a.x, -a.y, -a.z); }
-inline V operator*(float s, V a) { return V(s * a.x, s * a.y, s * a.z); }
-inline V operator*(V a, float s) { return V(s * a.x, s * a.y, s * a.z); }
-inline V operator/(V a, float s) { return V(a.x / s, a.y / s, a.z / s); }
-inline float dot(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline V operator*(Real s, V a) { return V(s * a.x, s * a.y, s * a.z); }
+inline V operator*(V a, Real s) { return V(s * a.x, s * a.y, s * a.z); }
+inline V operator/(V a, Real s) { return V(a.x / s, a.y / s, a.z / s); }
+inline Real dot(V a, V b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 inline V cross(V a, V b) { return V(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
-inline float norm2(V a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
-inline float norm(V a) { return std::sqrt(norm2(a)); }
+inline Real norm2(V a) { return a.x * a.x + a.y * a.y + a.z * a.z; }
+inline Real norm(V a) { return std::sqrt(norm2(a)); }
 inline V normalized(V a) {
-  const float d = norm(a);
+  const Real d = norm(a);
   return V(a.x / d, a.y / d, a.z / d);
 }
-inline V vp(const float* p) { return V(p[0], p[1], p[2]); }
+template <typename T>
+inline V vp(const T* p) { return V(p[0], p[1], p[2]); }
 
 // ------------------------------------------------------------------ RNG
 // Philox4x32-10 (Salmon et al., SC'11) keyed by the reference's integer seed.
 struct Rng {
-  uint32_t key, draw = 0, buf[4];
-  explicit Rng(uint32_t seed) : key(seed) {}
+  uint32_t key, key_hi, draw = 0, buf[4];
+  // key_hi: the second key word of every stream (the overlay's 0x5350504D);
+  // another value gives streams that share nothing with those.
+  explicit Rng(uint32_t seed, uint32_t hi = 0x5350504Du) : key(seed), key_hi(hi) {}
   static void philox(uint32_t c0, uint32_t c1, uint32_t c2, uint32_t c3, uint32_t k0, uint32_t k1, uint32_t o[4]) {
     for (int r = 0; r < 10; ++r) {
       if (r) { k0 += 0x9E3779B9u; k1 += 0xBB67AE85u; }
@@ -78,46 +90,46 @@ struct Rng {
   }
   uint32_t u24() {
     const uint32_t lane = draw & 3u;
-    if (!lane) philox(draw >> 2, 0, 0, 0, key, 0x5350504Du, buf);
+    if (!lane) philox(draw >> 2, 0, 0, 0, key, key_hi, buf);
     ++draw;
     return buf[lane] >> 8;
   }
   // RandomMT::genrand64_real1/real2 (MT.h:30-37)
-  double real() { return (double)((float)u24() * (1.0f / 16777216.0f)); }
+  double real() { return (double)((Real)u24() * (1.0f / 16777216.0f)); }
 };
 
 // ------------------------------------------------------------------ scene
 struct Texture {
   int w = 0, h = 0;
-  std::vector<float> c;  // RGBA, value / 255.0f (TextureUtility.cpp:28)
+  std::vector<Real> c;  // RGBA, value / 255.0f (TextureUtility.cpp:28)
 };
 struct Material {
   int type, sppm, opaque, tex_albedo, tex_rough, tex_bump;
   V albedo, radiance;
-  float index, roughness, extinction, reflectance;
+  Real index, roughness, extinction, reflectance;
 };
 struct Facet {
   V p[3], n[3];
-  float uv[3][2];
+  Real uv[3][2];
   int attr;
 };
-struct AliasBin { float prob = 1.0f; int left = -1, right = -1; };
+struct AliasBin { Real prob = 1.0f; int left = -1, right = -1; };
 struct Table {  // TableSampler<T> (TableSampler.h:9-169)
   std::vector<AliasBin> bins;
-  std::vector<float> values;
-  float average = 0;
+  std::vector<Real> values;
+  Real average = 0;
   int n = 0;
   // TableSampler::Init (TableSampler.h:44-120)
-  void init(const std::vector<float>& v) {
+  void init(const std::vector<Real>& v) {
     n = (int)v.size();
     values = v;
     bins.assign(n, AliasBin());
     average = 0.0f;
-    for (int i = 0; i < n; ++i) average += std::max(0.0f, v[i]);
+    for (int i = 0; i < n; ++i) average += std::max<Real>(0.0f, v[i]);
     average /= n;
-    std::vector<std::pair<float, int>> bigger, smaller;
+    std::vector<std::pair<Real, int>> bigger, smaller;
     for (int i = 0; i < n; ++i) {
-      const float x = std::max(0.0f, v[i]);
+      const Real x = std::max<Real>(0.0f, v[i]);
       if (x >= average) bigger.push_back({x / average, i});
       else smaller.push_back({x / average, i});
     }
@@ -145,7 +157,7 @@ struct Table {  // TableSampler<T> (TableSampler.h:9-169)
       }
     }
   }
-  float pdf(int i) const { return values[i] / average / (float)n; }  // TableSampler.h:122-124
+  Real pdf(int i) const { return values[i] / average / (Real)n; }  // TableSampler.h:122-124
   // TableSampler::Sample (TableSampler.h:126-129)
   int sample(Rng& mt) const {
     const AliasBin& bin = bins[(size_t)((double)n * mt.real())];
@@ -163,35 +175,35 @@ struct Light {
 struct Camera {
   int type, W, H;
   V pos, dir, e1, e2;
-  float fov, pw, ph, lw, lh, F, dist;
+  Real fov, pw, ph, lw, lh, F, dist;
 };
 
 struct Ray {
   V o, d;
-  float index;
+  Real index;
 };
 
 // --------------------------------------------------------------- texture
 // LinearSampler::Sample (TextureSampler.h:61-79)
-inline void tex_sample(const Texture& t, float u, float v, float out[4]) {
+inline void tex_sample(const Texture& t, Real u, Real v, Real out[4]) {
   const int W = t.w, H = t.h;
   const int x1 = std::abs(int(W * u)) % W;
   const int y1 = std::abs(int(H * v)) % H;
-  const float* c00 = &t.c[4 * (size_t)(x1 + y1 * W)];
-  const float* c10 = &t.c[4 * (size_t)(std::min(W - 1, x1 + 1) + y1 * W)];
-  const float* c01 = &t.c[4 * (size_t)(x1 + std::min(H - 1, y1 + 1) * W)];
-  const float* c11 = &t.c[4 * (size_t)(std::min(W - 1, x1 + 1) + std::min(H - 1, y1 + 1) * W)];
-  const float w = (std::abs(u * W) - std::abs(int(W * u)));
-  const float h = (std::abs(v * H) - std::abs(int(H * v)));
+  const Real* c00 = &t.c[4 * (size_t)(x1 + y1 * W)];
+  const Real* c10 = &t.c[4 * (size_t)(std::min(W - 1, x1 + 1) + y1 * W)];
+  const Real* c01 = &t.c[4 * (size_t)(x1 + std::min(H - 1, y1 + 1) * W)];
+  const Real* c11 = &t.c[4 * (size_t)(std::min(W - 1, x1 + 1) + std::min(H - 1, y1 + 1) * W)];
+  const Real w = (std::abs(u * W) - std::abs(int(W * u)));
+  const Real h = (std::abs(v * H) - std::abs(int(H * v)));
   for (int k = 0; k < 4; ++k) {
-    const float up = c00[k] * (float)(1.0 - w) + c10[k] * w;
-    const float down = c01[k] * (float)(1.0 - w) + c11[k] * w;
-    out[k] = up * (float)(1.0 - h) + down * h;
+    const Real up = c00[k] * (Real)(1.0 - w) + c10[k] * w;
+    const Real down = c01[k] * (Real)(1.0 - w) + c11[k] * w;
+    out[k] = up * (Real)(1.0 - h) + down * h;
   }
 }
 
 // ------------------------------------------------------------------- BVH
-struct BNode { float lo[3], hi[3]; int left, right, first, count; };
+struct BNode { Real lo[3], hi[3]; int left, right, first, count; };
 struct BVH {
   std::vector<BNode> nodes;
   std::vector<int> idx;
@@ -210,7 +222,7 @@ struct BVH {
   int rec(const std::vector<Facet>& F, const std::vector<V>& cen, int first, int count) {
     BNode n;
     for (int a = 0; a < 3; ++a) { n.lo[a] = FLT_MAX; n.hi[a] = -FLT_MAX; }
-    float clo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, chi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    Real clo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, chi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
     for (int i = first; i < first + count; ++i) {
       const Facet& f = F[idx[i]];
       for (int k = 0; k < 3; ++k)
@@ -242,14 +254,14 @@ struct BVH {
 };
 
 // Isc::Intersect(Ray, Triangle_ID) (Intersect.cpp:67-89)
-inline bool intersect(const Ray& ray, const Facet& p, float& t, float& u, float& v) {
+inline bool intersect(const Ray& ray, const Facet& p, Real& t, Real& u, Real& v) {
   const V dd = ray.d;
   const V e1 = p.p[1] - p.p[0];
   const V e2 = p.p[2] - p.p[0];
   const V ps = cross(dd, e2);
-  const float a = dot(e1, ps);
+  const Real a = dot(e1, ps);
   if (a > -FLT_MIN && a < FLT_MIN) return false;
-  const float f = 1.0f / a;
+  const Real f = 1.0f / a;
   const V s = ray.o - p.p[0];
   u = f * dot(s, ps);
   if (u < 0.0 || u > 1.0) return false;
@@ -260,26 +272,69 @@ inline bool intersect(const Ray& ray, const Facet& p, float& t, float& u, float&
   return true;
 }
 
-inline bool box_hit(const BNode& n, const Ray& r, float tmin, float tmax) {
-  float t0 = tmin, t1 = tmax;
+// Watertight ray-triangle test (Woop, Benthin and Wald, "Watertight
+// Ray/Triangle Intersection", JCGT 2(1), 2013), the precision mode's test:
+// the same float and double operations, in the same order, as the GPU's
+// intersect_watertight (csrc/fr_trace.cuh).  u, v are the weights of p[1]
+// and p[2], as Moller-Trumbore's.
+inline Real axis_of(const V& a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); }
+
+inline bool intersect_watertight(const Ray& ray, const Facet& p, Real& t, Real& u, Real& v) {
+  const V dir = ray.d;
+  const Real adx = std::fabs(dir.x), ady = std::fabs(dir.y), adz = std::fabs(dir.z);
+  const int kz = adx > ady ? (adx > adz ? 0 : 2) : (ady > adz ? 1 : 2);
+  int kx = kz == 2 ? 0 : kz + 1;
+  int ky = kx == 2 ? 0 : kx + 1;
+  const Real dz = axis_of(dir, kz);
+  if (dz < 0.0f) std::swap(kx, ky);
+  const Real Sx = axis_of(dir, kx) / dz, Sy = axis_of(dir, ky) / dz, Sz = 1.0f / dz;
+  const V A = p.p[0] - ray.o, B = p.p[1] - ray.o, C = p.p[2] - ray.o;
+  const Real Az0 = axis_of(A, kz), Bz0 = axis_of(B, kz), Cz0 = axis_of(C, kz);
+  const Real Ax = axis_of(A, kx) - Sx * Az0, Ay = axis_of(A, ky) - Sy * Az0;
+  const Real Bx = axis_of(B, kx) - Sx * Bz0, By = axis_of(B, ky) - Sy * Bz0;
+  const Real Cx = axis_of(C, kx) - Sx * Cz0, Cy = axis_of(C, ky) - Sy * Cz0;
+  Real U = Cx * By - Cy * Bx, W2 = Ax * Cy - Ay * Cx, W = Bx * Ay - By * Ax;
+  if (U == 0.0f || W2 == 0.0f || W == 0.0f) {
+    U = (Real)((double)Cx * (double)By - (double)Cy * (double)Bx);
+    W2 = (Real)((double)Ax * (double)Cy - (double)Ay * (double)Cx);
+    W = (Real)((double)Bx * (double)Ay - (double)By * (double)Ax);
+  }
+  if ((U < 0.0f || W2 < 0.0f || W < 0.0f) && (U > 0.0f || W2 > 0.0f || W > 0.0f)) return false;
+  const Real det = U + W2 + W;
+  if (det == 0.0f) return false;
+  const Real T = U * (Sz * Az0) + W2 * (Sz * Bz0) + W * (Sz * Cz0);
+  const Real rcp = 1.0f / det;
+  t = T * rcp;
+  u = W2 * rcp;
+  v = W * rcp;
+  return true;
+}
+
+// The triangle test of a renderer's mode.
+inline bool intersect(const Ray& ray, const Facet& p, Real& t, Real& u, Real& v, bool watertight) {
+  return watertight ? intersect_watertight(ray, p, t, u, v) : intersect(ray, p, t, u, v);
+}
+
+inline bool box_hit(const BNode& n, const Ray& r, Real tmin, Real tmax) {
+  Real t0 = tmin, t1 = tmax;
   for (int a = 0; a < 3; ++a) {
     const double inv = 1.0 / (double)r.d[a];
     double ta = ((double)n.lo[a] - r.o[a]) * inv, tb = ((double)n.hi[a] - r.o[a]) * inv;
     if (ta > tb) std::swap(ta, tb);
     if (std::isnan(ta) || std::isnan(tb)) continue;
-    t0 = (float)std::max((double)t0, ta);
-    t1 = (float)std::min((double)t1, tb);
+    t0 = (Real)std::max((double)t0, ta);
+    t1 = (Real)std::min((double)t1, tb);
   }
   return t0 <= t1;
 }
 
-struct Hit { float t, u, v; int facet; };
+struct Hit { Real t, u, v; int facet; };
 
 // N_BVH8::findClosestElement semantics (bvh8.h:568-641): nearest t > MinT.
-bool closest(const BVH& b, const std::vector<Facet>& F, const Ray& ray, Hit& h) {
-  float best = FLT_MAX;
+bool closest(const BVH& b, const std::vector<Facet>& F, const Ray& ray, Hit& h, bool wt = false) {
+  Real best = FLT_MAX;
   int bf = -1;
-  float bu = 0, bv = 0;
+  Real bu = 0, bv = 0;
   int stack[128];
   int sp = 0;
   stack[sp++] = 0;
@@ -289,8 +344,8 @@ bool closest(const BVH& b, const std::vector<Facet>& F, const Ray& ray, Hit& h) 
     if (n.left < 0) {
       for (int i = n.first; i < n.first + n.count; ++i) {
         const int f = b.idx[i];
-        float t, u, v;
-        if (intersect(ray, F[f], t, u, v) && t > RAY_OFFSET && (t < best || (t == best && f > bf))) {
+        Real t, u, v;
+        if (intersect(ray, F[f], t, u, v, wt) && t > RAY_OFFSET && (t < best || (t == best && f > bf))) {
           best = t; bf = f; bu = u; bv = v;
         }
       }
@@ -305,7 +360,7 @@ bool closest(const BVH& b, const std::vector<Facet>& F, const Ray& ray, Hit& h) 
 }
 
 // findAnyElement (bvh8.h:643-707)
-bool any_hit(const BVH& b, const std::vector<Facet>& F, const Ray& ray, float tmin, float tmax) {
+bool any_hit(const BVH& b, const std::vector<Facet>& F, const Ray& ray, Real tmin, Real tmax, bool wt = false) {
   int stack[128];
   int sp = 0;
   stack[sp++] = 0;
@@ -314,8 +369,8 @@ bool any_hit(const BVH& b, const std::vector<Facet>& F, const Ray& ray, float tm
     if (!box_hit(n, ray, tmin, tmax)) continue;
     if (n.left < 0) {
       for (int i = n.first; i < n.first + n.count; ++i) {
-        float t, u, v;
-        if (intersect(ray, F[b.idx[i]], t, u, v) && tmax >= t && t > tmin) return true;
+        Real t, u, v;
+        if (intersect(ray, F[b.idx[i]], t, u, v, wt) && tmax >= t && t > tmin) return true;
       }
     } else {
       stack[sp++] = n.right;
@@ -329,7 +384,7 @@ bool any_hit(const BVH& b, const std::vector<Facet>& F, const Ray& ray, float tm
 const V INVALID_DIR(1e-3, 1e-3, 1e-3);  // RayUtility.h:8
 inline bool valid_dir(V d) { return norm2(d) > 0.9999f; }  // RayUtility.cpp:36-38
 
-struct FP { V in, out, n; float from, to, rough, absorb, refl; };  // material.h:12-34
+struct FP { V in, out, n; Real from, to, rough, absorb, refl; };  // material.h:12-34
 
 inline void basis(V e1, V& e2, V& e3) {
   if (std::abs(e1.x) > 0.000001) e2 = normalized(cross(V(0, 1, 0), e1));
@@ -338,15 +393,15 @@ inline void basis(V e1, V& e2, V& e3) {
 }
 
 // Sampling::Cos_Sampling (Sampling.cpp:7-28)
-V cos_sampling(Rng& mt, V normal, float* pdf) {
+V cos_sampling(Rng& mt, V normal, Real* pdf) {
   V e2, e3;
   const V e1 = normal;
   basis(e1, e2, e3);
-  const float ph = mt.real() * 2.0f * PI;
-  const float th = mt.real();
-  const float th2 = std::sqrt(th);
-  V r = e1 * (float)std::sqrt(1.000000001 - th) + e2 * (float)std::cos((double)ph) * th2 +
-        e3 * (float)std::sin((double)ph) * th2;
+  const Real ph = mt.real() * 2.0f * PI;
+  const Real th = mt.real();
+  const Real th2 = std::sqrt(th);
+  V r = e1 * (Real)std::sqrt(1.000000001 - th) + e2 * (Real)std::cos((double)ph) * th2 +
+        e3 * (Real)std::sin((double)ph) * th2;
   r = normalized(r);
   if (pdf) *pdf = std::max(sMin, dot(r, normal) / PI);
   return r;
@@ -354,202 +409,202 @@ V cos_sampling(Rng& mt, V normal, float* pdf) {
 // Sampling::Reflect_Sampling (Sampling.cpp:293-295)
 V reflect(V n, V in) { return normalized(in - 2.0f * (dot(n, in)) * n); }
 // Sampling::Fresnel_Reflectance (Sampling.cpp:297-313)
-float fresnel(V n, V in, float ni, float no) {
-  const float r12 = ni / no;
-  const float cosA = std::abs(dot(n, in));
-  const float sinA = std::sqrt(1.0000001f - cosA * cosA);
-  const float sinB = r12 * sinA;
+Real fresnel(V n, V in, Real ni, Real no) {
+  const Real r12 = ni / no;
+  const Real cosA = std::abs(dot(n, in));
+  const Real sinA = std::sqrt(1.0000001f - cosA * cosA);
+  const Real sinB = r12 * sinA;
   if (sinB > 0.999999) return 1.0f;
-  const float cosB = std::sqrt(1.0000001f - sinB * sinB);
-  const float rp = (no * cosA - ni * cosB) / (no * cosA + ni * cosB);
-  const float rs = (ni * cosA - no * cosB) / (ni * cosA + no * cosB);
+  const Real cosB = std::sqrt(1.0000001f - sinB * sinB);
+  const Real rp = (no * cosA - ni * cosB) / (no * cosA + ni * cosB);
+  const Real rs = (ni * cosA - no * cosB) / (ni * cosA + no * cosB);
   return (0.5f * rs * rs) + (0.5f * rp * rp);
 }
 // RUtil::Refract (RayUtility.cpp:10-17)
-V refract(V in, V n, float from, float into) {
+V refract(V in, V n, Real from, Real into) {
   const V NN = dot(in, n) < 0 ? n : -n;
-  const float eta = from / into;
-  const float LN = -dot(in, NN);
-  const float sq = std::max(0.0f, 1.0f - eta * eta * (1.0f - LN * LN));
+  const Real eta = from / into;
+  const Real LN = -dot(in, NN);
+  const Real sq = std::max<Real>(0.0f, 1.0f - eta * eta * (1.0f - LN * LN));
   return normalized(-NN * std::sqrt(sq) - eta * (-in - LN * NN));
 }
 inline bool is_reflect(V in, V out, V n) { return dot(n, in) * dot(n, out) < 0.0f; }  // RayUtility.cpp:34-36
 // RUtil::GetMicrofacetNormal_FromRefraction (RayUtility.cpp:21-33)
-V mfn_refraction(V in, V out, float from, float into) {
-  const float c = std::abs(dot(in, out));
-  const float eta = into / from;
-  const float isq = eta * eta - 2.0f * eta * c + 1.0f;
+V mfn_refraction(V in, V out, Real from, Real into) {
+  const Real c = std::abs(dot(in, out));
+  const Real eta = into / from;
+  const Real isq = eta * eta - 2.0f * eta * c + 1.0f;
   if (isq < 1e-8) return V(0, 0, 0);
-  const float ss = 1.0f / std::sqrt(isq);
+  const Real ss = 1.0f / std::sqrt(isq);
   const V h = normalized(-eta * ss * out + ss * in);
   return into > from ? h : -h;
 }
-inline float powm2(float x) { return std::pow(x, -2.0f); }
+inline Real powm2(Real x) { return std::pow(x, -2.0f); }
 
 // Sampling::GGX_Sampling (Sampling.cpp:123-157)
-V ggx_sampling(Rng& mt, V normal, V in, float alpha, float* pdf) {
+V ggx_sampling(Rng& mt, V normal, V in, Real alpha, Real* pdf) {
   const V e1 = normal;
-  const float phi = mt.real() * 2.0f * PI;
-  const float e = mt.real();
-  const float cth = (float)std::sqrt((1.0 - e) / (e * (alpha * alpha - 1.0f) + 1.0f));
+  const Real phi = mt.real() * 2.0f * PI;
+  const Real e = mt.real();
+  const Real cth = (Real)std::sqrt((1.0 - e) / (e * (alpha * alpha - 1.0f) + 1.0f));
   V e2, e3;
   basis(e1, e2, e3);
-  const float cph = (float)std::cos((double)phi), sph = (float)std::sin((double)phi);
-  const float sth = std::sqrt(1.0f - cth * cth);
+  const Real cph = (Real)std::cos((double)phi), sph = (Real)std::sin((double)phi);
+  const Real sth = std::sqrt(1.0f - cth * cth);
   const V mN = normalized(e3 * sth * cph + e2 * sth * sph + e1 * cth);
   if (dot(mN, in) > 0.0) { *pdf = sMin; return INVALID_DIR; }
   const V r = reflect(mN, in);
   if (dot(r, normal) < 0.0) { *pdf = sMin; return INVALID_DIR; }
-  const float wm_N = dot(mN, normal), wo_wm = dot(r, mN);
+  const Real wm_N = dot(mN, normal), wo_wm = dot(r, mN);
   const double x = 1.0f - (1.0f - alpha * alpha) * wm_N * wm_N;
-  *pdf = (float)((alpha * alpha) / (PI * (x * x)) * wm_N / (4.0f * wo_wm));
+  *pdf = (Real)((alpha * alpha) / (PI * (x * x)) * wm_N / (4.0f * wo_wm));
   return r;
 }
 // Sampling::GGX_Sampling_PDF (Sampling.cpp:158-180)
-float ggx_pdf(V out, V normal, V in, float a) {
+Real ggx_pdf(V out, V normal, V in, Real a) {
   if (!is_reflect(in, out, normal)) return sMin;
   const V h = normalized(-in + out);
-  const float h_n = dot(h, normal);
+  const Real h_n = dot(h, normal);
   if (h_n < 0.0f) return sMin;
   if (-dot(in, h) < 0.0f) return sMin;
-  const float wo_h = dot(out, h);
+  const Real wo_h = dot(out, h);
   if (wo_h < 0.0f) return sMin;
-  const float jc = 1.0f / (4.0f * wo_h);
+  const Real jc = 1.0f / (4.0f * wo_h);
   return (a * a / PI * powm2(1.0f - (1.0f - a * a) * h_n * h_n)) * h_n * jc;
 }
 // Sampling::GGXGlass_Sampling (Sampling.cpp:181-248)
-V glass_sampling(Rng& mt, V normal, V in, float alpha, float Ii, float Io, float* pdf) {
-  constexpr float small = 1e-12f;
+V glass_sampling(Rng& mt, V normal, V in, Real alpha, Real Ii, Real Io, Real* pdf) {
+  constexpr Real small = 1e-12f;
   const V NN = dot(in, normal) < 0 ? normal : -normal;
   *pdf = 1.0f;
   const V e1 = NN;
-  const float phi = mt.real() * 2.0f * PI;
-  const float e = mt.real();
-  const float cth = (float)std::sqrt((1.0000001 - e) / (e * (alpha * alpha - 0.99999) + 1.0f));
+  const Real phi = mt.real() * 2.0f * PI;
+  const Real e = mt.real();
+  const Real cth = (Real)std::sqrt((1.0000001 - e) / (e * (alpha * alpha - 0.99999) + 1.0f));
   V e2, e3;
   basis(e1, e2, e3);
-  const float cph = (float)std::cos((double)phi), sph = (float)std::sin((double)phi);
-  const float sth = std::sqrt(1.00000001f - cth * cth);
+  const Real cph = (Real)std::cos((double)phi), sph = (Real)std::sin((double)phi);
+  const Real sth = std::sqrt(1.00000001f - cth * cth);
   const V mN = normalized(e3 * sth * cph + e2 * sth * sph + e1 * cth);
-  const float wi_wm = -dot(in, mN), wm_N = dot(mN, NN), wi_N = -dot(in, NN);
+  const Real wi_wm = -dot(in, mN), wm_N = dot(mN, NN), wi_N = -dot(in, NN);
   if (wi_N < small || wi_wm < small || wm_N < small) { *pdf = sMin; return INVALID_DIR; }
-  const float refl = fresnel(mN, in, Ii, Io);
-  const float y = 1.0f - (1.0f - alpha * alpha) * wm_N * wm_N;
+  const Real refl = fresnel(mN, in, Ii, Io);
+  const Real y = 1.0f - (1.0f - alpha * alpha) * wm_N * wm_N;
   if (refl > mt.real()) {
     *pdf = refl;
     const V r = reflect(mN, in);
-    const float wo_wm = dot(r, mN);
+    const Real wo_wm = dot(r, mN);
     if (wo_wm < small) return INVALID_DIR;
     if (dot(r, NN) * dot(in, NN) > small) { *pdf = sMin; return INVALID_DIR; }
     *pdf = refl * (wm_N / (4.0f * wo_wm) * alpha * alpha / (PI * (y * y)));
     return r;
   }
   const V r = refract(in, mN, Ii, Io);
-  const float wo_wm = -dot(r, mN), wo_N = -dot(r, NN);
+  const Real wo_wm = -dot(r, mN), wo_N = -dot(r, NN);
   if (wi_N * wo_N < small || wo_N < small || wo_wm < small) { *pdf = sMin; return INVALID_DIR; }
   const double s = Ii * wi_wm + Io * wo_wm;
-  *pdf = (float)((1.0f - refl) * wm_N * (Io * Io * wo_wm / (s * s)) * alpha * alpha / (PI * (y * y)));
+  *pdf = (Real)((1.0f - refl) * wm_N * (Io * Io * wo_wm / (s * s)) * alpha * alpha / (PI * (y * y)));
   return r;
 }
 // Sampling::GGXGlass_Sampling_PDF (Sampling.cpp:249-288)
-float glass_pdf(V out, V normal, V in, float a, float Ii, float Io) {
+Real glass_pdf(V out, V normal, V in, Real a, Real Ii, Real Io) {
   if (is_reflect(in, out, normal)) {
     const V h = normalized(-in + out);
-    const float h_n = dot(h, normal);
+    const Real h_n = dot(h, normal);
     if (h_n < 0.0f) return sMin;
     if (-dot(in, h) < 0.0f) return sMin;
-    const float wo_h = dot(out, h);
+    const Real wo_h = dot(out, h);
     if (wo_h < 0.0f) return sMin;
-    const float refl = fresnel(h, in, Ii, Io);
-    const float jc = 1.0f / (4.0f * wo_h);
+    const Real refl = fresnel(h, in, Ii, Io);
+    const Real jc = 1.0f / (4.0f * wo_h);
     return refl * h_n * (a * a / PI * powm2(1.0f - (1.0f - a * a) * h_n * h_n)) * jc;
   }
   const V h = mfn_refraction(in, out, Ii, Io);
-  const float h_n = dot(h, normal);
+  const Real h_n = dot(h, normal);
   if (h_n < 0.0f) return sMin;
-  const float wi_h = -dot(in, h);
+  const Real wi_h = -dot(in, h);
   if (wi_h < 0.0f) return sMin;
-  const float wo_h = -dot(out, h);
+  const Real wo_h = -dot(out, h);
   if (wo_h < 0.0f) return sMin;
-  const float refl = fresnel(h, in, Ii, Io);
-  const float jc = Io * Io * wo_h * powm2(Ii * wi_h + Io * wo_h);
+  const Real refl = fresnel(h, in, Ii, Io);
+  const Real jc = Io * Io * wo_h * powm2(Ii * wi_h + Io * wo_h);
   return (1.0f - refl) * h_n * (a * a / PI * powm2(1.0f - (1.0f - a * a) * h_n * h_n)) * jc;
 }
 inline bool opaque_reflect(const FP& p) { return dot(p.in, -p.n) > 1e-4 && dot(p.out, p.n) > 1e-4; }  // material.h:139-141
 
 // Roughconductor::BRDF (material.h:227-274)
-float conductor_brdf(const FP& p) {
-  constexpr float small = 1e-10f;
+Real conductor_brdf(const FP& p) {
+  constexpr Real small = 1e-10f;
   if (dot(p.in, p.n) > -small || dot(p.out, p.n) < small) return 0.0f;
-  const float k = p.absorb, eta = p.to / p.from, alpha = p.rough;
+  const Real k = p.absorb, eta = p.to / p.from, alpha = p.rough;
   const V h = normalized(-p.in + p.out);
-  const float ccs = dot(h, p.n);
+  const Real ccs = dot(h, p.n);
   if (ccs < small || dot(h, p.in) > -small || dot(h, p.out) < small) return 0.0f;
-  const float dd = 1.0001f - (1.0f - alpha * alpha) * ccs * ccs;
-  const float D = std::max(sMin, (alpha * alpha) / (PI * (dd * dd)));
-  const float lc = std::max(0.0f, std::min(0.9999f, dot(p.in, -p.n)));
-  const float lv = std::max(0.0f, std::min(0.9999f, dot(p.out, p.n)));
+  const Real dd = 1.0001f - (1.0f - alpha * alpha) * ccs * ccs;
+  const Real D = std::max(sMin, (alpha * alpha) / (PI * (dd * dd)));
+  const Real lc = std::max<Real>(0.0f, std::min<Real>(0.9999f, dot(p.in, -p.n)));
+  const Real lv = std::max<Real>(0.0f, std::min<Real>(0.9999f, dot(p.out, p.n)));
   if (lc < sMin || lv < sMin) return 0.0f;
-  const float L_l = (-1.0f + std::sqrt(1.0f + alpha * alpha * (1.0f / (lc * lc) - 1.0))) * 0.5;
-  const float L_v = (-1.0f + std::sqrt(1.0f + alpha * alpha * (1.0f / (lv * lv) - 1.0))) * 0.5;
-  const float G = 1.0f / ((1.0f + L_l) * (1.0f + L_v));
-  const float fcos = dot(p.n, -p.in);
-  const float temp = eta * eta - k * k - (1.0f - fcos * fcos);
-  const float apb = std::sqrt(temp * temp + k * k * eta * eta);
-  const float a = std::sqrt((apb + temp) * 0.5);
-  const float tm1 = apb + fcos * fcos;
-  const float tm2 = a * 2.0f * fcos;
-  const float rs2 = (tm1 - tm2) / (tm1 + tm2);
-  const float tm3 = apb * fcos * fcos + (1.0f - fcos * fcos) * (1.0 - fcos * fcos);
-  const float tm4 = tm2 * (1.0f - fcos * fcos);
-  const float rp2 = rs2 * (tm3 - tm4) / (tm3 + tm4);
-  const float F = 0.5 * (rp2 + rs2);
-  const float fx = (4.0f * dot(p.in, -p.n) * dot(p.out, p.n));
+  const Real L_l = (-1.0f + std::sqrt(1.0f + alpha * alpha * (1.0f / (lc * lc) - 1.0))) * 0.5;
+  const Real L_v = (-1.0f + std::sqrt(1.0f + alpha * alpha * (1.0f / (lv * lv) - 1.0))) * 0.5;
+  const Real G = 1.0f / ((1.0f + L_l) * (1.0f + L_v));
+  const Real fcos = dot(p.n, -p.in);
+  const Real temp = eta * eta - k * k - (1.0f - fcos * fcos);
+  const Real apb = std::sqrt(temp * temp + k * k * eta * eta);
+  const Real a = std::sqrt((apb + temp) * 0.5);
+  const Real tm1 = apb + fcos * fcos;
+  const Real tm2 = a * 2.0f * fcos;
+  const Real rs2 = (tm1 - tm2) / (tm1 + tm2);
+  const Real tm3 = apb * fcos * fcos + (1.0f - fcos * fcos) * (1.0 - fcos * fcos);
+  const Real tm4 = tm2 * (1.0f - fcos * fcos);
+  const Real rp2 = rs2 * (tm3 - tm4) / (tm3 + tm4);
+  const Real F = 0.5 * (rp2 + rs2);
+  const Real fx = (4.0f * dot(p.in, -p.n) * dot(p.out, p.n));
   return (F * G * D) / fx;
 }
 // GGXGlass::EstimateN (material.h:297-309)
-V estimate_n(V in, V out, float Ii, float Io) {
-  const float c = std::abs(dot(in, out));
-  const float eta = Io / Ii;
-  const float isq = eta * eta - 2.0f * eta * c + 1.0f;
+V estimate_n(V in, V out, Real Ii, Real Io) {
+  const Real c = std::abs(dot(in, out));
+  const Real eta = Io / Ii;
+  const Real isq = eta * eta - 2.0f * eta * c + 1.0f;
   if (isq < sMin) return V(0, 0, 0);
-  const float ss = 1.0f / std::sqrt(isq);
+  const Real ss = 1.0f / std::sqrt(isq);
   const V h = normalized(-eta * ss * out + ss * in);
   return Io > Ii ? h : -h;
 }
 // GGXGlass::BRDF (material.h:314-390)
-float glass_brdf(const FP& p) {
-  constexpr float small = 1e-8f;
+Real glass_brdf(const FP& p) {
+  constexpr Real small = 1e-8f;
   const bool refl = dot(p.n, p.in) * dot(p.n, p.out) < 0;
-  const float a = p.rough, Ii = p.from, Io = p.to;
+  const Real a = p.rough, Ii = p.from, Io = p.to;
   if (refl) {
     const V h = normalized(-p.in + p.out);
-    const float n_h = dot(p.n, h);
+    const Real n_h = dot(p.n, h);
     if (n_h < 0) return 0.0f;
-    const float D = (a * a) * powm2(1.0f - (1.0f - a * a) * n_h * n_h) / PI;
-    const float L_l = (-1.0f + std::sqrt(1.0001f + a * a * (powm2(dot(p.n, -p.in)) - 1.0f))) * 0.5f;
-    const float L_v = (-1.0f + std::sqrt(1.0001f + a * a * (powm2(dot(p.n, p.out)) - 1.0f))) * 0.5f;
-    const float G = 1.0f / (L_l + L_v + 1.0f);
-    const float F = fresnel(h, p.in, Ii, Io);
-    const float wo_n = std::max(0.0f, std::min(1.0f, dot(p.out, h)));
-    const float wi_n = std::max(0.0f, std::min(1.0f, -dot(p.in, h)));
+    const Real D = (a * a) * powm2(1.0f - (1.0f - a * a) * n_h * n_h) / PI;
+    const Real L_l = (-1.0f + std::sqrt(1.0001f + a * a * (powm2(dot(p.n, -p.in)) - 1.0f))) * 0.5f;
+    const Real L_v = (-1.0f + std::sqrt(1.0001f + a * a * (powm2(dot(p.n, p.out)) - 1.0f))) * 0.5f;
+    const Real G = 1.0f / (L_l + L_v + 1.0f);
+    const Real F = fresnel(h, p.in, Ii, Io);
+    const Real wo_n = std::max<Real>(0.0f, std::min<Real>(1.0f, dot(p.out, h)));
+    const Real wi_n = std::max<Real>(0.0f, std::min<Real>(1.0f, -dot(p.in, h)));
     if (wo_n < small || wi_n < small) return 0.0f;
     return F * G * D / (4.0f * wo_n * wi_n);
   }
-  const float eta = Io / Ii;
+  const Real eta = Io / Ii;
   if (std::abs(eta - 1.0f) < small) return 1.0;
   if (dot(p.in, p.out) < 0.0) return 0.0f;
   const V h = estimate_n(p.in, p.out, p.from, p.to);
   if (norm(h) < small) return 0.0f;
-  const float n_h = dot(h, p.n);
+  const Real n_h = dot(h, p.n);
   if (n_h < small) return 0.0f;
-  const float D = (a * a) * powm2(1.0f - (1.0f - a * a) * n_h * n_h) / PI;
-  const float L_l = (-1.0f + std::sqrt(1.0001f + a * a * (powm2(dot(p.n, -p.in)) - 1.0f))) * 0.5f;
-  const float L_v = (-1.0f + std::sqrt(1.0001f + a * a * (powm2(dot(p.n, -p.out)) - 1.0f))) * 0.5f;
-  const float G = 1.0f / (L_l + L_v + 1.0f);
-  const float F = fresnel(h, p.in, Ii, Io);
-  const float wi_wm = -dot(p.in, h), wo_wm = -dot(p.out, h);
-  const float wi_n = -dot(p.in, p.n), wo_n = -dot(p.out, p.n);
+  const Real D = (a * a) * powm2(1.0f - (1.0f - a * a) * n_h * n_h) / PI;
+  const Real L_l = (-1.0f + std::sqrt(1.0001f + a * a * (powm2(dot(p.n, -p.in)) - 1.0f))) * 0.5f;
+  const Real L_v = (-1.0f + std::sqrt(1.0001f + a * a * (powm2(dot(p.n, -p.out)) - 1.0f))) * 0.5f;
+  const Real G = 1.0f / (L_l + L_v + 1.0f);
+  const Real F = fresnel(h, p.in, Ii, Io);
+  const Real wi_wm = -dot(p.in, h), wo_wm = -dot(p.out, h);
+  const Real wi_n = -dot(p.in, p.n), wo_n = -dot(p.out, p.n);
   if (wo_wm < small || wi_wm < small) return 0.0f;
   if (wi_n < small || wo_n < small) return 0.0f;
   return (wi_wm * wo_wm) / (wi_n * wo_n) * (Io * Io) * (1.0f - F) * G * D * powm2(Ii * wo_wm + Io * wi_wm);
@@ -558,18 +613,18 @@ float glass_brdf(const FP& p) {
 // ------------------------------------------- the demo's further surfaces
 inline V facing(V n, V in) { return dot(n, in) < 0 ? n : -n; }
 // Sampling::Refract_Sampling (Sampling.cpp:329-337)
-V refract_sampling(V n, V in, float ii, float io) {
-  const float eta = ii / io;
+V refract_sampling(V n, V in, Real ii, Real io) {
+  const Real eta = ii / io;
   const V NN = (dot(in, n) > 0) ? -n : n;
-  const float LN = -dot(in, NN);
-  const float sq = std::max(0.00000001f, 1.0f - eta * eta * (1.0f - LN * LN));
+  const Real LN = -dot(in, NN);
+  const Real sq = std::max<Real>(0.00000001f, 1.0f - eta * eta * (1.0f - LN * LN));
   return normalized(-NN * std::sqrt(sq) - eta * (-in - LN * NN));
 }
 inline bool if_reflect(V n, V in, V out) { return dot(n, in) * dot(n, out) < 0.0f; }
 inline V reflect_by_n(V r, V n) { return r - 2.0f * dot(n, r) * n; }  // material.h:683-686
 
 // BiMetalSurface (material.h:427-463)
-float bimetal_brdf(const FP& p) {
+Real bimetal_brdf(const FP& p) {
   const V N = facing(p.n, p.in);
   if (!opaque_reflect(p)) return 0.0f;
   const V r = reflect(N, p.in);
@@ -578,29 +633,29 @@ float bimetal_brdf(const FP& p) {
 }
 // GlassSurface (material.h:465-531); its Reflect is Reflect_Sampling's
 // expression, its Refract Refract_Sampling's.
-V glasssurf_sample(Rng& mt, const FP& p, float* pdf) {
+V glasssurf_sample(Rng& mt, const FP& p, Real* pdf) {
   const V NN = facing(p.n, p.in);
-  const float reflectance = fresnel(NN, p.in, p.from, p.to);
+  const Real reflectance = fresnel(NN, p.in, p.from, p.to);
   if (reflectance > mt.real()) {
     *pdf = reflectance;
     return reflect(NN, p.in);
   }
   *pdf = 1.0f - reflectance;
-  const float eta = p.from / p.to;
-  const float LN = -dot(p.in, NN);
-  const float sq = 1.0f - eta * eta * (1.0 - LN * LN);
+  const Real eta = p.from / p.to;
+  const Real LN = -dot(p.in, NN);
+  const Real sq = 1.0f - eta * eta * (1.0 - LN * LN);
   if (sq < 0.000001) return reflect(p.n, p.in);
   return refract_sampling(p.n, p.in, p.from, p.to);
 }
-float glasssurf_brdf(const FP& p) {
+Real glasssurf_brdf(const FP& p) {
   const V NN = facing(p.n, p.in);
-  const float reflectance = fresnel(NN, p.in, p.from, p.to);
+  const Real reflectance = fresnel(NN, p.in, p.from, p.to);
   if (if_reflect(p.n, p.in, p.out)) return 1.0f * reflectance / (std::abs(dot(p.out, NN)) + 0.0001);
   return 1.0f * (1.0f - reflectance) / (std::abs(dot(p.out, NN)) + 0.0001);
 }
-float glasssurf_pdf(const FP& p) {
+Real glasssurf_pdf(const FP& p) {
   const V NN = facing(p.n, p.in);
-  const float reflectance = fresnel(NN, p.in, p.from, p.to);
+  const Real reflectance = fresnel(NN, p.in, p.from, p.to);
   if (if_reflect(p.n, p.in, p.out)) {
     const V r = reflect(NN, p.in);
     return std::abs(dot(r, p.out)) > 0.99 ? 1.0f * reflectance : sMin;
@@ -609,7 +664,7 @@ float glasssurf_pdf(const FP& p) {
   return std::abs(dot(rac, p.out)) > 0.99 ? 1.0f * (1.0f - reflectance) : sMin;
 }
 // DiffuseTransmitSurface (material.h:637-675)
-V difftrans_sample(Rng& mt, const FP& p, float* pdf) {
+V difftrans_sample(Rng& mt, const FP& p, Real* pdf) {
   const V n = dot(p.n, p.in) > 0 ? p.n : -p.n;
   V rs;
   if (p.refl > mt.real()) {
@@ -621,13 +676,13 @@ V difftrans_sample(Rng& mt, const FP& p, float* pdf) {
   }
   return rs;
 }
-float difftrans_brdf(const FP& p) { return if_reflect(p.n, p.in, p.out) ? p.refl / PI : (1.0f - p.refl) / PI; }
-float difftrans_pdf(const FP& p) {
-  const float c = std::abs(dot(p.out, p.n) + 0.00001);
+Real difftrans_brdf(const FP& p) { return if_reflect(p.n, p.in, p.out) ? p.refl / PI : (1.0f - p.refl) / PI; }
+Real difftrans_pdf(const FP& p) {
+  const Real c = std::abs(dot(p.out, p.n) + 0.00001);
   return if_reflect(p.n, p.in, p.out) ? p.refl * c / PI : (1.0f - p.refl) * c / PI;
 }
 // GlossTransmitSurface (material.h:677-766)
-V glosstrans_sample(Rng& mt, const FP& p, float* pdf) {
+V glosstrans_sample(Rng& mt, const FP& p, Real* pdf) {
   const V n = facing(p.n, p.in);
   V rs;
   if (p.refl > mt.real()) {
@@ -639,36 +694,36 @@ V glosstrans_sample(Rng& mt, const FP& p, float* pdf) {
   }
   return rs;
 }
-float glosstrans_brdf(const FP& p) {
-  const float power = if_reflect(p.n, p.in, p.out) ? p.refl : 1.0f - p.refl;
+Real glosstrans_brdf(const FP& p) {
+  const Real power = if_reflect(p.n, p.in, p.out) ? p.refl : 1.0f - p.refl;
   const V in = p.in;
   const V N = facing(p.n, in);
   V out = p.out;
   if (dot(out, N) < 0) out = reflect_by_n(out, N);
-  constexpr float small = 1e-10;
+  constexpr Real small = 1e-10;
   if (dot(in, N) > -small || dot(out, N) < small) return 0.0f;
-  const float alpha = p.rough;
+  const Real alpha = p.rough;
   const V h = normalized(-in + out);
-  const float ccs = dot(h, N);
+  const Real ccs = dot(h, N);
   if (ccs < small || dot(h, in) > -small || dot(h, out) < small) return 0.0f;
-  const float dd = 1.0001f - (1.0f - alpha * alpha) * ccs * ccs;
-  const float D = std::max(sMin, (alpha * alpha) / (PI * (dd * dd)));  // pow(x, 2.0f): folded to x * x
-  const float lc = std::max(0.0f, std::min(0.9999f, dot(in, -N)));
-  const float lv = std::max(0.0f, std::min(0.9999f, dot(out, N)));
+  const Real dd = 1.0001f - (1.0f - alpha * alpha) * ccs * ccs;
+  const Real D = std::max(sMin, (alpha * alpha) / (PI * (dd * dd)));  // pow(x, 2.0f): folded to x * x
+  const Real lc = std::max<Real>(0.0f, std::min<Real>(0.9999f, dot(in, -N)));
+  const Real lv = std::max<Real>(0.0f, std::min<Real>(0.9999f, dot(out, N)));
   if (lc < sMin || lv < sMin) return 0.0f;
-  const float L_l = (-1.0f + std::sqrt(1.0f + alpha * alpha * (1.0f / (lc * lc) - 1.0))) * 0.5;
-  const float L_v = (-1.0f + std::sqrt(1.0f + alpha * alpha * (1.0f / (lv * lv) - 1.0))) * 0.5;
-  const float G = 1.0f / ((1.0f + L_l) * (1.0f + L_v));
-  const float fx = (4.0f * dot(in, -N) * dot(out, N));
+  const Real L_l = (-1.0f + std::sqrt(1.0f + alpha * alpha * (1.0f / (lc * lc) - 1.0))) * 0.5;
+  const Real L_v = (-1.0f + std::sqrt(1.0f + alpha * alpha * (1.0f / (lv * lv) - 1.0))) * 0.5;
+  const Real G = 1.0f / ((1.0f + L_l) * (1.0f + L_v));
+  const Real fx = (4.0f * dot(in, -N) * dot(out, N));
   return power * (G * D) / fx;
 }
-float glosstrans_pdf(const FP& p) {
+Real glosstrans_pdf(const FP& p) {
   if (if_reflect(p.n, p.in, p.out)) return p.refl * ggx_pdf(p.out, p.n, p.in, p.rough);
   return (1.0f - p.refl) * ggx_pdf(reflect_by_n(p.out, p.n), p.n, p.in, p.rough);
 }
 
 // Surface virtual interface (material.h:137-146) over the eight surfaces.
-V surf_sample(int type, Rng& mt, const FP& p, float* pdf) {
+V surf_sample(int type, Rng& mt, const FP& p, Real* pdf) {
   switch (type) {
     case 0: return cos_sampling(mt, p.n, pdf);                          // DiffuseSurface (material.h:165-167)
     case 1: *pdf = 1.0f; return reflect(p.n, p.in);                     // MetalSurface (material.h:398-403)
@@ -680,7 +735,7 @@ V surf_sample(int type, Rng& mt, const FP& p, float* pdf) {
     default: return difftrans_sample(mt, p, pdf);
   }
 }
-float surf_brdf(int type, const FP& p) {
+Real surf_brdf(int type, const FP& p) {
   switch (type) {
     case 0: return opaque_reflect(p) ? 1.0f / PI : 0.0f;  // material.h:168-173
     case 1: {                                             // material.h:404-415
@@ -697,7 +752,7 @@ float surf_brdf(int type, const FP& p) {
     default: return difftrans_brdf(p);
   }
 }
-float surf_pdf(int type, const FP& p) {
+Real surf_pdf(int type, const FP& p) {
   switch (type) {
     case 0: return std::max(sMin, dot(p.out, p.n) / PI);  // material.h:174-176
     case 1: return dot(reflect(p.n, p.in), p.out) > 1.0f - 1.0f / 1.0f ? 1.0f : sMin;  // material.h:416-424
@@ -713,21 +768,21 @@ float surf_pdf(int type, const FP& p) {
 // ------------------------------------------------------------- renderer
 struct Geometry {  // SPPM.h:56-68
   V pos, normal;
-  float uvx, uvy;
+  Real uvx, uvy;
   const Material* m;
   V albedo, radiance;
-  float rough, translucency;
+  Real rough, translucency;
 };
 struct HitPoint {  // SPPM.h:83-110
   int type = 0;    // 0 NONE, 1 HIT, 2 ONLY_DIRECTLIGHT
   V pos, normal, out, weight;
   V dl;            // DirectLight: environment light at the path's end
-  float rough = 0;
+  Real rough = 0;
   int facet = -1;
   const Material* m = nullptr;
 };
-struct Photon { V pos, flux, dir; float index, pdf; bool valid = false; };  // SPPM.h:128-143
-struct Shared { V rad; int n = 0; float r = 0; int g = 0; V dl; int ndl = 0; };  // SPPM.h:112-126
+struct Photon { V pos, flux, dir; Real index, pdf; bool valid = false; };  // SPPM.h:128-143
+struct Shared { V rad; int n = 0; Real r = 0; int g = 0; V dl; int ndl = 0; };  // SPPM.h:112-126
 
 struct KdNode { int photon, axis, left, right; };
 
@@ -742,8 +797,17 @@ struct Renderer {
   Texture ibl;            // environment map, converted as LightSampler.cpp:24 does
   bool has_ibl = false;
   int P = 0;
-  float alpha = 0.9f, r0 = 0.015f;
+  Real alpha = 0.9f, r0 = 0.015f;
   bool fix_stale = false;
+  bool watertight = false;  // FR_FLAG_WATERTIGHT: the watertight triangle test
+  // FR_FLAG_END_DEGENERATE_PATHS: end a path whose sampled BSDF value or pdf
+  // is NaN or whose pdf is zero, and a photon path whose flux or PDF product
+  // is no longer finite.
+  bool end_degenerate = false;
+  uint32_t stream_key = 0x5350504Du;  // second Philox key word of every stream
+  // Pixels the eye pass and the gather cover: [x0, x1) x [y0, y1); the rest
+  // get no hitpoint (for oracle images of a window of the frame).
+  int win_x0 = 0, win_y0 = 0, win_x1 = 1 << 30, win_y1 = 1 << 30;
   int step = 0;
   long long total_photons = 0;
   std::vector<Shared> sp;
@@ -761,15 +825,15 @@ struct Renderer {
   long long ray_stride = 0;
   size_t ray_cap = 0;
   mutable std::mutex ray_mu;
-  mutable std::vector<float> ray_sample;
+  mutable std::vector<Real> ray_sample;
 
   bool trace(const Ray& r, Hit& h, int pass) const {
     if (ray_stride > 0 && ray_count.fetch_add(1) % ray_stride == 0) {
       std::lock_guard<std::mutex> lock(ray_mu);
       if (ray_sample.size() < ray_cap * 8)
-        ray_sample.insert(ray_sample.end(), {r.o.x, r.o.y, r.o.z, r.d.x, r.d.y, r.d.z, r.index, (float)pass});
+        ray_sample.insert(ray_sample.end(), {r.o.x, r.o.y, r.o.z, r.d.x, r.d.y, r.d.z, r.index, (Real)pass});
     }
-    return closest(bvh, F, r, h);
+    return closest(bvh, F, r, h, watertight);
   }
 
   // calculateGeometry (SPPM.cpp:36-77)
@@ -786,10 +850,10 @@ struct Renderer {
     g.rough = m.roughness;
     g.translucency = 0.0f;
     if (norm2(g.radiance) > 1e-6) g.albedo = V(1, 1, 1);
-    float c[4];
+    Real c[4];
     if (m.tex_rough >= 0) {
       tex_sample(texs[m.tex_rough], g.uvx, g.uvy, c);
-      g.rough = std::min(0.8f, std::max(0.05f, 0.5f * c[0]));
+      g.rough = std::min<Real>(0.8f, std::max<Real>(0.05f, 0.5f * c[0]));
     }
     if (m.tex_albedo >= 0) {
       tex_sample(texs[m.tex_albedo], g.uvx, g.uvy, c);
@@ -805,11 +869,11 @@ struct Renderer {
       const V e1 = std::abs(e2.y) > 0.9 ? cross(e2, V(1, 0, 0)) : cross(e2, V(0, 1, 0));
       const V e3 = normalized(cross(e1, e2));
       // CreateMatrixFromColumns({e1, e2, e3}).inv() (Matrix.h:180-184, Matrix.cpp:22-34)
-      const float M[3][3] = {{e1.x, e2.x, e3.x}, {e1.y, e2.y, e3.y}, {e1.z, e2.z, e3.z}};
-      float C[3][3];
+      const Real M[3][3] = {{e1.x, e2.x, e3.x}, {e1.y, e2.y, e3.y}, {e1.z, e2.z, e3.z}};
+      Real C[3][3];
       for (int r = 0; r < 3; ++r)
         for (int col = 0; col < 3; ++col) {
-          float m2[2][2];
+          Real m2[2][2];
           for (int i = 0, rr = 0; i < 3; ++i) {
             if (i == r) continue;
             for (int j = 0, cc = 0; j < 3; ++j) {
@@ -820,8 +884,8 @@ struct Renderer {
           }
           C[r][col] = (m2[0][0] * m2[1][1] - m2[0][1] * m2[1][0]) * ((r + col) % 2 ? -1 : 1);
         }
-      const float det = M[0][0] * C[0][0] + M[1][0] * C[1][0] + M[2][0] * C[2][0];
-      const float ix = 1.0f / det;
+      const Real det = M[0][0] * C[0][0] + M[1][0] * C[1][0] + M[2][0] * C[2][0];
+      const Real ix = 1.0f / det;
       V rows[3];
       for (int i = 0; i < 3; ++i) rows[i] = V(ix * C[0][i], ix * C[1][i], ix * C[2][i]);
       g.normal = normalized(V(dot(rows[0], nm), dot(rows[1], nm), dot(rows[2], nm)));
@@ -829,38 +893,38 @@ struct Renderer {
   }
 
   // Camera::SampleCameraRay (Camera.h:73-83 pinhole, 103-129 thin lens)
-  Ray camera_ray(float u, float v, Rng& mt, float& pdf) const {
-    const float s0 = mt.real(), s1 = mt.real(), s2 = mt.real();
+  Ray camera_ray(Real u, Real v, Rng& mt, Real& pdf) const {
+    const Real s0 = mt.real(), s1 = mt.real(), s2 = mt.real();
     if (cam.type == 0) {
-      const V off = V(s0, s1, s2) * V(cam.pw, cam.ph, 0) / V((float)cam.W, (float)cam.H, 1.0f);
+      const V off = V(s0, s1, s2) * V(cam.pw, cam.ph, 0) / V((Real)cam.W, (Real)cam.H, 1.0f);
       const V image = cam.pos - cam.dir * cam.dist + (u - 0.5f + off.x) * cam.e1 * cam.pw + (v - 0.5f + off.y) * cam.e2 * cam.ph;
       pdf = 1.0f;
       return Ray{image, normalized(normalized(cam.pos - image)), 1.0f};
     }
-    const float pdf_area = 1.0f / (cam.lw * cam.lh);
+    const Real pdf_area = 1.0f / (cam.lw * cam.lh);
     const V lens = cam.pos + (s0 - 0.5f) * cam.e1 * cam.lw + (s1 - 0.5f) * cam.e2 * cam.lh;
     const V image = cam.pos - cam.dir * cam.dist + (u - 0.5f) * cam.e1 * cam.pw + (v - 0.5f) * cam.e2 * cam.ph;
-    const float A = cam.dist, B = (A * cam.F) / (A - cam.F);
+    const Real A = cam.dist, B = (A * cam.F) / (A - cam.F);
     const V target = image + (cam.pos - image) * (A + B) / A;
-    const float cs = dot(cam.dir, normalized(lens - image));
-    const float d2 = norm2(lens - image);
+    const Real cs = dot(cam.dir, normalized(lens - image));
+    const Real d2 = norm2(lens - image);
     pdf = pdf_area * (d2 / cam.F / cam.F) / cs;
     return Ray{lens, normalized(normalized(target - lens)), 1.0f};
   }
 
-  static bool near1(float s) { return std::abs(s - 1.0f) < 0.00001; }  // SPPM.h:27-29
+  static bool near1(Real s) { return std::abs(s - 1.0f) < 0.00001; }  // SPPM.h:27-29
 
   // IBL::GetIBLColorFromDirection (IBL.h:122-129) with the SPHERE mapping of
   // GetUVFromDirection (IBL.h:96-104): acos of a float is the double ::acos.
   V ibl_color(V dir) const {
-    float u = 0.0f, v = 0.0f;
+    Real u = 0.0f, v = 0.0f;
     if (!(std::abs(dir.x) < 1e-6 && std::abs(dir.z) < 1e-6)) {
       const V xz = normalized(V(dir.x, 0.0f, dir.z));
       const double ax = ::acos((double)xz.x);
-      u = (float)((xz.z >= 0 ? ax : (double)(2.0f * PI) - ax) / (double)(2.0f * PI));
-      v = (float)(::acos((double)dir.y) / (double)PI);
+      u = (Real)((xz.z >= 0 ? ax : (double)(2.0f * PI) - ax) / (double)(2.0f * PI));
+      v = (Real)(::acos((double)dir.y) / (double)PI);
     }
-    float c[4];
+    Real c[4];
     tex_sample(ibl, u, v, c);
     return V(c[0], c[1], c[2]);
   }
@@ -869,12 +933,12 @@ struct Renderer {
   // after it reaches the image without an environment light).
   HitPoint eye(int i) const {
     const int W = cam.W, H = cam.H;
-    Rng mt((uint32_t)i + (uint32_t)(W * H) * (uint32_t)step);  // SPPM.cpp:334
+    Rng mt((uint32_t)i + (uint32_t)(W * H) * (uint32_t)step, stream_key);  // SPPM.cpp:334
     const int w = i % W, h = i / W;
-    const float u = w / (float)W, v = h / (float)H;
-    float cam_pdf = 1.0f;
+    const Real u = w / (Real)W, v = h / (Real)H;
+    Real cam_pdf = 1.0f;
     Ray cur = camera_ray(u, v, mt, cam_pdf), nxt = cur;
-    float PDF = 1.0f;
+    Real PDF = 1.0f;
     V thr(1, 1, 1);
     int depth = 0;
     HitPoint hp;
@@ -882,7 +946,7 @@ struct Renderer {
     while (true) {
       if (depth > 6) break;
       if (depth > 4) {
-        const float rus = std::exp(4 - depth);
+        const Real rus = std::exp(4 - depth);
         if (mt.real() > rus) break;
         PDF *= rus;
       }
@@ -917,11 +981,11 @@ struct Renderer {
         // nothing after the hitpoint reaches the image.
         if (!has_ibl) return hp;
       }
-      float Ii, Io;
+      Real Ii, Io;
       if (near1(cur.index)) { Ii = 1.0f; Io = g.m->index; }
       else { Ii = cur.index; Io = 1.0f; }
       FP p{cur.d, nxt.d, g.normal, Ii, Io, g.rough, g.m->extinction, g.m->reflectance};
-      float pdf = 1.0f;
+      Real pdf = 1.0f;
       nxt.d = surf_sample(g.m->type, mt, p, &pdf);
       if (!valid_dir(nxt.d)) break;
       if (g.m->opaque) {
@@ -933,10 +997,11 @@ struct Renderer {
       pdf = surf_pdf(g.m->type, p);
       const V on = dot(g.normal, nxt.d) > 0 ? g.normal : -g.normal;
       nxt.o = nxt.o + on * RAY_OFFSET;
-      const float brdf = surf_brdf(g.m->type, p);
-      const float cs = std::max(0.0f, std::min(1.0f, dot(nxt.d, on)));
+      const Real brdf = surf_brdf(g.m->type, p);
+      const Real cs = std::max<Real>(0.0f, std::min<Real>(1.0f, dot(nxt.d, on)));
       if (brdf < 1e-8) break;
       if (pdf < 0) break;
+      if (end_degenerate && !(brdf >= 1e-8 && pdf > 0)) break;
       thr = thr * (g.albedo * cs * brdf);
       PDF *= pdf;
       cur = nxt;
@@ -948,13 +1013,13 @@ struct Renderer {
 
   // createPhotonMap body for path i (SPPM.cpp:508-673)
   void photon_path(int i) {
-    Rng mt((uint32_t)i + 135u + (uint32_t)step * (uint32_t)P);  // SPPM.cpp:520
+    Rng mt((uint32_t)i + 135u + (uint32_t)step * (uint32_t)P, stream_key);  // SPPM.cpp:520
     Photon* arr = &slots[(size_t)i * SLOTS];
     // generateLightRay (SPPM.cpp:453-471)
     const Light& L = lights[light_table.sample(mt)];
     V pos, rad;
-    float pdf_area;
-    const float area = 0.5f * norm(cross(L.f.p[1] - L.f.p[0], L.f.p[2] - L.f.p[0]));
+    Real pdf_area;
+    const Real area = 0.5f * norm(cross(L.f.p[1] - L.f.p[0], L.f.p[2] - L.f.p[0]));
     if (L.textured) {  // SamplePointOnAreaLight (LightSampler.cpp:68-75)
       const int e = L.table.sample(mt);
       const V w = L.uvw[e];
@@ -962,7 +1027,7 @@ struct Renderer {
       rad = L.L[e];
       pdf_area = (L.table.pdf(e) * NUM_SAMPLE) / area;
     } else {  // PointOnTriangle (Sampling.cpp:339-349), LightSampler.cpp:76-79
-      float u = mt.real(), v = mt.real();
+      Real u = mt.real(), v = mt.real();
       if (v > u) { u *= 0.5f; v -= u; }
       else { v *= 0.5f; u -= v; }
       pdf_area = 2.0f / std::abs(norm(cross(L.f.p[1] - L.f.p[0], L.f.p[2] - L.f.p[0])));
@@ -971,12 +1036,12 @@ struct Renderer {
     }
     pdf_area *= light_table.pdf((int)(&L - &lights[0]));
     const V ln = normalized(L.f.n[0] + L.f.n[1] + L.f.n[2]);
-    float pdf_dir = 1.0f;
+    Real pdf_dir = 1.0f;
     const V od = cos_sampling(mt, ln, &pdf_dir);
-    rad = rad * std::min(1.0f, std::max(0.0f, dot(ln, od)));
+    rad = rad * std::min<Real>(1.0f, std::max<Real>(0.0f, dot(ln, od)));
     Ray cur{pos + ln * RAY_OFFSET, normalized(od), 1.0f}, nxt = cur;
     const V flux = rad;
-    float PDF = pdf_area * pdf_dir;
+    Real PDF = pdf_area * pdf_dir;
     V thr(1, 1, 1);
     arr[0] = Photon{cur.o, flux * thr * PI, cur.d, cur.index, PDF, true};
     int k = 0, loop = 0, depth = 0;
@@ -998,15 +1063,15 @@ struct Renderer {
       // russianRulette_PhotonMapping (SPPM.h:33-52)
       if (depth > 16) break;
       const V a = g.albedo;
-      const float pdf_rus = 0.98f * (a.x > a.y ? (a.x > a.z ? a.x : a.z) : (a.y > a.z ? a.y : a.z));
+      const Real pdf_rus = 0.98f * (a.x > a.y ? (a.x > a.z ? a.x : a.z) : (a.y > a.z ? a.y : a.z));
       if (mt.real() > pdf_rus) break;
       PDF *= pdf_rus;
-      float Ii, Io;
+      Real Ii, Io;
       if (near1(cur.index)) { Ii = 1.0f; Io = g.m->index; }
       else { Ii = cur.index; Io = 1.0f; }
       FP p{cur.d, nxt.d, g.normal, Ii, Io, g.rough, g.m->extinction, g.m->reflectance};
       if (g.m->sppm) arr[k++] = Photon{g.pos, flux * thr * g.albedo, cur.d, cur.index, PDF, true};
-      float pdf = 1.0f;
+      Real pdf = 1.0f;
       nxt.d = surf_sample(g.m->type, mt, p, &pdf);
       if (!valid_dir(nxt.d)) break;
       if (g.m->opaque) {
@@ -1018,12 +1083,17 @@ struct Renderer {
       pdf = surf_pdf(g.m->type, p);
       const V on = dot(g.normal, nxt.d) > 0 ? g.normal : -g.normal;
       nxt.o = nxt.o + on * RAY_OFFSET;
-      const float brdf = surf_brdf(g.m->type, p);
-      const float cs = std::max(0.0f, std::min(1.0f, dot(nxt.d, on)));
+      const Real brdf = surf_brdf(g.m->type, p);
+      const Real cs = std::max<Real>(0.0f, std::min<Real>(1.0f, dot(nxt.d, on)));
       if (brdf < 1e-8) break;
       if (pdf < 0) break;
+      if (end_degenerate && !(brdf >= 1e-8 && pdf > 0)) break;
       thr = thr * (g.albedo * cs * brdf);
       PDF *= pdf;
+      if (end_degenerate) {
+        const V f = flux * thr;
+        if (!(std::isfinite(PDF) && std::isfinite(f.x) && std::isfinite(f.y) && std::isfinite(f.z))) break;
+      }
       cur = nxt;
       ++depth;
     }
@@ -1035,7 +1105,7 @@ struct Renderer {
   // Median-split kd-tree over photons (replaces kdtree.h:348-431).
   int kd_build(std::vector<int>& ids, int lo, int hi) {
     if (lo >= hi) return -1;
-    float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+    Real mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
     for (int i = lo; i < hi; ++i)
       for (int a = 0; a < 3; ++a) {
         mn[a] = std::min(mn[a], photons[ids[i]].pos[a]);
@@ -1059,7 +1129,7 @@ struct Renderer {
   // GetElementsInsideBox (kdtree.h:457-482) then the sphere filter
   // (SPPM.cpp:432); left subtree holds coordinates <= the split.
   template <typename Fn>
-  void query(int node, V bmin, V bmax, V x, float R2, Fn&& fn) const {
+  void query(int node, V bmin, V bmax, V x, Real R2, Fn&& fn) const {
     if (node < 0) return;
     const KdNode& n = kd[node];
     const Photon& p = photons[n.photon];
@@ -1095,7 +1165,10 @@ struct Renderer {
     kd_build(ids, 0, (int)ids.size());
     // Eye pass (SPPM.cpp:776-779, 836).
 #pragma omp parallel for schedule(dynamic, 64)
-    for (int i = 0; i < npix; ++i) hp[i] = eye(i);
+    for (int i = 0; i < npix; ++i) {
+      const int x = i % cam.W, y = i / cam.W;
+      hp[i] = (x >= win_x0 && x < win_x1 && y >= win_y0 && y < win_y1) ? eye(i) : HitPoint();
+    }
     // Gather and update (applyHitPointInfo, SPPM.cpp:395-451).
 #pragma omp parallel for schedule(dynamic, 64)
     for (int v = 0; v < npix; ++v) {
@@ -1114,8 +1187,8 @@ struct Renderer {
       int m = 0;
       query(kd.empty() ? -1 : 0, bmin, bmax, h.pos, s.r * s.r, [&](int j) {
         const Photon& p = photons[j];
-        const float Ii = p.index;
-        const float Io = near1(p.index) ? h.m->index : 1.0f;
+        const Real Ii = p.index;
+        const Real Io = near1(p.index) ? h.m->index : 1.0f;
         const V nn = dot(p.dir, h.normal) < 0 ? h.normal : -h.normal;
         const FP fp{p.dir, h.out, nn, Ii, Io, h.rough, h.m->extinction, h.m->reflectance};
         add = add + h.weight * surf_brdf(h.m->type, fp) * p.flux / p.pdf;
@@ -1124,7 +1197,7 @@ struct Renderer {
       gather_m[v] = m;
       gather_phi[v] = add;
       if (m > 0) {
-        const float a = s.n + alpha * m, b = (float)(s.n + m);
+        const Real a = s.n + alpha * m, b = (Real)(s.n + m);
         s.rad = (s.rad + add) * a / b;
         s.r *= std::sqrt(a / b);
         s.n += m * alpha;
@@ -1135,12 +1208,12 @@ struct Renderer {
   }
 
   // reconstructImageFromSharedPoints (SPPM.cpp:473-493)
-  void resolve(float* out) const {
+  void resolve(Real* out) const {
     const int npix = cam.W * cam.H;
     for (int i = 0; i < npix; ++i) {
       const Shared& s = sp[i];
-      const float d = ((float)total_photons * (s.g + 0.0001f) / (0.0001f + (float)step)) * PI * s.r * s.r;
-      const V L = s.dl / (float)(s.ndl + 0.0001f) + s.rad / d;
+      const Real d = ((Real)total_photons * (s.g + 0.0001f) / (0.0001f + (Real)step)) * PI * s.r * s.r;
+      const V L = s.dl / (Real)(s.ndl + 0.0001f) + s.rad / d;
       out[4 * i] = std::pow(L.x, 1.0f / 1.2f);
       out[4 * i + 1] = std::pow(L.y, 1.0f / 1.2f);
       out[4 * i + 2] = std::pow(L.z, 1.0f / 1.2f);
@@ -1150,8 +1223,8 @@ struct Renderer {
 };
 
 // QRandSequence::HaltonCore (QRandSequence.h:10-25)
-float halton(int n, int B) {
-  float result = 0.0f;
+Real halton(int n, int B) {
+  Real result = 0.0f;
   if (n <= 0) return result;
   const int keta = std::log2(n) / std::log2(B) + 1;
   for (int i = 0; i < keta; ++i) {
@@ -1167,6 +1240,8 @@ using namespace port;
 
 extern "C" {
 
+// Material and camera parameters stay float in every build (the scene's own
+// values); arrays and scalars of the calls below are Real.
 struct port_material {
   int32_t type, sppm, opaque, tex_albedo, tex_rough, tex_bump;
   float albedo[3], emission[3], index, roughness, extinction, reflectance;
@@ -1176,9 +1251,9 @@ struct port_camera {
   float pos[3], target[3], fov, focal, dist, aspect, lens;
 };
 
-void* port_create(int32_t T, const float* pos, const float* nrm, const float* uv, const int32_t* mat, int32_t nm,
+void* port_create(int32_t T, const Real* pos, const Real* nrm, const Real* uv, const int32_t* mat, int32_t nm,
                   const port_material* mats, int32_t nt, const int32_t* tex_wh, const uint8_t* const* texels,
-                  const port_camera* c, int32_t photons, float alpha, float r0, int32_t fix_stale) {
+                  const port_camera* c, int32_t photons, Real alpha, Real r0, int32_t fix_stale) {
   Renderer* r = new Renderer();
   r->F.resize(T);
   for (int t = 0; t < T; ++t) {
@@ -1205,25 +1280,25 @@ void* port_create(int32_t T, const float* pos, const float* nrm, const float* uv
     r->texs.push_back(std::move(tx));
   }
   // Scene::CreateScene lights (Scene.cpp:145-154), LightSampler (LightSampler.cpp:6-66).
-  std::vector<float> fl;
+  std::vector<Real> fl;
   for (int t = 0; t < T; ++t) {
     const Material& m = r->mats[r->F[t].attr];
     if (!(m.radiance.x + m.radiance.y + m.radiance.z > 0.00001f)) continue;
     Light L;
     L.f = r->F[t];
     const Facet& f = L.f;
-    const float area = 0.5f * norm(cross(f.p[1] - f.p[0], f.p[2] - f.p[0]));
+    const Real area = 0.5f * norm(cross(f.p[1] - f.p[0], f.p[2] - f.p[0]));
     if (m.tex_albedo >= 0) {
       L.textured = true;
       V total(0, 0, 0);
-      std::vector<float> vals;
+      std::vector<Real> vals;
       for (int i = 0; i < NUM_SAMPLE; ++i) {
-        V w(i / (float)NUM_SAMPLE, halton(i, 2), halton(i, 3));
+        V w(i / (Real)NUM_SAMPLE, halton(i, 2), halton(i, 3));
         if (w.y > w.x) { w.x *= 0.5f; w.y -= w.x; }
         else { w.y *= 0.5f; w.x -= w.y; }
-        const float u = w.x * f.uv[0][0] + w.y * f.uv[1][0] + (1.0f - w.x - w.y) * f.uv[2][0];
-        const float v = w.x * f.uv[0][1] + w.y * f.uv[1][1] + (1.0f - w.x - w.y) * f.uv[2][1];
-        float c4[4];
+        const Real u = w.x * f.uv[0][0] + w.y * f.uv[1][0] + (1.0f - w.x - w.y) * f.uv[2][0];
+        const Real v = w.x * f.uv[0][1] + w.y * f.uv[1][1] + (1.0f - w.x - w.y) * f.uv[2][1];
+        Real c4[4];
         tex_sample(r->texs[m.tex_albedo], u, v, c4);
         V l = V(c4[0], c4[1], c4[2]) * m.radiance;
         if (norm2(l) < 0.01f) l = V(0, 0, 0);
@@ -1235,7 +1310,7 @@ void* port_create(int32_t T, const float* pos, const float* nrm, const float* uv
         L.L[0] = 1e-6 * V(1, 1, 1);
         L.uvw[0] = V(0, 0, 0);
       } else {
-        total = total * (2.0f * PI * area / (float)NUM_SAMPLE);
+        total = total * (2.0f * PI * area / (Real)NUM_SAMPLE);
       }
       for (int i = 0; i < NUM_SAMPLE; ++i) vals.push_back(norm(L.L[i]));
       L.table.init(vals);
@@ -1303,13 +1378,28 @@ void port_sample_rays(void* h, int64_t stride, int64_t cap) {
   r->ray_sample.clear();
 }
 // Copies the kept rays (8 floats each) to out when out is not NULL; returns their count.
-int64_t port_read_ray_sample(void* h, float* out) {
+int64_t port_read_ray_sample(void* h, Real* out) {
   Renderer* r = static_cast<Renderer*>(h);
-  if (out) std::memcpy(out, r->ray_sample.data(), r->ray_sample.size() * sizeof(float));
+  if (out) std::memcpy(out, r->ray_sample.data(), r->ray_sample.size() * sizeof(Real));
   return (int64_t)(r->ray_sample.size() / 8);
 }
 
 void port_seek(void* h, int32_t first_step) { static_cast<Renderer*>(h)->step = first_step; }
+
+// The precision mode's watertight triangle test (FR_FLAG_WATERTIGHT) on or off.
+void port_set_watertight(void* h, int32_t on) { static_cast<Renderer*>(h)->watertight = on != 0; }
+
+// FR_FLAG_END_DEGENERATE_PATHS on or off.
+void port_set_end_degenerate(void* h, int32_t on) { static_cast<Renderer*>(h)->end_degenerate = on != 0; }
+
+// Second Philox key word of every stream (default 0x5350504D).
+void port_set_stream_key(void* h, uint32_t key) { static_cast<Renderer*>(h)->stream_key = key; }
+
+// Eye pass and gather only for pixels [x0, x1) x [y0, y1).
+void port_set_window(void* h, int32_t x0, int32_t y0, int32_t x1, int32_t y1) {
+  Renderer* r = static_cast<Renderer*>(h);
+  r->win_x0 = x0; r->win_y0 = y0; r->win_x1 = x1; r->win_y1 = y1;
+}
 
 // Photon pass only (for a bounded CPU timing sample).
 void port_photon_pass(void* h, int32_t first, int32_t count) {
@@ -1318,16 +1408,16 @@ void port_photon_pass(void* h, int32_t first, int32_t count) {
   for (int i = first; i < first + count; ++i) r->photon_path(i);
 }
 
-void port_resolve(void* h, float* out) { static_cast<Renderer*>(h)->resolve(out); }
+void port_resolve(void* h, Real* out) { static_cast<Renderer*>(h)->resolve(out); }
 
-void port_trace_closest(void* h, const float* rays, int32_t n, int32_t* facet, float* tuv) {
+void port_trace_closest(void* h, const Real* rays, int32_t n, int32_t* facet, Real* tuv) {
   Renderer* r = static_cast<Renderer*>(h);
 #pragma omp parallel for schedule(dynamic, 64)
   for (int i = 0; i < n; ++i) {
-    const float* q = rays + 7 * (size_t)i;
+    const Real* q = rays + 7 * (size_t)i;
     Ray ray{vp(q), vp(q + 3), q[6]};
     Hit hit;
-    if (closest(r->bvh, r->F, ray, hit)) {
+    if (closest(r->bvh, r->F, ray, hit, r->watertight)) {
       facet[i] = hit.facet;
       tuv[3 * i] = hit.t; tuv[3 * i + 1] = hit.u; tuv[3 * i + 2] = hit.v;
     } else {
@@ -1337,25 +1427,25 @@ void port_trace_closest(void* h, const float* rays, int32_t n, int32_t* facet, f
   }
 }
 
-void port_trace_any(void* h, const float* rays, int32_t n, int32_t* hit) {
+void port_trace_any(void* h, const Real* rays, int32_t n, int32_t* hit) {
   Renderer* r = static_cast<Renderer*>(h);
 #pragma omp parallel for schedule(dynamic, 64)
   for (int i = 0; i < n; ++i) {
-    const float* q = rays + 8 * (size_t)i;
-    hit[i] = any_hit(r->bvh, r->F, Ray{vp(q), vp(q + 3), 1.0f}, q[6], q[7]) ? 1 : 0;
+    const Real* q = rays + 8 * (size_t)i;
+    hit[i] = any_hit(r->bvh, r->F, Ray{vp(q), vp(q + 3), 1.0f}, q[6], q[7], r->watertight) ? 1 : 0;
   }
 }
 
 // Hitpoints of the last iteration: type, facet; pos/nrm/out/w (3 floats each), rough.
-void port_read_hitpoints(void* h, int32_t* type, int32_t* facet, float* pos, float* nrm, float* out, float* w,
-                         float* rough) {
+void port_read_hitpoints(void* h, int32_t* type, int32_t* facet, Real* pos, Real* nrm, Real* out, Real* w,
+                         Real* rough) {
   Renderer* r = static_cast<Renderer*>(h);
   for (size_t i = 0; i < r->hp.size(); ++i) {
     const HitPoint& p = r->hp[i];
     type[i] = p.type;
     facet[i] = p.facet;
     const V* src[4] = {&p.pos, &p.normal, &p.out, &p.weight};
-    float* dst[4] = {pos, nrm, out, w};
+    Real* dst[4] = {pos, nrm, out, w};
     for (int k = 0; k < 4; ++k) { dst[k][3 * i] = src[k]->x; dst[k][3 * i + 1] = src[k]->y; dst[k][3 * i + 2] = src[k]->z; }
     rough[i] = p.rough;
   }
@@ -1364,11 +1454,11 @@ void port_read_hitpoints(void* h, int32_t* type, int32_t* facet, float* pos, flo
 int64_t port_num_photons(void* h) { return (int64_t) static_cast<Renderer*>(h)->photons.size(); }
 
 // Compacted photons of the last iteration: N x 11 {pos, flux, dir, index, pdf}, path, slot.
-void port_read_photons(void* h, float* ph, int32_t* path, int32_t* slot) {
+void port_read_photons(void* h, Real* ph, int32_t* path, int32_t* slot) {
   Renderer* r = static_cast<Renderer*>(h);
   for (size_t i = 0; i < r->photons.size(); ++i) {
     const Photon& p = r->photons[i];
-    float* d = ph + 11 * i;
+    Real* d = ph + 11 * i;
     d[0] = p.pos.x; d[1] = p.pos.y; d[2] = p.pos.z;
     d[3] = p.flux.x; d[4] = p.flux.y; d[5] = p.flux.z;
     d[6] = p.dir.x; d[7] = p.dir.y; d[8] = p.dir.z;
@@ -1378,7 +1468,7 @@ void port_read_photons(void* h, float* ph, int32_t* path, int32_t* slot) {
   }
 }
 
-void port_read_gather(void* h, int32_t* m, float* phi) {
+void port_read_gather(void* h, int32_t* m, Real* phi) {
   Renderer* r = static_cast<Renderer*>(h);
   for (size_t i = 0; i < r->gather_m.size(); ++i) {
     m[i] = r->gather_m[i];
@@ -1396,14 +1486,14 @@ void port_set_ibl(void* h, int32_t w, int32_t hh, const uint8_t* texels) {
   r->ibl.c.resize((size_t)w * hh * 4);
   for (size_t i = 0; i < (size_t)w * hh; ++i)
     for (int k = 0; k < 4; ++k) {
-      const float c = k < 3 ? texels[4 * i + k] / 255.0f : 0.0f;
+      const Real c = k < 3 ? texels[4 * i + k] / 255.0f : 0.0f;
       r->ibl.c[4 * i + k] = 0.4f * (c * c);
     }
   r->has_ibl = true;
 }
 
 // Per-hitpoint direct light of the last iteration and per-pixel sums and counts.
-void port_read_direct(void* h, float* hp_dl, float* sp_dl, int32_t* sp_ndl) {
+void port_read_direct(void* h, Real* hp_dl, Real* sp_dl, int32_t* sp_ndl) {
   Renderer* r = static_cast<Renderer*>(h);
   for (size_t i = 0; i < r->sp.size(); ++i) {
     const HitPoint& p = r->hp[i];
@@ -1414,7 +1504,7 @@ void port_read_direct(void* h, float* hp_dl, float* sp_dl, int32_t* sp_ndl) {
   }
 }
 
-void port_read_state(void* h, float* rad, int32_t* n, float* rr, int32_t* g) {
+void port_read_state(void* h, Real* rad, int32_t* n, Real* rr, int32_t* g) {
   Renderer* r = static_cast<Renderer*>(h);
   for (size_t i = 0; i < r->sp.size(); ++i) {
     const Shared& s = r->sp[i];
@@ -1426,7 +1516,7 @@ void port_read_state(void* h, float* rad, int32_t* n, float* rr, int32_t* g) {
 }
 
 // Radius query over given hitpoints (x, y, z, R) and photons (x, y, z): counts.
-void port_radius_count(const float* hp, int32_t nh, const float* ph, int32_t np, int32_t* counts) {
+void port_radius_count(const Real* hp, int32_t nh, const Real* ph, int32_t np, int32_t* counts) {
   Renderer r;
   r.photons.resize(np);
   for (int i = 0; i < np; ++i) r.photons[i].pos = vp(ph + 3 * (size_t)i);
@@ -1437,7 +1527,7 @@ void port_radius_count(const float* hp, int32_t nh, const float* ph, int32_t np,
 #pragma omp parallel for schedule(dynamic, 64)
   for (int i = 0; i < nh; ++i) {
     const V x = vp(hp + 4 * (size_t)i);
-    const float R = hp[4 * (size_t)i + 3];
+    const Real R = hp[4 * (size_t)i + 3];
     int m = 0;
     r.query(r.kd.empty() ? -1 : 0, x - R * V(1, 1, 1), x + R * V(1, 1, 1), x, R * R, [&](int) { ++m; });
     counts[i] = m;

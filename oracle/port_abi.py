@@ -27,23 +27,31 @@ class PortCamera(C.Structure):
                 ('lens', C.c_float)]
 
 
-_lib = None
+_libs = {}
+_lib = None  # the float build (the parity restatement)
+
+# Builds: 'f32' the parity restatement (the reference's float arithmetic),
+# 'f64' the FP64 oracle (the same estimator in double, FR_PORT_REAL=double;
+# its C API takes and returns doubles), 'timing' the restatement compiled
+# with the reference's own optimisation flags for the CPU baseline.
+LIBS = {'f32': LIB, 'f64': os.path.join(HERE, '_build', 'libfrport64.so'),
+        'timing': os.path.join(HERE, '_build', 'libfrport_timing.so')}
 
 
-def load():
+def load(kind='f32'):
     global _lib
-    if _lib is None:
-        if not os.path.exists(LIB):
-            import importlib.util
-            spec = importlib.util.spec_from_file_location('build_oracle', os.path.join(HERE, 'build_oracle.py'))
-            m = importlib.util.module_from_spec(spec)
-            spec.loader.exec_module(m)
-            m.build_port()
-        lib = C.CDLL(LIB)
+    if kind not in _libs:
+        import importlib.util
+        spec = importlib.util.spec_from_file_location('build_oracle', os.path.join(HERE, 'build_oracle.py'))
+        m = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(m)
+        m.build_port(kind)
+        lib = C.CDLL(LIBS[kind])
         vp = C.c_void_p
+        real = C.c_double if kind == 'f64' else C.c_float
         lib.port_create.restype = vp
         lib.port_create.argtypes = [C.c_int32, vp, vp, vp, vp, C.c_int32, vp, C.c_int32, vp, vp,
-                                    C.POINTER(PortCamera), C.c_int32, C.c_float, C.c_float, C.c_int32]
+                                    C.POINTER(PortCamera), C.c_int32, real, real, C.c_int32]
         for name in ('port_destroy',):
             getattr(lib, name).argtypes = [vp]
             getattr(lib, name).restype = None
@@ -51,6 +59,10 @@ def load():
         lib.port_set_ibl.argtypes = [vp, C.c_int32, C.c_int32, vp]
         lib.port_read_direct.argtypes = [vp, vp, vp, vp]
         lib.port_seek.argtypes = [vp, C.c_int32]
+        lib.port_set_watertight.argtypes = [vp, C.c_int32]
+        lib.port_set_stream_key.argtypes = [vp, C.c_uint32]
+        lib.port_set_end_degenerate.argtypes = [vp, C.c_int32]
+        lib.port_set_window.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
         lib.port_sample_rays.argtypes = [vp, C.c_int64, C.c_int64]
         lib.port_read_ray_sample.argtypes = [vp, vp]
         lib.port_read_ray_sample.restype = C.c_int64
@@ -68,8 +80,10 @@ def load():
         lib.port_philox.argtypes = [vp, vp, vp]
         lib.port_set_threads.argtypes = [C.c_int32]
         lib.port_max_threads.restype = C.c_int32
-        _lib = lib
-    return _lib
+        _libs[kind] = lib
+        if kind == 'f32':
+            _lib = lib
+    return _libs[kind]
 
 
 def _p(a):
@@ -104,12 +118,15 @@ def radius_count(hp_pos, hp_r, photons):
 class PortRenderer:
     """The CPU restatement on a scene dict from frsppm.scenes."""
 
-    def __init__(self, scene, photons, alpha=0.9, radius=0.015, fix_stale=False):
-        lib = load()
+    def __init__(self, scene, photons, alpha=0.9, radius=0.015, fix_stale=False, watertight=False, kind='f32'):
+        """kind: 'f32' (the parity restatement), 'f64' (the FP64 oracle: its
+        arrays are float64) or 'timing' (the reference's optimisation flags)."""
+        lib = self.lib = load(kind)
+        self.dt = dt = np.float64 if kind == 'f64' else np.float32
         self._keep = []
-        pos = np.ascontiguousarray(scene['pos'], np.float32)
-        nrm = np.ascontiguousarray(scene['nrm'], np.float32)
-        uv = np.ascontiguousarray(scene['uv'], np.float32)
+        pos = np.ascontiguousarray(scene['pos'], dt)
+        nrm = np.ascontiguousarray(scene['nrm'], dt)
+        uv = np.ascontiguousarray(scene['uv'], dt)
         mat = np.ascontiguousarray(scene['mat'], np.int32)
         texs = [np.ascontiguousarray(t, np.uint8) for t in scene['textures']]
         wh = np.array([[t.shape[1], t.shape[0]] for t in texs] or [[0, 0]], np.int32)
@@ -131,6 +148,8 @@ class PortRenderer:
                                  int(fix_stale))
         if not self.h:
             raise RuntimeError('port_create failed (no emissive facets?)')
+        if watertight:
+            lib.port_set_watertight(self.h, 1)
         if scene.get('ibl') is not None:
             ibl = np.ascontiguousarray(scene['ibl'], np.uint8)
             lib.port_set_ibl(self.h, ibl.shape[1], ibl.shape[0], _p(ibl))
@@ -138,7 +157,7 @@ class PortRenderer:
 
     def close(self):
         if getattr(self, 'h', None):
-            _lib.port_destroy(self.h)
+            self.lib.port_destroy(self.h)
             self.h = None
 
     def __del__(self):
@@ -154,78 +173,78 @@ class PortRenderer:
         self.close()
 
     def iterate(self, n=1):
-        _lib.port_iterate(self.h, int(n))
+        self.lib.port_iterate(self.h, int(n))
 
     def seek(self, first_step):
         """The next iteration runs step first_step + 1."""
-        _lib.port_seek(self.h, int(first_step))
+        self.lib.port_seek(self.h, int(first_step))
 
     def sample_rays(self, stride, cap):
         """Keep every stride-th closest-hit ray the next iterations trace (up to cap)."""
-        _lib.port_sample_rays(self.h, int(stride), int(cap))
+        self.lib.port_sample_rays(self.h, int(stride), int(cap))
 
     def ray_sample(self):
         """The kept rays: (N x 7 float32 {origin, direction, index}, N pass tags 0 eye / 1 photon)."""
-        n = int(_lib.port_read_ray_sample(self.h, None))
-        out = np.empty((n, 8), np.float32)
-        _lib.port_read_ray_sample(self.h, _p(out))
+        n = int(self.lib.port_read_ray_sample(self.h, None))
+        out = np.empty((n, 8), self.dt)
+        self.lib.port_read_ray_sample(self.h, _p(out))
         return np.ascontiguousarray(out[:, :7]), out[:, 7].astype(np.int32)
 
     def photon_pass(self, first, count):
-        _lib.port_photon_pass(self.h, int(first), int(count))
+        self.lib.port_photon_pass(self.h, int(first), int(count))
 
     def resolve(self):
-        out = np.empty((self.width * self.height, 4), np.float32)
-        _lib.port_resolve(self.h, _p(out))
+        out = np.empty((self.width * self.height, 4), self.dt)
+        self.lib.port_resolve(self.h, _p(out))
         return out
 
     def trace_closest(self, rays):
-        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 7)
+        rays = np.ascontiguousarray(rays, self.dt).reshape(-1, 7)
         f = np.empty(len(rays), np.int32)
-        tuv = np.empty((len(rays), 3), np.float32)
-        _lib.port_trace_closest(self.h, _p(rays), len(rays), _p(f), _p(tuv))
+        tuv = np.empty((len(rays), 3), self.dt)
+        self.lib.port_trace_closest(self.h, _p(rays), len(rays), _p(f), _p(tuv))
         return f, tuv
 
     def trace_any(self, rays):
-        rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+        rays = np.ascontiguousarray(rays, self.dt).reshape(-1, 8)
         hit = np.empty(len(rays), np.int32)
-        _lib.port_trace_any(self.h, _p(rays), len(rays), _p(hit))
+        self.lib.port_trace_any(self.h, _p(rays), len(rays), _p(hit))
         return hit
 
     def read_hitpoints(self):
         n = self.width * self.height
         t, f = np.empty(n, np.int32), np.empty(n, np.int32)
-        a = [np.empty((n, 3), np.float32) for _ in range(4)]
-        rough = np.empty(n, np.float32)
-        _lib.port_read_hitpoints(self.h, _p(t), _p(f), *[_p(x) for x in a], _p(rough))
+        a = [np.empty((n, 3), self.dt) for _ in range(4)]
+        rough = np.empty(n, self.dt)
+        self.lib.port_read_hitpoints(self.h, _p(t), _p(f), *[_p(x) for x in a], _p(rough))
         return dict(type=t, facet=f, pos=a[0], nrm=a[1], out=a[2], w=a[3], rough=rough)
 
     def read_direct(self):
         """Direct (environment) light: per hitpoint of the last iteration, and
         per pixel the sum and count (SharedHitPoint::DirectLight, NumDirectLight)."""
         n = self.width * self.height
-        hp, sp = np.empty((n, 3), np.float32), np.empty((n, 3), np.float32)
+        hp, sp = np.empty((n, 3), self.dt), np.empty((n, 3), self.dt)
         cnt = np.empty(n, np.int32)
-        _lib.port_read_direct(self.h, _p(hp), _p(sp), _p(cnt))
+        self.lib.port_read_direct(self.h, _p(hp), _p(sp), _p(cnt))
         return hp, sp, cnt
 
     def compacted_photons(self):
-        n = int(_lib.port_num_photons(self.h))
-        ph = np.empty((n, 11), np.float32)
+        n = int(self.lib.port_num_photons(self.h))
+        ph = np.empty((n, 11), self.dt)
         path, slot = np.empty(n, np.int32), np.empty(n, np.int32)
-        _lib.port_read_photons(self.h, _p(ph), _p(path), _p(slot))
+        self.lib.port_read_photons(self.h, _p(ph), _p(path), _p(slot))
         return ph, path, slot
 
     def read_gather(self):
         n = self.width * self.height
         m = np.empty(n, np.int32)
-        phi = np.empty((n, 3), np.float32)
-        _lib.port_read_gather(self.h, _p(m), _p(phi))
+        phi = np.empty((n, 3), self.dt)
+        self.lib.port_read_gather(self.h, _p(m), _p(phi))
         return m, phi
 
     def read_state(self):
         n = self.width * self.height
-        rad = np.empty((n, 3), np.float32)
-        N, r, g = np.empty(n, np.int32), np.empty(n, np.float32), np.empty(n, np.int32)
-        _lib.port_read_state(self.h, _p(rad), _p(N), _p(r), _p(g))
+        rad = np.empty((n, 3), self.dt)
+        N, r, g = np.empty(n, np.int32), np.empty(n, self.dt), np.empty(n, np.int32)
+        self.lib.port_read_state(self.h, _p(rad), _p(N), _p(r), _p(g))
         return dict(tau=rad, n=N, r=r, g=g)

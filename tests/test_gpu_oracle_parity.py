@@ -6,12 +6,21 @@ import pytest
 pytestmark = pytest.mark.gpu
 
 CASES = {
-    # name: (scene factory, photons, iterations, alpha, radius[, fix_stale])
+    # name: (scene factory, photons, iterations, alpha, radius[, options])
+    # options: fix_stale (FR_FLAG_FIX_STALE_PHOTON_SLOT), watertight
+    # (FR_FLAG_WATERTIGHT), each against the oracle's switch.
     'cornell96': (lambda s: s.cornell_box(width=96, height=96), 20000, 4, 0.7, 0.02),
     # The Cornell-box configuration at full size: 256^2 pinhole, 100k paths.
     'cornell256_100k': (lambda s: s.cornell_box(), 100000, 2, 0.7, 0.02),
     # FR_FLAG_FIX_STALE_PHOTON_SLOT against the oracle's switch.
-    'cornell96_fixstale': (lambda s: s.cornell_box(width=96, height=96), 20000, 3, 0.7, 0.02, True),
+    'cornell96_fixstale': (lambda s: s.cornell_box(width=96, height=96), 20000, 3, 0.7, 0.02, {'fix_stale': True}),
+    # The precision mode's watertight triangle test.
+    'cornell96_watertight': (lambda s: s.cornell_box(width=96, height=96), 20000, 3, 0.7, 0.02,
+                             {'watertight': True}),
+    'mixed128x72_watertight': (lambda s: s.mixed_materials(width=128, height=72, n_spheres=24, field_n=48,
+                                                           tex_size=128, light_tex=64, n_lat=12, n_lon=16,
+                                                           extent=0.8, aperture=0.05),
+                               20000, 3, 0.7, 0.02, {'watertight': True}),
     'mixed128x72': (lambda s: s.mixed_materials(width=128, height=72, n_spheres=24, field_n=48, tex_size=128,
                                                 light_tex=64, n_lat=12, n_lon=16, extent=0.8, aperture=0.05),
                     20000, 3, 0.7, 0.02),
@@ -41,10 +50,12 @@ def test_gpu_matches_oracle(name):
     import port_abi
     from frsppm import abi
     _, photons, iters, alpha, radius = CASES[name][:5]
-    fix = len(CASES[name]) > 5 and CASES[name][5]
+    opt = CASES[name][5] if len(CASES[name]) > 5 else {}
+    fix, wt = opt.get('fix_stale', False), opt.get('watertight', False)
     scene = _scene(name)
-    with abi.Renderer(scene, photons, alpha=alpha, radius=radius, flags=1 if fix else 0) as g, \
-            port_abi.PortRenderer(scene, photons, alpha=alpha, radius=radius, fix_stale=fix) as c:
+    flags = (abi.FLAG_FIX_STALE_PHOTON_SLOT if fix else 0) | (abi.FLAG_WATERTIGHT if wt else 0)
+    with abi.Renderer(scene, photons, alpha=alpha, radius=radius, flags=flags) as g, \
+            port_abi.PortRenderer(scene, photons, alpha=alpha, radius=radius, fix_stale=fix, watertight=wt) as c:
         for s in range(iters):
             g.iterate(1)
             c.iterate(1)
