@@ -20,11 +20,15 @@ each step, two buffers in turn) and a wait for the previous step's image, so
 the copy overlaps the next iteration; the scene is uploaded once by fr_create
 (reported as setup).
 guided_vs_plain: the metric's second half, on the caustic scene (198,936
-triangles, 1024^2, 2M photon paths/iteration): relMSE against a long plain
-render of plain and guided SPPM at equal wall time, and the guided run's time
-to reach the plain run's final error (guide_eval; --guide-eval runs it alone).
+triangles, 1024^2, 2M photon paths/iteration): relMSE against the FP64
+CPU-converged oracle (tests/golden/fp64_caustic_crop.npz) of plain and guided
+SPPM at equal wall time, and the guided run's time to reach the plain run's
+errors, over three seeds (guide_eval; --guide-eval runs it alone).
+fp64_image_errors: relMSE of plain renders of the Cornell box and of the
+mixed-materials construction at 320x180 against their FP64 oracles.
 --impl reference: the CPU restatement of the reference path (oracle/port,
-pinned bit-exact to the reference's own outputs) on the host cores.
+pinned bit-exact to the reference's own outputs), compiled with the
+reference's own optimisation flags, on all host cores in a child process.
 """
 from __future__ import annotations
 
@@ -36,6 +40,8 @@ import subprocess
 import sys
 import threading
 import time
+
+import numpy as np
 
 REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(REPO, 'friendsrender-r-public_gb300'))
@@ -167,60 +173,73 @@ def measured_peaks():
     return 6800.0, 'fallback'
 
 
-def cpu_baseline(scene, seconds_target=20.0):
-    """The oracle (CPU restatement of the reference path) on the host cores:
-    full iterations of the same workload, as many as fit ~seconds_target."""
+# The CPU side runs the oracle's timing build (oracle/port compiled with the
+# reference's own optimisation flags, SPPM/SPPM/makefile: -O2 -ffast-math
+# -Ofast -fopenmp; its x86-only -mavx left out) on all host threads.
+CPU_FLAGS = '-O2 -ffast-math -Ofast -fopenmp (the reference makefile\'s flags without its x86-only -mavx)'
+
+
+def cpu_measure(photons, warmup, steps, budget_s=None):
+    """Times the oracle's timing build on the mixed-materials workload (full
+    eye pass, grid, gather every iteration): warmup untimed iterations, then
+    steps timed ones.  With budget_s the photons per iteration shrink so the
+    whole run stays near budget_s seconds.  Runs in this process; callers run
+    it in a child process, so the GPU process never maps the oracle."""
+    from frsppm import scenes
     sys.path.insert(0, os.path.join(REPO, 'oracle'))
     import port_abi
+    port_abi.load('timing')
     port_abi.set_threads(os.cpu_count() or 1)
     threads = port_abi.max_threads()
-    with port_abi.PortRenderer(scene, PHOTONS, alpha=ALPHA, radius=RADIUS) as r:
+    scene = scenes.mixed_materials()
+    if budget_s is not None:
+        with port_abi.PortRenderer(scene, photons, alpha=ALPHA, radius=RADIUS, kind='timing') as r:
+            t0 = time.perf_counter()
+            r.iterate(1)
+            per_full = time.perf_counter() - t0
+        per_budget = budget_s / max(1, steps + warmup)
+        if per_full > per_budget:
+            photons = max(50_000, int(photons * per_budget / per_full))
+    with port_abi.PortRenderer(scene, photons, alpha=ALPHA, radius=RADIUS, kind='timing') as r:
+        for _ in range(warmup):
+            r.iterate(1)
         t0 = time.perf_counter()
-        r.iterate(1)
-        first = time.perf_counter() - t0
-        n = max(1, min(4, int(seconds_target / max(first, 1e-3)) - 1))
-        t0 = time.perf_counter()
-        r.iterate(n)
+        r.iterate(steps)
         dt = time.perf_counter() - t0
-    return {'value': PHOTONS * n / dt, 'unit': UNIT, 'cores': threads, 'kind': 'port',
-            'sample': '%d full iterations of the workload (1M paths each) after 1 untimed, %d OpenMP threads, '
-                      '%.2f s' % (n, threads, dt)}
+    return {'value': photons * steps / dt, 'unit': UNIT, 'cores': threads, 'kind': 'port',
+            'build': CPU_FLAGS, 'photons_per_step': photons, 'steps': steps, 'warmup': warmup, 'seconds': dt,
+            'sample': '%d iterations of the workload (%d photon paths each, full 1280x720 eye pass, grid, gather) '
+                      'after %d untimed, %d OpenMP threads, %.2f s' % (steps, photons, warmup, threads, dt)}
+
+
+def cpu_child(args_json):
+    """Runs cpu_measure in a child process and returns its JSON result."""
+    cmd = [sys.executable, os.path.abspath(__file__), '--cpu-measure', args_json]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=900)
+    if r.returncode != 0:
+        raise RuntimeError('CPU measurement failed: ' + r.stderr[-2000:])
+    return json.loads(r.stdout.strip().splitlines()[-1])
+
+
+def cpu_baseline():
+    """The CPU baseline beside the GPU number: 4 full iterations of the same
+    workload (1M paths each) after 1 untimed, in a child process."""
+    return cpu_child(json.dumps({'photons': PHOTONS, 'warmup': 1, 'steps': 4}))
 
 
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
         return 0
-    from frsppm import scenes
-    sys.path.insert(0, os.path.join(REPO, 'oracle'))
-    import port_abi
-    port_abi.set_threads(os.cpu_count() or 1)
-    threads = port_abi.max_threads()
-    scene = scenes.mixed_materials()
     # Each step is one iteration of the workload; the photon count per step is
-    # reduced when K + W full iterations would run past ~3 minutes.
-    budget = 150.0 / max(1, args.steps + args.warmup)
-    photons = PHOTONS
-    with port_abi.PortRenderer(scene, PHOTONS, alpha=ALPHA, radius=RADIUS) as r:
-        t0 = time.perf_counter()
-        r.iterate(1)
-        per_full = time.perf_counter() - t0
-    if per_full > budget:
-        photons = max(50_000, int(PHOTONS * budget / per_full))
-    with port_abi.PortRenderer(scene, photons, alpha=ALPHA, radius=RADIUS) as r:
-        for _ in range(args.warmup):
-            r.iterate(1)
-        t0 = time.perf_counter()
-        r.iterate(args.steps)
-        dt = time.perf_counter() - t0
-    value = photons * args.steps / dt
-    sample = ('%d iterations of %d photon paths each (full 1280x720 eye pass, grid, gather) after %d warm-up, '
-              '%d OpenMP threads' % (args.steps, photons, args.warmup, threads))
+    # reduced when K + W full iterations would run past ~2.5 minutes.
+    cb = cpu_child(json.dumps({'photons': PHOTONS, 'warmup': args.warmup, 'steps': args.steps, 'budget_s': 150.0}))
+    value = cb['value']
     out = {'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps,
-           'warmup': args.warmup, 'ms_per_step': dt * 1000.0 / args.steps, 'higher_is_better': True,
+           'warmup': args.warmup, 'ms_per_step': cb['seconds'] * 1000.0 / args.steps, 'higher_is_better': True,
            'scaling': 'weak', 'vs_baseline': None, 'dtype': 'f32', 'data': 'synthetic (seeded scene)',
-           'config': {'workload': WORKLOAD, 'photons_per_step': photons}, 'impl': 'reference',
-           'cpu_baseline': {'value': value, 'unit': UNIT, 'cores': threads, 'kind': 'port', 'sample': sample},
+           'config': {'workload': WORKLOAD, 'photons_per_step': cb['photons_per_step']}, 'impl': 'reference',
+           'cpu_baseline': cb,
            'e2e': {'value': value, 'unit': UNIT, 'h2d_bytes_per_step': 0, 'd2h_bytes_per_step': 0}}
     print(json.dumps(out))
     return 0
@@ -235,11 +254,12 @@ TRACE_TRAFFIC_PROFILE = os.path.join(REPO, 'profiles', 'k_wave_trace_traffic_mix
 
 
 def trace_traffic_per_launch():
-    """DRAM bytes (read + write) per k_wave_trace launch from the committed
-    ncu capture of this workload, or None."""
+    """DRAM bytes (read + write) per k_wave_trace launch that traced rays (the
+    rounds of one iteration that ran, skipped rounds left out), from the
+    committed ncu capture of this workload, or None."""
     try:
         for line in open(TRACE_TRAFFIC_PROFILE):
-            if line.startswith('bytes_per_launch:'):
+            if line.startswith('bytes_per_nonempty_launch:'):
                 return float(line.split(':', 1)[1])
     except OSError:
         pass
@@ -266,44 +286,56 @@ def rel_mse(img, ref):
     return float(((a - b) ** 2 / (b * b + REL_MSE_EPS)).mean())
 
 
-def guide_eval(plain_iters=128, ref_iters=1024, photons=CAUSTIC_PHOTONS, scene=None, log=None, eager=False):
-    """Plain and guided SPPM on the caustic box against a long plain run (the
-    reference image, FP64 tau), all resolved with the standard estimate
-    tau / (pi R^2 photons emitted) and with paths ended where the reference's
-    rough-dielectric BSDF turns NaN (which would leave NaN pixels).  The reference run's random streams start
-    past every step the two runs draw (fr_seek), so it shares no seed with
-    them.  The plain run's error after plain_iters iterations is the target;
-    the guided run's wall time to first reach it (checked at iteration marks
-    12.5% apart) and its error at the plain run's wall time are reported.
-    Wall time is fr_iterate + fr_synchronize, the guide's training included;
-    the resolves at the marks are not timed.  eager: iterations launched
-    directly (stage profiler on) instead of as the captured graph, whose
-    conditional nodes ncu cannot profile into; for kernel profiles only."""
+GOLDEN = os.path.join(REPO, 'tests', 'golden')
+
+
+def fp64_oracle(name):
+    """A committed FP64 CPU-converged oracle image (tests/golden/fp64_<name>.npz,
+    made by tests/golden/make_fp64_oracle.py): linear radiance (h, w, 3), the
+    window of the frame it covers (x0, y0, x1, y1; zeros for the whole frame)
+    and the photon paths it holds."""
+    d = np.load(os.path.join(GOLDEN, 'fp64_%s.npz' % name))
+    return d['radiance'].astype(np.float64), tuple(int(v) for v in d['window']), int(d['photon_paths'])
+
+
+def rel_mse_linear(img, width, ref, window):
+    """relMSE of a resolved image (fr_resolve: radiance^(1/1.2)) against linear
+    reference radiance over the reference's window of the frame, both scaled
+    so that the reference's mean is 1 (the 1e-2 in the denominator is then
+    relative to the image's own brightness)."""
+    a = _linear(img).reshape(-1, width, 3)
+    if window != (0, 0, 0, 0):
+        x0, y0, x1, y1 = window
+        a = a[y0:y1, x0:x1]
+    k = 1.0 / ref.mean()
+    a, b = a * k, ref * k
+    return float(((a - b) ** 2 / (b * b + REL_MSE_EPS)).mean())
+
+
+GUIDE_SEEDS = (1, 2, 3)
+
+
+def guide_eval(plain_iters=128, photons=CAUSTIC_PHOTONS, scene=None, log=None, eager=False, seeds=GUIDE_SEEDS):
+    """Plain and guided SPPM on the caustic box against the FP64 CPU-converged
+    oracle (the 256^2 window in the middle of the 1024^2 frame), all resolved
+    with the standard estimate tau / (pi R^2 photons emitted) and with
+    degenerate paths ended.  For each seed (the guide's initial weights, and
+    both runs' random streams moved by fr_seek), the plain run's error after
+    1/4, 1/2 and all of plain_iters iterations are the targets; the guided
+    run's wall time to first reach each (checked at iteration marks 12.5%
+    apart) and its error at the plain run's final wall time are reported, with
+    the minimum and median over the seeds.  Wall time is fr_iterate +
+    fr_synchronize, the guide's training included; the resolves at the marks
+    are not timed.  eager: iterations launched directly (stage profiler on)
+    instead of as the captured graph, whose conditional nodes ncu cannot
+    profile into; for kernel profiles only."""
     from frsppm import abi, scenes
     scene = scene or scenes.caustic_box()
+    ref, window, ref_paths = fp64_oracle('caustic_crop')
+    width = scene['camera']['width']
     kw = dict(alpha=CAUSTIC_ALPHA, radius=CAUSTIC_RADIUS,
               flags=abi.FLAG_STANDARD_RESOLVE | abi.FLAG_END_DEGENERATE_PATHS)
     max_run = 4 * plain_iters
-    first = max_run + 16
-    npix = scene['camera']['width'] * scene['camera']['height']
-    if (first + ref_iters + 1) * max(photons, npix) >= 1 << 32:
-        raise ValueError('reference run would wrap the 32-bit seeds into the compared runs')
-    t0 = time.perf_counter()
-    def direct(r, iters):
-        if eager:
-            r.profile(True, max_iterations=iters + 1)
-
-    with abi.Renderer(scene, photons, **kw) as ref:
-        ref.seek(first)
-        direct(ref, ref_iters)
-        done = 0
-        while done < ref_iters:
-            n = min(64, ref_iters - done)
-            ref.iterate(n)
-            done += n
-        reference = ref.resolve()
-    ref_s = time.perf_counter() - t0
-
     marks, m = [], 1.0
     while int(m) < plain_iters:
         if not marks or int(m) > marks[-1]:
@@ -311,11 +343,13 @@ def guide_eval(plain_iters=128, ref_iters=1024, photons=CAUSTIC_PHOTONS, scene=N
         m *= 1.125
     marks.append(plain_iters)
 
-    def run(guided, stop):
+    def run(guided, seed, stop):
         curve = []
-        extra = dict(guide=True) if guided else {}
+        extra = dict(guide=True, guide_seed=seed) if guided else {}
         with abi.Renderer(scene, photons, **kw, **extra) as r:
-            direct(r, max_run + len(marks))
+            r.seek(1000 * seed)
+            if eager:
+                r.profile(True, max_iterations=max_run + len(marks) + 1)
             r.synchronize()
             t, done, k = 0.0, 0, 0
             while True:
@@ -324,33 +358,83 @@ def guide_eval(plain_iters=128, ref_iters=1024, photons=CAUSTIC_PHOTONS, scene=N
                 r.iterate(target - done)
                 t += time.perf_counter() - t1
                 done = target
-                curve.append((done, t, rel_mse(r.resolve(), reference)))
+                curve.append((done, t, rel_mse_linear(r.resolve(), width, ref, window)))
                 if log:
-                    log('%s %d iterations %.3f s relMSE %.5f' % ('guided' if guided else 'plain', *curve[-1]))
+                    log('%s seed %d: %d iterations %.3f s relMSE %.5f' % ('guided' if guided else 'plain', seed,
+                                                                          *curve[-1]))
                 k += 1
                 if stop(done, t):
                     return curve
 
-    plain = run(False, lambda n, t: n >= plain_iters)
-    t_plain, e_plain = plain[-1][1], plain[-1][2]
-    guided = run(True, lambda n, t: t >= 1.02 * t_plain or n >= max_run)
-    reach = next(((n, t) for n, t, e in guided if e <= e_plain), None)
-    at_equal = [e for n, t, e in guided if t <= t_plain]
+    per_seed = []
+    for seed in seeds:
+        plain = run(False, seed, lambda n, t: n >= plain_iters)
+        t_plain = plain[-1][1]
+        guided = run(True, seed, lambda n, t: t >= 1.02 * t_plain or n >= max_run)
+        targets = {}
+        for frac in (4, 2, 1):
+            n_t = plain_iters // frac
+            e_t, t_t = next((e, t) for n, t, e in plain if n >= n_t)
+            reach = next(((n, t) for n, t, e in guided if e <= e_t), None)
+            targets['plain_%d_iterations' % n_t] = {
+                'rel_mse': e_t, 'plain_wall_s': t_t,
+                'guided_iterations': reach[0] if reach else None, 'guided_wall_s': reach[1] if reach else None,
+                'speedup': (t_t / reach[1]) if reach else None}
+        at_equal = [e for n, t, e in guided if t <= t_plain]
+        per_seed.append({
+            'seed': seed,
+            'plain': {'iterations': plain_iters, 'wall_s': t_plain, 'rel_mse': plain[-1][2],
+                      'ms_per_iteration': 1e3 * t_plain / plain_iters},
+            'guided': {'rel_mse_at_equal_time': at_equal[-1] if at_equal else None,
+                       'ms_per_iteration': 1e3 * guided[-1][1] / guided[-1][0]},
+            'time_to_target': targets,
+            'curves': {'plain': [[n, round(t, 4), round(e, 6)] for n, t, e in plain],
+                       'guided': [[n, round(t, 4), round(e, 6)] for n, t, e in guided]}})
+
+    def stat(key):
+        v = [p['time_to_target'][key]['speedup'] for p in per_seed]
+        ok = [x for x in v if x is not None]
+        return {'min': min(ok) if len(ok) == len(v) else None, 'median': float(np.median(ok)) if ok else None,
+                'per_seed': v}
+    keys = list(per_seed[0]['time_to_target'])
     return {
         'workload': CAUSTIC_WORKLOAD,
-        'reference': '%d plain iterations (%d photon paths), FP64 tau, standard resolve, %.1f s'
-                     % (ref_iters, ref_iters * photons, ref_s),
-        'rel_mse': 'mean of (x - ref)^2 / (ref^2 + %g) over pixels and RGB, linear radiance' % REL_MSE_EPS,
-        'plain': {'iterations': plain_iters, 'wall_s': t_plain, 'rel_mse': e_plain,
-                  'ms_per_iteration': 1e3 * t_plain / plain_iters},
-        'guided': {'iterations_to_plain_error': reach[0] if reach else None,
-                   'wall_s_to_plain_error': reach[1] if reach else None,
-                   'rel_mse_at_equal_time': at_equal[-1] if at_equal else None,
-                   'ms_per_iteration': 1e3 * guided[-1][1] / guided[-1][0]},
-        'time_to_plain_error_speedup': (t_plain / reach[1]) if reach else None,
-        'curves': {'plain': [[n, round(t, 4), round(e, 6)] for n, t, e in plain],
-                   'guided': [[n, round(t, 4), round(e, 6)] for n, t, e in guided]},
+        'reference': ('FP64 CPU-converged oracle (oracle/port in double, standard resolve, degenerate paths '
+                      'ended, own random streams): the %dx%d window at (%d, %d), %d photon paths'
+                      % (window[2] - window[0], window[3] - window[1], window[0], window[1], ref_paths)),
+        'rel_mse': ('mean of (x - ref)^2 / (ref^2 + %g) over the window\'s pixels and RGB, linear radiance '
+                    'scaled so that the reference\'s mean is 1' % REL_MSE_EPS),
+        'seeds': list(seeds),
+        'time_to_plain_error_speedup': {k: stat(k) for k in keys},
+        'rel_mse_at_equal_time': {'plain': [p['plain']['rel_mse'] for p in per_seed],
+                                  'guided': [p['guided']['rel_mse_at_equal_time'] for p in per_seed]},
+        'per_seed': per_seed,
     }
+
+
+def fp64_image_errors():
+    """relMSE of plain GPU renders against their FP64 CPU-converged oracles
+    (standard resolve): the Cornell box (256^2, 100k paths, its 16 iterations
+    and more) and the mixed-materials construction at 320x180 (1M paths, its 64
+    iterations)."""
+    from frsppm import abi, scenes
+    out = {}
+    cases = (('cornell', lambda: scenes.cornell_box(), 100_000, 0.7, 0.02, (16, 64, 256)),
+             ('mixed_small', lambda: scenes.mixed_materials(width=320, height=180), 1_000_000, 0.7, 0.02, (16, 64)))
+    for name, factory, photons, alpha, radius, marks in cases:
+        ref, window, ref_paths = fp64_oracle(name)
+        scene = factory()
+        width = scene['camera']['width']
+        errs = {}
+        with abi.Renderer(scene, photons, alpha=alpha, radius=radius, flags=abi.FLAG_STANDARD_RESOLVE) as r:
+            done = 0
+            for m in marks:
+                r.iterate(m - done)
+                done = m
+                errs[str(m)] = rel_mse_linear(r.resolve(), width, ref, window)
+        out[name] = {'photons_per_iteration': photons, 'rel_mse_by_iterations': errs,
+                     'oracle_photon_paths': ref_paths}
+    return out
 
 
 LARGE_PHOTONS = 8_000_000
@@ -562,6 +646,31 @@ def run_update(args):
     return 0
 
 
+def other_workloads():
+    """The batched uneven scenes (64 contexts, fr_iterate_batch) and the large
+    scene (20M triangles, 3840x2160, 8M paths, guide on), each measured by its
+    own --workload run in a child process (so each starts with the GPU to
+    itself); their JSON lines, shortened."""
+    out = {}
+    for name, extra in (('batch', ['--steps', '3', '--warmup', '3']), ('large', ['--steps', '5', '--warmup', '3'])):
+        cmd = [sys.executable, os.path.abspath(__file__), '--workload', name] + extra
+        t0 = time.perf_counter()
+        try:
+            r = subprocess.run(cmd, capture_output=True, text=True, timeout=900)
+            line = json.loads(r.stdout.strip().splitlines()[-1]) if r.returncode == 0 else None
+        except (subprocess.TimeoutExpired, ValueError, IndexError):
+            line = None
+        if line is None:
+            out[name] = {'unavailable': 'the --workload %s run failed' % name}
+            continue
+        keep = ('value', 'unit', 'ms_per_step', 'steps', 'warmup', 'hitpoint_updates_per_s', 'e2e', 'gpu_launches',
+                'clocks', 'batch_speedup', 'sequential', 'setup')
+        out[name] = {k: line[k] for k in keep if k in line}
+        out[name]['workload'] = line['config']['workload']
+        out[name]['run_s'] = time.perf_counter() - t0
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument('--gpus', type=int, default=1)
@@ -575,7 +684,6 @@ def main():
     ap.add_argument('--guide-eval', action='store_true', help='only the guided-vs-plain caustic comparison')
     ap.add_argument('--no-guide-eval', action='store_true')
     ap.add_argument('--guide-plain-iters', type=int, default=128)
-    ap.add_argument('--guide-ref-iters', type=int, default=1024)
     ap.add_argument('--guide-photons', type=int, default=CAUSTIC_PHOTONS)
     ap.add_argument('--eager', action='store_true', help='guide eval: direct launches (for ncu)')
     ap.add_argument('--workload', default='mixed', choices=['mixed', 'large', 'batch', 'update'],
@@ -584,7 +692,13 @@ def main():
     ap.add_argument('--no-autotune', action='store_true')
     ap.add_argument('--bvh', default='sah', choices=['sah', 'lbvh'],
                     help='scene BVH: host binned SAH (default) or the device LBVH build')
+    ap.add_argument('--cpu-measure', default=None, help=argparse.SUPPRESS)
+    ap.add_argument('--no-other-workloads', action='store_true',
+                    help='skip the batched-scenes and large-scene lines embedded in the default line')
     args = ap.parse_args()
+    if args.cpu_measure is not None:
+        print(json.dumps(cpu_measure(**json.loads(args.cpu_measure))))
+        return 0
     if args.steps is None:
         args.steps = 200 if args.impl == 'ours' and args.workload in ('mixed', 'update') else 10
     if args.impl == 'reference':
@@ -596,7 +710,7 @@ def main():
     if args.workload == 'update':
         return run_update(args)
     if args.guide_eval:
-        out = guide_eval(args.guide_plain_iters, args.guide_ref_iters, args.guide_photons,
+        out = guide_eval(args.guide_plain_iters, args.guide_photons,
                          log=lambda s: print(s, file=sys.stderr, flush=True), eager=args.eager)
         print(json.dumps(out))
         return 0
@@ -686,10 +800,13 @@ def main():
     value = world * args.photons * args.steps / (total_ms / 1000.0)
     per = {k: stage_ms[k] / args.steps for k in stage_ms}
     peak, peak_kind = measured_peaks()
-    trace_launches = (stage_n['eye_trace'] + stage_n['photon_trace']) / args.steps
+    # Trace launches that traced rays (rounds that ran; the skipped rounds'
+    # launches return at once and their few microseconds stay in trace_s).
+    trace_launches = int((eye_q[:-1] > 0).sum() + (photon_q[:-1] > 0).sum())
     trace_s = (stage_ms['eye_trace'] + stage_ms['photon_trace']) / 1000.0 / args.steps
-    bytes_per_launch = rays * TRACE_BYTES_PER_RAY / trace_launches
-    achieved = bytes_per_launch / (trace_s / trace_launches) / 1e9
+    bytes_per_step = rays * TRACE_BYTES_PER_RAY
+    bytes_per_launch = bytes_per_step / trace_launches
+    achieved = bytes_per_step / trace_s / 1e9
     clocks = clk.summary()
     out = {
         'metric': METRIC, 'value': value, 'unit': UNIT, 'n_gpus': world, 'steps': args.steps, 'warmup': W,
@@ -704,6 +821,7 @@ def main():
         'roofline': {'bound': 'hbm', 'kernel': 'k_wave_trace', 'achieved': achieved, 'peak': peak, 'unit': 'GB/s',
                      'frac': achieved / peak, 'traffic': trace_traffic_per_launch(), 'peak_source': peak_kind,
                      'algorithmic_bytes_per_launch': bytes_per_launch, 'launches_per_step': trace_launches,
+                     'per': 'launch that traced rays (traffic and algorithmic bytes alike)',
                      'note': 'latency-bound BVH traversal; eye and photon launches overlap in time'},
         'traversal': traversal_block(rays, eye_rays, photon_rays, trace_s, eye_q, photon_q, clocks),
         'e2e': {'value': world * args.photons * args.steps / e2e_s, 'unit': UNIT, 'h2d_bytes_per_step': 0,
@@ -715,9 +833,12 @@ def main():
     }
     if world == 1 and not args.no_guide_eval:
         # equal-time relMSE, guided vs plain SPPM (caustic scene; not the timed workload)
-        out['guided_vs_plain'] = guide_eval(args.guide_plain_iters, args.guide_ref_iters, args.guide_photons)
+        out['guided_vs_plain'] = guide_eval(args.guide_plain_iters, args.guide_photons)
+        out['fp64_image_errors'] = fp64_image_errors()
     if world == 1 and not args.no_cpu_baseline:
-        out['cpu_baseline'] = cpu_baseline(scene)
+        out['cpu_baseline'] = cpu_baseline()
+    if world == 1 and not args.no_other_workloads:
+        out['other_workloads'] = other_workloads()
     print(json.dumps(out))
     return 0
 

@@ -97,6 +97,8 @@ def test_iterations_match_reference(name):
         img = r.resolve()
     ref = gold['image']
     assert np.isfinite(img).all()
-    assert np.abs(img - ref).max() <= 1e-4 * np.abs(ref).max()
-    big = np.abs(ref) > 1e-3 * np.abs(ref).max()
-    assert _rel(img[big], ref[big], 1e-30).max() < 1e-4
+    # Per pixel and channel: within 1e-4 of the reference's own value, with
+    # an absolute floor of 1e-7 of the image maximum for pixels near zero.
+    a, b = img[:, :3].astype(np.float64), ref[:, :3].astype(np.float64)
+    bad = np.abs(a - b) > 1e-4 * np.abs(b) + 1e-7 * np.abs(b).max()
+    assert not bad.any(), (int(bad.sum()), _rel(img[:, :3][bad], ref[:, :3][bad], 1e-30).max())
