@@ -201,7 +201,7 @@ __global__ void __launch_bounds__(128) k_guide_train(GuideGPU g) {
     first = false;
   }
   // ---- gradient sums of this CTA to its own row of grad_part (thread t:
-  // unit t); k_guide_reduce adds the rows in CTA order, so the step's
+  // unit t); k_guide_adam (and k_guide_reduce) add the rows in CTA order, so the step's
   // gradient does not depend on which CTA finishes first.
   float* gp = g.grad_part + (size_t)blockIdx.x * kGuideParams;
   if (!first && sy.ok) {
@@ -259,23 +259,61 @@ __global__ void k_guide_prepare(GuideGPU g) {
   }
 }
 
-// Adam on the mean gradient (sum / sum of importance); the padding outputs
-// 40-47 stay zero.  Clears the gradient sums for the next step.
+// The step's gradient sum for parameter p: the training CTAs' rows added in
+// CTA order (rows of CTAs that had no tile are not read).
+__device__ __forceinline__ uint32_t guide_rows(const GuideGPU& g) {
+  const uint32_t n_all = min(*g.batch_count, (uint32_t)g.batch_cap);
+  return min((n_all + 127) / 128, (uint32_t)g.train_ctas);
+}
+__device__ __forceinline__ float guide_grad_sum(const GuideGPU& g, uint32_t rows, int p) {
+  float sum = 0.0f;
+  for (uint32_t r = 0; r < rows; ++r) sum += g.grad_part[(size_t)r * kGuideParams + p];
+  return sum;
+}
+__device__ __forceinline__ float guide_weight_sum(const GuideGPU& g, uint32_t rows) {
+  float ws = 0.0f;
+  for (uint32_t r = 0; r < rows; ++r) ws += g.wsum_part[r];
+  return ws;
+}
+__device__ __forceinline__ bool guide_pad(int p) {
+  return (p >= kOffW4 + kGuideOut * 64 && p < kOffB4) || p >= kOffB4 + kGuideOut;
+}
+
+// One training step after the gradient pass, in one kernel: the gradient sum
+// of each parameter (rows in CTA order), Adam on the mean gradient (sum / sum
+// of importance; learning rate g.lr, beta 0.9 / 0.999), and the parameter's
+// BF16 entries in the forward and transposed weight tiles (W2, W3, W4; W1 and
+// the biases stay FP32).  The padding outputs 40-47 stay zero.  Block 0 also
+// stores the importance sum for k_guide_step_done.
 __global__ void k_guide_adam(GuideGPU g) {
+  const uint32_t rows = guide_rows(g);
+  const float ws = guide_weight_sum(g, rows);  // the same value in every thread
+  if (blockIdx.x == 0 && threadIdx.x == 0) *g.weight_sum = ws;
   const uint32_t step = *g.adam_step + 1;
-  const float ws = *g.weight_sum;
   const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;
   const float c1 = 1.0f - powf(b1, (float)step), c2 = 1.0f - powf(b2, (float)step);
   for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < kGuideParams; p += gridDim.x * blockDim.x) {
-    const float gr = ws > 0.0f ? g.grad[p] / ws : 0.0f;
-    g.grad[p] = 0.0f;
-    const bool pad = (p >= kOffW4 + kGuideOut * 64 && p < kOffB4) || p >= kOffB4 + kGuideOut;
-    if (pad || !(ws > 0.0f)) continue;
+    if (guide_pad(p) || !(ws > 0.0f)) continue;
+    const float gr = guide_grad_sum(g, rows, p) / ws;
     const float m = b1 * g.adam_m[p] + (1.0f - b1) * gr;
     const float v = b2 * g.adam_v[p] + (1.0f - b2) * gr * gr;
     g.adam_m[p] = m;
     g.adam_v[p] = v;
-    g.params[p] -= g.lr * (m / c1) / (sqrtf(v / c2) + eps);
+    const float w = g.params[p] - g.lr * (m / c1) / (sqrtf(v / c2) + eps);
+    g.params[p] = w;
+    if (p >= kOffW2 && p < kOffB2) {
+      const int r = (p - kOffW2) / 64, k = (p - kOffW2) % 64;
+      st_bf16(g.tiles + kTileW2, r, k, 64, w);
+      st_bf16(g.tiles + kTileW2T, k, r, 64, w);
+    } else if (p >= kOffW3 && p < kOffB3) {
+      const int r = (p - kOffW3) / 64, k = (p - kOffW3) % 64;
+      st_bf16(g.tiles + kTileW3, r, k, 64, w);
+      st_bf16(g.tiles + kTileW3T, k, r, 64, w);
+    } else if (p >= kOffW4 && p < kOffB4) {
+      const int r = (p - kOffW4) / 64, k = (p - kOffW4) % 64;
+      st_bf16(g.tiles + kTileW4, r, k, 64, w);
+      st_bf16(g.tiles + kTileW4T, k, r, 48, w);
+    }
   }
 }
 
@@ -357,22 +395,13 @@ __global__ void __launch_bounds__(kSelectBlock) k_guide_select_write(GuideGPU g,
   }
 }
 
-// The step's gradient and importance sums: the training CTAs' rows added in
-// CTA order.  Rows of CTAs that had no tile are not read.
+// The step's gradient and importance sums alone (fr_guide_gradient): the
+// same sums k_guide_adam forms.
 __global__ void k_guide_reduce(GuideGPU g) {
-  const uint32_t n_all = min(*g.batch_count, (uint32_t)g.batch_cap);
-  const uint32_t rows = min((n_all + 127) / 128, (uint32_t)g.train_ctas);
-  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < kGuideParams; p += gridDim.x * blockDim.x) {
-    float sum = 0.0f;
-    for (uint32_t r = 0; r < rows; ++r) sum += g.grad_part[(size_t)r * kGuideParams + p];
-    const bool pad = (p >= kOffW4 + kGuideOut * 64 && p < kOffB4) || p >= kOffB4 + kGuideOut;
-    g.grad[p] = pad ? 0.0f : sum;
-  }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    float ws = 0.0f;
-    for (uint32_t r = 0; r < rows; ++r) ws += g.wsum_part[r];
-    *g.weight_sum = ws;
-  }
+  const uint32_t rows = guide_rows(g);
+  for (int p = blockIdx.x * blockDim.x + threadIdx.x; p < kGuideParams; p += gridDim.x * blockDim.x)
+    g.grad[p] = guide_pad(p) ? 0.0f : guide_grad_sum(g, rows, p);
+  if (blockIdx.x == 0 && threadIdx.x == 0) *g.weight_sum = guide_weight_sum(g, rows);
 }
 
 inline void launch_guide_select(const GuideGPU& g, int paths, cudaStream_t s) {
@@ -392,12 +421,10 @@ int launch_guide_train(const GuideGPU& g, int paths, cudaStream_t s) {
   launch_guide_select(g, paths, s);
   for (int k = 0; k < g.steps; ++k) {
     k_guide_train<<<g.train_ctas, 128, kTrainSmem, s>>>(g);
-    k_guide_reduce<<<(kGuideParams + 255) / 256, 256, 0, s>>>(g);
     k_guide_adam<<<(kGuideParams + 255) / 256, 256, 0, s>>>(g);
-    k_guide_prepare<<<16, 256, 0, s>>>(g);
     k_guide_step_done<<<1, 1, 0, s>>>(g, k == g.steps - 1);
   }
-  return 3 + 5 * g.steps;
+  return 3 + 3 * g.steps;
 }
 
 void launch_guide_prepare(const GuideGPU& g, cudaStream_t s) { k_guide_prepare<<<16, 256, 0, s>>>(g); }
