@@ -502,7 +502,8 @@ def run_large(args):
 BATCH_WORKLOAD = ('batched uneven SPPM: 64 seeded scenes of the mixed-materials construction, triangles '
                   'log-uniform over 10k-2M (30.5M in all), resolutions uniform over 128^2/256^2/512^2/1024^2, '
                   '50k-1M photon paths/iteration each (33.8M in all), 256^2 textures, alpha 0.7, r0 0.02; '
-                  'all contexts advanced together by fr_iterate_batch, each autotuned by fr_autotune')
+                  'each context autotuned by fr_autotune, then all advanced by one batch graph (fr_batch_create: '
+                  'one graph launch per step for all 64 scenes)')
 
 
 def run_batch(args):
@@ -541,12 +542,22 @@ def run_batch(args):
         r.synchronize()
         seq_ms += a.elapsed_time(b) / 2
     W = max(3, args.warmup)
+    # The same steps with one graph per context (fr_iterate_batch), for
+    # comparison with the batch graph below.
     abi.iterate_batch(rs, W)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    abi.iterate_batch(rs, args.steps)
+    per_context_dt = time.perf_counter() - t0
+    # One graph holding an iteration of every scene (fr_batch_create): one
+    # graph launch per step.
+    batch = abi.Batch(rs)
+    batch.iterate(W)
     torch.cuda.synchronize()
     l0 = sum(r.profile_read()[2] for r in rs)
     with ClockSampler(0) as clk:
         t0 = time.perf_counter()
-        abi.iterate_batch(rs, args.steps)
+        batch.iterate(args.steps)
         dt = time.perf_counter() - t0
     launches = sum(r.profile_read()[2] for r in rs) - l0
     # End to end: every step, every scene's image copied into pinned host
@@ -558,7 +569,7 @@ def run_batch(args):
     t0 = time.perf_counter()
     prev = None
     for k in range(args.steps):
-        abi.iterate_batch(rs, 1)
+        batch.iterate(1, sync=False)
         tickets = [r.resolve_async(h[k % 2].data_ptr()) for r, h in zip(rs, hosts)]
         if prev is not None:
             for r, t in zip(rs, prev):
@@ -572,6 +583,7 @@ def run_batch(args):
     pixels = sum(r.width * r.height for r in rs)
     dev = sum(r.stats()['device_bytes'] for r in rs)
     tris = sum(len(sc['pos']) for sc in scene_list)
+    batch.close()
     for r in rs:
         r.close()
     hist = {}
@@ -587,6 +599,10 @@ def run_batch(args):
            'sequential': {'ms_per_step': seq_ms, 'value': photons / (seq_ms / 1e3),
                           'note': 'sum over the scenes of one graph replay alone (CUDA events)'},
            'batch_speedup': seq_ms / (1e3 * dt / args.steps),
+           'graph_launches_per_step': 1,
+           'per_context_graphs': {'ms_per_step': 1e3 * per_context_dt / args.steps,
+                                  'value': photons * args.steps / per_context_dt,
+                                  'note': 'fr_iterate_batch: one graph launch per scene and step'},
            'autotune': {'photon_tail_min_chosen': hist},
            'setup': {'scene_generation_s': gen_s, 'contexts_s': setup_s, 'device_bytes': int(dev)},
            'e2e': {'value': photons * args.steps / e2e_dt, 'unit': UNIT, 'h2d_bytes_per_step': 0,
@@ -664,7 +680,7 @@ def other_workloads():
             out[name] = {'unavailable': 'the --workload %s run failed' % name}
             continue
         keep = ('value', 'unit', 'ms_per_step', 'steps', 'warmup', 'hitpoint_updates_per_s', 'e2e', 'gpu_launches',
-                'clocks', 'batch_speedup', 'sequential', 'setup')
+                'clocks', 'batch_speedup', 'sequential', 'setup', 'graph_launches_per_step', 'per_context_graphs')
         out[name] = {k: line[k] for k in keep if k in line}
         out[name]['workload'] = line['config']['workload']
         out[name]['run_s'] = time.perf_counter() - t0

@@ -11,6 +11,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <thread>
@@ -964,6 +965,99 @@ int fr_iterate_batch(fr_ctx* const* ctxs, int count, int n) {
     }
   return FR_OK;
 }
+
+struct fr_batch {
+  std::vector<fr_ctx*> ctxs;
+  std::vector<int64_t> launches;  // per context: kernels of one iteration
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr, done = nullptr;
+  std::vector<cudaEvent_t> ready;  // per context: its stream's prior work
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  ~fr_batch() {
+    if (exec) cudaGraphExecDestroy(exec);
+    if (graph) cudaGraphDestroy(graph);
+    for (cudaEvent_t e : ready) cudaEventDestroy(e);
+    if (fork) cudaEventDestroy(fork);
+    if (done) cudaEventDestroy(done);
+    if (stream) cudaStreamDestroy(stream);
+  }
+};
+
+// One capture on the batch's stream: a fork event joins every context's main
+// stream (and through enqueue_iteration its eye stream and the streams of the
+// conditional photon rounds), each context enqueues one iteration, and the
+// batch stream joins them all.
+int fr_batch_create(fr_ctx* const* ctxs, int count, fr_batch** out) {
+  if (!ctxs || count < 1 || !out) return fail(FR_ERR_INVALID, "fr_batch_create: bad arguments");
+  *out = nullptr;
+  for (int j = 0; j < count; ++j) {
+    if (!ctxs[j]) return fail(FR_ERR_INVALID, "fr_batch_create: context %d is NULL", j);
+    if (ctxs[j]->profiling) return fail(FR_ERR_INVALID, "fr_batch_create: context %d has the stage profiler on", j);
+  }
+  std::unique_ptr<fr_batch> b(new fr_batch());
+  b->ctxs.assign(ctxs, ctxs + count);
+  FR_CUDA(cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking));
+  FR_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+  FR_CUDA(cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming));
+  b->ready.resize(count);
+  for (int j = 0; j < count; ++j) FR_CUDA(cudaEventCreateWithFlags(&b->ready[j], cudaEventDisableTiming));
+  std::vector<cudaEvent_t> join(count);
+  for (int j = 0; j < count; ++j) FR_CUDA(cudaEventCreateWithFlags(&join[j], cudaEventDisableTiming));
+  auto drop_joins = [&]() {
+    for (cudaEvent_t e : join) cudaEventDestroy(e);
+  };
+  FR_CUDA(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+  int rc = FR_OK;
+  cudaEventRecord(b->fork, b->stream);
+  for (int j = 0; j < count && !rc; ++j) {
+    fr_ctx* c = ctxs[j];
+    cudaStreamWaitEvent(c->stream, b->fork, 0);
+    const int64_t before = c->launches;
+    c->capturing = true;
+    rc = enqueue_iteration(c);
+    c->capturing = false;
+    b->launches.push_back(c->launches - before);
+    c->launches = before;
+    cudaEventRecord(join[j], c->stream);
+    cudaStreamWaitEvent(b->stream, join[j], 0);
+  }
+  cudaGraph_t g = nullptr;
+  const cudaError_t ec = cudaStreamEndCapture(b->stream, &g);
+  drop_joins();
+  if (rc) {
+    if (g) cudaGraphDestroy(g);
+    return rc;
+  }
+  if (ec != cudaSuccess) return fail(FR_ERR_CUDA, "batch capture: %s", cudaGetErrorString(ec));
+  b->graph = g;
+  FR_CUDA(cudaGraphInstantiate(&b->exec, b->graph, 0));
+  *out = b.release();
+  return FR_OK;
+}
+
+int fr_batch_iterate(fr_batch* b, int n) {
+  if (!b || n < 0) return fail(FR_ERR_INVALID, "fr_batch_iterate: bad arguments");
+  if (!n) return FR_OK;
+  const size_t count = b->ctxs.size();
+  for (size_t j = 0; j < count; ++j) {
+    if (b->ctxs[j]->profiling) return fail(FR_ERR_INVALID, "fr_batch_iterate: context %zu has the stage profiler on", j);
+    FR_CUDA(cudaEventRecord(b->ready[j], b->ctxs[j]->stream));
+    FR_CUDA(cudaStreamWaitEvent(b->stream, b->ready[j], 0));
+  }
+  for (int k = 0; k < n; ++k) FR_CUDA(cudaGraphLaunch(b->exec, b->stream));
+  FR_CUDA(cudaEventRecord(b->done, b->stream));
+  for (size_t j = 0; j < count; ++j) {
+    fr_ctx* c = b->ctxs[j];
+    FR_CUDA(cudaStreamWaitEvent(c->stream, b->done, 0));
+    c->iterations += n;
+    c->photons_total += (int64_t)c->P * n;
+    c->launches += b->launches[j] * n;
+  }
+  return FR_OK;
+}
+
+void fr_batch_destroy(fr_batch* b) { delete b; }
 
 namespace {
 // Graph replay time of `iterations` iterations (ms); the graph is captured

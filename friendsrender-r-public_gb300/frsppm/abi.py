@@ -77,7 +77,8 @@ EXPORTS = ['fr_last_error', 'fr_create', 'fr_iterate', 'fr_synchronize', 'fr_res
            'fr_resolve_rgba8', 'fr_export_png', 'fr_write_png', 'fr_check_tc_gemm', 'fr_guide_params',
            'fr_guide_set_params', 'fr_read_guide_importance', 'fr_guide_gradient', 'fr_seek', 'fr_iterate_batch',
            'fr_autotune', 'fr_update_dev', 'fr_read_direct', 'fr_scene_load_obj', 'fr_scene_get_desc',
-           'fr_scene_material_name', 'fr_scene_free', 'fr_texture_load', 'fr_resolve_async', 'fr_resolve_wait']
+           'fr_scene_material_name', 'fr_scene_free', 'fr_texture_load', 'fr_resolve_async', 'fr_resolve_wait',
+           'fr_batch_create', 'fr_batch_iterate', 'fr_batch_destroy']
 
 STAGES = ('eye', 'photon', 'grid', 'gather', 'eye_trace', 'photon_trace')
 
@@ -143,6 +144,10 @@ def load(path=None):
     lib.fr_scene_free.argtypes = [vp]
     lib.fr_scene_free.restype = None
     lib.fr_texture_load.argtypes = [C.c_char_p, C.POINTER(i32), C.POINTER(i32), C.POINTER(i32), vp]
+    lib.fr_batch_create.argtypes = [C.POINTER(vp), C.c_int, C.POINTER(vp)]
+    lib.fr_batch_iterate.argtypes = [vp, C.c_int]
+    lib.fr_batch_destroy.argtypes = [vp]
+    lib.fr_batch_destroy.restype = None
     _lib = lib
     return lib
 
@@ -454,6 +459,35 @@ def check_tc_gemm(seed=1):
     err = np.zeros(3, np.float64)
     _check(lib.fr_check_tc_gemm(int(seed), _ptr(err)), 'fr_check_tc_gemm')
     return err
+
+
+class Batch:
+    """fr_batch_create over Renderer objects: one CUDA graph holding one
+    iteration of every scene; iterate(n) launches it n times."""
+
+    def __init__(self, renderers):
+        self.renderers = list(renderers)
+        arr = (C.c_void_p * len(self.renderers))(*[r.h.value if isinstance(r.h, C.c_void_p) else r.h
+                                                   for r in self.renderers])
+        self.h = C.c_void_p()
+        _check(_lib.fr_batch_create(arr, len(self.renderers), C.byref(self.h)), 'fr_batch_create')
+
+    def iterate(self, n=1, sync=True):
+        _check(_lib.fr_batch_iterate(self.h, int(n)), 'fr_batch_iterate')
+        if sync:
+            for r in self.renderers:
+                r.synchronize()
+
+    def close(self):
+        if getattr(self, 'h', None):
+            _lib.fr_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
 
 
 def iterate_batch(renderers, n=1, sync=True):

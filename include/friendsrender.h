@@ -262,6 +262,24 @@ int fr_synchronize(fr_ctx* ctx);
  * Asynchronous; fr_synchronize each context. */
 int fr_iterate_batch(fr_ctx* const* ctxs, int count, int n);
 
+/* A batch graph (no counterpart in the reference): one CUDA graph holding one
+ * iteration of every context of the batch, captured once by fr_batch_create,
+ * so that fr_batch_iterate advances all the scenes with one graph launch per
+ * iteration (fr_iterate_batch launches one graph per context).  The scenes'
+ * iterations are independent branches of the graph and run concurrently.
+ * Results are those of fr_iterate.  The batch keeps pointers to the
+ * contexts: destroy it before them, and create it after fr_autotune (a
+ * context's photon wavefront threshold is part of the captured graph).
+ * fr_batch_iterate orders itself after the work already enqueued on each
+ * context's stream and before the work enqueued there after it, so
+ * fr_synchronize, fr_resolve and the other calls on a context see its
+ * iterations; asynchronous like fr_iterate.  No context may have the stage
+ * profiler on. */
+typedef struct fr_batch fr_batch;
+int fr_batch_create(fr_ctx* const* ctxs, int count, fr_batch** out);
+int fr_batch_iterate(fr_batch* batch, int n);
+void fr_batch_destroy(fr_batch* batch);
+
 /* Autotuner (no counterpart in the reference): picks the context's photon
  * wavefront threshold (a round with fewer live paths hands them to the tail
  * kernel) from 4096, 8192, 16384, 32768 and 65536 by timing `iterations`

@@ -58,3 +58,27 @@ def test_autotune_iterations_are_ordinary():
         a.iterate(2)
         b.iterate(2)
         _same(a, b)
+
+
+def test_batch_graph_equals_single():
+    """fr_batch_create / fr_batch_iterate: one graph launch per iteration for
+    all the scenes gives each scene what fr_iterate gives it, also when
+    batch iterations and a context's own iterations alternate."""
+    from frsppm import abi
+    pairs = [(abi.Renderer(sc, p, alpha=0.7, radius=0.02), abi.Renderer(sc, p, alpha=0.7, radius=0.02))
+             for sc, p in _scenes()]
+    try:
+        with abi.Batch([a for a, _ in pairs]) as batch:
+            batch.iterate(2)
+            pairs[1][0].iterate(1)
+            batch.iterate(1)
+        for j, (_, b) in enumerate(pairs):
+            b.iterate(4 if j == 1 else 3)
+        for a, b in pairs:
+            _same(a, b)
+            np.testing.assert_array_equal(a.resolve(), a.resolve())
+        assert pairs[0][0].stats()['iterations'] == 3
+    finally:
+        for a, b in pairs:
+            a.close()
+            b.close()
