@@ -102,12 +102,15 @@ def test_gpu_matches_oracle(name):
     _image_close(ig, ic)
 
 
-# The mixed-materials and caustic configurations at full size: 1280x720 thin
-# lens with 1M photon paths (997,444 triangles, textures), and the 1024^2
-# caustic box with 2M photon paths (198,936 triangles).
+# The mixed-materials, caustic and large-scene configurations at full size:
+# 1280x720 thin lens with 1M photon paths (997,444 triangles, textures), the
+# 1024^2 caustic box with 2M photon paths (198,936 triangles), and the large
+# scene (20,000,004 triangles, 4096^2 textures, 3840x2160 thin lens) with 8M
+# photon paths, without its learned guide (the oracle has none).
 FULL = {
     'mixed_materials_1280x720_1M': (lambda s: s.mixed_materials(), 1_000_000, 2, 0.7, 0.02),
     'caustic_box_1024_2M': (lambda s: s.caustic_box(), 2_000_000, 1, 0.7, 0.01),
+    'large_scene_3840x2160_8M': (lambda s: s.large_scene(), 8_000_000, 1, 0.7, 0.02),
 }
 
 
