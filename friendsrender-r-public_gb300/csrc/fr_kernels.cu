@@ -31,6 +31,20 @@
 
 namespace fr {
 
+// Occupancy floor (blocks of 128 threads per SM) for the trace kernels'
+// register allocation, as a __launch_bounds__ minimum: 7 blocks keep them at
+// 72 registers with the near/far plane loads of visit_node, which take 80
+// otherwise (6 blocks per SM; mixed materials 4.05 ms per iteration against
+// 3.98 with the floor).  0 states only the block size.
+#ifndef FR_TRACE_MIN_BLOCKS
+#define FR_TRACE_MIN_BLOCKS 7
+#endif
+#if FR_TRACE_MIN_BLOCKS > 0
+#define FR_TRACE_BOUNDS __launch_bounds__(128, FR_TRACE_MIN_BLOCKS)
+#else
+#define FR_TRACE_BOUNDS __launch_bounds__(128)
+#endif
+
 namespace {
 
 __device__ __forceinline__ bool near1(float s) { return fabsf(s - 1.0f) < kLt1e5; }  // SPPM.h:27-29
@@ -349,7 +363,7 @@ __global__ void __launch_bounds__(128) k_ew_start(CameraGPU cam, IterParams it, 
 // Closest hit of every path in queue `round`, for queues of coherent rays
 // (camera rays in pixel order): each warp takes 32 consecutive entries.
 template <bool kWT>
-__global__ void __launch_bounds__(128) k_wave_trace_static(SceneGPU sc, PathWave w, int round, int* err) {
+__global__ void FR_TRACE_BOUNDS k_wave_trace_static(SceneGPU sc, PathWave w, int round, int* err) {
   if (round_skipped(w, round)) return;
   const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
   const uint32_t* q = w.queue[round & 1];
@@ -371,7 +385,7 @@ __global__ void __launch_bounds__(128) k_wave_trace_static(SceneGPU sc, PathWave
 // The traversal is trace_closest's (fr_trace.cuh), one node visit or leaf per
 // loop pass, so the hits are the same.
 template <bool kWT>
-__global__ void __launch_bounds__(128) k_wave_trace(SceneGPU sc, PathWave w, int round, int* err) {
+__global__ void FR_TRACE_BOUNDS k_wave_trace(SceneGPU sc, PathWave w, int round, int* err) {
   if (round_skipped(w, round)) return;
   const uint32_t n = *(volatile uint32_t*)(w.qcount + round);
   const uint32_t* q = w.queue[round & 1];

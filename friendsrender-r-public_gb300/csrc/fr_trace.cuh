@@ -131,6 +131,40 @@ struct NodeVisit {
   uint32_t meta_lo, meta_hi;
 };
 
+// Child slab tests.  With FR_NEAR_FAR (the default) each axis reads its near
+// plane from the lo array and its far plane from the hi array when the ray's
+// inverse direction on that axis is positive, and the other way round when
+// it is negative: fma(b, idir, -o*idir) is monotonic in b, so these are the
+// min and the max of the two plane distances without computing both and
+// comparing (the same t0 and t1 bit for bit, for boxes with lo <= hi; empty
+// slots are masked out by their meta byte).  FR_MINMAX3 takes the entry and
+// exit distances with three-input min/max instructions.
+#ifndef FR_NEAR_FAR
+#define FR_NEAR_FAR 1
+#endif
+#ifndef FR_MINMAX3
+#define FR_MINMAX3 0
+#endif
+
+__device__ __forceinline__ float max3f(float a, float b, float c) {
+#if FR_MINMAX3
+  float d;
+  asm("max.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+#else
+  return fmaxf(fmaxf(a, b), c);
+#endif
+}
+__device__ __forceinline__ float min3f(float a, float b, float c) {
+#if FR_MINMAX3
+  float d;
+  asm("min.f32 %0, %1, %2, %3;" : "=f"(d) : "f"(a), "f"(b), "f"(c));
+  return d;
+#else
+  return fminf(fminf(a, b), c);
+#endif
+}
+
 __device__ __forceinline__ void visit_node(const BVHNodeW* nodes, uint32_t ni, const RayPre& r, float tmin,
                                            float tmax, NodeVisit& nv) {
   const float4* q = reinterpret_cast<const float4*>(nodes + ni);
@@ -141,7 +175,14 @@ __device__ __forceinline__ void visit_node(const BVHNodeW* nodes, uint32_t ni, c
     arr[0] = a_.x; arr[1] = a_.y; arr[2] = a_.z; arr[3] = a_.w;   \
     arr[4] = b_.x; arr[5] = b_.y; arr[6] = b_.z; arr[7] = b_.w;   \
   }
+#if FR_NEAR_FAR
+  // lx/ly/lz: near planes, hx/hy/hz: far planes (float4 offsets: lo x 0, lo y
+  // 2, lo z 4, hi x 6, hi y 8, hi z 10).
+  const int nx = r.idx < 0.0f ? 6 : 0, ny = r.idy < 0.0f ? 8 : 2, nz = r.idz < 0.0f ? 10 : 4;
+  FR_LD8(lx, nx) FR_LD8(ly, ny) FR_LD8(lz, nz) FR_LD8(hx, 6 - nx) FR_LD8(hy, 10 - ny) FR_LD8(hz, 14 - nz)
+#else
   FR_LD8(lx, 0) FR_LD8(ly, 2) FR_LD8(lz, 4) FR_LD8(hx, 6) FR_LD8(hy, 8) FR_LD8(hz, 10)
+#endif
 #undef FR_LD8
   const uint4 m0 = __ldg(reinterpret_cast<const uint4*>(q + 12));
   const uint4 m1 = __ldg(reinterpret_cast<const uint4*>(q + 13));
@@ -158,8 +199,13 @@ __device__ __forceinline__ void visit_node(const BVHNodeW* nodes, uint32_t ni, c
     const float ax = fmaf(lx[c], r.idx, -ox), bx = fmaf(hx[c], r.idx, -ox);
     const float ay = fmaf(ly[c], r.idy, -oy), by = fmaf(hy[c], r.idy, -oy);
     const float az = fmaf(lz[c], r.idz, -oz), bz = fmaf(hz[c], r.idz, -oz);
-    const float t0 = fmaxf(fmaxf(fminf(ax, bx), fminf(ay, by)), fmaxf(fminf(az, bz), tmin));
-    const float t1 = fminf(fminf(fmaxf(ax, bx), fmaxf(ay, by)), fminf(fmaxf(az, bz), tmax));
+#if FR_NEAR_FAR
+    const float t0 = max3f(ax, ay, fmaxf(az, tmin));
+    const float t1 = min3f(bx, by, fminf(bz, tmax));
+#else
+    const float t0 = max3f(fminf(ax, bx), fminf(ay, by), fmaxf(fminf(az, bz), tmin));
+    const float t1 = min3f(fmaxf(ax, bx), fmaxf(ay, by), fminf(fmaxf(az, bz), tmax));
+#endif
     const uint32_t mw = c < 4 ? m1.x : m1.y;
     const bool valid = ((mw >> (8 * (c & 3))) & 0xFFu) != 0u;
     nv.key[c] = (valid && t0 <= t1) ? ((__float_as_uint(t0) & ~7u) | (uint32_t)c) : 0xFFFFFFFFu;
