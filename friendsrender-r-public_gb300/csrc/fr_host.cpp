@@ -1481,14 +1481,15 @@ int fr_update(fr_ctx* c, const int32_t* m, const float* phi) {
   for (size_t i = 0; i < np; ++i) phi4[i] = make_float4(phi[3 * i], phi[3 * i + 1], phi[3 * i + 2], 0.0f);
   FR_CUDA(cudaMemcpyAsync(c->dbg_m, m, sizeof(int32_t) * np, cudaMemcpyHostToDevice, c->stream));
   FR_CUDA(cudaMemcpyAsync(c->dbg_phi, phi4.data(), sizeof(float4) * np, cudaMemcpyHostToDevice, c->stream));
-  launch_update(c->st, c->dbg_m, c->dbg_phi, (int)np, c->alpha, c->stream);
+  launch_update(c->st, c->dbg_m, c->dbg_phi, (int)np, c->alpha, (c->flags & kFlagFloatPhotonCount) != 0u, c->stream);
   return fr_synchronize(c);
 }
 
 int fr_update_dev(fr_ctx* c, const int32_t* m_dev, const float* phi4_dev) {
   if (!c || !m_dev || !phi4_dev) return fail(FR_ERR_INVALID, "fr_update_dev: bad arguments");
   if ((reinterpret_cast<uintptr_t>(phi4_dev) & 15u) != 0) return fail(FR_ERR_INVALID, "fr_update_dev: phi4 not 16-byte aligned");
-  launch_update(c->st, m_dev, reinterpret_cast<const float4*>(phi4_dev), c->W * c->H, c->alpha, c->stream);
+  launch_update(c->st, m_dev, reinterpret_cast<const float4*>(phi4_dev), c->W * c->H, c->alpha,
+                (c->flags & kFlagFloatPhotonCount) != 0u, c->stream);
   FR_CUDA(cudaGetLastError());
   return FR_OK;
 }

@@ -1166,6 +1166,25 @@ __device__ __forceinline__ double tau_update(double tau, float phi, float a, flo
   return (tau + (double)phi) * ((double)q.h + (double)q.l);
 }
 
+// The N/R update factors of SPPM.cpp:444-449, a = N + alpha M and b = N + M,
+// and the new N.  The reference keeps N as an int, so N += M * alpha
+// truncates (SPPM.h:119, SPPM.cpp:447); with kFlagFloatPhotonCount the same
+// four bytes hold N as a float and nothing is truncated.
+__device__ __forceinline__ void photon_count_update(int32_t n_bits, int M, float alpha, bool float_n, float& a,
+                                                    float& b, int32_t& n_new) {
+  if (float_n) {
+    const float N = __int_as_float(n_bits);
+    a = N + alpha * (float)M;
+    b = N + (float)M;
+    n_new = __float_as_int(N + (float)M * alpha);
+  } else {
+    const int N = n_bits;
+    a = (float)N + alpha * (float)M;
+    b = (float)(N + M);
+    n_new = (int)((float)N + (float)M * alpha);
+  }
+}
+
 // applyHitPointInfo (SPPM.cpp:395-451) with one group of G lanes per hitpoint
 // of the hitpoint list (32 / G hitpoints per warp at a time: a hitpoint's
 // work is a chain of dependent loads, so several in flight per warp hide
@@ -1295,15 +1314,15 @@ __global__ void __launch_bounds__(256) k_gather(SceneGPU sc, IterParams it, Hitp
     }
     if (M > 0 && gl < 3) {
       // N/tau/R update (SPPM.cpp:444-449); group lane c updates tau component c.
-      const int N = st.n[i];
-      const float a = (float)N + it.alpha * (float)M;
-      const float b = (float)(N + M);
+      float a, b;
+      int32_t n_new;
+      photon_count_update(st.n[i], M, it.alpha, (it.flags & kFlagFloatPhotonCount) != 0u, a, b, n_new);
       double* tau = st.tau + 3 * (size_t)i + gl;
       const float v = gl == 0 ? vx : (gl == 1 ? vy : vz);
       *tau = tau_update(*tau, v, a, b);
       if (gl == 0) {
         st.r[i] = R * sqrtf(a / b);
-        st.n[i] = (int)((float)N + (float)M * it.alpha);
+        st.n[i] = n_new;
         st.g[i] += 1;
       }
     }
@@ -1312,21 +1331,22 @@ __global__ void __launch_bounds__(256) k_gather(SceneGPU sc, IterParams it, Hitp
 
 // The N/tau/R update alone (SPPM.cpp:444-449) from given per-pixel photon
 // counts m and flux sums phi; the same arithmetic as the gather's update.
-__global__ void k_update(PixelState st, const int32_t* m, const float4* phi, int pixels, float alpha) {
+__global__ void k_update(PixelState st, const int32_t* m, const float4* phi, int pixels, float alpha,
+                         bool float_n) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= pixels) return;
   const int M = m[i];
   if (M <= 0) return;
-  const int N = st.n[i];
-  const float a = (float)N + alpha * (float)M;
-  const float b = (float)(N + M);
+  float a, b;
+  int32_t n_new;
+  photon_count_update(st.n[i], M, alpha, float_n, a, b, n_new);
   const float4 v = phi[i];
   double* tau = st.tau + 3 * (size_t)i;
   tau[0] = tau_update(tau[0], v.x, a, b);
   tau[1] = tau_update(tau[1], v.y, a, b);
   tau[2] = tau_update(tau[2], v.z, a, b);
   st.r[i] = st.r[i] * sqrtf(a / b);
-  st.n[i] = (int)((float)N + (float)M * alpha);
+  st.n[i] = n_new;
   st.g[i] += 1;
 }
 
@@ -1624,8 +1644,9 @@ int gather_blocks_per_sm() {
   return b;
 }
 
-void launch_update(PixelState st, const int32_t* m, const float4* phi, int pixels, float alpha, cudaStream_t s) {
-  k_update<<<blocks_for(pixels, 256), 256, 0, s>>>(st, m, phi, pixels, alpha);
+void launch_update(PixelState st, const int32_t* m, const float4* phi, int pixels, float alpha, bool float_n,
+                   cudaStream_t s) {
+  k_update<<<blocks_for(pixels, 256), 256, 0, s>>>(st, m, phi, pixels, alpha, float_n);
 }
 
 void launch_export_rgba8(const float4* img, int width, int height, uint32_t* out, cudaStream_t s) {

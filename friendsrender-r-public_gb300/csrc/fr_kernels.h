@@ -171,7 +171,9 @@ int gather_blocks_per_sm();
 // ExportPNG's resample and 8-bit quantization of a resolved image.
 void launch_export_rgba8(const float4* img, int width, int height, uint32_t* out, cudaStream_t s);
 // The N/tau/R update from given per-pixel photon counts and flux sums.
-void launch_update(PixelState st, const int32_t* m, const float4* phi, int pixels, float alpha, cudaStream_t s);
+// float_n: N held as float bits (kFlagFloatPhotonCount).
+void launch_update(PixelState st, const int32_t* m, const float4* phi, int pixels, float alpha, bool float_n,
+                   cudaStream_t s);
 void launch_resolve(PixelState st, int pixels, double photons_total, double iterations, bool standard, float4* out,
                     cudaStream_t s);
 

@@ -154,6 +154,7 @@ constexpr uint32_t kFlagFixStaleSlot = 1u;  // drop the stale photon slot quirk 
 constexpr uint32_t kFlagStandardResolve = 2u;  // resolve with tau / (pi R^2 * photons emitted)
 constexpr uint32_t kFlagEndDegenerate = 4u;    // end paths with a NaN BSDF value or pdf, or a zero pdf
 constexpr uint32_t kFlagWatertight = 8u;       // watertight triangle test instead of Moller-Trumbore
+constexpr uint32_t kFlagFloatPhotonCount = 16u;  // per-pixel N kept as float bits, not a truncated int
 
 // Entries of the per-thread traversal stack (a wide node pushes at most 7).
 constexpr int kTraversalStackEntries = 96;

@@ -59,6 +59,7 @@ FLAG_FIX_STALE_PHOTON_SLOT = 1   # FR_FLAG_FIX_STALE_PHOTON_SLOT
 FLAG_STANDARD_RESOLVE = 2        # FR_FLAG_STANDARD_RESOLVE
 FLAG_END_DEGENERATE_PATHS = 4    # FR_FLAG_END_DEGENERATE_PATHS
 FLAG_WATERTIGHT = 8              # FR_FLAG_WATERTIGHT
+FLAG_FLOAT_PHOTON_COUNT = 16     # FR_FLAG_FLOAT_PHOTON_COUNT
 BVH_HOST_SAH, BVH_DEVICE_LBVH = 0, 1  # FR_BVH_*
 
 

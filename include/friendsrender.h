@@ -139,7 +139,14 @@ enum {
    * where Moller-Trumbore's rounding can let it pass between them.  Same
    * acceptance rule (t > 1e-4, nearest t, equal t to the larger facet index)
    * and the same (u, v) meaning.  Off by default (the reference's test). */
-  FR_FLAG_WATERTIGHT = 8u
+  FR_FLAG_WATERTIGHT = 8u,
+  /* Keep each pixel's accumulated photon count N (SharedHitPoint::NumPhoton,
+   * SPPM.h:119) as a float.  The reference keeps an int, so N += M * alpha
+   * truncates (SPPM.cpp:447) and the radius shrinks on a count that loses
+   * up to one photon per update.  The per-pixel N that fr_read_state and the
+   * checkpoint return then holds the float's bits.  Off by default (the
+   * reference's count). */
+  FR_FLAG_FLOAT_PHOTON_COUNT = 16u
 };
 
 typedef struct fr_sppm_params {

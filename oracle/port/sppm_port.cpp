@@ -782,7 +782,8 @@ struct HitPoint {  // SPPM.h:83-110
   const Material* m = nullptr;
 };
 struct Photon { V pos, flux, dir; Real index, pdf; bool valid = false; };  // SPPM.h:128-143
-struct Shared { V rad; int n = 0; Real r = 0; int g = 0; V dl; int ndl = 0; };  // SPPM.h:112-126
+// SPPM.h:112-126; nf is N as a float (FR_FLAG_FLOAT_PHOTON_COUNT).
+struct Shared { V rad; int n = 0; Real r = 0; int g = 0; V dl; int ndl = 0; float nf = 0.0f; };
 
 struct KdNode { int photon, axis, left, right; };
 
@@ -804,6 +805,7 @@ struct Renderer {
   // is NaN or whose pdf is zero, and a photon path whose flux or PDF product
   // is no longer finite.
   bool end_degenerate = false;
+  bool float_count = false;  // FR_FLAG_FLOAT_PHOTON_COUNT
   uint32_t stream_key = 0x5350504Du;  // second Philox key word of every stream
   // Pixels the eye pass and the gather cover: [x0, x1) x [y0, y1); the rest
   // get no hitpoint (for oracle images of a window of the frame).
@@ -1197,10 +1199,17 @@ struct Renderer {
       gather_m[v] = m;
       gather_phi[v] = add;
       if (m > 0) {
-        const Real a = s.n + alpha * m, b = (Real)(s.n + m);
-        s.rad = (s.rad + add) * a / b;
-        s.r *= std::sqrt(a / b);
-        s.n += m * alpha;
+        if (float_count) {  // N as a float: nothing truncated
+          const Real a = s.nf + alpha * m, b = s.nf + (Real)m;
+          s.rad = (s.rad + add) * a / b;
+          s.r *= std::sqrt(a / b);
+          s.nf = (float)(s.nf + m * alpha);
+        } else {
+          const Real a = s.n + alpha * m, b = (Real)(s.n + m);
+          s.rad = (s.rad + add) * a / b;
+          s.r *= std::sqrt(a / b);
+          s.n += m * alpha;
+        }
         s.g++;
       }
     }
@@ -1389,6 +1398,9 @@ void port_seek(void* h, int32_t first_step) { static_cast<Renderer*>(h)->step = 
 // The precision mode's watertight triangle test (FR_FLAG_WATERTIGHT) on or off.
 void port_set_watertight(void* h, int32_t on) { static_cast<Renderer*>(h)->watertight = on != 0; }
 
+// FR_FLAG_FLOAT_PHOTON_COUNT on or off.
+void port_set_float_count(void* h, int32_t on) { static_cast<Renderer*>(h)->float_count = on != 0; }
+
 // FR_FLAG_END_DEGENERATE_PATHS on or off.
 void port_set_end_degenerate(void* h, int32_t on) { static_cast<Renderer*>(h)->end_degenerate = on != 0; }
 
@@ -1509,7 +1521,8 @@ void port_read_state(void* h, Real* rad, int32_t* n, Real* rr, int32_t* g) {
   for (size_t i = 0; i < r->sp.size(); ++i) {
     const Shared& s = r->sp[i];
     rad[3 * i] = s.rad.x; rad[3 * i + 1] = s.rad.y; rad[3 * i + 2] = s.rad.z;
-    n[i] = s.n;
+    if (r->float_count) std::memcpy(&n[i], &s.nf, 4);  // the float's bits, as the GPU returns them
+    else n[i] = s.n;
     rr[i] = s.r;
     g[i] = s.g;
   }

@@ -62,6 +62,7 @@ def load(kind='f32'):
         lib.port_set_watertight.argtypes = [vp, C.c_int32]
         lib.port_set_stream_key.argtypes = [vp, C.c_uint32]
         lib.port_set_end_degenerate.argtypes = [vp, C.c_int32]
+        lib.port_set_float_count.argtypes = [vp, C.c_int32]
         lib.port_set_window.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
         lib.port_sample_rays.argtypes = [vp, C.c_int64, C.c_int64]
         lib.port_read_ray_sample.argtypes = [vp, vp]
@@ -118,7 +119,8 @@ def radius_count(hp_pos, hp_r, photons):
 class PortRenderer:
     """The CPU restatement on a scene dict from frsppm.scenes."""
 
-    def __init__(self, scene, photons, alpha=0.9, radius=0.015, fix_stale=False, watertight=False, kind='f32'):
+    def __init__(self, scene, photons, alpha=0.9, radius=0.015, fix_stale=False, watertight=False, kind='f32',
+                 float_count=False):
         """kind: 'f32' (the parity restatement), 'f64' (the FP64 oracle: its
         arrays are float64) or 'timing' (the reference's optimisation flags)."""
         lib = self.lib = load(kind)
@@ -150,6 +152,8 @@ class PortRenderer:
             raise RuntimeError('port_create failed (no emissive facets?)')
         if watertight:
             lib.port_set_watertight(self.h, 1)
+        if float_count:
+            lib.port_set_float_count(self.h, 1)
         if scene.get('ibl') is not None:
             ibl = np.ascontiguousarray(scene['ibl'], np.uint8)
             lib.port_set_ibl(self.h, ibl.shape[1], ibl.shape[0], _p(ibl))

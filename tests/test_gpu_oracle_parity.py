@@ -17,6 +17,9 @@ CASES = {
     # The precision mode's watertight triangle test.
     'cornell96_watertight': (lambda s: s.cornell_box(width=96, height=96), 20000, 3, 0.7, 0.02,
                              {'watertight': True}),
+    # N kept as a float (FR_FLAG_FLOAT_PHOTON_COUNT), not the reference's truncated int.
+    'cornell96_floatcount': (lambda s: s.cornell_box(width=96, height=96), 20000, 4, 0.7, 0.02,
+                             {'float_count': True}),
     'mixed128x72_watertight': (lambda s: s.mixed_materials(width=128, height=72, n_spheres=24, field_n=48,
                                                            tex_size=128, light_tex=64, n_lat=12, n_lon=16,
                                                            extent=0.8, aperture=0.05),
@@ -89,11 +92,13 @@ def test_gpu_matches_oracle(name):
     from frsppm import abi
     _, photons, iters, alpha, radius = CASES[name][:5]
     opt = CASES[name][5] if len(CASES[name]) > 5 else {}
-    fix, wt = opt.get('fix_stale', False), opt.get('watertight', False)
+    fix, wt, fc = opt.get('fix_stale', False), opt.get('watertight', False), opt.get('float_count', False)
     scene = _scene(name)
-    flags = (abi.FLAG_FIX_STALE_PHOTON_SLOT if fix else 0) | (abi.FLAG_WATERTIGHT if wt else 0)
+    flags = ((abi.FLAG_FIX_STALE_PHOTON_SLOT if fix else 0) | (abi.FLAG_WATERTIGHT if wt else 0) |
+             (abi.FLAG_FLOAT_PHOTON_COUNT if fc else 0))
     with abi.Renderer(scene, photons, alpha=alpha, radius=radius, flags=flags) as g, \
-            port_abi.PortRenderer(scene, photons, alpha=alpha, radius=radius, fix_stale=fix, watertight=wt) as c:
+            port_abi.PortRenderer(scene, photons, alpha=alpha, radius=radius, fix_stale=fix, watertight=wt,
+                                  float_count=fc) as c:
         for s in range(iters):
             g.iterate(1)
             c.iterate(1)
