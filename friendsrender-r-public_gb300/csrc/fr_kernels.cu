@@ -39,6 +39,11 @@ namespace fr {
 #ifndef FR_TRACE_MIN_BLOCKS
 #define FR_TRACE_MIN_BLOCKS 7
 #endif
+// k_wave_trace keeps its stack's top entry in registers (1) or pushes every
+// entry to the local-memory stack (0).
+#ifndef FR_STACK_TOP_REG
+#define FR_STACK_TOP_REG 1
+#endif
 #if FR_TRACE_MIN_BLOCKS > 0
 #define FR_TRACE_BOUNDS __launch_bounds__(128, FR_TRACE_MIN_BLOCKS)
 #else
@@ -405,6 +410,12 @@ __global__ void FR_TRACE_BOUNDS k_wave_trace(SceneGPU sc, PathWave w, int round,
   uint32_t ref = 0;
   int sp = 0;
   uint2 stack[kTraversalStack];
+#if FR_STACK_TOP_REG
+  // The stack's top entry in registers: the entry pushed last is the nearest
+  // of a node's remaining children, the one popped next after a leaf.
+  uint2 top = make_uint2(0u, 0u);
+  bool has_top = false;
+#endif
   while (true) {
     unsigned idle = __ballot_sync(0xffffffffu, !active);
     while (idle && !exhausted) {
@@ -433,6 +444,9 @@ __global__ void FR_TRACE_BOUNDS k_wave_trace(SceneGPU sc, PathWave w, int round,
         ref = 0;
         tref = kRayOffset;
         sp = 0;
+#if FR_STACK_TOP_REG
+        has_top = false;
+#endif
         active = true;
       }
       pool += take;
@@ -452,6 +466,21 @@ __global__ void FR_TRACE_BOUNDS k_wave_trace(SceneGPU sc, PathWave w, int round,
           int cnt = 1;
 #pragma unroll
           for (int k = 1; k < 8; ++k) cnt += nv.key[k] != 0xFFFFFFFFu;
+#if FR_STACK_TOP_REG
+          if (sp + (has_top ? 1 : 0) + cnt - 1 > kTraversalStack) {
+            atomicOr(err, kErrStack);
+            best_tri = -1;
+            sp = 0;
+            has_top = false;
+          } else {
+#pragma unroll
+            for (int k = 7; k >= 1; --k)
+              if (k < cnt) {
+                if (has_top) stack[sp++] = top;
+                top = make_uint2(child_ref(nv, nv.key[k] & 7u), nv.key[k] & ~7u);
+                has_top = true;
+              }
+#else
           if (sp + cnt - 1 > kTraversalStack) {
             atomicOr(err, kErrStack);
             best_tri = -1;
@@ -460,6 +489,7 @@ __global__ void FR_TRACE_BOUNDS k_wave_trace(SceneGPU sc, PathWave w, int round,
 #pragma unroll
             for (int k = 7; k >= 1; --k)
               if (k < cnt) stack[sp++] = make_uint2(child_ref(nv, nv.key[k] & 7u), nv.key[k] & ~7u);
+#endif
             ref = child_ref(nv, nv.key[0] & 7u);
             tref = __uint_as_float(nv.key[0] & ~7u);
             pop = false;
@@ -481,12 +511,22 @@ __global__ void FR_TRACE_BOUNDS k_wave_trace(SceneGPU sc, PathWave w, int round,
       }
     }
     if (pop) {
-      if (sp == 0) {
+#if FR_STACK_TOP_REG
+      const bool empty = !has_top && sp == 0;
+#else
+      const bool empty = sp == 0;
+#endif
+      if (empty) {
         w.hit[i] = best_tri >= 0 ? make_float4(bu, bv, __int_as_float(best_tri), __int_as_float(best_facet))
                                  : make_float4(0.f, 0.f, __int_as_float(-1), __int_as_float(-1));
         active = false;
       } else {
+#if FR_STACK_TOP_REG
+        const uint2 e = has_top ? top : stack[--sp];
+        has_top = false;
+#else
         const uint2 e = stack[--sp];
+#endif
         ref = e.x;
         tref = __uint_as_float(e.y);
       }
