@@ -206,9 +206,16 @@ __device__ __forceinline__ void visit_node(const BVHNodeW* nodes, uint32_t ni, c
     const float t0 = max3f(fminf(ax, bx), fminf(ay, by), fmaxf(fminf(az, bz), tmin));
     const float t1 = min3f(fmaxf(ax, bx), fmaxf(ay, by), fminf(fmaxf(az, bz), tmax));
 #endif
+#if FR_NEAR_FAR
+    // An empty slot's box is lo = +inf, hi = -inf (collapse_bvh8), so its near
+    // plane distance is +inf and its far one -inf: t0 > t1 culls it without
+    // reading its meta byte.
+    nv.key[c] = t0 <= t1 ? ((__float_as_uint(t0) & ~7u) | (uint32_t)c) : 0xFFFFFFFFu;
+#else
     const uint32_t mw = c < 4 ? m1.x : m1.y;
     const bool valid = ((mw >> (8 * (c & 3))) & 0xFFu) != 0u;
     nv.key[c] = (valid && t0 <= t1) ? ((__float_as_uint(t0) & ~7u) | (uint32_t)c) : 0xFFFFFFFFu;
+#endif
   }
 }
 
