@@ -223,18 +223,26 @@ struct fr_ctx {
   uint32_t* counts = nullptr;
   PathWave wave{};               // photon-pass wavefront state
   PathWave eye_wave{};           // eye-pass wavefront state (the passes run concurrently)
-  cudaStream_t side = nullptr;   // the eye pass's stream, forked from and joined to `stream`
+  // Two streams.  `stream` runs the photon pass and the grid build; `side`,
+  // the pixel stream, runs the eye pass, the gather (with the guide's
+  // training) and fr_resolve_async's resolve.  Events order them:
+  // fork_ev (main -> side), join_ev (side -> main).
+  cudaStream_t side = nullptr;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   int photon_blocks = 0;         // grid of the wavefront round kernels
   int tail_blocks = 0;           // grid of the photon tail kernel
-  uint32_t* step_dev = nullptr;  // device iteration counter (IterParams::step)
-  uint32_t step_base = 0;        // fr_seek: the counter runs at step_base + iterations
+  // Device iteration counters (IterParams::step): [0] the photon pass's,
+  // [1] the eye pass's; each pass advances its own, so the two passes of an
+  // iteration read the same number however their kernels interleave.
+  uint32_t* step_dev = nullptr;
+  uint32_t step_base = 0;        // fr_seek: the counters run at step_base + iterations
   cudaStream_t body[kPhotonRounds] = {};  // capture the bodies of the graph's nested round nodes
   uint32_t* rounds_run = nullptr;  // gated photon rounds run so far (device)
-  bool capturing = false;        // enqueue_iteration is building the iteration graph
-  cudaGraph_t graph = nullptr;   // one captured iteration
-  cudaGraphExec_t graph_exec = nullptr;
-  int64_t graph_launches = 0;    // kernels per replay of the graph
+  bool capturing = false;        // an iteration part is being captured into a graph
+  // One graph per part of an iteration (kPart*), each replayed on its stream.
+  cudaGraph_t part_graph[4] = {};
+  cudaGraphExec_t part_exec[4] = {};
+  int64_t part_launches[4] = {};  // kernels per replay of each part
   int gather_blocks = 0;         // grid of the gather (one warp per hitpoint)
   int sms = 0;                   // streaming multiprocessors of the device
   bool guided = false;           // learned photon-emission guide on
@@ -292,8 +300,10 @@ struct fr_ctx {
       if (copied[k]) cudaEventDestroy(copied[k]);
     }
     if (copy_stream) cudaStreamDestroy(copy_stream);
-    if (graph_exec) cudaGraphExecDestroy(graph_exec);
-    if (graph) cudaGraphDestroy(graph);
+    for (int k = 0; k < 4; ++k) {
+      if (part_exec[k]) cudaGraphExecDestroy(part_exec[k]);
+      if (part_graph[k]) cudaGraphDestroy(part_graph[k]);
+    }
     if (side) cudaStreamDestroy(side);
     for (cudaStream_t b : body)
       if (b) cudaStreamDestroy(b);
@@ -458,9 +468,13 @@ struct StageMark {
   }
 };
 
-// Per-iteration counters: both passes' round queues, the hitpoint list,
-// both passes' shade queues and trace fetch counters.
-constexpr size_t kCounters = 2 * (kWaveRounds + 2) + 1 + 2 * kWaveRounds * kShadeQueues + 2 * kWaveRounds;
+// Per-iteration counters, one block per pass (each pass clears its own):
+// the eye pass's round queues, the hitpoint list, its shade queues and trace
+// fetch counters; then the photon pass's round queues, shade queues and
+// trace fetch counters.
+constexpr size_t kEyeCounters = (kWaveRounds + 2) + 1 + kWaveRounds * kShadeQueues + kWaveRounds;
+constexpr size_t kPhotonCounters = (kWaveRounds + 2) + kWaveRounds * kShadeQueues + kWaveRounds;
+constexpr size_t kCounters = kEyeCounters + kPhotonCounters;
 
 // Photon rounds r, r+1, ... as nested conditional (IF) nodes of the graph
 // being captured on stream s: k_round_gate sets the node's condition, and
@@ -502,122 +516,189 @@ int enqueue_gated_photon_rounds(fr_ctx* c, const IterParams& it, int r, cudaStre
   return FR_OK;
 }
 
-// Enqueues one iteration (the kernels read the iteration number from
-// c->step_dev, which the first kernel advances).
-int enqueue_iteration(fr_ctx* c) {
+// The parts of an iteration and the stream each runs on.
+enum { kPartPhoton = 0, kPartEye = 1, kPartGrid = 2, kPartGather = 3 };
+
+IterParams iter_params(const fr_ctx* c, uint32_t* step) {
   IterParams it{};
-  it.step = c->step_dev;
+  it.step = step;
   it.photons = c->P;
   it.width = c->W;
   it.height = c->H;
   it.alpha = c->alpha;
   it.flags = c->flags;
-  cudaStream_t s = c->stream;
+  return it;
+}
+
+// Photon pass (main stream): the photon pass's iteration counter, its
+// counters, emission, the wavefront rounds (the late ones as conditional
+// graph nodes while capturing) and the tail.
+int enqueue_photon_pass(fr_ctx* c, cudaStream_t s) {
+  const IterParams it = iter_params(c, c->step_dev);
   launch_next_step(c->step_dev, s);
-  // Queue counters of both passes and the hitpoint-list count.
-  FR_CUDA(cudaMemsetAsync(c->eye_wave.qcount, 0, sizeof(uint32_t) * kCounters, s));
-  // The eye pass (side stream) and the photon pass (main stream) share
-  // nothing but the error word, so they run concurrently: each fills the
-  // SMs that the other's last, nearly empty rounds leave idle.  The grid
-  // needs both (cell size from the hitpoint radii).
-  FR_CUDA(cudaEventRecord(c->fork_ev, s));
-  FR_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
+  FR_CUDA(cudaMemsetAsync(c->wave.qcount, 0, sizeof(uint32_t) * kPhotonCounters, s));
+  StageMark m(c, FR_STAGE_PHOTON, s);
   const int grid = c->photon_blocks;
-  {
-    cudaStream_t e = c->side;
-    StageMark m(c, FR_STAGE_EYE, e);
-    const int sort_grid = (int)std::min<size_t>(((size_t)c->W * c->H + 255) / 256, 4 * (size_t)grid);
-    if (c->sc.env) FR_CUDA(cudaMemsetAsync(c->hp.dl, 0, sizeof(float4) * (size_t)c->W * c->H, e));
-    launch_ew_start(c->cam, it, c->eye_wave, e);
-    for (int r = 0; r < kEyeRounds; ++r) {
-      {
-        StageMark t(c, FR_STAGE_EYE_TRACE, e);
-        launch_wave_trace(c->sc, c->eye_wave, r, grid, r == 0, c->err, e);
-      }
-      launch_wave_sort(c->sc, c->eye_wave, r, sort_grid, e);
-      launch_ew_shade(c->sc, it, c->rr_eye, c->eye_wave, c->hp, c->st, c->gi, r, grid, e);
+  const int sort_grid = (int)std::min<size_t>(((size_t)c->P + 255) / 256, 4 * (size_t)grid);
+  if (c->guided)
+    launch_pw_emit_guided(c->sc, it, c->ph, c->wave, c->counts, c->guide, s);
+  else
+    launch_pw_emit(c->sc, it, c->ph, c->wave, c->counts, s);
+  for (int r = 0; r < kPhotonRounds; ++r) {
+    if (c->capturing && r == kPhotonGatedFrom) {
+      const int rc = enqueue_gated_photon_rounds(c, it, r, s, grid, sort_grid);
+      if (rc) return rc;
+      break;
     }
-    launch_ew_tail(c->sc, it, c->rr_eye, c->eye_wave, c->hp, c->st, c->gi, kEyeRounds, grid, c->err, e);
-  }
-  FR_CUDA(cudaEventRecord(c->join_ev, c->side));
-  {
-    StageMark m(c, FR_STAGE_PHOTON, s);
-    const int sort_grid = (int)std::min<size_t>(((size_t)c->P + 255) / 256, 4 * (size_t)grid);
-    if (c->guided)
-      launch_pw_emit_guided(c->sc, it, c->ph, c->wave, c->counts, c->guide, s);
-    else
-      launch_pw_emit(c->sc, it, c->ph, c->wave, c->counts, s);
-    for (int r = 0; r < kPhotonRounds; ++r) {
-      if (c->capturing && r == kPhotonGatedFrom) {
-        const int rc = enqueue_gated_photon_rounds(c, it, r, s, grid, sort_grid);
-        if (rc) return rc;
-        break;
-      }
-      {
-        StageMark t(c, FR_STAGE_PHOTON_TRACE, s);
-        launch_wave_trace(c->sc, c->wave, r, grid, false, c->err, s);
-      }
-      launch_wave_sort(c->sc, c->wave, r, sort_grid, s);
-      launch_pw_shade(c->sc, it, c->ph, c->wave, c->counts, r, grid, s);
-      c->launches += 3;
+    {
+      StageMark t(c, FR_STAGE_PHOTON_TRACE, s);
+      launch_wave_trace(c->sc, c->wave, r, grid, false, c->err, s);
     }
-    launch_pw_tail(c->sc, it, c->ph, c->wave, c->counts, kPhotonRounds, c->tail_blocks, c->err, s);
+    launch_wave_sort(c->sc, c->wave, r, sort_grid, s);
+    launch_pw_shade(c->sc, it, c->ph, c->wave, c->counts, r, grid, s);
+    c->launches += 3;
   }
-  FR_CUDA(cudaStreamWaitEvent(s, c->join_ev, 0));
-  {
-    StageMark m(c, FR_STAGE_GRID, s);
-    launch_grid_setup(c->gi, c->sc, c->cell_scale, c->r0, s);
-    FR_CUDA(cudaMemsetAsync(c->grid.cell_count, 0, sizeof(uint32_t) * (size_t)c->grid.table, s));
-    launch_photon_count(c->ph, c->counts, c->P, kPhotonSlots, c->grid, c->gi, s);
-    c->launches += launch_scan(c->grid.cell_count, c->grid.cell_start, c->grid.table + 1, c->scan, s);
-    launch_photon_scatter(c->ph, c->counts, c->P, kPhotonSlots, c->grid, s);
-  }
-  {
-    StageMark m(c, FR_STAGE_GATHER, s);
-    FR_CUDA(cudaMemsetAsync(c->dbg_m, 0, sizeof(int32_t) * (size_t)c->W * c->H, s));
-    FR_CUDA(cudaMemsetAsync(c->dbg_phi, 0, sizeof(float4) * (size_t)c->W * c->H, s));
-    launch_gather_update(c->sc, it, c->hp, c->grid, c->gi, c->st, c->dbg_m, c->dbg_phi,
-                         c->guided ? c->guide.importance : nullptr, c->gather_blocks, s);
-  }
-  if (c->guided) {
-    // select, then per Adam step: train, Adam, weight tiles, step bookkeeping
-    c->launches += launch_guide_train(c->guide, c->P, s);
-  }
-  // iteration counter, eye pass (start, rounds of trace/sort/shade, tail),
-  // photon emission and tail, grid setup, count, scatter, gather
-  c->launches += 5 + (2 + 3 * kEyeRounds) + 2;
+  launch_pw_tail(c->sc, it, c->ph, c->wave, c->counts, kPhotonRounds, c->tail_blocks, c->err, s);
+  c->launches += 3;  // counter, emission, tail
   FR_CUDA(cudaGetLastError());
   return FR_OK;
 }
 
-// One iteration: a replay of the captured iteration graph, or (while the
-// stage profiler records events) direct launches.
-int run_iteration(fr_ctx* c) {
-  if (c->profiling) {
-    const int rc = enqueue_iteration(c);
-    if (rc) return rc;
-  } else {
-    if (!c->graph_exec) {
-      const int64_t before = c->launches;
-      FR_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-      c->capturing = true;
-      const int rc = enqueue_iteration(c);
-      c->capturing = false;
-      cudaGraph_t g = nullptr;
-      const cudaError_t ec = cudaStreamEndCapture(c->stream, &g);
-      if (rc) {
-        if (g) cudaGraphDestroy(g);
-        return rc;
-      }
-      if (ec != cudaSuccess) return fail(FR_ERR_CUDA, "iteration capture: %s", cudaGetErrorString(ec));
-      c->graph = g;
-      FR_CUDA(cudaGraphInstantiate(&c->graph_exec, c->graph, 0));
-      c->graph_launches = c->launches - before;
-      c->launches = before;
+// Eye pass (pixel stream): the eye pass's iteration counter, its counters
+// and the hitpoint list, then the wavefront rounds and the tail.  It writes
+// the hitpoints the gather reads, so it follows the previous gather.
+int enqueue_eye_pass(fr_ctx* c, cudaStream_t e) {
+  const IterParams it = iter_params(c, c->step_dev + 1);
+  launch_next_step(c->step_dev + 1, e);
+  FR_CUDA(cudaMemsetAsync(c->eye_wave.qcount, 0, sizeof(uint32_t) * kEyeCounters, e));
+  StageMark m(c, FR_STAGE_EYE, e);
+  const int grid = c->photon_blocks;
+  const int sort_grid = (int)std::min<size_t>(((size_t)c->W * c->H + 255) / 256, 4 * (size_t)grid);
+  if (c->sc.env) FR_CUDA(cudaMemsetAsync(c->hp.dl, 0, sizeof(float4) * (size_t)c->W * c->H, e));
+  launch_ew_start(c->cam, it, c->eye_wave, e);
+  for (int r = 0; r < kEyeRounds; ++r) {
+    {
+      StageMark t(c, FR_STAGE_EYE_TRACE, e);
+      launch_wave_trace(c->sc, c->eye_wave, r, grid, r == 0, c->err, e);
     }
-    FR_CUDA(cudaGraphLaunch(c->graph_exec, c->stream));
-    c->launches += c->graph_launches;
+    launch_wave_sort(c->sc, c->eye_wave, r, sort_grid, e);
+    launch_ew_shade(c->sc, it, c->rr_eye, c->eye_wave, c->hp, c->st, c->gi, r, grid, e);
   }
+  launch_ew_tail(c->sc, it, c->rr_eye, c->eye_wave, c->hp, c->st, c->gi, kEyeRounds, grid, c->err, e);
+  c->launches += 3 + 3 * kEyeRounds;  // counter, start, rounds, tail
+  FR_CUDA(cudaGetLastError());
+  return FR_OK;
+}
+
+// Photon grid (main stream): cell size from this iteration's hitpoint radii,
+// then count, scan and scatter of the stored photons into the grid's own
+// sorted copy, which is all the gather reads of them.
+int enqueue_grid(fr_ctx* c, cudaStream_t s) {
+  StageMark m(c, FR_STAGE_GRID, s);
+  launch_grid_setup(c->gi, c->sc, c->cell_scale, c->r0, s);
+  FR_CUDA(cudaMemsetAsync(c->grid.cell_count, 0, sizeof(uint32_t) * (size_t)c->grid.table, s));
+  launch_photon_count(c->ph, c->counts, c->P, kPhotonSlots, c->grid, c->gi, s);
+  c->launches += launch_scan(c->grid.cell_count, c->grid.cell_start, c->grid.table + 1, c->scan, s);
+  launch_photon_scatter(c->ph, c->counts, c->P, kPhotonSlots, c->grid, s);
+  c->launches += 3;
+  FR_CUDA(cudaGetLastError());
+  return FR_OK;
+}
+
+// Gather with the N/tau/R update (pixel stream), then the guide's training.
+int enqueue_gather(fr_ctx* c, cudaStream_t e) {
+  const IterParams it = iter_params(c, c->step_dev + 1);
+  {
+    StageMark m(c, FR_STAGE_GATHER, e);
+    FR_CUDA(cudaMemsetAsync(c->dbg_m, 0, sizeof(int32_t) * (size_t)c->W * c->H, e));
+    FR_CUDA(cudaMemsetAsync(c->dbg_phi, 0, sizeof(float4) * (size_t)c->W * c->H, e));
+    launch_gather_update(c->sc, it, c->hp, c->grid, c->gi, c->st, c->dbg_m, c->dbg_phi,
+                         c->guided ? c->guide.importance : nullptr, c->gather_blocks, e);
+    c->launches += 1;
+  }
+  // select, then per Adam step: train, Adam, weight tiles, step bookkeeping
+  if (c->guided) c->launches += launch_guide_train(c->guide, c->P, e);
+  FR_CUDA(cudaGetLastError());
+  return FR_OK;
+}
+
+int enqueue_part(fr_ctx* c, int part, cudaStream_t s) {
+  switch (part) {
+    case kPartPhoton: return enqueue_photon_pass(c, s);
+    case kPartEye: return enqueue_eye_pass(c, s);
+    case kPartGrid: return enqueue_grid(c, s);
+    default: return enqueue_gather(c, s);
+  }
+}
+
+// One part on stream s: a replay of its graph (captured on first use), or
+// direct launches while the stage profiler records events or while a batch
+// graph is being captured.
+int run_part(fr_ctx* c, int part, cudaStream_t s, bool graphs) {
+  if (!graphs) return enqueue_part(c, part, s);
+  if (!c->part_exec[part]) {
+    const int64_t before = c->launches;
+    FR_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    c->capturing = true;
+    const int rc = enqueue_part(c, part, s);
+    c->capturing = false;
+    cudaGraph_t g = nullptr;
+    const cudaError_t ec = cudaStreamEndCapture(s, &g);
+    if (rc) {
+      if (g) cudaGraphDestroy(g);
+      return rc;
+    }
+    if (ec != cudaSuccess) return fail(FR_ERR_CUDA, "iteration capture (part %d): %s", part, cudaGetErrorString(ec));
+    c->part_graph[part] = g;
+    FR_CUDA(cudaGraphInstantiate(&c->part_exec[part], g, 0));
+    c->part_launches[part] = c->launches - before;
+    c->launches = before;
+  }
+  FR_CUDA(cudaGraphLaunch(c->part_exec[part], s));
+  c->launches += c->part_launches[part];
+  return FR_OK;
+}
+
+// The pixel stream waits for the main stream's work so far, or the reverse.
+int side_after_main(fr_ctx* c) {
+  FR_CUDA(cudaEventRecord(c->fork_ev, c->stream));
+  FR_CUDA(cudaStreamWaitEvent(c->side, c->fork_ev, 0));
+  return FR_OK;
+}
+int main_after_side(fr_ctx* c) {
+  FR_CUDA(cudaEventRecord(c->join_ev, c->side));
+  FR_CUDA(cudaStreamWaitEvent(c->stream, c->join_ev, 0));
+  return FR_OK;
+}
+
+// One iteration on the context's two streams:
+//   main:  photon pass ........ wait(eye) grid
+//   pixel: eye pass ---------^             wait(grid) gather [guide training]
+// The gather is left running on the pixel stream: the next iteration's
+// photon pass starts as soon as this grid is built (it overwrites only the
+// photon slots, which the grid has copied), and its eye pass follows the
+// gather on the pixel stream (it rewrites the hitpoints the gather reads).
+// A guided iteration's emission samples the network this gather trains, so
+// then the main stream waits for it.  Every call that reads or writes the
+// per-pixel state from the main stream first makes it wait for the pixel
+// stream (main_after_side).
+int issue_iteration(fr_ctx* c, bool graphs) {
+  int rc = side_after_main(c);  // calls that wrote state on the main stream since the last iteration
+  if (!rc) rc = run_part(c, kPartPhoton, c->stream, graphs);
+  if (!rc) rc = run_part(c, kPartEye, c->side, graphs);
+  if (!rc) rc = main_after_side(c);
+  if (!rc) rc = run_part(c, kPartGrid, c->stream, graphs);
+  if (!rc) rc = side_after_main(c);
+  if (!rc) rc = run_part(c, kPartGather, c->side, graphs);
+  if (!rc && c->guided) rc = main_after_side(c);
+  return rc;
+}
+
+// One iteration: replays of the four part graphs, or (while the stage
+// profiler records events) direct launches.
+int run_iteration(fr_ctx* c) {
+  const int rc = issue_iteration(c, !c->profiling);
+  if (rc) return rc;
   ++c->iterations;
   c->photons_total += c->P;
   return FR_OK;
@@ -854,20 +935,22 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
       (rc = c->alloc(&c->wave.qcount, kCounters)) || (rc = c->alloc(&c->hp.list, npix)) ||
       (rc = c->alloc(&c->wave.mq, (size_t)kShadeQueues * wave_n)) ||
       (rc = c->alloc(&c->eye_wave.mq, (size_t)kShadeQueues * npix)) ||
-      (rc = c->alloc(&c->gi, 1)) || (rc = c->alloc(&c->step_dev, 1)) || (rc = c->alloc(&c->rounds_run, 1)) ||
+      (rc = c->alloc(&c->gi, 1)) || (rc = c->alloc(&c->step_dev, 2)) || (rc = c->alloc(&c->rounds_run, 1)) ||
       (rc = c->alloc(&c->err, 1)) ||
       (rc = c->alloc(&c->dbg_m, npix)) || (rc = c->alloc(&c->dbg_phi, npix)) || (rc = c->alloc(&c->image, npix)) ||
       (rc = c->alloc(&c->image_b, npix)) || (rc = c->alloc(&c->image8, npix)))
     return bail(rc);
-  // Counters (one memset per iteration): eye rounds, photon rounds, the
-  // hitpoint list, eye and photon shade queues, eye and photon trace fetches.
+  // Counters, one contiguous block per pass (each pass clears its own):
+  // eye rounds, the hitpoint list, eye shade queues, eye trace fetches; then
+  // photon rounds, photon shade queues, photon trace fetches.
   c->eye_wave.qcount = c->wave.qcount;
-  c->wave.qcount += kWaveRounds + 2;
-  c->hp.list_count = c->eye_wave.qcount + 2 * (kWaveRounds + 2);
+  c->hp.list_count = c->eye_wave.qcount + (kWaveRounds + 2);
   c->eye_wave.mcount = c->hp.list_count + 1;
-  c->wave.mcount = c->eye_wave.mcount + kWaveRounds * kShadeQueues;
-  c->eye_wave.tfetch = c->wave.mcount + kWaveRounds * kShadeQueues;
-  c->wave.tfetch = c->eye_wave.tfetch + kWaveRounds;
+  c->eye_wave.tfetch = c->eye_wave.mcount + kWaveRounds * kShadeQueues;
+  c->wave.qcount = c->eye_wave.qcount + kEyeCounters;
+  c->wave.mcount = c->wave.qcount + (kWaveRounds + 2);
+  c->wave.tfetch = c->wave.mcount + kWaveRounds * kShadeQueues;
+  static_assert(kEyeCounters == (kWaveRounds + 2) + 1 + kWaveRounds * kShadeQueues + kWaveRounds, "eye block");
   c->eye_wave.cap = (uint32_t)npix;
   c->wave.cap = (uint32_t)wave_n;
   c->eye_wave.min_live = kEyeTailMin;
@@ -940,7 +1023,7 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
   cudaMemsetAsync(c->ph.pos, 0, nslots * sizeof(float4), c->stream);
   cudaMemsetAsync(c->ph.flux, 0, nslots * sizeof(float4), c->stream);
   cudaMemsetAsync(c->gi, 0, sizeof(GridInfo), c->stream);
-  cudaMemsetAsync(c->step_dev, 0, sizeof(uint32_t), c->stream);
+  cudaMemsetAsync(c->step_dev, 0, 2 * sizeof(uint32_t), c->stream);
   cudaMemsetAsync(c->rounds_run, 0, sizeof(uint32_t), c->stream);
   cudaMemsetAsync(c->err, 0, sizeof(int), c->stream);
   cudaMemsetAsync(c->hp.pos, 0, npix * sizeof(float4), c->stream);
@@ -993,9 +1076,9 @@ struct fr_batch {
 };
 
 // One capture on the batch's stream: a fork event joins every context's main
-// stream (and through enqueue_iteration its eye stream and the streams of the
-// conditional photon rounds), each context enqueues one iteration, and the
-// batch stream joins them all.
+// stream (and through issue_iteration its pixel stream and the streams of the
+// conditional photon rounds), each context enqueues one iteration ending
+// with its pixel stream joined back, and the batch stream joins them all.
 int fr_batch_create(fr_ctx* const* ctxs, int count, fr_batch** out) {
   if (!ctxs || count < 1 || !out) return fail(FR_ERR_INVALID, "fr_batch_create: bad arguments");
   *out = nullptr;
@@ -1023,7 +1106,8 @@ int fr_batch_create(fr_ctx* const* ctxs, int count, fr_batch** out) {
     cudaStreamWaitEvent(c->stream, b->fork, 0);
     const int64_t before = c->launches;
     c->capturing = true;
-    rc = enqueue_iteration(c);
+    rc = issue_iteration(c, false);
+    if (!rc) rc = main_after_side(c);  // the capture joins every stream it forked
     c->capturing = false;
     b->launches.push_back(c->launches - before);
     c->launches = before;
@@ -1050,6 +1134,8 @@ int fr_batch_iterate(fr_batch* b, int n) {
   const size_t count = b->ctxs.size();
   for (size_t j = 0; j < count; ++j) {
     if (b->ctxs[j]->profiling) return fail(FR_ERR_INVALID, "fr_batch_iterate: context %zu has the stage profiler on", j);
+    const int rc = main_after_side(b->ctxs[j]);  // a gather still running from fr_iterate
+    if (rc) return rc;
     FR_CUDA(cudaEventRecord(b->ready[j], b->ctxs[j]->stream));
     FR_CUDA(cudaStreamWaitEvent(b->stream, b->ready[j], 0));
   }
@@ -1078,6 +1164,7 @@ int timed_iterations(fr_ctx* c, int iterations, float* ms) {
   FR_CUDA(cudaEventCreate(&b));
   FR_CUDA(cudaEventRecord(a, c->stream));
   for (int k = 0; k < iterations && !rc; ++k) rc = run_iteration(c);
+  if (!rc) rc = main_after_side(c);  // the last gather
   FR_CUDA(cudaEventRecord(b, c->stream));
   FR_CUDA(cudaEventSynchronize(b));
   FR_CUDA(cudaEventElapsedTime(ms, a, b));
@@ -1087,15 +1174,18 @@ int timed_iterations(fr_ctx* c, int iterations, float* ms) {
 }
 
 void drop_graph(fr_ctx* c) {
-  if (c->graph_exec) cudaGraphExecDestroy(c->graph_exec);
-  if (c->graph) cudaGraphDestroy(c->graph);
-  c->graph_exec = nullptr;
-  c->graph = nullptr;
+  for (int k = 0; k < 4; ++k) {
+    if (c->part_exec[k]) cudaGraphExecDestroy(c->part_exec[k]);
+    if (c->part_graph[k]) cudaGraphDestroy(c->part_graph[k]);
+    c->part_exec[k] = nullptr;
+    c->part_graph[k] = nullptr;
+  }
 }
 }  // namespace
 
 int fr_autotune(fr_ctx* c, int iterations, uint32_t* photon_tail_min) {
   if (!c || iterations < 1) return fail(FR_ERR_INVALID, "fr_autotune: bad arguments");
+  { const int jrc = main_after_side(c); if (jrc) return jrc; }
   if (c->profiling) return fail(FR_ERR_INVALID, "fr_autotune: stage profiler on");
   static const uint32_t kCandidates[] = {4096u, 8192u, 16384u, 32768u, 65536u};
   uint32_t best = c->wave.min_live;
@@ -1119,29 +1209,42 @@ int fr_autotune(fr_ctx* c, int iterations, uint32_t* photon_tail_min) {
 
 int fr_synchronize(fr_ctx* c) {
   if (!c) return fail(FR_ERR_INVALID, "fr_synchronize: NULL context");
+  const int rc = main_after_side(c);
+  if (rc) return rc;
   FR_CUDA(cudaStreamSynchronize(c->stream));
   FR_CUDA(cudaGetLastError());
   return check_device_error(c);
 }
 
-int fr_resolve_dev(fr_ctx* c, float* rgba_dev) {
-  if (!c || !rgba_dev) return fail(FR_ERR_INVALID, "fr_resolve_dev: bad arguments");
+namespace {
+int enqueue_resolve(fr_ctx* c, float4* out, cudaStream_t s) {
   launch_resolve(c->st, c->W * c->H, (double)c->photons_total, (double)c->iterations,
-                 (c->flags & kFlagStandardResolve) != 0, reinterpret_cast<float4*>(rgba_dev), c->stream);
+                 (c->flags & kFlagStandardResolve) != 0, out, s);
   FR_CUDA(cudaGetLastError());
   return FR_OK;
+}
+}  // namespace
+
+int fr_resolve_dev(fr_ctx* c, float* rgba_dev) {
+  if (!c || !rgba_dev) return fail(FR_ERR_INVALID, "fr_resolve_dev: bad arguments");
+  const int rc = main_after_side(c);
+  return rc ? rc : enqueue_resolve(c, reinterpret_cast<float4*>(rgba_dev), c->stream);
 }
 
 int fr_resolve_async(fr_ctx* c, float* rgba, uint64_t* ticket) {
   if (!c || !rgba) return fail(FR_ERR_INVALID, "fr_resolve_async: bad arguments");
   const int b = (int)(c->async_seq & 1u);
   float4* img = b ? c->image_b : c->image;
-  // The copy that last read this image (two calls ago) must have landed
-  // before the resolve overwrites it; a never-recorded event is no wait.
-  FR_CUDA(cudaStreamWaitEvent(c->stream, c->copied[b], 0));
-  int rc = fr_resolve_dev(c, reinterpret_cast<float*>(img));
+  // The resolve runs on the pixel stream after the last gather, so the next
+  // iteration's photon pass does not wait for it.  The copy that last read
+  // this image (two calls ago) must have landed before the resolve
+  // overwrites it; a never-recorded event is no wait.
+  int rc = side_after_main(c);
   if (rc) return rc;
-  FR_CUDA(cudaEventRecord(c->ready[b], c->stream));
+  FR_CUDA(cudaStreamWaitEvent(c->side, c->copied[b], 0));
+  rc = enqueue_resolve(c, img, c->side);
+  if (rc) return rc;
+  FR_CUDA(cudaEventRecord(c->ready[b], c->side));
   FR_CUDA(cudaStreamWaitEvent(c->copy_stream, c->ready[b], 0));
   FR_CUDA(cudaMemcpyAsync(rgba, img, sizeof(float4) * (size_t)c->W * c->H, cudaMemcpyDeviceToHost, c->copy_stream));
   FR_CUDA(cudaEventRecord(c->copied[b], c->copy_stream));
@@ -1200,12 +1303,17 @@ int fr_get_stats(fr_ctx* c, fr_stats* o) {
   return FR_OK;
 }
 
-void* fr_stream(fr_ctx* c) { return c ? (void*)c->stream : nullptr; }
+void* fr_stream(fr_ctx* c) {
+  if (!c) return nullptr;
+  main_after_side(c);  // work the caller puts on the stream sees the last gather
+  return (void*)c->stream;
+}
 
 void fr_destroy(fr_ctx* c) { delete c; }
 
 int fr_profile_enable(fr_ctx* c, int32_t on, int32_t max_iterations) {
   if (!c) return fail(FR_ERR_INVALID, "fr_profile_enable: NULL context");
+  { const int jrc = main_after_side(c); if (jrc) return jrc; }
   FR_CUDA(cudaStreamSynchronize(c->stream));
   c->ev_marks.clear();
   c->ev_used = 0;
@@ -1222,6 +1330,7 @@ int fr_profile_enable(fr_ctx* c, int32_t on, int32_t max_iterations) {
 
 int fr_profile_read(fr_ctx* c, double* stage_ms, int64_t* stage_count, int64_t* launches) {
   if (!c) return fail(FR_ERR_INVALID, "fr_profile_read: NULL context");
+  { const int jrc = main_after_side(c); if (jrc) return jrc; }
   FR_CUDA(cudaStreamSynchronize(c->stream));
   for (int k = 0; k < FR_STAGES; ++k) {
     if (stage_ms) stage_ms[k] = 0.0;
@@ -1245,6 +1354,7 @@ int fr_profile_read(fr_ctx* c, double* stage_ms, int64_t* stage_count, int64_t* 
 
 int fr_trace_closest(fr_ctx* c, const float* rays, int32_t n, int32_t* facet, float* tuv) {
   if (!c || n < 0 || (n && (!rays || !facet || !tuv))) return fail(FR_ERR_INVALID, "fr_trace_closest: bad arguments");
+  { const int jrc = main_after_side(c); if (jrc) return jrc; }
   if (!n) return FR_OK;
   float *d_rays = nullptr, *d_tuv = nullptr;
   int32_t* d_facet = nullptr;
@@ -1262,6 +1372,7 @@ int fr_trace_closest(fr_ctx* c, const float* rays, int32_t n, int32_t* facet, fl
 
 int fr_trace_any(fr_ctx* c, const float* rays, int32_t n, int32_t* hit) {
   if (!c || n < 0 || (n && (!rays || !hit))) return fail(FR_ERR_INVALID, "fr_trace_any: bad arguments");
+  { const int jrc = main_after_side(c); if (jrc) return jrc; }
   if (!n) return FR_OK;
   float* d_rays = nullptr;
   int32_t* d_hit = nullptr;
@@ -1280,6 +1391,7 @@ int fr_radius_query(fr_ctx* c, const float* hp, int32_t nh, const float* photons
   if (!c || nh < 0 || np < 0 || (nh && (!hp || !counts)) || (np && !photons_xyz) || !(cell > 0.0f) ||
       !(cell <= 3.0e38f) || (pairs && !pair_count))
     return fail(FR_ERR_INVALID, "fr_radius_query: bad arguments");
+  { const int jrc = main_after_side(c); if (jrc) return jrc; }
   if (!nh) return FR_OK;
   if (!np) {
     std::fill(counts, counts + nh, 0);
@@ -1400,6 +1512,7 @@ static_assert(kWaveRounds <= FR_MAX_WAVE_ROUNDS, "round counters exceed FR_MAX_W
 int fr_read_wave_counts(fr_ctx* c, uint32_t* eye_counts, uint32_t* photon_counts, int32_t* eye_rounds,
                         int32_t* photon_rounds) {
   if (!c || !eye_counts || !photon_counts) return fail(FR_ERR_INVALID, "fr_read_wave_counts: bad arguments");
+  { const int jrc = main_after_side(c); if (jrc) return jrc; }
   FR_CUDA(cudaMemcpyAsync(eye_counts, c->eye_wave.qcount, sizeof(uint32_t) * (kEyeRounds + 1), cudaMemcpyDeviceToHost,
                           c->stream));
   FR_CUDA(cudaMemcpyAsync(photon_counts, c->wave.qcount, sizeof(uint32_t) * (kPhotonRounds + 1),
@@ -1422,6 +1535,7 @@ int fr_read_wave_counts(fr_ctx* c, uint32_t* eye_counts, uint32_t* photon_counts
 
 int fr_read_direct(fr_ctx* c, float* last3, float* sum3, int32_t* count) {
   if (!c) return fail(FR_ERR_INVALID, "fr_read_direct: NULL context");
+  { const int jrc = main_after_side(c); if (jrc) return jrc; }
   const size_t np = (size_t)c->W * c->H;
   std::vector<float4> a(last3 ? np : 0), b((sum3 || count) ? np : 0);
   if (last3) FR_CUDA(cudaMemcpyAsync(a.data(), c->hp.dl, 16 * np, cudaMemcpyDeviceToHost, c->stream));
@@ -1438,6 +1552,7 @@ int fr_read_direct(fr_ctx* c, float* last3, float* sum3, int32_t* count) {
 
 int fr_read_hitpoints(fr_ctx* c, float* pos_type, float* nrm_rough, float* out_mat, float* wgt_facet) {
   if (!c) return fail(FR_ERR_INVALID, "fr_read_hitpoints: NULL context");
+  { const int jrc = main_after_side(c); if (jrc) return jrc; }
   const size_t bytes = sizeof(float4) * (size_t)c->W * c->H;
   if (pos_type) FR_CUDA(cudaMemcpyAsync(pos_type, c->hp.pos, bytes, cudaMemcpyDeviceToHost, c->stream));
   if (nrm_rough) FR_CUDA(cudaMemcpyAsync(nrm_rough, c->hp.nrm, bytes, cudaMemcpyDeviceToHost, c->stream));
@@ -1448,6 +1563,7 @@ int fr_read_hitpoints(fr_ctx* c, float* pos_type, float* nrm_rough, float* out_m
 
 int fr_read_photon_slots(fr_ctx* c, float* pos, float* flux, float* dir, uint32_t* counts) {
   if (!c) return fail(FR_ERR_INVALID, "fr_read_photon_slots: NULL context");
+  { const int jrc = main_after_side(c); if (jrc) return jrc; }
   const size_t bytes = sizeof(float4) * (size_t)c->P * kPhotonSlots;
   if (pos) FR_CUDA(cudaMemcpyAsync(pos, c->ph.pos, bytes, cudaMemcpyDeviceToHost, c->stream));
   if (flux) FR_CUDA(cudaMemcpyAsync(flux, c->ph.flux, bytes, cudaMemcpyDeviceToHost, c->stream));
@@ -1458,6 +1574,7 @@ int fr_read_photon_slots(fr_ctx* c, float* pos, float* flux, float* dir, uint32_
 
 int fr_read_gather(fr_ctx* c, int32_t* m, float* phi4) {
   if (!c) return fail(FR_ERR_INVALID, "fr_read_gather: NULL context");
+  { const int jrc = main_after_side(c); if (jrc) return jrc; }
   const size_t n = (size_t)c->W * c->H;
   if (m) FR_CUDA(cudaMemcpyAsync(m, c->dbg_m, 4 * n, cudaMemcpyDeviceToHost, c->stream));
   if (phi4) FR_CUDA(cudaMemcpyAsync(phi4, c->dbg_phi, 16 * n, cudaMemcpyDeviceToHost, c->stream));
@@ -1466,6 +1583,7 @@ int fr_read_gather(fr_ctx* c, int32_t* m, float* phi4) {
 
 int fr_read_state(fr_ctx* c, double* tau, int32_t* n, float* r, int32_t* g) {
   if (!c) return fail(FR_ERR_INVALID, "fr_read_state: NULL context");
+  { const int jrc = main_after_side(c); if (jrc) return jrc; }
   const size_t np = (size_t)c->W * c->H;
   if (tau) FR_CUDA(cudaMemcpyAsync(tau, c->st.tau, 24 * np, cudaMemcpyDeviceToHost, c->stream));
   if (n) FR_CUDA(cudaMemcpyAsync(n, c->st.n, 4 * np, cudaMemcpyDeviceToHost, c->stream));
@@ -1476,6 +1594,7 @@ int fr_read_state(fr_ctx* c, double* tau, int32_t* n, float* r, int32_t* g) {
 
 int fr_update(fr_ctx* c, const int32_t* m, const float* phi) {
   if (!c || !m || !phi) return fail(FR_ERR_INVALID, "fr_update: bad arguments");
+  { const int jrc = main_after_side(c); if (jrc) return jrc; }
   const size_t np = (size_t)c->W * c->H;
   std::vector<float4> phi4(np);
   for (size_t i = 0; i < np; ++i) phi4[i] = make_float4(phi[3 * i], phi[3 * i + 1], phi[3 * i + 2], 0.0f);
@@ -1487,6 +1606,7 @@ int fr_update(fr_ctx* c, const int32_t* m, const float* phi) {
 
 int fr_update_dev(fr_ctx* c, const int32_t* m_dev, const float* phi4_dev) {
   if (!c || !m_dev || !phi4_dev) return fail(FR_ERR_INVALID, "fr_update_dev: bad arguments");
+  { const int jrc = main_after_side(c); if (jrc) return jrc; }
   if ((reinterpret_cast<uintptr_t>(phi4_dev) & 15u) != 0) return fail(FR_ERR_INVALID, "fr_update_dev: phi4 not 16-byte aligned");
   launch_update(c->st, m_dev, reinterpret_cast<const float4*>(phi4_dev), c->W * c->H, c->alpha,
                 (c->flags & kFlagFloatPhotonCount) != 0u, c->stream);
@@ -1497,12 +1617,14 @@ int fr_update_dev(fr_ctx* c, const int32_t* m_dev, const float* phi4_dev) {
 // ------------------------------------------------------------ guide
 int fr_guide_params(fr_ctx* c, float* params) {
   if (!c || !params || !c->guided) return fail(FR_ERR_INVALID, "fr_guide_params: no guide");
+  { const int jrc = main_after_side(c); if (jrc) return jrc; }
   FR_CUDA(cudaMemcpyAsync(params, c->guide.params, sizeof(float) * kGuideParams, cudaMemcpyDeviceToHost, c->stream));
   return fr_synchronize(c);
 }
 
 int fr_guide_set_params(fr_ctx* c, const float* params) {
   if (!c || !params || !c->guided) return fail(FR_ERR_INVALID, "fr_guide_set_params: no guide");
+  { const int jrc = main_after_side(c); if (jrc) return jrc; }
   FR_CUDA(cudaMemcpyAsync(c->guide.params, params, sizeof(float) * kGuideParams, cudaMemcpyHostToDevice, c->stream));
   launch_guide_prepare(c->guide, c->stream);
   return fr_synchronize(c);
@@ -1510,6 +1632,7 @@ int fr_guide_set_params(fr_ctx* c, const float* params) {
 
 int fr_read_guide_importance(fr_ctx* c, float* importance) {
   if (!c || !importance || !c->guided) return fail(FR_ERR_INVALID, "fr_read_guide_importance: no guide");
+  { const int jrc = main_after_side(c); if (jrc) return jrc; }
   std::vector<unsigned long long> fx(2 * (size_t)c->P);
   FR_CUDA(cudaMemcpyAsync(fx.data(), c->guide.importance, sizeof(unsigned long long) * fx.size(),
                           cudaMemcpyDeviceToHost, c->stream));
@@ -1522,6 +1645,7 @@ int fr_read_guide_importance(fr_ctx* c, float* importance) {
 int fr_guide_gradient(fr_ctx* c, int32_t n, const float* samples, float* grad, float* weight_sum) {
   if (!c || !c->guided || n < 0 || n > c->P || n > c->guide.batch_cap || (n && !samples) || !grad || !weight_sum)
     return fail(FR_ERR_INVALID, "fr_guide_gradient: bad arguments");
+  { const int jrc = main_after_side(c); if (jrc) return jrc; }
   const GuideGPU& g = c->guide;
   std::vector<float4> f(n), d(n);
   std::vector<unsigned long long> imp(2 * (size_t)c->P, 0ull);
@@ -1607,6 +1731,7 @@ int fr_save_state(fr_ctx* c, void* buf, size_t* size) {
     return FR_OK;
   }
   if (*size < need) return fail(FR_ERR_INVALID, "fr_save_state: buffer of %zu bytes, %zu needed", *size, need);
+  { const int jrc = main_after_side(c); if (jrc) return jrc; }
   StateHeader h{};
   std::memcpy(h.magic, kStateMagic, 8);
   h.width = c->W;
@@ -1631,6 +1756,7 @@ int fr_save_state(fr_ctx* c, void* buf, size_t* size) {
 
 int fr_load_state(fr_ctx* c, const void* buf, size_t size) {
   if (!c || !buf) return fail(FR_ERR_INVALID, "fr_load_state: bad arguments");
+  { const int jrc = main_after_side(c); if (jrc) return jrc; }
   if (size < sizeof(StateHeader)) return fail(FR_ERR_INVALID, "fr_load_state: %zu bytes, no header", size);
   StateHeader h;
   std::memcpy(&h, buf, sizeof h);
@@ -1647,8 +1773,8 @@ int fr_load_state(fr_ctx* c, const void* buf, size_t size) {
     FR_CUDA(cudaMemcpyAsync(part.dev, p, part.bytes, cudaMemcpyHostToDevice, c->stream));
     p += part.bytes;
   }
-  const uint32_t step = h.step_base + (uint32_t)h.iterations;
-  FR_CUDA(cudaMemcpyAsync(c->step_dev, &step, sizeof step, cudaMemcpyHostToDevice, c->stream));
+  const uint32_t step = h.step_base + (uint32_t)h.iterations, steps[2] = {step, step};
+  FR_CUDA(cudaMemcpyAsync(c->step_dev, steps, sizeof steps, cudaMemcpyHostToDevice, c->stream));
   if (c->guided) launch_guide_prepare(c->guide, c->stream);
   FR_CUDA(cudaStreamSynchronize(c->stream));
   c->step_base = h.step_base;
@@ -1659,9 +1785,11 @@ int fr_load_state(fr_ctx* c, const void* buf, size_t size) {
 
 int fr_seek(fr_ctx* c, uint32_t first_step) {
   if (!c) return fail(FR_ERR_INVALID, "fr_seek: bad arguments");
+  { const int jrc = main_after_side(c); if (jrc) return jrc; }
   if (c->iterations != 0) return fail(FR_ERR_INVALID, "fr_seek: %lld iterations already run", (long long)c->iterations);
   FR_CUDA(cudaStreamSynchronize(c->stream));
-  FR_CUDA(cudaMemcpyAsync(c->step_dev, &first_step, sizeof first_step, cudaMemcpyHostToDevice, c->stream));
+  const uint32_t steps[2] = {first_step, first_step};
+  FR_CUDA(cudaMemcpyAsync(c->step_dev, steps, sizeof steps, cudaMemcpyHostToDevice, c->stream));
   FR_CUDA(cudaStreamSynchronize(c->stream));
   c->step_base = first_step;
   return FR_OK;
