@@ -251,13 +251,19 @@ void fr_scene_free(fr_scene* scene);
  * rgba + 4*width*j, the file's row order). */
 int fr_texture_load(const char* file, int32_t* width, int32_t* height, int32_t* channels, uint8_t* rgba);
 
-/* Enqueues n SPPM iterations on the context's stream (the loop body of
- * RenderImage_FixRenderTime, SPPM.cpp:768-848, with a fixed photon count).
- * Iteration k (counted from 1 over the context's life) uses the reference's
- * seeds for step k.  Asynchronous; see fr_synchronize. */
+/* Enqueues n SPPM iterations (the loop body of RenderImage_FixRenderTime,
+ * SPPM.cpp:768-848, with a fixed photon count).  Iteration k (counted from 1
+ * over the context's life) uses the reference's seeds for step k.
+ * Asynchronous; see fr_synchronize.  A context has two streams: the photon
+ * pass and the photon grid run on the context's stream (fr_stream), the eye
+ * pass and the gather on a pixel stream, and an iteration's gather overlaps
+ * the next iteration's photon pass.  Every other call on the context, and
+ * fr_stream itself, first makes the context's stream wait for the pixel
+ * stream, so work queued on it after any of them sees every iteration
+ * enqueued so far. */
 int fr_iterate(fr_ctx* ctx, int n);
 
-/* Waits for the context's stream and reports kernel errors. */
+/* Waits for the context's streams and reports kernel errors. */
 int fr_synchronize(fr_ctx* ctx);
 
 /* Batched rendering of uneven scenes (no counterpart in the reference, which
@@ -305,7 +311,9 @@ int fr_resolve_dev(fr_ctx* ctx, float* rgba_dev);
 /* fr_resolve without the wait, so that the read-back overlaps the next
  * fr_iterate: queues the image of the current state and its copy into the
  * host buffer rgba (pinned memory lets the copy run alongside the next
- * iteration) on a copy stream of the context, and returns a ticket.
+ * iteration) on a copy stream of the context, and returns a ticket.  The
+ * resolve runs on the pixel stream after the last gather, so the next
+ * iteration's photon pass does not wait for it.
  * fr_resolve_wait(ticket) returns once that copy has landed; rgba must stay
  * valid until then.  The context holds two device images, used in turn, so
  * a third call's resolve waits on the device for the first call's copy.
@@ -329,16 +337,18 @@ int fr_write_png(const char* path, int32_t width, int32_t height, const uint8_t*
 
 int fr_get_stats(fr_ctx* ctx, fr_stats* out);
 
-/* The context's cudaStream_t (as void*), for callers that record events on it. */
+/* The context's cudaStream_t (as void*), for callers that record events or
+ * queue work on it; the stream first waits for the pixel stream (see
+ * fr_iterate), so what follows on it sees every iteration enqueued so far. */
 void* fr_stream(fr_ctx* ctx);
 
 void fr_destroy(fr_ctx* ctx);
 
 /* Stage profiler.  While enabled, fr_iterate records CUDA events around each
  * stage of an iteration and around each trace-round kernel (FR_STAGE_*), on
- * the stream the stage runs on (the eye pass has a stream of its own, joined
- * to the context's stream before the grid stage, so the eye and photon stages
- * overlap in time); fr_profile_read synchronizes, returns the summed
+ * the stream the stage runs on (the eye pass and the gather run on the pixel
+ * stream, so the eye and photon stages, and a gather and the next photon
+ * stage, overlap in time); fr_profile_read synchronizes, returns the summed
  * milliseconds and the number of timed intervals per stage, then clears them.
  * max_iterations bounds the iterations profiled between reads (events are
  * created here).  *launches is the number of kernels fr_iterate has launched
