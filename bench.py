@@ -669,6 +669,28 @@ def run_update(args):
     return 0
 
 
+def run_ncu_pass(args):
+    """--ncu-pass: args.steps iterations of the mixed-materials workload with
+    the stage profiler on from the first one, so that every kernel is a direct
+    launch in issue order (per iteration: the photon pass, then the eye pass,
+    the grid and the gather), each iteration after a 256 MB L2 flush."""
+    import torch
+    from frsppm import abi, scenes
+    r = abi.Renderer(scenes.mixed_materials(), args.photons, alpha=ALPHA, radius=RADIUS)
+    r.profile(True, max_iterations=max(1, args.steps))
+    stream = torch.cuda.ExternalStream(r.stream())
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device='cuda')
+    for _ in range(args.steps):
+        with torch.cuda.stream(stream):
+            flush.zero_()
+        r.iterate(1)
+    stage_ms, _, launches = r.profile_read()
+    r.close()
+    print(json.dumps({'ncu_pass': True, 'photons': args.photons, 'steps': args.steps, 'launches': launches,
+                      'stage_ms': stage_ms}))
+    return 0
+
+
 def other_workloads():
     """The batched uneven scenes (64 contexts, fr_iterate_batch) and the large
     scene (20M triangles, 3840x2160, 8M paths, guide on), each measured by its
@@ -716,6 +738,10 @@ def main():
     ap.add_argument('--bvh', default='sah', choices=['sah', 'lbvh'],
                     help='scene BVH: host binned SAH (default) or the device LBVH build')
     ap.add_argument('--cpu-measure', default=None, help=argparse.SUPPRESS)
+    ap.add_argument('--ncu-pass', action='store_true',
+                    help='only --steps iterations of the mixed-materials workload with the stage profiler on (every '
+                         'kernel a direct launch, none inside a graph), each after a 256 MB L2 flush: the pass '
+                         'that kernel-profiler captures select launches from')
     ap.add_argument('--no-other-workloads', action='store_true',
                     help='skip the batched-scenes and large-scene lines embedded in the default line')
     args = ap.parse_args()
@@ -726,6 +752,8 @@ def main():
         args.steps = 200 if args.impl == 'ours' and args.workload in ('mixed', 'update') else 10
     if args.impl == 'reference':
         return run_reference(args)
+    if args.ncu_pass:
+        return run_ncu_pass(args)
     if args.workload == 'large':
         return run_large(args)
     if args.workload == 'batch':
