@@ -599,7 +599,7 @@ int enqueue_grid(fr_ctx* c, cudaStream_t s) {
   FR_CUDA(cudaMemsetAsync(c->grid.cell_count, 0, sizeof(uint32_t) * (size_t)c->grid.table, s));
   launch_photon_count(c->ph, c->counts, c->P, kPhotonSlots, c->grid, c->gi, s);
   c->launches += launch_scan(c->grid.cell_count, c->grid.cell_start, c->grid.table + 1, c->scan, s);
-  launch_photon_scatter(c->ph, c->counts, c->P, kPhotonSlots, c->grid, s);
+  launch_photon_scatter(c->ph, c->counts, c->P, kPhotonSlots, c->grid, c->gi, s);
   c->launches += 3;
   FR_CUDA(cudaGetLastError());
   return FR_OK;
@@ -968,8 +968,7 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
   const size_t cap = nslots;
   if ((rc = c->alloc(&c->grid.pos, cap)) || (rc = c->alloc(&c->grid.flux, cap)) || (rc = c->alloc(&c->grid.dir, cap)) ||
       (rc = c->alloc(&c->grid.cell_count, (size_t)c->grid.table + 1)) ||
-      (rc = c->alloc(&c->grid.cell_start, (size_t)c->grid.table + 1)) || (rc = c->alloc(&c->grid.slot_key, nslots)) ||
-      (rc = c->alloc(&c->grid.slot_rank, nslots)))
+      (rc = c->alloc(&c->grid.cell_start, (size_t)c->grid.table + 1)))
     return bail(rc);
   const uint32_t words = scan_temp_words(c->grid.table + 1, c->scan);
   uint32_t* sw;
@@ -1441,8 +1440,6 @@ int fr_radius_query(fr_ctx* c, const float* hp, int32_t nh, const float* photons
   g.pos = (float4*)dalloc(npp * 16); g.flux = (float4*)dalloc(npp * 16); g.dir = (float4*)dalloc(npp * 16);
   g.cell_count = (uint32_t*)dalloc(4 * ((size_t)g.table + 1));
   g.cell_start = (uint32_t*)dalloc(4 * ((size_t)g.table + 1));
-  g.slot_key = (uint32_t*)dalloc(4 * npp);
-  g.slot_rank = (uint32_t*)dalloc(4 * npp);
   uint32_t* d_ones = (uint32_t*)dalloc(4 * npp);
   uint32_t* sw = (uint32_t*)dalloc(4 * (size_t)words);
   GridInfo* d_gi = (GridInfo*)dalloc(sizeof(GridInfo));
@@ -1467,7 +1464,7 @@ int fr_radius_query(fr_ctx* c, const float* hp, int32_t nh, const float* photons
     cudaMemsetAsync(d_pc, 0, 4, s);
     launch_photon_count(ph, d_ones, np, 1, g, d_gi, s);
     launch_scan(g.cell_count, g.cell_start, g.table + 1, st, s);
-    launch_photon_scatter(ph, d_ones, np, 1, g, s);
+    launch_photon_scatter(ph, d_ones, np, 1, g, d_gi, s);
     launch_radius_count(d_hp, nh, g, d_gi, d_m, d_pairs, pair_capacity, d_pc, c->err, s);
     cudaMemcpyAsync(counts, d_m, 4 * (size_t)nh, cudaMemcpyDeviceToHost, s);
     if (pairs) {

@@ -1084,22 +1084,30 @@ __global__ void __launch_bounds__(256) k_photon_count(PhotonSlots ph, const uint
   const uint32_t n = counts[i];
   for (uint32_t k = 0; k < n; ++k) {
     const float4 p = ph.pos[base + k];
-    const uint32_t h = cell_hash(cell_of(p.x, ox, inv), cell_of(p.y, oy, inv), cell_of(p.z, oz, inv), mask);
-    g.slot_key[base + k] = h;
-    g.slot_rank[base + k] = atomicAdd(g.cell_count + h, 1u);
+    atomicAdd(g.cell_count + cell_hash(cell_of(p.x, ox, inv), cell_of(p.y, oy, inv), cell_of(p.z, oz, inv), mask), 1u);
   }
 }
 
+// Each photon's bucket is hashed again from its position (the same float
+// operations as k_photon_count) and its place in the bucket taken by counting
+// the bucket's count down, which leaves the counts zero; the gather reads only
+// cell_start.  (The order within a bucket follows the atomics, as the count's
+// ranks would.)  Per-slot bucket and rank arrays, 128 bytes apart per path,
+// cost a DRAM line per 4-byte read.
 __global__ void __launch_bounds__(256) k_photon_scatter(PhotonSlots ph, const uint32_t* counts, int paths,
-                                                        int stride, PhotonGrid g) {
+                                                        int stride, PhotonGrid g, const GridInfo* gi) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= paths) return;
+  const float ox = gi->origin[0], oy = gi->origin[1], oz = gi->origin[2], inv = gi->inv_cell;
+  const uint32_t mask = g.table - 1u;
   const size_t base = (size_t)i * stride;
   const uint32_t n = counts[i];
   for (uint32_t k = 0; k < n; ++k) {
     const size_t s = base + k;
-    const uint32_t dst = g.cell_start[g.slot_key[s]] + g.slot_rank[s];
-    g.pos[dst] = ph.pos[s];
+    const float4 p = ph.pos[s];
+    const uint32_t h = cell_hash(cell_of(p.x, ox, inv), cell_of(p.y, oy, inv), cell_of(p.z, oz, inv), mask);
+    const uint32_t dst = g.cell_start[h] + atomicSub(g.cell_count + h, 1u) - 1u;
+    g.pos[dst] = p;
     g.flux[dst] = ph.flux[s];
     float4 d = ph.dir[s];
     d.w = __uint_as_float((uint32_t)s);
@@ -1618,8 +1626,8 @@ void launch_photon_count(PhotonSlots ph, const uint32_t* counts, int paths, int 
 }
 
 void launch_photon_scatter(PhotonSlots ph, const uint32_t* counts, int paths, int stride, PhotonGrid g,
-                           cudaStream_t s) {
-  k_photon_scatter<<<blocks_for(paths, 256), 256, 0, s>>>(ph, counts, paths, stride, g);
+                           const GridInfo* gi, cudaStream_t s) {
+  k_photon_scatter<<<blocks_for(paths, 256), 256, 0, s>>>(ph, counts, paths, stride, g, gi);
 }
 
 uint32_t scan_temp_words(uint32_t n, ScanTemp& t) {

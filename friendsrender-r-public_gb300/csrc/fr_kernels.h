@@ -38,10 +38,8 @@ struct PhotonGrid {
   float4* pos;
   float4* flux;
   float4* dir;
-  uint32_t* cell_count;  // [table]  photons per bucket
+  uint32_t* cell_count;  // [table]  photons per bucket (counted down to zero by the scatter)
   uint32_t* cell_start;  // [table + 1] exclusive prefix of cell_count
-  uint32_t* slot_key;    // [paths * kPhotonSlots]  bucket of each valid slot
-  uint32_t* slot_rank;   // [paths * kPhotonSlots]  rank within its bucket
   uint32_t table;        // bucket count, power of two
 };
 
@@ -157,7 +155,7 @@ void launch_photon_count(PhotonSlots ph, const uint32_t* counts, int paths, int 
 // Returns the number of kernels launched.
 int launch_scan(uint32_t* data_in, uint32_t* data_out, uint32_t n, ScanTemp& tmp, cudaStream_t s);
 void launch_photon_scatter(PhotonSlots ph, const uint32_t* counts, int paths, int stride, PhotonGrid g,
-                           cudaStream_t s);
+                           const GridInfo* gi, cudaStream_t s);
 // Words of block-sum scratch launch_scan needs for n elements; fills the level sizes of t.
 uint32_t scan_temp_words(uint32_t n, ScanTemp& t);
 // One warp per listed hitpoint; resident_blocks blocks of 256 threads.
