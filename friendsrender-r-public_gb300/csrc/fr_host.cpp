@@ -206,6 +206,21 @@ struct DevBuf {
 
 }  // namespace
 
+// Shares (percent) of the resident grid given to the eye pass's round kernels
+// and to the gather.  Both run on the pixel stream beside the photon pass, the
+// iteration's critical path; their kernels fetch work until their queues are
+// empty, so a block holds its SM slots until the end of the launch, and a
+// smaller grid leaves the photon pass more of the GPU (the eye pass has
+// slack).  Mixed materials, ms per iteration: eye pass at 50% 3.55-3.58, 40%
+// 3.57, 65% 3.59, 100% 3.62-3.63, 33% 3.62; the gather (its waits are its own
+// critical path) at 75% 3.55, 50% 3.65-3.66.
+#ifndef FR_EYE_GRID_PCT
+#define FR_EYE_GRID_PCT 50
+#endif
+#ifndef FR_GATHER_GRID_PCT
+#define FR_GATHER_GRID_PCT 100
+#endif
+
 struct fr_ctx {
   cudaStream_t stream = nullptr;
   std::vector<DevBuf> bufs;
@@ -229,7 +244,8 @@ struct fr_ctx {
   // fork_ev (main -> side), join_ev (side -> main).
   cudaStream_t side = nullptr;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
-  int photon_blocks = 0;         // grid of the wavefront round kernels
+  int photon_blocks = 0;         // grid of the photon pass's wavefront round kernels
+  int eye_blocks = 0;            // grid of the eye pass's wavefront round kernels
   int tail_blocks = 0;           // grid of the photon tail kernel
   // Device iteration counters (IterParams::step): [0] the photon pass's,
   // [1] the eye pass's; each pass advances its own, so the two passes of an
@@ -572,7 +588,7 @@ int enqueue_eye_pass(fr_ctx* c, cudaStream_t e) {
   launch_next_step(c->step_dev + 1, e);
   FR_CUDA(cudaMemsetAsync(c->eye_wave.qcount, 0, sizeof(uint32_t) * kEyeCounters, e));
   StageMark m(c, FR_STAGE_EYE, e);
-  const int grid = c->photon_blocks;
+  const int grid = c->eye_blocks;
   const int sort_grid = (int)std::min<size_t>(((size_t)c->W * c->H + 255) / 256, 4 * (size_t)grid);
   if (c->sc.env) FR_CUDA(cudaMemsetAsync(c->hp.dl, 0, sizeof(float4) * (size_t)c->W * c->H, e));
   launch_ew_start(c->cam, it, c->eye_wave, e);
@@ -783,8 +799,9 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
   if ((rc = exact_tables(dev, &tabs))) return bail(rc);
   upload_tables(tabs.sincos, tabs.sqrt1m, c->stream);
   c->photon_blocks = std::max(1, photon_pass_blocks_per_sm()) * sms;
+  c->eye_blocks = std::max(1, c->photon_blocks * FR_EYE_GRID_PCT / 100);
   c->tail_blocks = std::max(1, pw_tail_blocks_per_sm()) * sms;
-  c->gather_blocks = std::max(1, gather_blocks_per_sm()) * sms;
+  c->gather_blocks = std::max(1, std::max(1, gather_blocks_per_sm()) * sms * FR_GATHER_GRID_PCT / 100);
   c->sms = sms;
 
   // ---- geometry
