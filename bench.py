@@ -895,7 +895,9 @@ def main():
                      'frac': achieved / peak, 'traffic': trace_traffic_per_launch(), 'peak_source': peak_kind,
                      'algorithmic_bytes_per_launch': bytes_per_launch, 'launches_per_step': trace_launches,
                      'per': 'launch that traced rays (traffic and algorithmic bytes alike)',
-                     'note': 'latency-bound BVH traversal; eye and photon launches overlap in time'},
+                     'note': 'latency-bound BVH traversal; eye and photon launches overlap in time, and the '
+                             'eye rounds run on half the resident grid (leaving the photon pass, the critical '
+                             'path, the rest), which lengthens their launches'},
         'traversal': traversal_block(rays, eye_rays, photon_rays, trace_s, eye_q, photon_q, clocks),
         'e2e': {'value': world * args.photons * args.steps / e2e_s, 'unit': UNIT, 'h2d_bytes_per_step': 0,
                 'd2h_bytes_per_step': npix * 16, 'setup_s': setup_s,
