@@ -90,8 +90,7 @@ __global__ void __launch_bounds__(128) k_guide_train(GuideGPU g) {
     V3 d = v3(0.f, 0.f, 1.f);
     float I = 0.0f;
     if (j0 < n_all) {
-      const uint32_t i = g.batch[j0];
-      const float4 f = g.feat[i], dd = g.dir[i];
+      const float4 f = g.batch_feat[j0], dd = g.batch_dir[j0];
       x[0] = f.x; x[1] = f.y; x[2] = f.z; x[3] = f.w; x[4] = dd.x;
       d = v3(dd.y, dd.z, dd.w);
       I = g.batch_w[j0];
@@ -392,6 +391,8 @@ __global__ void __launch_bounds__(kSelectBlock) k_guide_select_write(GuideGPU g,
   if (take && slot < (uint32_t)g.batch_cap) {
     g.batch[slot] = (uint32_t)i;
     g.batch_w[slot] = importance_value(g.importance[2 * (size_t)i], g.importance[2 * (size_t)i + 1]);
+    g.batch_feat[slot] = g.feat[i];
+    g.batch_dir[slot] = g.dir[i];
   }
 }
 
@@ -415,16 +416,32 @@ inline void launch_guide_select(const GuideGPU& g, int paths, cudaStream_t s) {
 
 int guide_train_smem() { return kTrainSmem; }
 
-// One sample selection, then g.steps Adam steps on the same samples (each a
-// gradient pass with the current weights).  Returns the kernels launched.
-int launch_guide_train(const GuideGPU& g, int paths, cudaStream_t s) {
+// The sample selection of an iteration: its paths with importance, their
+// importance, inputs and directions copied into the batch.  Returns the
+// kernels launched.
+int launch_guide_select_batch(const GuideGPU& g, int paths, cudaStream_t s) {
   launch_guide_select(g, paths, s);
+  return 3;
+}
+
+// g.steps Adam steps on the selected samples (each a gradient pass with the
+// current weights).  Returns the kernels launched.
+int launch_guide_steps(const GuideGPU& g, cudaStream_t s) {
   for (int k = 0; k < g.steps; ++k) {
     k_guide_train<<<g.train_ctas, 128, kTrainSmem, s>>>(g);
     k_guide_adam<<<(kGuideParams + 255) / 256, 256, 0, s>>>(g);
     k_guide_step_done<<<1, 1, 0, s>>>(g, k == g.steps - 1);
   }
-  return 3 + 3 * g.steps;
+  return 3 * g.steps;
+}
+
+// The training's weights become the emission's (two device copies).
+int launch_guide_publish(const GuideGPU& g, cudaStream_t s) {
+  if (cudaMemcpyAsync(g.emit_params, g.params, sizeof(float) * kGuideParams, cudaMemcpyDeviceToDevice, s) !=
+          cudaSuccess ||
+      cudaMemcpyAsync(g.emit_tiles, g.tiles, kTileBytes, cudaMemcpyDeviceToDevice, s) != cudaSuccess)
+    return -1;
+  return 0;
 }
 
 void launch_guide_prepare(const GuideGPU& g, cudaStream_t s) { k_guide_prepare<<<16, 256, 0, s>>>(g); }

@@ -64,15 +64,22 @@ __host__ __device__ inline float importance_value(unsigned long long hi, unsigne
 }
 
 struct GuideGPU {
-  float* params;        // kGuideParams FP32 master weights
+  float* params;        // kGuideParams FP32 master weights (the training's)
   float* adam_m;        // Adam moments
   float* adam_v;
-  uint8_t* tiles;       // kTileBytes BF16 weight tiles
+  uint8_t* tiles;       // kTileBytes BF16 weight tiles (the training's)
+  // The network the emission samples: the training's weights as they were
+  // before the last selection (copied by launch_guide_publish), so that the
+  // emission of iteration s + 1 can run while iteration s's training does.
+  float* emit_params;
+  uint8_t* emit_tiles;
   float4* feat;         // per path: inputs x0..x3
   float4* dir;          // per path: input x4, emission direction
   unsigned long long* importance;  // per path {hi, lo}: flux deposited at hitpoints this iteration
   uint32_t* batch;      // training samples (path indices), in path order
   float* batch_w;       // their importance
+  float4* batch_feat;   // their inputs and directions (copies of feat and dir, which
+  float4* batch_dir;    // the next emission rewrites while the training runs)
   uint32_t* batch_count;
   uint32_t* select_part;  // per selection block: paths taken, then their first batch slot
   float* grad_part;     // per training CTA: kGuideParams gradient sums

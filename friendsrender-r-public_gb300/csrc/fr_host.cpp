@@ -244,6 +244,11 @@ struct fr_ctx {
   // fork_ev (main -> side), join_ev (side -> main).
   cudaStream_t side = nullptr;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
+  // Guided contexts: the guide's training runs on train_stream after the
+  // selection (sel_ev), beside the next iteration's passes; train_ev marks
+  // it done (the next publish of its weights waits for it).
+  cudaStream_t train_stream = nullptr;
+  cudaEvent_t sel_ev = nullptr, train_ev = nullptr;
   int photon_blocks = 0;         // grid of the photon pass's wavefront round kernels
   int eye_blocks = 0;            // grid of the eye pass's wavefront round kernels
   int tail_blocks = 0;           // grid of the photon tail kernel
@@ -256,9 +261,9 @@ struct fr_ctx {
   uint32_t* rounds_run = nullptr;  // gated photon rounds run so far (device)
   bool capturing = false;        // an iteration part is being captured into a graph
   // One graph per part of an iteration (kPart*), each replayed on its stream.
-  cudaGraph_t part_graph[4] = {};
-  cudaGraphExec_t part_exec[4] = {};
-  int64_t part_launches[4] = {};  // kernels per replay of each part
+  cudaGraph_t part_graph[5] = {};
+  cudaGraphExec_t part_exec[5] = {};
+  int64_t part_launches[5] = {};  // kernels per replay of each part
   int gather_blocks = 0;         // grid of the gather (one warp per hitpoint)
   int sms = 0;                   // streaming multiprocessors of the device
   bool guided = false;           // learned photon-emission guide on
@@ -306,21 +311,23 @@ struct fr_ctx {
   ~fr_ctx() {
     if (stream) cudaStreamSynchronize(stream);
     if (side) cudaStreamSynchronize(side);
+    if (train_stream) cudaStreamSynchronize(train_stream);
     for (cudaEvent_t e : ev_pool) cudaEventDestroy(e);
     for (auto& b : bufs) cudaFree(b.p);
     if (copy_stream) cudaStreamSynchronize(copy_stream);
-    if (fork_ev) cudaEventDestroy(fork_ev);
-    if (join_ev) cudaEventDestroy(join_ev);
+    for (cudaEvent_t e : {fork_ev, join_ev, sel_ev, train_ev})
+      if (e) cudaEventDestroy(e);
     for (int k = 0; k < 2; ++k) {
       if (ready[k]) cudaEventDestroy(ready[k]);
       if (copied[k]) cudaEventDestroy(copied[k]);
     }
     if (copy_stream) cudaStreamDestroy(copy_stream);
-    for (int k = 0; k < 4; ++k) {
+    for (int k = 0; k < 5; ++k) {
       if (part_exec[k]) cudaGraphExecDestroy(part_exec[k]);
       if (part_graph[k]) cudaGraphDestroy(part_graph[k]);
     }
     if (side) cudaStreamDestroy(side);
+    if (train_stream) cudaStreamDestroy(train_stream);
     for (cudaStream_t b : body)
       if (b) cudaStreamDestroy(b);
     if (stream) cudaStreamDestroy(stream);
@@ -533,7 +540,7 @@ int enqueue_gated_photon_rounds(fr_ctx* c, const IterParams& it, int r, cudaStre
 }
 
 // The parts of an iteration and the stream each runs on.
-enum { kPartPhoton = 0, kPartEye = 1, kPartGrid = 2, kPartGather = 3 };
+enum { kPartPhoton = 0, kPartEye = 1, kPartGrid = 2, kPartGather = 3, kPartTrain = 4 };
 
 IterParams iter_params(const fr_ctx* c, uint32_t* step) {
   IterParams it{};
@@ -621,7 +628,10 @@ int enqueue_grid(fr_ctx* c, cudaStream_t s) {
   return FR_OK;
 }
 
-// Gather with the N/tau/R update (pixel stream), then the guide's training.
+// Gather with the N/tau/R update (pixel stream).  Guided: then the training's
+// weights (from the previous iteration's training) become the emission's,
+// and this iteration's samples are selected; the training itself is the
+// next part.
 int enqueue_gather(fr_ctx* c, cudaStream_t e) {
   const IterParams it = iter_params(c, c->step_dev + 1);
   {
@@ -632,8 +642,18 @@ int enqueue_gather(fr_ctx* c, cudaStream_t e) {
                          c->guided ? c->guide.importance : nullptr, c->gather_blocks, e);
     c->launches += 1;
   }
-  // select, then per Adam step: train, Adam, weight tiles, step bookkeeping
-  if (c->guided) c->launches += launch_guide_train(c->guide, c->P, e);
+  if (c->guided) {
+    if (launch_guide_publish(c->guide, e)) return fail(FR_ERR_CUDA, "guide: weight copy failed");
+    c->launches += launch_guide_select_batch(c->guide, c->P, e);
+  }
+  FR_CUDA(cudaGetLastError());
+  return FR_OK;
+}
+
+// The guide's training on the selected samples: per Adam step, gradients,
+// Adam with the weight tiles, step bookkeeping.
+int enqueue_train(fr_ctx* c, cudaStream_t t) {
+  c->launches += launch_guide_steps(c->guide, t);
   FR_CUDA(cudaGetLastError());
   return FR_OK;
 }
@@ -643,7 +663,8 @@ int enqueue_part(fr_ctx* c, int part, cudaStream_t s) {
     case kPartPhoton: return enqueue_photon_pass(c, s);
     case kPartEye: return enqueue_eye_pass(c, s);
     case kPartGrid: return enqueue_grid(c, s);
-    default: return enqueue_gather(c, s);
+    case kPartGather: return enqueue_gather(c, s);
+    default: return enqueue_train(c, s);
   }
 }
 
@@ -686,31 +707,60 @@ int main_after_side(fr_ctx* c) {
   FR_CUDA(cudaStreamWaitEvent(c->stream, c->join_ev, 0));
   return FR_OK;
 }
+// The main stream waits for all of the context's work: the pixel stream and
+// the guide's training.
+int join_streams(fr_ctx* c) {
+  const int rc = main_after_side(c);
+  if (rc || !c->guided) return rc;
+  FR_CUDA(cudaStreamWaitEvent(c->stream, c->train_ev, 0));
+  return FR_OK;
+}
 
-// One iteration on the context's two streams:
+// One iteration on the context's streams:
 //   main:  photon pass ........ wait(eye) grid
-//   pixel: eye pass ---------^             wait(grid) gather [guide training]
+//   pixel: eye pass ---------^             wait(grid) gather [publish, selection]
+//   train (guided):                                                  wait(selection) training
 // The gather is left running on the pixel stream: the next iteration's
 // photon pass starts as soon as this grid is built (it overwrites only the
 // photon slots, which the grid has copied), and its eye pass follows the
 // gather on the pixel stream (it rewrites the hitpoints the gather reads).
-// A guided iteration's emission samples the network this gather trains, so
-// then the main stream waits for it.  Every call that reads or writes the
-// per-pixel state from the main stream first makes it wait for the pixel
-// stream (main_after_side).
+// Guided: the next emission clears the importance this gather accumulates
+// and rewrites the inputs and directions of the paths, so the main stream
+// waits for the selection, which has copied the samples; the emission
+// samples the weights published before the selection (the training of the
+// iteration before), so the training runs beside the next iteration, and the
+// next publish waits for it.  In a batch graph's capture the training runs
+// on the pixel stream instead (the capture may not wait on events recorded
+// outside it); the weights each emission samples are the same.  Every call
+// that reads or writes the per-pixel state or the guide from the main stream
+// first makes it wait for the other streams (join_streams).
 int issue_iteration(fr_ctx* c, bool graphs) {
+  const bool batch = c->capturing;
+  const bool train_apart = c->guided && !batch;
   int rc = side_after_main(c);  // calls that wrote state on the main stream since the last iteration
+  if (!rc && train_apart) FR_CUDA(cudaStreamWaitEvent(c->stream, c->sel_ev, 0));
   if (!rc) rc = run_part(c, kPartPhoton, c->stream, graphs);
   if (!rc) rc = run_part(c, kPartEye, c->side, graphs);
   if (!rc) rc = main_after_side(c);
   if (!rc) rc = run_part(c, kPartGrid, c->stream, graphs);
   if (!rc) rc = side_after_main(c);
+  if (!rc && train_apart) FR_CUDA(cudaStreamWaitEvent(c->side, c->train_ev, 0));
   if (!rc) rc = run_part(c, kPartGather, c->side, graphs);
-  if (!rc && c->guided) rc = main_after_side(c);
+  if (!rc && c->guided) {
+    if (train_apart) {
+      FR_CUDA(cudaEventRecord(c->sel_ev, c->side));
+      FR_CUDA(cudaStreamWaitEvent(c->train_stream, c->sel_ev, 0));
+      rc = run_part(c, kPartTrain, c->train_stream, graphs);
+      if (!rc) FR_CUDA(cudaEventRecord(c->train_ev, c->train_stream));
+    } else {
+      rc = run_part(c, kPartTrain, c->side, graphs);
+      if (!rc) rc = main_after_side(c);
+    }
+  }
   return rc;
 }
 
-// One iteration: replays of the four part graphs, or (while the stage
+// One iteration: replays of the part graphs, or (while the stage
 // profiler records events) direct launches.
 int run_iteration(fr_ctx* c) {
   const int rc = issue_iteration(c, !c->profiling);
@@ -769,8 +819,11 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
   cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high);
   if (cudaStreamCreateWithPriority(&c->stream, cudaStreamNonBlocking, prio_high) != cudaSuccess ||
       cudaStreamCreateWithPriority(&c->side, cudaStreamNonBlocking, prio_low) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&c->train_stream, cudaStreamNonBlocking, prio_low) != cudaSuccess ||
       cudaEventCreateWithFlags(&c->fork_ev, cudaEventDisableTiming) != cudaSuccess ||
-      cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming) != cudaSuccess)
+      cudaEventCreateWithFlags(&c->join_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->sel_ev, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&c->train_ev, cudaEventDisableTiming) != cudaSuccess)
     return bail(fail(FR_ERR_CUDA, "cudaStreamCreate/cudaEventCreate failed"));
   for (cudaStream_t& b : c->body)
     if (cudaStreamCreateWithFlags(&b, cudaStreamNonBlocking) != cudaSuccess)
@@ -1004,9 +1057,11 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
     g.train_ctas = std::max(1, c->sms);
     if ((rc = c->alloc(&g.params, kGuideParams)) || (rc = c->alloc(&g.grad, kGuideParams)) ||
         (rc = c->alloc(&g.adam_m, kGuideParams)) || (rc = c->alloc(&g.adam_v, kGuideParams)) ||
-        (rc = c->alloc(&g.tiles, kTileBytes)) || (rc = c->alloc(&g.feat, (size_t)c->P)) ||
+        (rc = c->alloc(&g.tiles, kTileBytes)) || (rc = c->alloc(&g.emit_params, kGuideParams)) ||
+        (rc = c->alloc(&g.emit_tiles, kTileBytes)) || (rc = c->alloc(&g.feat, (size_t)c->P)) ||
         (rc = c->alloc(&g.dir, (size_t)c->P)) || (rc = c->alloc(&g.importance, 2 * (size_t)c->P)) ||
         (rc = c->alloc(&g.batch, (size_t)g.batch_cap)) || (rc = c->alloc(&g.batch_w, (size_t)g.batch_cap)) ||
+        (rc = c->alloc(&g.batch_feat, (size_t)g.batch_cap)) || (rc = c->alloc(&g.batch_dir, (size_t)g.batch_cap)) ||
         (rc = c->alloc(&g.batch_count, 1)) || (rc = c->alloc(&g.select_part, (size_t)guide_select_blocks(c->P))) ||
         (rc = c->alloc(&g.grad_part, (size_t)g.train_ctas * kGuideParams)) ||
         (rc = c->alloc(&g.wsum_part, (size_t)g.train_ctas)) || (rc = c->alloc(&g.weight_sum, 1)) ||
@@ -1023,6 +1078,7 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
     FR_CUDA(cudaMemsetAsync(g.adam_step, 0, 4, c->stream));
     FR_CUDA(cudaMemsetAsync(g.importance, 0, 2 * sizeof(unsigned long long) * (size_t)c->P, c->stream));
     launch_guide_prepare(g, c->stream);
+    if (launch_guide_publish(g, c->stream)) return bail(fail(FR_ERR_CUDA, "guide: weight copy failed"));
     c->guided = true;
   }
 
@@ -1150,7 +1206,7 @@ int fr_batch_iterate(fr_batch* b, int n) {
   const size_t count = b->ctxs.size();
   for (size_t j = 0; j < count; ++j) {
     if (b->ctxs[j]->profiling) return fail(FR_ERR_INVALID, "fr_batch_iterate: context %zu has the stage profiler on", j);
-    const int rc = main_after_side(b->ctxs[j]);  // a gather still running from fr_iterate
+    const int rc = join_streams(b->ctxs[j]);  // a gather or training still running from fr_iterate
     if (rc) return rc;
     FR_CUDA(cudaEventRecord(b->ready[j], b->ctxs[j]->stream));
     FR_CUDA(cudaStreamWaitEvent(b->stream, b->ready[j], 0));
@@ -1180,7 +1236,7 @@ int timed_iterations(fr_ctx* c, int iterations, float* ms) {
   FR_CUDA(cudaEventCreate(&b));
   FR_CUDA(cudaEventRecord(a, c->stream));
   for (int k = 0; k < iterations && !rc; ++k) rc = run_iteration(c);
-  if (!rc) rc = main_after_side(c);  // the last gather
+  if (!rc) rc = join_streams(c);  // the last gather and training
   FR_CUDA(cudaEventRecord(b, c->stream));
   FR_CUDA(cudaEventSynchronize(b));
   FR_CUDA(cudaEventElapsedTime(ms, a, b));
@@ -1190,7 +1246,7 @@ int timed_iterations(fr_ctx* c, int iterations, float* ms) {
 }
 
 void drop_graph(fr_ctx* c) {
-  for (int k = 0; k < 4; ++k) {
+  for (int k = 0; k < 5; ++k) {
     if (c->part_exec[k]) cudaGraphExecDestroy(c->part_exec[k]);
     if (c->part_graph[k]) cudaGraphDestroy(c->part_graph[k]);
     c->part_exec[k] = nullptr;
@@ -1201,7 +1257,7 @@ void drop_graph(fr_ctx* c) {
 
 int fr_autotune(fr_ctx* c, int iterations, uint32_t* photon_tail_min) {
   if (!c || iterations < 1) return fail(FR_ERR_INVALID, "fr_autotune: bad arguments");
-  { const int jrc = main_after_side(c); if (jrc) return jrc; }
+  { const int jrc = join_streams(c); if (jrc) return jrc; }
   if (c->profiling) return fail(FR_ERR_INVALID, "fr_autotune: stage profiler on");
   static const uint32_t kCandidates[] = {4096u, 8192u, 16384u, 32768u, 65536u};
   uint32_t best = c->wave.min_live;
@@ -1225,7 +1281,7 @@ int fr_autotune(fr_ctx* c, int iterations, uint32_t* photon_tail_min) {
 
 int fr_synchronize(fr_ctx* c) {
   if (!c) return fail(FR_ERR_INVALID, "fr_synchronize: NULL context");
-  const int rc = main_after_side(c);
+  const int rc = join_streams(c);
   if (rc) return rc;
   FR_CUDA(cudaStreamSynchronize(c->stream));
   FR_CUDA(cudaGetLastError());
@@ -1321,7 +1377,7 @@ int fr_get_stats(fr_ctx* c, fr_stats* o) {
 
 void* fr_stream(fr_ctx* c) {
   if (!c) return nullptr;
-  main_after_side(c);  // work the caller puts on the stream sees the last gather
+  join_streams(c);  // work the caller puts on the stream sees the last gather and training
   return (void*)c->stream;
 }
 
@@ -1329,7 +1385,7 @@ void fr_destroy(fr_ctx* c) { delete c; }
 
 int fr_profile_enable(fr_ctx* c, int32_t on, int32_t max_iterations) {
   if (!c) return fail(FR_ERR_INVALID, "fr_profile_enable: NULL context");
-  { const int jrc = main_after_side(c); if (jrc) return jrc; }
+  { const int jrc = join_streams(c); if (jrc) return jrc; }
   FR_CUDA(cudaStreamSynchronize(c->stream));
   c->ev_marks.clear();
   c->ev_used = 0;
@@ -1346,7 +1402,7 @@ int fr_profile_enable(fr_ctx* c, int32_t on, int32_t max_iterations) {
 
 int fr_profile_read(fr_ctx* c, double* stage_ms, int64_t* stage_count, int64_t* launches) {
   if (!c) return fail(FR_ERR_INVALID, "fr_profile_read: NULL context");
-  { const int jrc = main_after_side(c); if (jrc) return jrc; }
+  { const int jrc = join_streams(c); if (jrc) return jrc; }
   FR_CUDA(cudaStreamSynchronize(c->stream));
   for (int k = 0; k < FR_STAGES; ++k) {
     if (stage_ms) stage_ms[k] = 0.0;
@@ -1370,7 +1426,7 @@ int fr_profile_read(fr_ctx* c, double* stage_ms, int64_t* stage_count, int64_t* 
 
 int fr_trace_closest(fr_ctx* c, const float* rays, int32_t n, int32_t* facet, float* tuv) {
   if (!c || n < 0 || (n && (!rays || !facet || !tuv))) return fail(FR_ERR_INVALID, "fr_trace_closest: bad arguments");
-  { const int jrc = main_after_side(c); if (jrc) return jrc; }
+  { const int jrc = join_streams(c); if (jrc) return jrc; }
   if (!n) return FR_OK;
   float *d_rays = nullptr, *d_tuv = nullptr;
   int32_t* d_facet = nullptr;
@@ -1388,7 +1444,7 @@ int fr_trace_closest(fr_ctx* c, const float* rays, int32_t n, int32_t* facet, fl
 
 int fr_trace_any(fr_ctx* c, const float* rays, int32_t n, int32_t* hit) {
   if (!c || n < 0 || (n && (!rays || !hit))) return fail(FR_ERR_INVALID, "fr_trace_any: bad arguments");
-  { const int jrc = main_after_side(c); if (jrc) return jrc; }
+  { const int jrc = join_streams(c); if (jrc) return jrc; }
   if (!n) return FR_OK;
   float* d_rays = nullptr;
   int32_t* d_hit = nullptr;
@@ -1407,7 +1463,7 @@ int fr_radius_query(fr_ctx* c, const float* hp, int32_t nh, const float* photons
   if (!c || nh < 0 || np < 0 || (nh && (!hp || !counts)) || (np && !photons_xyz) || !(cell > 0.0f) ||
       !(cell <= 3.0e38f) || (pairs && !pair_count))
     return fail(FR_ERR_INVALID, "fr_radius_query: bad arguments");
-  { const int jrc = main_after_side(c); if (jrc) return jrc; }
+  { const int jrc = join_streams(c); if (jrc) return jrc; }
   if (!nh) return FR_OK;
   if (!np) {
     std::fill(counts, counts + nh, 0);
@@ -1526,7 +1582,7 @@ static_assert(kWaveRounds <= FR_MAX_WAVE_ROUNDS, "round counters exceed FR_MAX_W
 int fr_read_wave_counts(fr_ctx* c, uint32_t* eye_counts, uint32_t* photon_counts, int32_t* eye_rounds,
                         int32_t* photon_rounds) {
   if (!c || !eye_counts || !photon_counts) return fail(FR_ERR_INVALID, "fr_read_wave_counts: bad arguments");
-  { const int jrc = main_after_side(c); if (jrc) return jrc; }
+  { const int jrc = join_streams(c); if (jrc) return jrc; }
   FR_CUDA(cudaMemcpyAsync(eye_counts, c->eye_wave.qcount, sizeof(uint32_t) * (kEyeRounds + 1), cudaMemcpyDeviceToHost,
                           c->stream));
   FR_CUDA(cudaMemcpyAsync(photon_counts, c->wave.qcount, sizeof(uint32_t) * (kPhotonRounds + 1),
@@ -1549,7 +1605,7 @@ int fr_read_wave_counts(fr_ctx* c, uint32_t* eye_counts, uint32_t* photon_counts
 
 int fr_read_direct(fr_ctx* c, float* last3, float* sum3, int32_t* count) {
   if (!c) return fail(FR_ERR_INVALID, "fr_read_direct: NULL context");
-  { const int jrc = main_after_side(c); if (jrc) return jrc; }
+  { const int jrc = join_streams(c); if (jrc) return jrc; }
   const size_t np = (size_t)c->W * c->H;
   std::vector<float4> a(last3 ? np : 0), b((sum3 || count) ? np : 0);
   if (last3) FR_CUDA(cudaMemcpyAsync(a.data(), c->hp.dl, 16 * np, cudaMemcpyDeviceToHost, c->stream));
@@ -1566,7 +1622,7 @@ int fr_read_direct(fr_ctx* c, float* last3, float* sum3, int32_t* count) {
 
 int fr_read_hitpoints(fr_ctx* c, float* pos_type, float* nrm_rough, float* out_mat, float* wgt_facet) {
   if (!c) return fail(FR_ERR_INVALID, "fr_read_hitpoints: NULL context");
-  { const int jrc = main_after_side(c); if (jrc) return jrc; }
+  { const int jrc = join_streams(c); if (jrc) return jrc; }
   const size_t bytes = sizeof(float4) * (size_t)c->W * c->H;
   if (pos_type) FR_CUDA(cudaMemcpyAsync(pos_type, c->hp.pos, bytes, cudaMemcpyDeviceToHost, c->stream));
   if (nrm_rough) FR_CUDA(cudaMemcpyAsync(nrm_rough, c->hp.nrm, bytes, cudaMemcpyDeviceToHost, c->stream));
@@ -1577,7 +1633,7 @@ int fr_read_hitpoints(fr_ctx* c, float* pos_type, float* nrm_rough, float* out_m
 
 int fr_read_photon_slots(fr_ctx* c, float* pos, float* flux, float* dir, uint32_t* counts) {
   if (!c) return fail(FR_ERR_INVALID, "fr_read_photon_slots: NULL context");
-  { const int jrc = main_after_side(c); if (jrc) return jrc; }
+  { const int jrc = join_streams(c); if (jrc) return jrc; }
   const size_t bytes = sizeof(float4) * (size_t)c->P * kPhotonSlots;
   if (pos) FR_CUDA(cudaMemcpyAsync(pos, c->ph.pos, bytes, cudaMemcpyDeviceToHost, c->stream));
   if (flux) FR_CUDA(cudaMemcpyAsync(flux, c->ph.flux, bytes, cudaMemcpyDeviceToHost, c->stream));
@@ -1588,7 +1644,7 @@ int fr_read_photon_slots(fr_ctx* c, float* pos, float* flux, float* dir, uint32_
 
 int fr_read_gather(fr_ctx* c, int32_t* m, float* phi4) {
   if (!c) return fail(FR_ERR_INVALID, "fr_read_gather: NULL context");
-  { const int jrc = main_after_side(c); if (jrc) return jrc; }
+  { const int jrc = join_streams(c); if (jrc) return jrc; }
   const size_t n = (size_t)c->W * c->H;
   if (m) FR_CUDA(cudaMemcpyAsync(m, c->dbg_m, 4 * n, cudaMemcpyDeviceToHost, c->stream));
   if (phi4) FR_CUDA(cudaMemcpyAsync(phi4, c->dbg_phi, 16 * n, cudaMemcpyDeviceToHost, c->stream));
@@ -1597,7 +1653,7 @@ int fr_read_gather(fr_ctx* c, int32_t* m, float* phi4) {
 
 int fr_read_state(fr_ctx* c, double* tau, int32_t* n, float* r, int32_t* g) {
   if (!c) return fail(FR_ERR_INVALID, "fr_read_state: NULL context");
-  { const int jrc = main_after_side(c); if (jrc) return jrc; }
+  { const int jrc = join_streams(c); if (jrc) return jrc; }
   const size_t np = (size_t)c->W * c->H;
   if (tau) FR_CUDA(cudaMemcpyAsync(tau, c->st.tau, 24 * np, cudaMemcpyDeviceToHost, c->stream));
   if (n) FR_CUDA(cudaMemcpyAsync(n, c->st.n, 4 * np, cudaMemcpyDeviceToHost, c->stream));
@@ -1608,7 +1664,7 @@ int fr_read_state(fr_ctx* c, double* tau, int32_t* n, float* r, int32_t* g) {
 
 int fr_update(fr_ctx* c, const int32_t* m, const float* phi) {
   if (!c || !m || !phi) return fail(FR_ERR_INVALID, "fr_update: bad arguments");
-  { const int jrc = main_after_side(c); if (jrc) return jrc; }
+  { const int jrc = join_streams(c); if (jrc) return jrc; }
   const size_t np = (size_t)c->W * c->H;
   std::vector<float4> phi4(np);
   for (size_t i = 0; i < np; ++i) phi4[i] = make_float4(phi[3 * i], phi[3 * i + 1], phi[3 * i + 2], 0.0f);
@@ -1620,7 +1676,7 @@ int fr_update(fr_ctx* c, const int32_t* m, const float* phi) {
 
 int fr_update_dev(fr_ctx* c, const int32_t* m_dev, const float* phi4_dev) {
   if (!c || !m_dev || !phi4_dev) return fail(FR_ERR_INVALID, "fr_update_dev: bad arguments");
-  { const int jrc = main_after_side(c); if (jrc) return jrc; }
+  { const int jrc = join_streams(c); if (jrc) return jrc; }
   if ((reinterpret_cast<uintptr_t>(phi4_dev) & 15u) != 0) return fail(FR_ERR_INVALID, "fr_update_dev: phi4 not 16-byte aligned");
   launch_update(c->st, m_dev, reinterpret_cast<const float4*>(phi4_dev), c->W * c->H, c->alpha,
                 (c->flags & kFlagFloatPhotonCount) != 0u, c->stream);
@@ -1631,22 +1687,23 @@ int fr_update_dev(fr_ctx* c, const int32_t* m_dev, const float* phi4_dev) {
 // ------------------------------------------------------------ guide
 int fr_guide_params(fr_ctx* c, float* params) {
   if (!c || !params || !c->guided) return fail(FR_ERR_INVALID, "fr_guide_params: no guide");
-  { const int jrc = main_after_side(c); if (jrc) return jrc; }
+  { const int jrc = join_streams(c); if (jrc) return jrc; }
   FR_CUDA(cudaMemcpyAsync(params, c->guide.params, sizeof(float) * kGuideParams, cudaMemcpyDeviceToHost, c->stream));
   return fr_synchronize(c);
 }
 
 int fr_guide_set_params(fr_ctx* c, const float* params) {
   if (!c || !params || !c->guided) return fail(FR_ERR_INVALID, "fr_guide_set_params: no guide");
-  { const int jrc = main_after_side(c); if (jrc) return jrc; }
+  { const int jrc = join_streams(c); if (jrc) return jrc; }
   FR_CUDA(cudaMemcpyAsync(c->guide.params, params, sizeof(float) * kGuideParams, cudaMemcpyHostToDevice, c->stream));
   launch_guide_prepare(c->guide, c->stream);
+  if (launch_guide_publish(c->guide, c->stream)) return fail(FR_ERR_CUDA, "guide: weight copy failed");
   return fr_synchronize(c);
 }
 
 int fr_read_guide_importance(fr_ctx* c, float* importance) {
   if (!c || !importance || !c->guided) return fail(FR_ERR_INVALID, "fr_read_guide_importance: no guide");
-  { const int jrc = main_after_side(c); if (jrc) return jrc; }
+  { const int jrc = join_streams(c); if (jrc) return jrc; }
   std::vector<unsigned long long> fx(2 * (size_t)c->P);
   FR_CUDA(cudaMemcpyAsync(fx.data(), c->guide.importance, sizeof(unsigned long long) * fx.size(),
                           cudaMemcpyDeviceToHost, c->stream));
@@ -1659,7 +1716,7 @@ int fr_read_guide_importance(fr_ctx* c, float* importance) {
 int fr_guide_gradient(fr_ctx* c, int32_t n, const float* samples, float* grad, float* weight_sum) {
   if (!c || !c->guided || n < 0 || n > c->P || n > c->guide.batch_cap || (n && !samples) || !grad || !weight_sum)
     return fail(FR_ERR_INVALID, "fr_guide_gradient: bad arguments");
-  { const int jrc = main_after_side(c); if (jrc) return jrc; }
+  { const int jrc = join_streams(c); if (jrc) return jrc; }
   const GuideGPU& g = c->guide;
   std::vector<float4> f(n), d(n);
   std::vector<unsigned long long> imp(2 * (size_t)c->P, 0ull);
@@ -1726,6 +1783,7 @@ std::vector<StatePart> state_parts(fr_ctx* c) {
     parts.push_back({c->guide.adam_m, 4 * (size_t)kGuideParams});
     parts.push_back({c->guide.adam_v, 4 * (size_t)kGuideParams});
     parts.push_back({c->guide.adam_step, 4});
+    parts.push_back({c->guide.emit_params, 4 * (size_t)kGuideParams});  // the weights the next emission samples
   }
   return parts;
 }
@@ -1745,7 +1803,7 @@ int fr_save_state(fr_ctx* c, void* buf, size_t* size) {
     return FR_OK;
   }
   if (*size < need) return fail(FR_ERR_INVALID, "fr_save_state: buffer of %zu bytes, %zu needed", *size, need);
-  { const int jrc = main_after_side(c); if (jrc) return jrc; }
+  { const int jrc = join_streams(c); if (jrc) return jrc; }
   StateHeader h{};
   std::memcpy(h.magic, kStateMagic, 8);
   h.width = c->W;
@@ -1770,7 +1828,7 @@ int fr_save_state(fr_ctx* c, void* buf, size_t* size) {
 
 int fr_load_state(fr_ctx* c, const void* buf, size_t size) {
   if (!c || !buf) return fail(FR_ERR_INVALID, "fr_load_state: bad arguments");
-  { const int jrc = main_after_side(c); if (jrc) return jrc; }
+  { const int jrc = join_streams(c); if (jrc) return jrc; }
   if (size < sizeof(StateHeader)) return fail(FR_ERR_INVALID, "fr_load_state: %zu bytes, no header", size);
   StateHeader h;
   std::memcpy(&h, buf, sizeof h);
@@ -1789,7 +1847,13 @@ int fr_load_state(fr_ctx* c, const void* buf, size_t size) {
   }
   const uint32_t step = h.step_base + (uint32_t)h.iterations, steps[2] = {step, step};
   FR_CUDA(cudaMemcpyAsync(c->step_dev, steps, sizeof steps, cudaMemcpyHostToDevice, c->stream));
-  if (c->guided) launch_guide_prepare(c->guide, c->stream);
+  if (c->guided) {  // both networks' BF16 tiles from their FP32 weights
+    launch_guide_prepare(c->guide, c->stream);
+    GuideGPU e = c->guide;
+    e.params = e.emit_params;
+    e.tiles = e.emit_tiles;
+    launch_guide_prepare(e, c->stream);
+  }
   FR_CUDA(cudaStreamSynchronize(c->stream));
   c->step_base = h.step_base;
   c->iterations = h.iterations;
@@ -1799,7 +1863,7 @@ int fr_load_state(fr_ctx* c, const void* buf, size_t size) {
 
 int fr_seek(fr_ctx* c, uint32_t first_step) {
   if (!c) return fail(FR_ERR_INVALID, "fr_seek: bad arguments");
-  { const int jrc = main_after_side(c); if (jrc) return jrc; }
+  { const int jrc = join_streams(c); if (jrc) return jrc; }
   if (c->iterations != 0) return fail(FR_ERR_INVALID, "fr_seek: %lld iterations already run", (long long)c->iterations);
   FR_CUDA(cudaStreamSynchronize(c->stream));
   const uint32_t steps[2] = {first_step, first_step};

@@ -905,13 +905,13 @@ __global__ void __launch_bounds__(128) k_pw_emit_guided(SceneGPU sc, IterParams 
   const bool live = i < it.photons;
   if (i == 0) w.qcount[0] = (uint32_t)it.photons;
   for (uint32_t e = t; e < (uint32_t)kTileW2T / 16; e += 128)
-    reinterpret_cast<uint4*>(W)[e] = reinterpret_cast<const uint4*>(g.tiles)[e];
-  for (uint32_t e = t; e < (uint32_t)kOffW2; e += 128) p1[e] = g.params[e];
+    reinterpret_cast<uint4*>(W)[e] = reinterpret_cast<const uint4*>(g.emit_tiles)[e];
+  for (uint32_t e = t; e < (uint32_t)kOffW2; e += 128) p1[e] = g.emit_params[e];
   for (uint32_t e = t; e < 64; e += 128) {
-    bias[e] = g.params[kOffB2 + e];
-    bias[64 + e] = g.params[kOffB3 + e];
+    bias[e] = g.emit_params[kOffB2 + e];
+    bias[64 + e] = g.emit_params[kOffB3 + e];
   }
-  for (uint32_t e = t; e < 48; e += 128) bias[128 + e] = g.params[kOffB4 + e];
+  for (uint32_t e = t; e < 48; e += 128) bias[128 + e] = g.emit_params[kOffB4 + e];
   Rng rng(photon_seed(it, i));
   LightPoint lp;
   float x[kGuideIn] = {0.f, 0.f, 0.f, 0.f, 0.f};

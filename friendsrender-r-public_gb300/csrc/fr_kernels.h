@@ -194,7 +194,9 @@ int guide_configure();  // opts the training kernel into its shared memory
 void launch_pw_emit_guided(const SceneGPU& sc, const IterParams& it, PhotonSlots ph, PathWave w, uint32_t* counts,
                            const GuideGPU& g, cudaStream_t s);
 int guide_train_smem();
-int launch_guide_train(const GuideGPU& g, int paths, cudaStream_t s);
+int launch_guide_select_batch(const GuideGPU& g, int paths, cudaStream_t s);  // kernels launched
+int launch_guide_steps(const GuideGPU& g, cudaStream_t s);                    // kernels launched
+int launch_guide_publish(const GuideGPU& g, cudaStream_t s);                  // 0, or -1 on a copy error
 void launch_guide_prepare(const GuideGPU& g, cudaStream_t s);
 // Sample selection and the gradient sums only (no update).
 void launch_guide_gradients(const GuideGPU& g, int paths, cudaStream_t s);

@@ -157,8 +157,10 @@ typedef struct fr_sppm_params {
   float grid_cell_scale;          /* photon grid cell = scale * mean hitpoint radius; <= 0 selects 2 */
   /* Learned photon-emission guide (no counterpart in the reference): photon
    * directions from a defensive mixture of cosine sampling and a network
-   * trained online, with the mixture's pdf in the photon weight.  Zero
-   * (guide = 0) is the reference's plain emission. */
+   * trained online, with the mixture's pdf in the photon weight.  Iteration
+   * k's photons train the network during iteration k + 1, so iteration k + 2
+   * is the first to sample it.  Zero (guide = 0) is the reference's plain
+   * emission. */
   int32_t guide;                  /* 1: guided emission */
   float guide_plain_fraction;     /* share of cosine sampling in the mixture; <= 0 selects 0.2 */
   int32_t guide_batch;            /* training samples per iteration; <= 0 selects 16384 */
@@ -434,7 +436,9 @@ int fr_check_tc_gemm(uint32_t seed, double* max_abs_err);
 int fr_check_exact_math(uint64_t samples, uint32_t seed, uint64_t* mismatches, uint64_t* fast_paths);
 
 /* The photon guide's state (contexts created with guide = 1).
- * fr_guide_params / fr_guide_set_params: the FP32 network parameters
+ * fr_guide_params / fr_guide_set_params: the FP32 network parameters (the
+ * training's latest; fr_guide_set_params also makes them the ones the next
+ * emission samples)
  * (FR_GUIDE_PARAMS floats: W1[64][5], b1, W2[64][64], b2, W3[64][64], b3,
  * W4[48][64] (rows 40-47 zero), b4[48]).  fr_read_guide_importance: per photon
  * path, the flux its photons brought to hitpoints in the last iteration.
