@@ -49,6 +49,19 @@ namespace fr {
 #else
 #define FR_TRACE_BOUNDS __launch_bounds__(128)
 #endif
+// The same for the photon pass's shade kernel, which waits on a chain of
+// dependent loads (hit, facet record, material, textures).  More resident
+// warps did not help: mixed materials 3.55-3.56 ms per iteration with no
+// floor (90 registers, 5 blocks per SM), 3.56 with 6 (78), 3.54-3.56 with 7
+// (72, 20-byte spills), 3.55-3.57 with 8 (64).  0 states only the block size.
+#ifndef FR_PW_SHADE_MIN_BLOCKS
+#define FR_PW_SHADE_MIN_BLOCKS 0
+#endif
+#if FR_PW_SHADE_MIN_BLOCKS > 0
+#define FR_PW_SHADE_BOUNDS __launch_bounds__(128, FR_PW_SHADE_MIN_BLOCKS)
+#else
+#define FR_PW_SHADE_BOUNDS __launch_bounds__(128)
+#endif
 
 namespace {
 
@@ -990,7 +1003,7 @@ __global__ void __launch_bounds__(128) k_pw_emit_guided(SceneGPU sc, IterParams 
 }
 
 template <bool kEndDegenerate>
-__global__ void __launch_bounds__(128) k_pw_shade(SceneGPU sc, IterParams it, PhotonSlots ph, PathWave w,
+__global__ void FR_PW_SHADE_BOUNDS k_pw_shade(SceneGPU sc, IterParams it, PhotonSlots ph, PathWave w,
                                                   uint32_t* counts, int round) {
   const ShadeQueues sq(w, round);
   const uint32_t n = sq.total();

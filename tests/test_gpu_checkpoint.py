@@ -38,24 +38,32 @@ def _check_same(a, b):
     np.testing.assert_allclose(ia, ib, rtol=1e-5, atol=1e-6)
 
 
-@pytest.mark.parametrize('flags', [0, 1])
-def test_resume_matches_uninterrupted(flags):
+@pytest.mark.parametrize('flags,guide', [(0, False), (1, False), (abi.FLAG_END_DEGENERATE_PATHS, True)])
+def test_resume_matches_uninterrupted(flags, guide):
+    """Guided: the checkpoint also holds the network, its optimizer state and
+    the copy the next emission samples (the training's weights one iteration
+    behind), so the resumed render trains the same network bit for bit."""
     scene = _scene()
-    with abi.Renderer(scene, 15000, alpha=0.7, radius=0.02, flags=flags) as a:
+    kw = dict(alpha=0.7, radius=0.02, flags=flags, guide=guide, guide_seed=5)
+    with abi.Renderer(scene, 15000, **kw) as a:
         a.iterate(3)
         ckpt = a.save_state()
         a.iterate(2)
         want = _snapshot(a)
         stats_a = a.stats()
-    with abi.Renderer(scene, 15000, alpha=0.7, radius=0.02, flags=flags) as b:
+        params_a = a.guide_params() if guide else None
+    with abi.Renderer(scene, 15000, **kw) as b:
         b.iterate(1)                       # state to be overwritten
         b.load_state(ckpt)
         b.iterate(2)
         got = _snapshot(b)
         stats_b = b.stats()
+        params_b = b.guide_params() if guide else None
     assert stats_a['iterations'] == stats_b['iterations'] == 5
     assert stats_a['photon_paths'] == stats_b['photon_paths']
     _check_same(want, got)
+    if guide:
+        np.testing.assert_array_equal(params_a, params_b)
 
 
 def test_checkpoint_size_and_refusals():
