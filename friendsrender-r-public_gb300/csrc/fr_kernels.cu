@@ -1048,6 +1048,27 @@ __device__ __forceinline__ uint32_t tail_paths_per_warp(uint32_t n, uint32_t nwa
   return ppw;
 }
 
+// The tail's photon shading (and closest hit) as out-of-line calls (1) or
+// inline (0).  A tail path alternates between traversal and shading, and the
+// inline kernel's largest stall is instruction fetch ("no instruction"); the
+// calls did not help: mixed materials 3.65 ms per iteration with the shading
+// out of line, 3.57 with both, 3.55-3.57 inline.
+#ifndef FR_TAIL_SHADE_NOINLINE
+#define FR_TAIL_SHADE_NOINLINE 0
+#endif
+#ifndef FR_TAIL_TRACE_NOINLINE
+#define FR_TAIL_TRACE_NOINLINE 0
+#endif
+template <bool kEndDegenerate>
+__device__ __noinline__ bool photon_bounce_call(const SceneGPU& sc, const IterParams& it, const PhotonSlots& ph, int i,
+                                                PhotonState& s, const Hit& h) {
+  return photon_shade<kEndDegenerate>(sc, it, ph, i, s, h) && photon_top(s);
+}
+template <bool kWT>
+__device__ __noinline__ bool trace_closest_call(const SceneGPU& sc, V3 o, V3 d, Hit& h, int* err) {
+  return trace_closest<kWT>(sc, o, d, kRayOffset, h, err);
+}
+
 template <bool kEndDegenerate, bool kWT>
 __global__ void __launch_bounds__(128) k_pw_tail(SceneGPU sc, IterParams it, PhotonSlots ph, PathWave w,
                                                  uint32_t* counts, int rounds, int* err) {
@@ -1065,8 +1086,16 @@ __global__ void __launch_bounds__(128) k_pw_tail(SceneGPU sc, IterParams it, Pho
     load_state(w, i, s);
     while (true) {
       Hit h;
+#if FR_TAIL_TRACE_NOINLINE
+      if (!trace_closest_call<kWT>(sc, s.o, s.d, h, err)) break;
+#else
       if (!trace_closest<kWT>(sc, s.o, s.d, kRayOffset, h, err)) break;
+#endif
+#if FR_TAIL_SHADE_NOINLINE
+      if (!photon_bounce_call<kEndDegenerate>(sc, it, ph, i, s, h)) break;
+#else
       if (!photon_shade<kEndDegenerate>(sc, it, ph, i, s, h) || !photon_top(s)) break;
+#endif
     }
     photon_finish(it, ph, counts, i, s.k);
   }
