@@ -240,8 +240,8 @@ struct fr_ctx {
   PathWave eye_wave{};           // eye-pass wavefront state (the passes run concurrently)
   // Two streams.  `stream` runs the photon pass and the grid build; `side`,
   // the pixel stream, runs the eye pass, the gather (with the guide's
-  // training) and fr_resolve_async's resolve.  Events order them:
-  // fork_ev (main -> side), join_ev (side -> main).
+  // publish and sample selection) and fr_resolve_async's resolve.  Events
+  // order them: fork_ev (main -> side), join_ev (side -> main).
   cudaStream_t side = nullptr;
   cudaEvent_t fork_ev = nullptr, join_ev = nullptr;
   // Guided contexts: the guide's training runs on train_stream after the

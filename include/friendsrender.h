@@ -256,13 +256,13 @@ int fr_texture_load(const char* file, int32_t* width, int32_t* height, int32_t* 
 /* Enqueues n SPPM iterations (the loop body of RenderImage_FixRenderTime,
  * SPPM.cpp:768-848, with a fixed photon count).  Iteration k (counted from 1
  * over the context's life) uses the reference's seeds for step k.
- * Asynchronous; see fr_synchronize.  A context has two streams: the photon
- * pass and the photon grid run on the context's stream (fr_stream), the eye
- * pass and the gather on a pixel stream, and an iteration's gather overlaps
- * the next iteration's photon pass.  Every other call on the context, and
- * fr_stream itself, first makes the context's stream wait for the pixel
- * stream, so work queued on it after any of them sees every iteration
- * enqueued so far. */
+ * Asynchronous; see fr_synchronize.  A context has three streams: the
+ * photon pass and the photon grid run on the context's stream (fr_stream),
+ * the eye pass and the gather on a pixel stream (an iteration's gather
+ * overlaps the next iteration's photon pass), and a guided context's
+ * training on a third.  Every other call on the context, and fr_stream
+ * itself, first makes the context's stream wait for the other two, so work
+ * queued on it after any of them sees every iteration enqueued so far. */
 int fr_iterate(fr_ctx* ctx, int n);
 
 /* Waits for the context's streams and reports kernel errors. */
