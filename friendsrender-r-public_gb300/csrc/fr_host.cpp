@@ -15,6 +15,7 @@
 #include <mutex>
 #include <string>
 #include <thread>
+#include <utility>
 #include <vector>
 
 #include "../../include/friendsrender.h"
@@ -989,6 +990,7 @@ int fr_create(const fr_scene_desc* scene, const fr_camera_desc* camera, const fr
   const size_t npix = (size_t)c->W * c->H;
   const size_t nslots = (size_t)c->P * kPhotonSlots;
   const size_t wave_n = (size_t)c->P;
+  c->ph.paths = (uint32_t)c->P;  // slot stride of the slot-major photon slots
   if ((rc = c->alloc(&c->hp.pos, npix)) || (rc = c->alloc(&c->hp.nrm, npix)) || (rc = c->alloc(&c->hp.out, npix)) ||
       (rc = c->alloc(&c->hp.wgt, npix)) || (rc = c->alloc(&c->st.tau, 3 * npix)) || (rc = c->alloc(&c->st.n, npix)) ||
       (rc = c->alloc(&c->st.r, npix)) || (rc = c->alloc(&c->st.g, npix)) || (rc = c->alloc(&c->st.dl, npix)) ||
@@ -1481,6 +1483,7 @@ int fr_radius_query(fr_ctx* c, const float* hp, int32_t nh, const float* photons
     for (int a = 0; a < 3; ++a) lo[a] = std::min(lo[a], hp[4 * i + a] - hp[4 * i + 3]);
   std::vector<uint32_t> ones(std::max(np, 1), 1u);
   PhotonSlots ph{};
+  ph.paths = (uint32_t)np;  // one photon per "path": slot 0 of photon i is i
   PhotonGrid g{};
   g.table = next_pow2(std::max<uint64_t>((uint64_t)np * 2, 1024));
   GridInfo gi{};
@@ -1634,10 +1637,18 @@ int fr_read_hitpoints(fr_ctx* c, float* pos_type, float* nrm_rough, float* out_m
 int fr_read_photon_slots(fr_ctx* c, float* pos, float* flux, float* dir, uint32_t* counts) {
   if (!c) return fail(FR_ERR_INVALID, "fr_read_photon_slots: NULL context");
   { const int jrc = join_streams(c); if (jrc) return jrc; }
-  const size_t bytes = sizeof(float4) * (size_t)c->P * kPhotonSlots;
-  if (pos) FR_CUDA(cudaMemcpyAsync(pos, c->ph.pos, bytes, cudaMemcpyDeviceToHost, c->stream));
-  if (flux) FR_CUDA(cudaMemcpyAsync(flux, c->ph.flux, bytes, cudaMemcpyDeviceToHost, c->stream));
-  if (dir) FR_CUDA(cudaMemcpyAsync(dir, c->ph.dir, bytes, cudaMemcpyDeviceToHost, c->stream));
+  // The device keeps the slots slot-major (slot k of path i at k * P + i);
+  // the caller gets them path-major (i * kPhotonSlots + k).
+  const size_t P = (size_t)c->P, ns = P * kPhotonSlots;
+  std::vector<float4> tmp((pos || flux || dir) ? ns : 0);
+  for (auto [dst, src] : {std::pair<float*, float4*>{pos, c->ph.pos}, {flux, c->ph.flux}, {dir, c->ph.dir}}) {
+    if (!dst) continue;
+    FR_CUDA(cudaMemcpyAsync(tmp.data(), src, sizeof(float4) * ns, cudaMemcpyDeviceToHost, c->stream));
+    FR_CUDA(cudaStreamSynchronize(c->stream));
+    float4* out = reinterpret_cast<float4*>(dst);
+    for (size_t k = 0; k < (size_t)kPhotonSlots; ++k)
+      for (size_t i = 0; i < P; ++i) out[i * kPhotonSlots + k] = tmp[k * P + i];
+  }
   if (counts) FR_CUDA(cudaMemcpyAsync(counts, c->counts, 4 * (size_t)c->P, cudaMemcpyDeviceToHost, c->stream));
   return fr_synchronize(c);
 }
@@ -1757,7 +1768,7 @@ int fr_guide_gradient(fr_ctx* c, int32_t n, const float* samples, float* grad, f
 // directions, each as on the device.
 namespace {
 struct StateHeader {
-  char magic[8];  // "FRSPPMS1"
+  char magic[8];  // "FRSPPMS2" (photon slots slot-major)
   int32_t width, height, photons, flags;
   float alpha, initial_radius;
   int32_t triangles;
@@ -1765,7 +1776,7 @@ struct StateHeader {
   int64_t iterations, photons_total;
 };
 static_assert(sizeof(StateHeader) == 56, "checkpoint header is 56 bytes");
-constexpr char kStateMagic[8] = {'F', 'R', 'S', 'P', 'P', 'M', 'S', '1'};
+constexpr char kStateMagic[8] = {'F', 'R', 'S', 'P', 'P', 'M', 'S', '2'};
 
 struct StatePart {
   void* dev;

@@ -754,9 +754,13 @@ __device__ __forceinline__ void light_point(const SceneGPU& sc, Rng& rng, LightP
 
 // The photon path from its light point and direction (generateLightRay,
 // SPPM.cpp:466-470) and the light-surface photon in slot 0 (SPPM.cpp:530-540).
+__device__ __forceinline__ size_t slot_index(const PhotonSlots& ph, int i, int k) {
+  return (size_t)k * ph.paths + (size_t)i;
+}
+
 __device__ __forceinline__ void photon_launch(const PhotonSlots& ph, int i, const LightPoint& lp, V3 d, float pdf_dir,
                                               const Rng& rng, PhotonState& s) {
-  const size_t base = (size_t)i * kPhotonSlots;
+  const size_t base = slot_index(ph, i, 0);
   const V3 rad = lp.rad * fminf(1.0f, fmaxf(0.0f, dot(lp.ln, d)));
   s.o = lp.pos + lp.ln * kRayOffset;
   s.d = normalized(d);
@@ -796,7 +800,6 @@ __device__ __forceinline__ bool photon_shade(const SceneGPU& sc, const IterParam
                                              PhotonState& s, const Hit& hit) {
   Rng rng(photon_seed(it, i));
   rng.seek(s.draw);
-  const size_t base = (size_t)i * kPhotonSlots;
   Geom g;
   calc_geometry(sc, hit, g);
   g.normal = dot(g.normal, s.d) > 0.0f ? -g.normal : g.normal;
@@ -817,7 +820,7 @@ __device__ __forceinline__ bool photon_shade(const SceneGPU& sc, const IterParam
   else { Ii = s.ix; Io = 1.0f; }
   FParam p{s.d, s.d, g.normal, Ii, Io, g.rough, g.extinction, g.reflectance};
   if (g.flags & kMatSPPM) {
-    const size_t slot = base + s.k;
+    const size_t slot = slot_index(ph, i, s.k);
     store_float4(ph.pos + slot, g.pos, s.ix);
     store_float4(ph.flux + slot, s.flux0 * s.thr * g.albedo, s.PDF);
     store_float4(ph.dir + slot, s.d, 1.0f);
@@ -862,16 +865,15 @@ __device__ __forceinline__ bool photon_shade(const SceneGPU& sc, const IterParam
 // the first invalid one, so a valid stale slot k joins this iteration.
 __device__ __forceinline__ void photon_finish(const IterParams& it, const PhotonSlots& ph, uint32_t* counts, int i,
                                               int k) {
-  const size_t base = (size_t)i * kPhotonSlots;
   uint32_t n;
   if (it.flags & kFlagFixStaleSlot) {
     const int term = k > 0 ? k : 1;
-    if (term < kPhotonSlots) ph.dir[base + term].w = 0.0f;
+    if (term < kPhotonSlots) ph.dir[slot_index(ph, i, term)].w = 0.0f;
     n = (uint32_t)term;
   } else {
     const int term = k + 1;
-    if (term < kPhotonSlots) ph.dir[base + term].w = 0.0f;
-    n = (k == 0 || ph.dir[base + k].w == 0.0f) ? (uint32_t)(k > 0 ? k : 1) : (uint32_t)(k + 1);
+    if (term < kPhotonSlots) ph.dir[slot_index(ph, i, term)].w = 0.0f;
+    n = (k == 0 || ph.dir[slot_index(ph, i, k)].w == 0.0f) ? (uint32_t)(k > 0 ? k : 1) : (uint32_t)(k + 1);
   }
   counts[i] = n;
 }
@@ -1122,10 +1124,9 @@ __global__ void __launch_bounds__(256) k_photon_count(PhotonSlots ph, const uint
   if (i >= paths) return;
   const float ox = gi->origin[0], oy = gi->origin[1], oz = gi->origin[2], inv = gi->inv_cell;
   const uint32_t mask = g.table - 1u;
-  const size_t base = (size_t)i * stride;
   const uint32_t n = counts[i];
   for (uint32_t k = 0; k < n; ++k) {
-    const float4 p = ph.pos[base + k];
+    const float4 p = ph.pos[slot_index(ph, i, (int)k)];
     atomicAdd(g.cell_count + cell_hash(cell_of(p.x, ox, inv), cell_of(p.y, oy, inv), cell_of(p.z, oz, inv), mask), 1u);
   }
 }
@@ -1142,17 +1143,16 @@ __global__ void __launch_bounds__(256) k_photon_scatter(PhotonSlots ph, const ui
   if (i >= paths) return;
   const float ox = gi->origin[0], oy = gi->origin[1], oz = gi->origin[2], inv = gi->inv_cell;
   const uint32_t mask = g.table - 1u;
-  const size_t base = (size_t)i * stride;
   const uint32_t n = counts[i];
   for (uint32_t k = 0; k < n; ++k) {
-    const size_t s = base + k;
+    const size_t s = slot_index(ph, i, (int)k);
     const float4 p = ph.pos[s];
     const uint32_t h = cell_hash(cell_of(p.x, ox, inv), cell_of(p.y, oy, inv), cell_of(p.z, oz, inv), mask);
     const uint32_t dst = g.cell_start[h] + atomicSub(g.cell_count + h, 1u) - 1u;
     g.pos[dst] = p;
     g.flux[dst] = ph.flux[s];
     float4 d = ph.dir[s];
-    d.w = __uint_as_float((uint32_t)s);
+    d.w = __uint_as_float((uint32_t)i * (uint32_t)stride + k);  // the photon's id
     g.dir[dst] = d;
   }
 }

@@ -27,10 +27,15 @@ struct HitpointBuf {
 //   pos  xyz position, w ray index of refraction
 //   flux xyz flux,     w pdf
 //   dir  xyz incoming direction, w 1 valid / 0 invalid
+// Photon slots, slot-major: slot k of path i at k * paths + i, so that the
+// emission's slot-0 stores and the grid's per-path reads are coalesced
+// across a warp's consecutive paths.  A photon's id (the grid's dir.w, the
+// path's importance) stays i * kPhotonSlots + k.
 struct PhotonSlots {
   float4* pos;
   float4* flux;
   float4* dir;
+  uint32_t paths;  // slot stride: the photon paths of the context (photons of a radius query)
 };
 
 // Photons sorted by cell of the hashed grid; dir.w holds the source slot id.
