@@ -466,8 +466,9 @@ int fr_read_wave_counts(fr_ctx* ctx, uint32_t* eye_counts, uint32_t* photon_coun
 int fr_read_hitpoints(fr_ctx* ctx, float* pos_type, float* nrm_rough, float* out_mat, float* wgt_facet);
 
 /* Photon slots after the last iteration: paths * 32 entries of 4 floats each
- * (pos+index, flux+pdf, dir+valid) and the per-path count of photons the
- * compactor takes (SPPM.cpp:812-822). */
+ * (pos+index, flux+pdf, dir+valid), path-major (path i's slot k at entry
+ * i * 32 + k), and the per-path count of photons the compactor takes
+ * (SPPM.cpp:812-822). */
 int fr_read_photon_slots(fr_ctx* ctx, float* pos, float* flux, float* dir, uint32_t* counts);
 
 /* Per-pixel photon count M and flux sum of the last iteration's gather. */
