@@ -504,7 +504,10 @@ int fr_update_dev(fr_ctx* ctx, const int32_t* m_dev, const float* phi4_dev);
  * per-pixel state and the photon slots; fr_load_state restores it into a
  * context created with the same scene, camera and parameters (checked:
  * resolution, photon paths, flags, alpha, initial radius, triangle count), after
- * which iterations continue exactly as they would have in the saved context. */
+ * which iterations continue exactly as they would have in the saved context.
+ * A guided context's checkpoint also holds the network, its optimizer state
+ * and the copy of the network the next emission samples.  Checkpoints of
+ * another layout version (their first 8 bytes) are refused. */
 int fr_save_state(fr_ctx* ctx, void* buf, size_t* size);
 int fr_load_state(fr_ctx* ctx, const void* buf, size_t size);
 
