@@ -265,7 +265,7 @@ struct fr_ctx {
   cudaGraph_t part_graph[5] = {};
   cudaGraphExec_t part_exec[5] = {};
   int64_t part_launches[5] = {};  // kernels per replay of each part
-  int gather_blocks = 0;         // grid of the gather (one warp per hitpoint)
+  int gather_blocks = 0;         // grid of the gather (one 16-lane group per hitpoint)
   int sms = 0;                   // streaming multiprocessors of the device
   bool guided = false;           // learned photon-emission guide on
   GuideGPU guide{};
