@@ -1638,16 +1638,18 @@ int fr_read_photon_slots(fr_ctx* c, float* pos, float* flux, float* dir, uint32_
   if (!c) return fail(FR_ERR_INVALID, "fr_read_photon_slots: NULL context");
   { const int jrc = join_streams(c); if (jrc) return jrc; }
   // The device keeps the slots slot-major (slot k of path i at k * P + i);
-  // the caller gets them path-major (i * kPhotonSlots + k).
-  const size_t P = (size_t)c->P, ns = P * kPhotonSlots;
-  std::vector<float4> tmp((pos || flux || dir) ? ns : 0);
+  // the caller gets them path-major (i * kPhotonSlots + k), one slot's row
+  // of P entries at a time.
+  const size_t P = (size_t)c->P;
+  std::vector<float4> row((pos || flux || dir) ? P : 0);
   for (auto [dst, src] : {std::pair<float*, float4*>{pos, c->ph.pos}, {flux, c->ph.flux}, {dir, c->ph.dir}}) {
     if (!dst) continue;
-    FR_CUDA(cudaMemcpyAsync(tmp.data(), src, sizeof(float4) * ns, cudaMemcpyDeviceToHost, c->stream));
-    FR_CUDA(cudaStreamSynchronize(c->stream));
     float4* out = reinterpret_cast<float4*>(dst);
-    for (size_t k = 0; k < (size_t)kPhotonSlots; ++k)
-      for (size_t i = 0; i < P; ++i) out[i * kPhotonSlots + k] = tmp[k * P + i];
+    for (size_t k = 0; k < (size_t)kPhotonSlots; ++k) {
+      FR_CUDA(cudaMemcpyAsync(row.data(), src + k * P, sizeof(float4) * P, cudaMemcpyDeviceToHost, c->stream));
+      FR_CUDA(cudaStreamSynchronize(c->stream));
+      for (size_t i = 0; i < P; ++i) out[i * kPhotonSlots + k] = row[i];
+    }
   }
   if (counts) FR_CUDA(cudaMemcpyAsync(counts, c->counts, 4 * (size_t)c->P, cudaMemcpyDeviceToHost, c->stream));
   return fr_synchronize(c);
